@@ -1,0 +1,415 @@
+"""Float64 numpy restatement of the reference's entropic-OT algorithms.
+
+TEST INFRASTRUCTURE ONLY: the checker that the CUDA path is compared with.
+Product code never imports this module.
+
+Each function names the reference lines (PythonOT/POT 0.9.7.dev0) whose
+behaviour it restates: iteration order, the every-10th-iteration stopping
+test, the error norm, the returned log keys and the warning events.  Warnings
+are not raised here; they are recorded in ``log["_warnings"]`` so that tests
+can compare them with the GPU path's warnings.
+"""
+import numpy as np
+
+NONCONV = "Sinkhorn did not converge"
+NUMERR = "numerical errors at iteration"
+
+
+def _f64(x):
+    return np.asarray(x, dtype=np.float64)
+
+
+def sqeuclidean(X, Y=None):
+    """Squared Euclidean cost, ``ot/utils.py:270-305`` (``euclidean_distances``,
+    squared=True): ``|x|^2 + |y|^2 - 2 x.y``, clamped at 0, zero diagonal when
+    ``Y`` is ``X``."""
+    same = Y is None or Y is X
+    X = _f64(X)
+    Y = X if same else _f64(Y)
+    c = -2.0 * (X @ Y.T)
+    c += np.einsum("ij,ij->i", X, X)[:, None]
+    c += np.einsum("ij,ij->i", Y, Y)[None, :]
+    c = np.maximum(c, 0.0)
+    if same:
+        np.fill_diagonal(c, 0.0)
+    return c
+
+
+def logsumexp(x, axis):
+    """Max-shifted log-sum-exp with the conventions of
+    ``scipy.special.logsumexp`` (what ``NumpyBackend.logsumexp``,
+    ``ot/backend.py:1306``, calls): an all ``-inf`` slice gives ``-inf``."""
+    mx = np.max(x, axis=axis, keepdims=True)
+    shift = np.where(np.isfinite(mx), mx, 0.0)
+    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+        s = np.sum(np.exp(x - shift), axis=axis, keepdims=True)
+        out = np.log(s) + shift
+    return np.squeeze(out, axis=axis)
+
+
+def _uniform_if_empty(a, b, M):
+    """Empty weight lists mean uniform, ``ot/bregman/_sinkhorn.py:592-595``."""
+    a = _f64(a)
+    b = _f64(b)
+    if a.size == 0:
+        a = np.full(M.shape[0], 1.0 / M.shape[0])
+    if b.size == 0:
+        b = np.full(M.shape[1], 1.0 / M.shape[1])
+    return a, b
+
+
+def sinkhorn_knopp(a, b, M, reg, numItermax=1000, stopThr=1e-9, warmstart=None):
+    """Scaling-form Sinkhorn, ``ot/bregman/_sinkhorn.py:487-687``.
+
+    Per iteration: ``v = b / (K^T u)``, ``u = 1 / ((1/a) K v)`` (``:629-631``);
+    zero / NaN / Inf in the new scalings reverts to the previous pair and
+    stops (``:633-645``); every 10th iteration the column-marginal L2
+    violation is logged and compared with ``stopThr`` (``:646-658``).
+    Returns ``(plan, log)`` for 1-D ``b`` and ``(losses, log)`` for 2-D ``b``
+    (``:676-687``).  ``log["niter"]`` is the last loop index.
+    """
+    M = _f64(M)
+    a, b = _uniform_if_empty(a, b, M)
+    n, m = M.shape
+    n_hists = b.shape[1] if b.ndim > 1 else 0
+    warns = []
+    if warmstart is None:
+        if n_hists:
+            u = np.ones((n, n_hists)) / n
+            v = np.ones((m, n_hists)) / m
+        else:
+            u = np.ones(n) / n
+            v = np.ones(m) / m
+    else:
+        u, v = np.exp(_f64(warmstart[0])), np.exp(_f64(warmstart[1]))
+    with np.errstate(all="ignore"):
+        K = np.exp(M / (-reg))
+        Kp = (1.0 / a).reshape(-1, 1) * K
+    errs = []
+    ii = 0
+    converged_or_broke = False
+    with np.errstate(all="ignore"):
+        for ii in range(numItermax):
+            uprev, vprev = u, v
+            Ktu = K.T @ u
+            v = b / Ktu
+            u = 1.0 / (Kp @ v)
+            if (np.any(Ktu == 0) or np.any(np.isnan(u)) or np.any(np.isnan(v))
+                    or np.any(np.isinf(u)) or np.any(np.isinf(v))):
+                warns.append("Warning: %s %d" % (NUMERR, ii))
+                u, v = uprev, vprev
+                converged_or_broke = True
+                break
+            if ii % 10 == 0:
+                if n_hists:
+                    col = np.einsum("ik,ij,jk->jk", u, K, v)
+                else:
+                    col = np.einsum("i,ij,j->j", u, K, v)
+                err = float(np.linalg.norm(col - b))
+                errs.append(err)
+                if err < stopThr:
+                    converged_or_broke = True
+                    break
+    if not converged_or_broke:
+        warns.append(NONCONV)
+    log = {"err": errs, "niter": ii, "u": u, "v": v, "_warnings": warns}
+    with np.errstate(all="ignore"):
+        if n_hists:
+            return np.einsum("ik,ij,jk,ij->k", u, K, v, M), log
+        return u.reshape(-1, 1) * K * v.reshape(1, -1), log
+
+
+def sinkhorn_log(a, b, M, reg, numItermax=1000, stopThr=1e-9, warmstart=None):
+    """Log-domain Sinkhorn, ``ot/bregman/_sinkhorn.py:690-918``.
+
+    Per iteration ``v = log b - LSE_i(-M/reg + u)`` then
+    ``u = log a - LSE_j(-M/reg + v)`` (``:881-882``); every 10th iteration the
+    column marginal of ``exp(-M/reg + u + v)`` is compared with ``b`` in L2
+    (``:884-899``).  2-D ``b`` recurses per histogram and returns the per
+    histogram losses with a log holding only the potentials (``:819-854``).
+    """
+    M = _f64(M)
+    a, b = _uniform_if_empty(a, b, M)
+    n_hists = b.shape[1] if b.ndim > 1 else 0
+    if n_hists:
+        ws = warmstart if warmstart is not None else [None] * n_hists
+        losses, lus, lvs, warns = [], [], [], []
+        for k in range(n_hists):
+            P, lg = sinkhorn_log(a, b[:, k], M, reg, numItermax, stopThr, ws[k])
+            losses.append(float(np.sum(M * P)))
+            lus.append(lg["log_u"])
+            lvs.append(lg["log_v"])
+            warns += lg["_warnings"]
+        log_u = np.stack(lus, 1)
+        log_v = np.stack(lvs, 1)
+        return np.array(losses), {"log_u": log_u, "log_v": log_v,
+                                  "u": np.exp(log_u), "v": np.exp(log_v),
+                                  "_warnings": warns}
+    Mr = -M / reg
+    if warmstart is None:
+        u = np.zeros(M.shape[0])
+        v = np.zeros(M.shape[1])
+    else:
+        u, v = _f64(warmstart[0]).copy(), _f64(warmstart[1]).copy()
+    with np.errstate(divide="ignore"):
+        loga, logb = np.log(a), np.log(b)
+    errs = []
+    ii = 0
+    stopped = False
+    with np.errstate(all="ignore"):
+        for ii in range(numItermax):
+            v = logb - logsumexp(Mr + u[:, None], 0)
+            u = loga - logsumexp(Mr + v[None, :], 1)
+            if ii % 10 == 0:
+                col = np.sum(np.exp(Mr + u[:, None] + v[None, :]), 0)
+                err = float(np.linalg.norm(col - b))
+                errs.append(err)
+                if err < stopThr:
+                    stopped = True
+                    break
+        P = np.exp(Mr + u[:, None] + v[None, :])
+    warns = [] if stopped else [NONCONV]
+    return P, {"err": errs, "niter": ii, "log_u": u, "log_v": v,
+               "u": np.exp(u), "v": np.exp(v), "_warnings": warns}
+
+
+def sinkhorn(a, b, M, reg, method="sinkhorn", **kw):
+    """Method dispatch of ``ot/bregman/_sinkhorn.py:164-234``."""
+    if method.lower() == "sinkhorn":
+        return sinkhorn_knopp(a, b, M, reg, **kw)
+    if method.lower() == "sinkhorn_log":
+        return sinkhorn_log(a, b, M, reg, **kw)
+    raise ValueError("Unknown method '%s'." % method)
+
+
+def sinkhorn2(a, b, M, reg, method="sinkhorn", **kw):
+    """Loss ``sum(M * plan)`` for 1-D ``b`` (``_sinkhorn.py:435-438``); the
+    solver's per-histogram losses for 2-D ``b`` (``:440-484``)."""
+    res, log = sinkhorn(a, b, M, reg, method=method, **kw)
+    if _f64(b).ndim < 2:
+        return float(np.sum(_f64(M) * res)), log
+    return res, log
+
+
+def log_projection_batch(K, a=None, b=None, max_iter=10000, tol=1e-5):
+    """Batched log-domain Bregman projection, ``ot/batch/_utils.py:165-290``.
+
+    ``K`` is ``-M/reg`` with shape (B, n, m).  The update order is u first,
+    then v (``:268-270``); every 10th iteration the largest L2 violation of
+    the ROW marginal over the batch is compared with ``tol`` (``:273-278``).
+    """
+    K = _f64(K)
+    B, n, m = K.shape
+    a = np.ones((B, n)) / n if a is None else _f64(a)
+    b = np.ones((B, m)) / m if b is None else _f64(b)
+    u = np.zeros((B, n))
+    v = np.zeros((B, m))
+    with np.errstate(divide="ignore"):
+        loga, logb = np.log(a), np.log(b)
+    it = 0
+    with np.errstate(all="ignore"):
+        for it in range(max_iter):
+            u = loga - logsumexp(K + v[:, None, :], 2)
+            v = logb - logsumexp(K + u[:, :, None], 1)
+            if it % 10 == 0:
+                T = np.exp(K + u[:, :, None] + v[:, None, :])
+                err = np.max(np.sqrt(np.sum((T.sum(2) - a) ** 2, 1)))
+                if err < tol:
+                    break
+        logT = K + u[:, :, None] + v[:, None, :]
+        T = np.exp(logT)
+    return {"T": T, "log_T": logT, "n_iters": it, "potentials": (u, v)}
+
+
+def scaling_projection_batch(K, a=None, b=None, max_iter=10000, tol=1e-5):
+    """Batched scaling-form Bregman projection, ``ot/batch/_utils.py:46-162``:
+    ``f = a / (K g)``, ``g = b / (K^T f)`` from ``f = g = 1``, same stopping
+    rule as the log form."""
+    K = _f64(K)
+    B, n, m = K.shape
+    a = np.ones((B, n)) / n if a is None else _f64(a)
+    b = np.ones((B, m)) / m if b is None else _f64(b)
+    f = np.ones((B, n))
+    g = np.ones((B, m))
+    it = 0
+    with np.errstate(all="ignore"):
+        for it in range(max_iter):
+            f = a / np.sum(K * g[:, None, :], 2)
+            g = b / np.sum(K * f[:, :, None], 1)
+            if it % 10 == 0:
+                T = K * f[:, :, None] * g[:, None, :]
+                err = np.max(np.sqrt(np.sum((T.sum(2) - a) ** 2, 1)))
+                if err < tol:
+                    break
+        T = K * f[:, :, None] * g[:, None, :]
+    return {"T": T, "n_iters": it, "potentials": (f, g)}
+
+
+def solve_batch(M, reg, a=None, b=None, max_iter=1000, tol=1e-5,
+                solver="log_sinkhorn", reg_type="entropy"):
+    """``ot/batch/_linear.py:236-357``: projection, then
+    ``value_linear = sum(M*T)`` and ``value = value_linear + reg * R(T)`` with
+    ``R = sum T log(T + 1e-16)`` (entropy) or ``sum T log(T/(a b^T) + 1e-16)``
+    (KL).  Returns a dict with the OTResult fields."""
+    M = _f64(M)
+    B, n, m = M.shape
+    a = np.ones((B, n)) / n if a is None else _f64(a)
+    b = np.ones((B, m)) / m if b is None else _f64(b)
+    if solver == "log_sinkhorn":
+        out = log_projection_batch(-M / reg, a, b, max_iter, tol)
+    elif solver == "sinkhorn":
+        with np.errstate(all="ignore"):
+            out = scaling_projection_batch(np.exp(-M / reg), a, b, max_iter, tol)
+    else:
+        raise ValueError("Unknown solver: %s" % solver)
+    T = out["T"]
+    value_linear = np.sum(M * T, axis=(1, 2))
+    with np.errstate(all="ignore"):
+        if reg_type.lower() == "entropy":
+            value = value_linear + reg * np.sum(T * np.log(T + 1e-16), axis=(1, 2))
+        else:
+            ref = np.einsum("bi,bj->bij", a, b)
+            value = value_linear + reg * np.sum(T * np.log(T / ref + 1e-16), axis=(1, 2))
+    return {"plan": T, "value": value, "value_linear": value_linear,
+            "potentials": out["potentials"], "n_iter": out["n_iters"]}
+
+
+def init_matrix_square_loss(C1, C2, p, q):
+    """``ot/gromov/_utils.py:153-241`` with the square-loss transforms of
+    ``:114-126``: ``constC = C1^2 p 1^T + 1 q^T (C2^2)^T``, ``hC1 = C1``,
+    ``hC2 = 2 C2``."""
+    C1, C2, p, q = _f64(C1), _f64(C2), _f64(p), _f64(q)
+    constC = np.outer((C1 ** 2) @ p, np.ones(len(q))) + np.outer(np.ones(len(p)), q @ (C2 ** 2).T)
+    return constC, C1, 2.0 * C2
+
+
+def tensor_product(constC, hC1, hC2, T):
+    """``ot/gromov/_utils.py:244-280``: ``constC - hC1 T hC2^T``."""
+    return constC - hC1 @ T @ hC2.T
+
+
+def entropic_gromov_wasserstein(C1, C2, p=None, q=None, epsilon=0.1, symmetric=None,
+                                G0=None, max_iter=1000, tol=1e-9, solver="PGD",
+                                warmstart=False, numItermax=1000, stopThr=1e-9):
+    """Entropic GW with square loss, ``ot/gromov/_bregman.py:25-253``.
+
+    Outer loop ``:198-242``: ``tens = 2 (constC - hC1 T hC2^T)`` (averaged
+    with the transposed problem when not symmetric, minus ``eps log T`` for
+    PPA), then ``T = sinkhorn(p, q, tens, eps, method='sinkhorn')``.  With
+    ``warmstart`` the scalings are carried as ``eps * log(u)`` and handed back
+    as the warm start of the next call (``:213-224``), which the Knopp solver
+    reads as ``log u``.  Every 10th outer iteration logs ``||T - Tprev||_F``.
+    Returns ``(T, log)`` with ``log = {"err", "gw_dist"}``.
+    """
+    C1, C2 = _f64(C1), _f64(C2)
+    n1, n2 = C1.shape[0], C2.shape[0]
+    p = np.full(n1, 1.0 / n1) if p is None else _f64(p)
+    q = np.full(n2, 1.0 / n2) if q is None else _f64(q)
+    T = np.outer(p, q) if G0 is None else _f64(G0)
+    constC, hC1, hC2 = init_matrix_square_loss(C1, C2, p, q)
+    if symmetric is None:
+        symmetric = np.allclose(C1, C1.T, atol=1e-10) and np.allclose(C2, C2.T, atol=1e-10)
+    if not symmetric:
+        constCt, hC1t, hC2t = init_matrix_square_loss(C1.T, C2.T, p, q)
+    if warmstart:
+        mu = np.zeros(n1) - np.log(n1)
+        nu = np.zeros(n2) - np.log(n2)
+    cpt, err, errs, warns = 0, 1.0, [], []
+    while err > tol and cpt < max_iter:
+        Tprev = T
+        if symmetric:
+            tens = 2.0 * tensor_product(constC, hC1, hC2, T)
+        else:
+            tens = 0.5 * (2.0 * tensor_product(constC, hC1, hC2, T)
+                          + 2.0 * tensor_product(constCt, hC1t, hC2t, T))
+        if solver == "PPA":
+            with np.errstate(divide="ignore"):
+                tens = tens - epsilon * np.log(T)
+        if warmstart:
+            T, lg = sinkhorn_knopp(p, q, tens, epsilon, numItermax, stopThr, (mu, nu))
+            with np.errstate(divide="ignore"):
+                mu = epsilon * np.log(lg["u"])
+                nu = epsilon * np.log(lg["v"])
+        else:
+            T, lg = sinkhorn_knopp(p, q, tens, epsilon, numItermax, stopThr)
+        warns += lg["_warnings"]
+        if cpt % 10 == 0:
+            err = float(np.linalg.norm(T - Tprev))
+            errs.append(err)
+        cpt += 1
+    if abs(np.sum(T) - 1) > 1e-5:
+        warns.append("Solver failed to produce a transport plan")
+    gw = float(np.sum(tensor_product(constC, hC1, hC2, T) * T))
+    return T, {"err": errs, "gw_dist": gw, "_warnings": warns, "n_outer": cpt}
+
+
+def entropic_gw_log_inner(C1, C2, p=None, q=None, epsilon=0.1, max_iter=50, tol=0.0,
+                          numItermax=1000, stopThr=1e-7):
+    """The entropic-GW outer loop of ``ot/gromov/_bregman.py:198-242``
+    (symmetric square loss, PGD) with the inner solve replaced by
+    ``sinkhorn_log`` (``_sinkhorn.py:690``) warm-started from the previous
+    outer iteration's ``(log_u, log_v)``.  The reference hard-codes the Knopp
+    inner solver; this variant is the log-domain restatement used for the
+    large entropic-GW workload."""
+    C1, C2 = _f64(C1), _f64(C2)
+    n1, n2 = C1.shape[0], C2.shape[0]
+    p = np.full(n1, 1.0 / n1) if p is None else _f64(p)
+    q = np.full(n2, 1.0 / n2) if q is None else _f64(q)
+    T = np.outer(p, q)
+    constC, hC1, hC2 = init_matrix_square_loss(C1, C2, p, q)
+    ws = None
+    cpt, err, errs, inner_iters = 0, 1.0, [], []
+    while err > tol and cpt < max_iter:
+        Tprev = T
+        tens = 2.0 * tensor_product(constC, hC1, hC2, T)
+        T, lg = sinkhorn_log(p, q, tens, epsilon, numItermax, stopThr, ws)
+        ws = (lg["log_u"], lg["log_v"])
+        inner_iters.append(lg["niter"])
+        if cpt % 10 == 0:
+            err = float(np.linalg.norm(T - Tprev))
+            errs.append(err)
+        cpt += 1
+    gw = float(np.sum(tensor_product(constC, hC1, hC2, T) * T))
+    return T, {"err": errs, "gw_dist": gw, "inner_niter": inner_iters,
+               "log_u": ws[0], "log_v": ws[1]}
+
+
+def empirical_sinkhorn_lazy(X, Y, reg, a=None, b=None, numIterMax=10000, stopThr=1e-9,
+                            batchSize=100, warmstart=None):
+    """Blockwise ("lazy") log-domain Sinkhorn on point clouds,
+    ``ot/bregman/_empirical.py:190-263``.
+
+    The cost ``sqeuclidean(X_blk, Y)`` is recomputed per block; per iteration
+    ``f = log a - LSE_j(g - C/reg)`` then ``g = log b - LSE_i(f - C/reg)``;
+    at every 10th iteration counted from one (``(i+1) % 10 == 0``) the L1
+    violation of the ROW marginal is compared with ``stopThr`` using ``<=``.
+    Returns ``(f, g, log)`` with ``log = {"err", "u": f, "v": g, "niter"}``.
+    """
+    X, Y = _f64(X), _f64(Y)
+    ns, nt = X.shape[0], Y.shape[0]
+    a = np.full(ns, 1.0 / ns) if a is None else _f64(a)
+    b = np.full(nt, 1.0 / nt) if b is None else _f64(b)
+    bs, bt = (batchSize, batchSize) if isinstance(batchSize, int) else batchSize
+    f = np.zeros(ns) if warmstart is None else _f64(warmstart[0]).copy()
+    g = np.zeros(nt) if warmstart is None else _f64(warmstart[1]).copy()
+    loga, logb = np.log(a), np.log(b)
+    errs, warns = [], []
+    i_ot = 0
+    stopped = False
+    for i_ot in range(numIterMax):
+        f = loga - np.concatenate([logsumexp(g[None, :] - sqeuclidean(X[i:i + bs], Y) / reg, 1)
+                                   for i in range(0, ns, bs)])
+        g = logb - np.concatenate([logsumexp(f[:, None] - sqeuclidean(X, Y[j:j + bt]) / reg, 0)
+                                   for j in range(0, nt, bt)])
+        if (i_ot + 1) % 10 == 0:
+            m1 = np.concatenate([np.sum(np.exp(f[i:i + bs, None] + g[None, :]
+                                               - sqeuclidean(X[i:i + bs], Y) / reg), 1)
+                                 for i in range(0, ns, bs)])
+            err = float(np.sum(np.abs(m1 - a)))
+            errs.append(err)
+            if err <= stopThr:
+                stopped = True
+                break
+    if not stopped:
+        warns.append(NONCONV)
+    return f, g, {"err": errs, "u": f, "v": g, "niter": i_ot, "_warnings": warns}

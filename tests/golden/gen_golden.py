@@ -1,0 +1,198 @@
+"""Generate the golden fixtures in this folder by running the REFERENCE.
+
+Run in a container that holds the reference source tree (it is imported
+through ``ref_import.py``); the GPU machine never runs this script, it only reads
+the ``.npz`` files it writes.  Every case records its inputs, the reference's
+outputs and, where the reference warns, the warnings it raised.
+
+    python tests/golden/gen_golden.py
+"""
+import os
+import sys
+import warnings
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+from ref_import import import_ot  # noqa: E402
+
+ot = import_ot()
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in arrays.items()})
+    print("wrote", name, os.path.getsize(path), "bytes")
+
+
+def call_warn(fn, *a, **k):
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        out = fn(*a, **k)
+    return out, [str(x.message) for x in w]
+
+
+def dense_case(name, a, b, M, reg, numItermax=1000, stopThr=1e-9):
+    """sinkhorn (Knopp) and sinkhorn_log on one dense problem."""
+    out = dict(a=a, b=b, M=M, reg=reg, numItermax=numItermax, stopThr=stopThr)
+    for method, tag in (("sinkhorn", "knopp"), ("sinkhorn_log", "log")):
+        (P, lg), w = call_warn(ot.sinkhorn, a, b, M, reg, method=method, numItermax=numItermax,
+                               stopThr=stopThr, log=True)
+        out[tag + "_plan"] = P
+        out[tag + "_loss"] = float(np.sum(M * P))
+        out[tag + "_niter"] = lg["niter"]
+        out[tag + "_err"] = np.array(lg["err"], dtype=np.float64)
+        out[tag + "_u"] = lg["u"]
+        out[tag + "_v"] = lg["v"]
+        out[tag + "_nwarn"] = len(w)
+        out[tag + "_warn_nonconv"] = int(any("did not converge" in s for s in w))
+        out[tag + "_warn_numerr"] = int(any("numerical errors" in s for s in w))
+    save(name, **out)
+
+
+def main():
+    # 1. reference doctest (ot/bregman/_sinkhorn.py:123-129, 342-347)
+    a = np.array([0.5, 0.5])
+    M = np.array([[0.0, 1.0], [1.0, 0.0]])
+    P = ot.sinkhorn(a, a, M, 1)
+    loss = ot.sinkhorn2(a, a, M, 1)
+    save("doctest_2x2", a=a, b=a, M=M, plan=P, loss=loss)
+
+    # 2. the plain dense CPU workload: 1024 points in R^2, N(0,I) vs N((1,1),0.5I)
+    rng = np.random.default_rng(20240601)
+    n = 1024
+    x = rng.standard_normal((n, 2))
+    y = rng.standard_normal((n, 2)) * np.sqrt(0.5) + 1.0
+    M = ot.dist(x, y)
+    M /= M.max()
+    u = ot.unif(n)
+    dense_case("dense_1024_gauss2d", u, u, M, 0.05, 1000, 1e-9)
+    # store the points too: tests rebuild M with the oracle's cost
+    d = dict(np.load(os.path.join(HERE, "dense_1024_gauss2d.npz")))
+    d.pop("M")
+    d.pop("knopp_plan")
+    d.pop("log_plan")
+    save("dense_1024_gauss2d", x=x, y=y, **d)
+
+    # 3. small and ragged shapes, random weights, two regularisations
+    rng = np.random.default_rng(7)
+    for (n, m) in [(1, 1), (2, 3), (3, 2), (31, 33), (127, 129), (100, 100), (5, 300)]:
+        for reg in (0.05, 0.5):
+            M = rng.random((n, m))
+            a = rng.dirichlet(np.ones(n)) if n > 1 else np.ones(1)
+            b = rng.dirichlet(np.ones(m)) if m > 1 else np.ones(1)
+            dense_case("dense_%dx%d_reg%g" % (n, m, reg), a, b, M, reg, 2000, 1e-9)
+
+    # 4. failure paths: non-convergence at numItermax=1, reg=0 numerical error
+    n = 100
+    a1 = ot.datasets.make_1D_gauss(n, m=30, s=10)
+    a2 = ot.datasets.make_1D_gauss(n, m=40, s=10)
+    M = ot.utils.dist0(n)
+    dense_case("fail_maxiter1", a1, a2, M, 1.0, 1, 0.0)
+    (P, lg), w = call_warn(ot.sinkhorn, a1, a2, M, 0.0, method="sinkhorn", log=True, warn=False)
+    save("fail_reg0_knopp", a=a1, b=a2, M=M, niter=lg["niter"], u=lg["u"], v=lg["v"],
+         warn_numerr=int(any("numerical errors" in s for s in w)))
+
+    # 5. several target histograms (2-D b), both methods
+    rng = np.random.default_rng(11)
+    n = 31
+    x = rng.standard_normal((n, 2))
+    M = ot.dist(x, x)
+    a = ot.unif(n)
+    B = np.stack([rng.dirichlet(np.ones(n)) for _ in range(3)], 1)
+    out = dict(a=a, b=B, M=M, reg=1.0)
+    for method, tag in (("sinkhorn", "knopp"), ("sinkhorn_log", "log")):
+        loss, lg = ot.sinkhorn2(a, B, M, 1.0, method=method, log=True, stopThr=1e-10)
+        out[tag + "_loss"] = np.asarray(loss)
+        out[tag + "_u"] = lg["u"]
+        out[tag + "_v"] = lg["v"]
+    save("multib_31x3", **out)
+
+    # 6. batch solvers (test/batch/test_solve_batch.py:28-62 setting)
+    rng = np.random.RandomState(0)
+    M = rng.rand(4, 16, 16)
+    out = dict(M=M, reg=0.1, tol=1e-5, max_iter=10000)
+    for solver in ("log_sinkhorn", "sinkhorn"):
+        for reg_type in ("entropy", "kl"):
+            res = ot.batch.solve_batch(M, 0.1, max_iter=10000, tol=1e-5, solver=solver,
+                                       reg_type=reg_type, grad="detach")
+            tag = "%s_%s" % (solver, reg_type)
+            out[tag + "_plan"] = res.plan
+            out[tag + "_value"] = res.value
+            out[tag + "_value_linear"] = res.value_linear
+            out[tag + "_pot_u"] = res.potentials[0]
+            out[tag + "_pot_v"] = res.potentials[1]
+            out[tag + "_n_iter"] = res.log["n_iter"]
+    save("batch_4x16", **out)
+    # ragged batch through zero-weight padding (uneven n, m in one padded batch)
+    rng = np.random.default_rng(5)
+    sizes = [(12, 9), (7, 16), (16, 16), (3, 5)]
+    Bn, Bm = 16, 16
+    M = rng.random((4, Bn, Bm))
+    A = np.zeros((4, Bn))
+    Bw = np.zeros((4, Bm))
+    for k, (n, m) in enumerate(sizes):
+        A[k, :n] = rng.dirichlet(np.ones(n))
+        Bw[k, :m] = rng.dirichlet(np.ones(m))
+    with np.errstate(all="ignore"), warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        res = ot.batch.solve_batch(M, 0.05, a=A, b=Bw, max_iter=20000, tol=1e-9, grad="detach")
+    save("batch_ragged_padded", M=M, a=A, b=Bw, sizes=np.array(sizes), reg=0.05,
+         plan=res.plan, value_linear=res.value_linear, n_iter=res.log["n_iter"])
+    # solve_sample_batch on point clouds
+    rng = np.random.default_rng(9)
+    X = rng.standard_normal((3, 20, 3))
+    Y = rng.standard_normal((3, 25, 3)) + 0.5
+    res = ot.batch.solve_sample_batch(X, Y, 0.5, max_iter=5000, tol=1e-7, grad="detach")
+    save("batch_sample_3x20x25", X=X, Y=Y, reg=0.5, plan=res.plan, value=res.value,
+         value_linear=res.value_linear, n_iter=res.log["n_iter"])
+
+    # 7. entropic GW (test/gromov/test_bregman.py:25-78 setting and variants)
+    xs = ot.datasets.make_2D_samples_gauss(10, np.array([0, 0]), np.eye(2), random_state=42)
+    xt = xs[::-1].copy()
+    C1 = ot.dist(xs, xs)
+    C2 = ot.dist(xt, xt)
+    C1 /= C1.max()
+    C2 /= C2.max()
+    p = ot.unif(10)
+    out = dict(C1=C1, C2=C2, p=p, q=p)
+    for tag, kw in (("pgd", {}), ("pgd_warm", {"warmstart": True}), ("ppa", {"solver": "PPA"})):
+        G, lg = ot.gromov.entropic_gromov_wasserstein(C1, C2, p, p, "square_loss", epsilon=1e-2,
+                                                      max_iter=10, log=True, **kw)
+        out[tag + "_T"] = G
+        out[tag + "_gw"] = lg["gw_dist"]
+        out[tag + "_err"] = np.array(lg["err"])
+    save("egw_10", **out)
+    rng = np.random.default_rng(3)
+    xs = rng.standard_normal((48, 3))
+    xt = rng.standard_normal((40, 8))
+    C1 = ot.dist(xs, xs)
+    C2 = ot.dist(xt, xt)
+    C1 /= C1.max()
+    C2 /= C2.max()
+    G, lg = ot.gromov.entropic_gromov_wasserstein(C1, C2, None, None, "square_loss", epsilon=5e-2,
+                                                  max_iter=20, tol=1e-9, log=True,
+                                                  numItermax=2000, stopThr=1e-9)
+    gw2 = ot.gromov.entropic_gromov_wasserstein2(C1, C2, None, None, "square_loss", epsilon=5e-2,
+                                                 max_iter=20, tol=1e-9, numItermax=2000,
+                                                 stopThr=1e-9)
+    save("egw_48x40", C1=C1, C2=C2, T=G, gw=lg["gw_dist"], err=np.array(lg["err"]), gw2=gw2,
+         epsilon=5e-2)
+    # asymmetric input
+    C1a = C1 + 0.05 * rng.random(C1.shape)
+    G, lg = ot.gromov.entropic_gromov_wasserstein(C1a, C2, None, None, "square_loss", epsilon=5e-2,
+                                                  max_iter=10, log=True)
+    save("egw_asym_48x40", C1=C1a, C2=C2, T=G, gw=lg["gw_dist"], err=np.array(lg["err"]))
+
+    # 8. lazy empirical Sinkhorn (ot/bregman/_empirical.py:190-263)
+    rng = np.random.default_rng(21)
+    X = rng.standard_normal((60, 3))
+    Y = rng.standard_normal((50, 3)) + 1.0
+    f, g, lg = ot.bregman.empirical_sinkhorn(X, Y, 1.0, isLazy=True, batchSize=7, numIterMax=500,
+                                             stopThr=1e-9, log=True)
+    save("lazy_60x50", X=X, Y=Y, reg=1.0, f=f, g=g, err=np.array(lg["err"]), niter=lg["niter"])
+
+
+if __name__ == "__main__":
+    main()

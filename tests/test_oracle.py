@@ -1,0 +1,117 @@
+"""Pin the CPU oracle to the reference: every golden vector the reference
+produced (tests/golden/gen_golden.py) and its own doctest values."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden, golden_names
+
+DENSE = golden_names("dense_") + ["fail_maxiter1"]
+
+
+def _M(g):
+    if "M" in g:
+        return g["M"]
+    M = oracle.sqeuclidean(g["x"], g["y"])
+    return M / M.max()
+
+
+def test_doctest_values():
+    g = golden("doctest_2x2")
+    P, _ = oracle.sinkhorn(g["a"], g["b"], g["M"], 1.0)
+    np.testing.assert_allclose(P, [[0.36552929, 0.13447071], [0.13447071, 0.36552929]], atol=1e-8)
+    loss, _ = oracle.sinkhorn2(g["a"], g["b"], g["M"], 1.0)
+    assert abs(loss - 0.26894142136999516) < 1e-15
+    np.testing.assert_allclose(P, g["plan"], rtol=1e-14)
+
+
+@pytest.mark.parametrize("name", DENSE)
+@pytest.mark.parametrize("tag", ["knopp", "log"])
+def test_dense_against_reference(name, tag):
+    g = golden(name)
+    M = _M(g)
+    fn = oracle.sinkhorn_knopp if tag == "knopp" else oracle.sinkhorn_log
+    P, lg = fn(g["a"], g["b"], M, float(g["reg"]), int(g["numItermax"]), float(g["stopThr"]))
+    assert lg["niter"] == int(g[tag + "_niter"])
+    np.testing.assert_allclose(lg["err"], g[tag + "_err"], rtol=1e-7, atol=1e-15)
+    np.testing.assert_allclose(lg["u"], g[tag + "_u"], rtol=1e-9)
+    np.testing.assert_allclose(lg["v"], g[tag + "_v"], rtol=1e-9)
+    assert abs(float(np.sum(M * P)) - float(g[tag + "_loss"])) <= 1e-10 * abs(float(g[tag + "_loss"])) + 1e-300
+    if tag + "_plan" in g:
+        np.testing.assert_allclose(P, g[tag + "_plan"], rtol=1e-8, atol=1e-300)
+    assert int(any("did not converge" in w for w in lg["_warnings"])) == int(g[tag + "_warn_nonconv"])
+
+
+def test_reg0_numerical_error_reverts():
+    g = golden("fail_reg0_knopp")
+    _, lg = oracle.sinkhorn_knopp(g["a"], g["b"], g["M"], 0.0)
+    assert lg["niter"] == int(g["niter"])
+    assert any("numerical errors" in w for w in lg["_warnings"]) == bool(g["warn_numerr"])
+    np.testing.assert_allclose(lg["u"], g["u"])
+    np.testing.assert_allclose(lg["v"], g["v"])
+
+
+@pytest.mark.parametrize("tag", ["knopp", "log"])
+def test_multi_histogram(tag):
+    g = golden("multib_31x3")
+    method = "sinkhorn" if tag == "knopp" else "sinkhorn_log"
+    loss, lg = oracle.sinkhorn2(g["a"], g["b"], g["M"], 1.0, method=method, stopThr=1e-10)
+    np.testing.assert_allclose(loss, g[tag + "_loss"], rtol=1e-10)
+    np.testing.assert_allclose(lg["u"], g[tag + "_u"], rtol=1e-8)
+    np.testing.assert_allclose(lg["v"], g[tag + "_v"], rtol=1e-8)
+
+
+@pytest.mark.parametrize("solver", ["log_sinkhorn", "sinkhorn"])
+@pytest.mark.parametrize("reg_type", ["entropy", "kl"])
+def test_batch(solver, reg_type):
+    g = golden("batch_4x16")
+    r = oracle.solve_batch(g["M"], 0.1, max_iter=10000, tol=1e-5, solver=solver, reg_type=reg_type)
+    tag = "%s_%s" % (solver, reg_type)
+    assert r["n_iter"] == int(g[tag + "_n_iter"])
+    np.testing.assert_allclose(r["plan"], g[tag + "_plan"], rtol=1e-9, atol=1e-300)
+    np.testing.assert_allclose(r["value"], g[tag + "_value"], rtol=1e-9)
+    np.testing.assert_allclose(r["value_linear"], g[tag + "_value_linear"], rtol=1e-9)
+    np.testing.assert_allclose(r["potentials"][0], g[tag + "_pot_u"], rtol=1e-9)
+
+
+def test_batch_padded_ragged():
+    g = golden("batch_ragged_padded")
+    r = oracle.solve_batch(g["M"], float(g["reg"]), g["a"], g["b"], max_iter=20000, tol=1e-9)
+    assert r["n_iter"] == int(g["n_iter"])
+    np.testing.assert_allclose(r["plan"], g["plan"], rtol=1e-8, atol=1e-300)
+
+
+def test_batch_sample():
+    g = golden("batch_sample_3x20x25")
+    X, Y = g["X"], g["Y"]
+    M = np.stack([oracle.sqeuclidean(X[k], Y[k]) for k in range(X.shape[0])])
+    r = oracle.solve_batch(M, float(g["reg"]), max_iter=5000, tol=1e-7)
+    assert r["n_iter"] == int(g["n_iter"])
+    np.testing.assert_allclose(r["plan"], g["plan"], rtol=1e-7, atol=1e-14)
+
+
+@pytest.mark.parametrize("tag,kw", [("pgd", {}), ("pgd_warm", {"warmstart": True}), ("ppa", {"solver": "PPA"})])
+def test_egw_small(tag, kw):
+    g = golden("egw_10")
+    T, lg = oracle.entropic_gromov_wasserstein(g["C1"], g["C2"], g["p"], g["q"], 1e-2, max_iter=10, **kw)
+    np.testing.assert_allclose(T, g[tag + "_T"], rtol=1e-8, atol=1e-14)
+    assert abs(lg["gw_dist"] - float(g[tag + "_gw"])) < 1e-10
+    np.testing.assert_allclose(lg["err"], g[tag + "_err"], rtol=1e-6, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["egw_48x40", "egw_asym_48x40"])
+def test_egw_medium(name):
+    g = golden(name)
+    kw = dict(max_iter=20, tol=1e-9, numItermax=2000, stopThr=1e-9) if name == "egw_48x40" else dict(max_iter=10)
+    T, lg = oracle.entropic_gromov_wasserstein(g["C1"], g["C2"], epsilon=5e-2, **kw)
+    np.testing.assert_allclose(T, g["T"], rtol=1e-7, atol=1e-13)
+    assert abs(lg["gw_dist"] - float(g["gw"])) < 1e-9
+
+
+def test_lazy():
+    g = golden("lazy_60x50")
+    f, gg, lg = oracle.empirical_sinkhorn_lazy(g["X"], g["Y"], 1.0, batchSize=7, numIterMax=500, stopThr=1e-9)
+    assert lg["niter"] == int(g["niter"])
+    np.testing.assert_allclose(f, g["f"], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(gg, g["g"], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(lg["err"], g["err"], rtol=1e-6, atol=1e-15)
