@@ -1,0 +1,94 @@
+/* pot_gb300 — C ABI of the GB300 entropic-OT kernels.
+ *
+ * Plain pointers and sizes only.  Every array argument is DEVICE memory of
+ * the current CUDA device unless stated otherwise; every call is
+ * asynchronous on `stream` and returns an OTG_* status code for argument or
+ * launch errors.  Results that the reference reports through its Python log
+ * dict (iteration index, marginal errors, warnings) are written to a small
+ * device "info" block that the caller reads after synchronising.
+ *
+ * The reference (PythonOT/POT) has no C interface for this path: its entry
+ * points are Python functions.  Each declaration names the reference
+ * function whose arithmetic it replaces.
+ */
+#ifndef POT_GB300_H
+#define POT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* element types */
+#define OTG_F32 0
+#define OTG_F64 1
+
+/* Sinkhorn forms */
+#define OTG_METHOD_KNOPP 0 /* scaling form,  ot/bregman/_sinkhorn.py:487 sinkhorn_knopp */
+#define OTG_METHOD_LOG 1   /* log form,      ot/bregman/_sinkhorn.py:690 sinkhorn_log   */
+
+/* return codes */
+#define OTG_OK 0
+#define OTG_ERR_ARG -1
+#define OTG_ERR_DTYPE -2
+#define OTG_ERR_WORKSPACE -3
+#define OTG_ERR_CUDA -4
+#define OTG_ERR_UNSUPPORTED -5
+
+/* solve status written to info[0] */
+#define OTG_STATUS_CONVERGED 0 /* error below stopThr at a check iteration      */
+#define OTG_STATUS_MAXITER 1   /* numItermax reached ("did not converge")      */
+#define OTG_STATUS_NUMERICAL 2 /* zero / NaN / Inf scaling: reverted (knopp)     */
+#define OTG_STATUS_ABORTED 3   /* a bounded device wait ran out                 */
+
+/* ------------------------------------------------------------------------
+ * Dense-cost Sinkhorn, one problem, the whole iteration loop in one
+ * persistent cooperative launch.
+ * Replaces the loops of ot/bregman/_sinkhorn.py:626-663 (sinkhorn_knopp) and
+ * :880-899 (sinkhorn_log) behind ot.sinkhorn / ot.sinkhorn2
+ * (ot/bregman/_sinkhorn.py:21, :237).
+ * ---------------------------------------------------------------------- */
+typedef struct OtgDenseProblem {
+  int32_t dtype;      /* OTG_F32 or OTG_F64: type of M, a, b, warm_*, out_* */
+  int32_t method;     /* OTG_METHOD_KNOPP or OTG_METHOD_LOG                  */
+  const void* M;      /* n x m cost, row-major, leading dimension ldm        */
+  int64_t n, m, ldm;
+  const void* a;      /* source weights (n)                                  */
+  const void* b;      /* target weights (m)                                  */
+  const void* warm_u; /* optional natural-log warm start (n) or NULL         */
+  const void* warm_v; /* optional natural-log warm start (m) or NULL         */
+  double reg;         /* entropic regularisation (> 0)                       */
+  int32_t max_iter;   /* numItermax                                          */
+  int32_t hist_cap;   /* capacity of the error history (>= max_iter/10 + 2)  */
+  double stop_thr;    /* stopThr on the L2 column-marginal violation         */
+  void* out_u;        /* knopp: scaling u; log: log_u (natural log)  (n)     */
+  void* out_v;        /* knopp: scaling v; log: log_v                (m)     */
+  size_t workspace_bytes;
+  int32_t grid;       /* CTAs (0 = all co-resident CTAs); tuning knob        */
+  int32_t timeout_ms; /* bound on any single device wait (0 = 4000 ms)       */
+} OtgDenseProblem;
+
+/* Workspace size for otg_sinkhorn_dense (device bytes, 256-byte aligned). */
+size_t otg_dense_workspace_bytes(int dtype, int64_t n, int64_t m, int hist_cap, int grid);
+/* Byte offset inside the workspace of the result block:
+ *   double err_hist[hist_cap]; then int32 info[8] 256-byte aligned after it
+ *   (info[0] status, info[1] niter = last loop index, info[2] number of
+ *   logged errors, info[3] abort flag). */
+size_t otg_dense_info_offset(int dtype, int64_t n, int64_t m, int hist_cap, int grid);
+int otg_sinkhorn_dense(const OtgDenseProblem* p, void* workspace, cudaStream_t stream);
+
+/* Plan and/or loss from potentials: P = exp(-M/reg + u + v) (log form) or
+ * diag(u) exp(-M/reg) diag(v) (scaling form); *loss = sum(M * P) in fp64.
+ * P or loss may be NULL.  Replaces the returns of ot/bregman/_sinkhorn.py:
+ * 681-687 and :915-918 and the loss of sinkhorn2 :435-438. */
+int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, int64_t ldm,
+                   const void* u, const void* v, double reg, void* P, int64_t ldp, double* loss,
+                   cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* POT_GB300_H */

@@ -1,0 +1,11 @@
+"""pot_gb300 — GB300-native entropic optimal transport.
+
+Drop-in GPU implementations of PythonOT/POT's entropic-OT hot path:
+``sinkhorn`` / ``sinkhorn2`` (methods 'sinkhorn' and 'sinkhorn_log'),
+``sinkhorn_knopp``, ``sinkhorn_log``.  All arithmetic runs in hand-written
+CUDA kernels for sm_103a (``pot_gb300/csrc``) behind the C ABI of
+``include/pot_gb300.h``; there is no CPU fallback.
+"""
+from .bregman import sinkhorn, sinkhorn2, sinkhorn_knopp, sinkhorn_log  # noqa: F401
+
+__version__ = "0.1.0"

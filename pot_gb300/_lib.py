@@ -1,0 +1,83 @@
+"""ctypes binding of the C ABI declared in ``include/pot_gb300.h``.
+
+The library is the only compute path: importing a solver without it on a GPU
+machine raises, there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import torch
+
+from . import _build
+
+OTG_F32, OTG_F64 = 0, 1
+OTG_METHOD_KNOPP, OTG_METHOD_LOG = 0, 1
+STATUS_CONVERGED, STATUS_MAXITER, STATUS_NUMERICAL, STATUS_ABORTED = 0, 1, 2, 3
+_ERRORS = {-1: "invalid argument", -2: "unsupported dtype", -3: "workspace too small",
+           -4: "CUDA launch error", -5: "unsupported configuration"}
+
+c_i32, c_i64, c_sz, c_dbl, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t, ctypes.c_double, ctypes.c_void_p
+
+
+class OtgDenseProblem(ctypes.Structure):
+    _fields_ = [("dtype", c_i32), ("method", c_i32), ("M", c_vp), ("n", c_i64), ("m", c_i64),
+                ("ldm", c_i64), ("a", c_vp), ("b", c_vp), ("warm_u", c_vp), ("warm_v", c_vp),
+                ("reg", c_dbl), ("max_iter", c_i32), ("hist_cap", c_i32), ("stop_thr", c_dbl),
+                ("out_u", c_vp), ("out_v", c_vp), ("workspace_bytes", c_sz), ("grid", c_i32),
+                ("timeout_ms", c_i32)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "otg_dense_workspace_bytes": (c_sz, [ctypes.c_int, c_i64, c_i64, ctypes.c_int, ctypes.c_int]),
+    "otg_dense_info_offset": (c_sz, [ctypes.c_int, c_i64, c_i64, ctypes.c_int, ctypes.c_int]),
+    "otg_sinkhorn_dense": (ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp]),
+    "otg_dense_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp,
+                                      c_dbl, c_vp, c_i64, c_vp, c_vp]),
+}
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load (and if needed build) the shared library; returns the ctypes handle."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("pot_gb300 CUDA library not built: %s" % path)
+        _build.build()
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc, what):
+    if rc != 0:
+        raise RuntimeError("%s failed: %s (code %d)" % (what, _ERRORS.get(rc, "error"), rc))
+
+
+def dtype_code(t):
+    if t == torch.float32:
+        return OTG_F32
+    if t == torch.float64:
+        return OTG_F64
+    raise TypeError("pot_gb300 kernels take float32 or float64 tensors, got %s" % t)
+
+
+def ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def stream_handle(device=None):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)

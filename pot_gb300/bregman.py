@@ -1,0 +1,269 @@
+"""Drop-in replacements for ``ot.sinkhorn``, ``ot.sinkhorn2``,
+``ot.bregman.sinkhorn_knopp`` and ``ot.bregman.sinkhorn_log``.
+
+Signatures, defaults, return values, log-dict keys and warnings follow
+PythonOT/POT ``ot/bregman/_sinkhorn.py`` (``sinkhorn`` :21-234, ``sinkhorn2``
+:237-484, ``sinkhorn_knopp`` :487-687, ``sinkhorn_log`` :690-918).  The
+iteration loop runs on the GPU in one persistent kernel
+(``csrc/dense.cu``); the host only reads the result block once per solve.
+"""
+import ctypes
+import warnings
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._arrays import Boundary, is_empty
+
+NONCONV_MSG = ("Sinkhorn did not converge. You might want to "
+               "increase the number of iterations `numItermax` "
+               "or the regularization parameter `reg`.")
+
+
+def _hist_cap(max_iter):
+    return max(2, max_iter // 10 + 2)
+
+
+class DenseResult:
+    __slots__ = ("u", "v", "status", "niter", "errs", "workspace", "layout")
+
+
+def default_grid(n, m):
+    """CTAs for one dense solve: small problems use few CTAs so the grid
+    barriers stay cheap; large ones fill every SM (0 = all co-resident CTAs)."""
+    elems = n * m
+    if elems >= (1 << 24):
+        return 0
+    return max(4, elems // 16384)
+
+
+def solve_dense(M, a, b, reg, method, max_iter, stop_thr, warm_u=None, warm_v=None, grid=None,
+                timeout_ms=0, read_back=True):
+    """Run one dense solve on device tensors (contiguous rows, same dtype).
+
+    Returns a DenseResult whose ``u, v`` are scalings (knopp) or natural-log
+    potentials (log).  With ``read_back`` the status, last loop index and
+    error history are copied to the host (one synchronisation)."""
+    lib = _lib.load()
+    n, m = M.shape
+    if grid is None:
+        grid = default_grid(n, m)
+    dt = _lib.dtype_code(M.dtype)
+    cap = _hist_cap(max_iter)
+    wsb = lib.otg_dense_workspace_bytes(dt, n, m, cap, grid)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=M.device)
+    out_u = torch.empty(n, dtype=M.dtype, device=M.device)
+    out_v = torch.empty(m, dtype=M.dtype, device=M.device)
+    p = _lib.OtgDenseProblem(
+        dtype=dt, method=method, M=M.data_ptr(), n=n, m=m, ldm=M.stride(0),
+        a=a.data_ptr(), b=b.data_ptr(),
+        warm_u=warm_u.data_ptr() if warm_u is not None else None,
+        warm_v=warm_v.data_ptr() if warm_v is not None else None,
+        reg=float(reg), max_iter=int(max_iter), hist_cap=cap, stop_thr=float(stop_thr),
+        out_u=out_u.data_ptr(), out_v=out_v.data_ptr(), workspace_bytes=wsb, grid=grid,
+        timeout_ms=timeout_ms)
+    _lib.check(lib.otg_sinkhorn_dense(ctypes.byref(p), ctypes.c_void_p(ws.data_ptr()),
+                                      _lib.stream_handle(M.device)), "otg_sinkhorn_dense")
+    r = DenseResult()
+    r.u, r.v, r.workspace = out_u, out_v, ws
+    r.status, r.niter, r.errs = None, None, None
+    r.layout = (dt, n, m, cap, grid)
+    if read_back:
+        read_result(r)
+    return r
+
+
+def read_result(r):
+    lib = _lib.load()
+    dt, n, m, cap, grid = r.layout
+    off = lib.otg_dense_info_offset(dt, n, m, cap, grid)
+    ctrl = (off + 8 * cap + 255) // 256 * 256
+    blk = r.workspace[off:ctrl + 32].cpu().numpy()
+    hist = blk[:8 * cap].view(np.float64)
+    info = blk[ctrl - off:ctrl - off + 32].view(np.int32)
+    r.status, r.niter = int(info[0]), int(info[1])
+    nchk = int(info[2])
+    if int(info[3]) != 0:
+        r.status = _lib.STATUS_ABORTED
+    r.errs = np.sqrt(hist[:nchk])
+    if r.status == _lib.STATUS_ABORTED:
+        raise RuntimeError("pot_gb300: a device-side wait timed out; the solve was abandoned")
+    return r
+
+
+def _errs_as(bd, errs, like):
+    if bd.kind == "numpy":
+        return [np.float64(e) for e in errs]
+    t = torch.as_tensor(np.asarray(errs, dtype=np.float64), dtype=like.dtype)
+    if not bd.host_torch:
+        t = t.to(like.device)
+    return list(t.unbind()) if len(errs) else []
+
+
+def _print_errs(errs, check_before_print):
+    for k, e in enumerate(errs):
+        ii = 10 * k
+        if not check_before_print and k == len(errs) - 1:
+            pass
+        if ii % 200 == 0:
+            print("{:5s}|{:12s}".format("It.", "Err") + "\n" + "-" * 19)
+        print("{:5d}|{:8e}|".format(ii, e))
+
+
+def _prep(a, b, M):
+    bd = Boundary(M, a, b)
+    Md = bd.to_dev(M)
+    if Md.dim() != 2:
+        raise ValueError("M must be a 2-D cost matrix")
+    if Md.stride(1) != 1 or Md.stride(0) < Md.shape[1]:
+        Md = Md.contiguous()
+    n, m = Md.shape
+    ad = torch.full((n,), 1.0 / n, dtype=Md.dtype, device=Md.device) if is_empty(a) else bd.to_dev(a, Md.dtype)
+    bdv = torch.full((m,), 1.0 / m, dtype=Md.dtype, device=Md.device) if is_empty(b) else bd.to_dev(b, Md.dtype)
+    return bd, Md, ad.contiguous(), bdv.contiguous()
+
+
+def _warm(bd, warmstart, dtype):
+    if warmstart is None:
+        return None, None
+    return bd.to_dev(warmstart[0], dtype).contiguous(), bd.to_dev(warmstart[1], dtype).contiguous()
+
+
+def _run_single(bd, a, b, M, reg, method, numItermax, stopThr, verbose, warn, warmstart, want_plan):
+    wu, wv = _warm(bd, warmstart, M.dtype)
+    r = solve_dense(M, a, b, reg, method, numItermax, stopThr, wu, wv)
+    if r.status == _lib.STATUS_NUMERICAL:
+        warnings.warn("Warning: numerical errors at iteration %d" % r.niter)
+    if verbose:
+        errs = r.errs
+        if method == _lib.OTG_METHOD_KNOPP and r.status == _lib.STATUS_CONVERGED:
+            errs = errs[:-1]  # the reference prints after its break test
+        _print_errs(errs, method == _lib.OTG_METHOD_LOG)
+    if r.status == _lib.STATUS_MAXITER and warn:
+        warnings.warn(NONCONV_MSG)
+    P = None
+    lib = _lib.load()
+    if want_plan:
+        P = torch.empty_like(M)
+        _lib.check(lib.otg_dense_plan(_lib.dtype_code(M.dtype), method, ctypes.c_void_p(M.data_ptr()),
+                                      M.shape[0], M.shape[1], M.stride(0), _lib.ptr(r.u), _lib.ptr(r.v),
+                                      float(reg), _lib.ptr(P), P.stride(0), None,
+                                      _lib.stream_handle(M.device)), "otg_dense_plan")
+    return r, P
+
+
+def _loss(M, r, reg, method):
+    lib = _lib.load()
+    acc = torch.zeros(1, dtype=torch.float64, device=M.device)
+    _lib.check(lib.otg_dense_plan(_lib.dtype_code(M.dtype), method, ctypes.c_void_p(M.data_ptr()),
+                                  M.shape[0], M.shape[1], M.stride(0), _lib.ptr(r.u), _lib.ptr(r.v),
+                                  float(reg), None, 0, _lib.ptr(acc), _lib.stream_handle(M.device)),
+               "otg_dense_plan")
+    return acc[0].to(M.dtype)
+
+
+def sinkhorn_knopp(a, b, M, reg, numItermax=1000, stopThr=1e-9, verbose=False, log=False,
+                   warn=True, warmstart=None, **kwargs):
+    """Scaling-form Sinkhorn on the GPU; see ``ot.bregman.sinkhorn_knopp``."""
+    bd, Md, ad, bdv = _prep(a, b, M)
+    if bdv.dim() > 1:
+        return _knopp_multi(bd, ad, bdv, Md, reg, numItermax, stopThr, verbose, log, warn, warmstart)
+    r, P = _run_single(bd, ad, bdv, Md, reg, _lib.OTG_METHOD_KNOPP, numItermax, stopThr, verbose,
+                       warn, warmstart, True)
+    if log:
+        lg = {"err": _errs_as(bd, r.errs, Md), "niter": r.niter, "u": bd.out(r.u), "v": bd.out(r.v)}
+        return bd.out(P), lg
+    return bd.out(P)
+
+
+def sinkhorn_log(a, b, M, reg, numItermax=1000, stopThr=1e-9, verbose=False, log=False,
+                 warn=True, warmstart=None, **kwargs):
+    """Log-domain Sinkhorn on the GPU; see ``ot.bregman.sinkhorn_log``."""
+    bd, Md, ad, bdv = _prep(a, b, M)
+    if bdv.dim() > 1:
+        return _log_multi(bd, ad, bdv, Md, reg, numItermax, stopThr, verbose, log, warmstart)
+    r, P = _run_single(bd, ad, bdv, Md, reg, _lib.OTG_METHOD_LOG, numItermax, stopThr, verbose,
+                       warn, warmstart, True)
+    if log:
+        lg = {"err": _errs_as(bd, r.errs, Md), "niter": r.niter, "log_u": bd.out(r.u),
+              "log_v": bd.out(r.v), "u": bd.out(torch.exp(r.u)), "v": bd.out(torch.exp(r.v))}
+        return bd.out(P), lg
+    return bd.out(P)
+
+
+def _log_multi(bd, a, B, M, reg, numItermax, stopThr, verbose, log, warmstart):
+    """Several target histograms: one solve per column, as the reference's
+    recursion (``_sinkhorn.py:819-854``) does; returns the per-histogram
+    losses and a log holding only the potentials."""
+    H = B.shape[1]
+    ws = warmstart if warmstart is not None else [None] * H
+    losses, lus, lvs = [], [], []
+    for k in range(H):
+        r, _ = _run_single(bd, a, B[:, k].contiguous(), M, reg, _lib.OTG_METHOD_LOG, numItermax,
+                           stopThr, verbose, True, ws[k], False)
+        losses.append(_loss(M, r, reg, _lib.OTG_METHOD_LOG))
+        lus.append(r.u)
+        lvs.append(r.v)
+    res = torch.stack(losses)
+    if log:
+        lu, lv = torch.stack(lus, 1), torch.stack(lvs, 1)
+        return bd.out(res), {"log_u": bd.out(lu), "log_v": bd.out(lv), "u": bd.out(torch.exp(lu)),
+                             "v": bd.out(torch.exp(lv))}
+    return bd.out(res)
+
+
+def _knopp_multi(bd, a, B, M, reg, numItermax, stopThr, verbose, log, warn, warmstart):
+    raise NotImplementedError("pot_gb300: scaling-form Sinkhorn with several target histograms "
+                              "is not implemented yet; use method='sinkhorn_log'")
+
+
+def sinkhorn(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, verbose=False,
+             log=False, warn=True, warmstart=None, **kwargs):
+    """GPU ``ot.sinkhorn``: dispatch on ``method`` (``_sinkhorn.py:164-234``)."""
+    meth = method.lower()
+    if meth == "sinkhorn":
+        return sinkhorn_knopp(a, b, M, reg, numItermax=numItermax, stopThr=stopThr, verbose=verbose,
+                              log=log, warn=warn, warmstart=warmstart, **kwargs)
+    if meth == "sinkhorn_log":
+        return sinkhorn_log(a, b, M, reg, numItermax=numItermax, stopThr=stopThr, verbose=verbose,
+                            log=log, warn=warn, warmstart=warmstart, **kwargs)
+    if meth in ("greenkhorn", "sinkhorn_stabilized", "sinkhorn_epsilon_scaling"):
+        raise NotImplementedError("pot_gb300 implements method='sinkhorn' and 'sinkhorn_log'; "
+                                  "'%s' is not on the GPU path" % method)
+    raise ValueError("Unknown method '%s'." % method)
+
+
+def sinkhorn2(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, verbose=False,
+              log=False, warn=False, warmstart=None, **kwargs):
+    """GPU ``ot.sinkhorn2``: the loss ``<P, M>`` (fp64 accumulation) for 1-D
+    ``b``; the per-histogram losses for 2-D ``b`` (``_sinkhorn.py:435-484``)."""
+    meth = method.lower()
+    if meth not in ("sinkhorn", "sinkhorn_log"):
+        if meth == "sinkhorn_stabilized":
+            raise NotImplementedError("pot_gb300: method='sinkhorn_stabilized' is not on the GPU path")
+        raise ValueError("Unknown method '%s'." % method)
+    bd, Md, ad, bdv = _prep(a, b, M)
+    code = _lib.OTG_METHOD_KNOPP if meth == "sinkhorn" else _lib.OTG_METHOD_LOG
+    if bdv.dim() > 1:
+        fn = sinkhorn_knopp if meth == "sinkhorn" else sinkhorn_log
+        return fn(a, b, M, reg, numItermax=numItermax, stopThr=stopThr, verbose=verbose, log=log,
+                  warn=warn, warmstart=warmstart)
+    need_grad = isinstance(M, torch.Tensor) and (M.requires_grad or
+                                                 (isinstance(a, torch.Tensor) and a.requires_grad) or
+                                                 (isinstance(b, torch.Tensor) and b.requires_grad))
+    r, P = _run_single(bd, ad, bdv, Md, reg, code, numItermax, stopThr, verbose, warn, warmstart,
+                       need_grad)
+    loss = _loss(Md, r, reg, code)
+    if need_grad:
+        from ._autograd import envelope_loss
+        loss = envelope_loss(loss, P, r, code, float(reg), a, b, M)
+    out = bd.scalar(loss)
+    if log:
+        if code == _lib.OTG_METHOD_KNOPP:
+            lg = {"err": _errs_as(bd, r.errs, Md), "niter": r.niter, "u": bd.out(r.u), "v": bd.out(r.v)}
+        else:
+            lg = {"err": _errs_as(bd, r.errs, Md), "niter": r.niter, "log_u": bd.out(r.u),
+                  "log_v": bd.out(r.v), "u": bd.out(torch.exp(r.u)), "v": bd.out(torch.exp(r.v))}
+        return out, lg
+    return out

@@ -1,0 +1,142 @@
+// Shared device helpers for the entropic-OT kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+
+#define OTG_LOG2E 1.4426950408889634
+#define OTG_LN2 0.6931471805599453
+
+namespace otg {
+
+// ---------------------------------------------------------------------------
+// exp2 / log2 in the working precision.  fp32 uses the MUFU ex2 instruction
+// (PTX ex2.approx.ftz.f32, relative error about 2^-22); fp64 calls the CUDA
+// library exp2.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ double ex2(double x) { return exp2(x); }
+__device__ __forceinline__ float lg2(float x) { return log2f(x); }
+__device__ __forceinline__ double lg2(double x) { return log2(x); }
+
+template <typename T> struct Vec;
+template <> struct Vec<float> { using type = float4; static constexpr int N = 4; };
+template <> struct Vec<double> { using type = double2; static constexpr int N = 2; };
+
+__device__ __forceinline__ void unpack(const float4& q, float* o) { o[0] = q.x; o[1] = q.y; o[2] = q.z; o[3] = q.w; }
+__device__ __forceinline__ void unpack(const double2& q, double* o) { o[0] = q.x; o[1] = q.y; }
+
+// Streaming 128-bit load that does not allocate in L1 (the cost matrix is
+// read once per pass).
+__device__ __forceinline__ float4 ld_stream(const float4* p) {
+  float4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ double2 ld_stream(const double2* p) {
+  double2 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.f64 {%0,%1}, [%2];"
+               : "=d"(r.x), "=d"(r.y) : "l"(p));
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// (max, sum) pairs of a base-2 log-sum-exp: the value is  mx + log2(s).
+// An empty pair is (-inf, 0).  Merging is associative and commutative, so
+// partial pairs from any split of a row or column combine in any order.
+// ---------------------------------------------------------------------------
+// A NaN maximum is dropped by fmax but poisons the sum through ex2(NaN), so
+// NaN inputs still give a NaN result, as they do in the reference.
+template <typename T>
+__device__ __forceinline__ void lse_merge(T& mx, T& s, T mx2, T s2) {
+  T nm = fmax(mx, mx2);
+  if (nm == -INFINITY) return;  // both empty
+  s = s * ex2(mx - nm) + s2 * ex2(mx2 - nm);
+  mx = nm;
+}
+
+template <typename T>
+__device__ __forceinline__ T lse_value(T mx, T s) {
+  if (mx == -INFINITY) return -INFINITY;
+  return mx + lg2(s);
+}
+
+template <typename T>
+__device__ __forceinline__ void warp_lse(T& mx, T& s) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T m2 = __shfl_xor_sync(0xffffffffu, mx, o);
+    T s2 = __shfl_xor_sync(0xffffffffu, s, o);
+    lse_merge(mx, s, m2, s2);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+__device__ __forceinline__ int warp_or(int x) { return __any_sync(0xffffffffu, x) ? 1 : 0; }
+
+// ---------------------------------------------------------------------------
+// Bounded grid barrier for cooperative (co-resident) launches.
+// bar[0] counts arrivals, bar[1] is the generation.  A block that waits
+// longer than `timeout_ns` (globaltimer) sets *abort and leaves; callers check
+// *abort after every barrier and return, so no wait is unbounded.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_acquire_i(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* abort_flag,
+                                             uint64_t timeout_ns) {
+  __syncthreads();
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned gen = ld_acquire(bar + 1);
+    __threadfence();
+    unsigned arrived = atomicAdd(bar, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      uint64_t t0 = globaltimer();
+      unsigned spins = 0;
+      while (ld_acquire(bar + 1) == gen) {
+        if (++spins > 64) __nanosleep(64);
+        if ((spins & 255u) == 0) {
+          if (ld_acquire_i(abort_flag)) { ok = 0; break; }
+          if (globaltimer() - t0 > timeout_ns) { atomicExch(abort_flag, 1); ok = 0; break; }
+        }
+      }
+    }
+    __threadfence();
+    if (ld_acquire_i(abort_flag)) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+}  // namespace otg

@@ -1,0 +1,573 @@
+// Dense-cost Sinkhorn (scaling and log-domain forms) as ONE persistent
+// cooperative kernel per solve, plus the plan / loss kernel.
+//
+// Reference behaviour restated here: PythonOT/POT ot/bregman/_sinkhorn.py
+//   sinkhorn_knopp  :487-687  (v = b / K^T u ; u = 1 / (diag(1/a) K v), NaN/zero
+//                              revert :633-645, L2 column-marginal check every
+//                              10th iteration :646-658)
+//   sinkhorn_log    :690-918  (v = log b - LSE_i(Mr + u) ; u = log a - LSE_j(Mr + v),
+//                              same check :884-899)
+//
+// One iteration is one COLUMN pass and one ROW pass over M:
+//   column pass  : partial column reductions over row chunks      -> barrier
+//   column merge : combine partials, v update, and the marginal error of the
+//                  PREVIOUS iteration when it was a check iteration  -> barrier
+//   row pass     : row reductions with the new v, u update fused    -> barrier
+// The column marginal of exp(Mr + u + v) after iteration k equals
+// exp(v_j + LSE_i(Mr + u)_j), and LSE_i(Mr + u) is exactly what iteration
+// k+1's column pass computes, so the stopping test costs no extra pass over M:
+// the solve stops one column pass later with (u, v) of iteration k, which is
+// what the reference returns.
+//
+// Log-domain arithmetic runs in base 2: x = M * c with c = -log2(e)/reg,
+// potentials are kept as log2 values, and exp is the MUFU ex2 instruction.
+#include <algorithm>
+#include "common.cuh"
+#include "../../include/pot_gb300.h"
+
+namespace otg {
+
+template <typename T> struct Pair { T mx, s; };
+
+template <typename T>
+__device__ __forceinline__ Pair<T> ldcg_pair(const Pair<T>* p) {
+  const T* q = reinterpret_cast<const T*>(p);
+  return Pair<T>{__ldcg(q), __ldcg(q + 1)};
+}
+
+template <typename T>
+struct DenseArgs {
+  const T* M; int64_t n, m, ldm;
+  const T* a; const T* b;
+  const T* warm_u; const T* warm_v;     // natural-log warm start or null
+  T c;                                  // -log2(e) / reg
+  int max_iter;
+  double stop_thr;
+  T *u0, *u1, *v0, *v1, *loga2, *logb2;
+  Pair<T>* pcol;                        // [Sr][m]
+  Pair<T>* prow;                        // [Sc][n]
+  int Sr, Sc;
+  int64_t rchunk, cchunk;
+  T *out_u, *out_v;                     // natural units
+  double* hist; int hist_cap;
+  int* info;                            // status, niter, nchecks, abort, numflag
+  unsigned* bar;
+  uint64_t timeout_ns;
+};
+
+constexpr int RW = 4;     // rows per warp in the row pass
+constexpr int GCOL = 4;   // rows folded per max update in the column pass
+
+// ---------------------------------------------------------------------------
+// Column pass: one warp-unit = (row chunk r, slab of 32*VW columns).
+// ---------------------------------------------------------------------------
+template <typename T, int METHOD, bool VEC>
+__device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, long gwarp, long nwarps, int lane) {
+  constexpr int VW = Vec<T>::N;
+  using V = typename Vec<T>::type;
+  const int64_t n = A.n, m = A.m;
+  const int64_t slab_w = 32 * VW;
+  const int64_t nslabs = (m + slab_w - 1) / slab_w;
+  const int64_t units = nslabs * A.Sr;
+  for (int64_t unit = gwarp; unit < units; unit += nwarps) {
+    const int64_t slab = unit % nslabs, r = unit / nslabs;
+    const int64_t i0 = r * A.rchunk, i1 = min(n, i0 + A.rchunk);
+    const int64_t j0 = slab * slab_w + lane * VW;
+    T mx[VW], s[VW];
+#pragma unroll
+    for (int k = 0; k < VW; ++k) { mx[k] = -INFINITY; s[k] = 0; }
+    if (j0 < m) {
+      for (int64_t i = i0; i < i1; i += GCOL) {
+        T x[GCOL][VW];
+        T ur[GCOL];
+#pragma unroll
+        for (int g = 0; g < GCOL; ++g) {
+          const int64_t row = i + g;
+          if (row < i1) {
+            const T* Mrow = A.M + row * A.ldm + j0;
+            if (VEC) {
+              V q = ld_stream(reinterpret_cast<const V*>(Mrow));
+              unpack(q, x[g]);
+            } else {
+#pragma unroll
+              for (int k = 0; k < VW; ++k) x[g][k] = (j0 + k < m) ? Mrow[k] : T(0);
+            }
+            ur[g] = __ldcg(u + row);
+          } else {
+#pragma unroll
+            for (int k = 0; k < VW; ++k) x[g][k] = T(0);
+            ur[g] = METHOD == OTG_METHOD_LOG ? T(-INFINITY) : T(0);
+          }
+        }
+        if (METHOD == OTG_METHOD_LOG) {
+#pragma unroll
+          for (int k = 0; k < VW; ++k) {
+            T t[GCOL];
+            T gm = -INFINITY;
+#pragma unroll
+            for (int g = 0; g < GCOL; ++g) { t[g] = fma(x[g][k], A.c, ur[g]); gm = fmax(gm, t[g]); }
+            T nm = fmax(mx[k], gm);
+            if (nm != -INFINITY) {
+              T acc = s[k] * ex2(mx[k] - nm);
+#pragma unroll
+              for (int g = 0; g < GCOL; ++g) acc += ex2(t[g] - nm);
+              s[k] = acc;
+              mx[k] = nm;
+            }
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < VW; ++k) {
+#pragma unroll
+            for (int g = 0; g < GCOL; ++g) s[k] = fma(ex2(x[g][k] * A.c), ur[g], s[k]);
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < VW; ++k)
+        if (j0 + k < m) A.pcol[r * m + j0 + k] = Pair<T>{mx[k], s[k]};
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Row pass: one warp-unit = (group of RW rows, column chunk cc).  With one
+// column chunk the potential update is applied directly; otherwise the
+// partial pairs are merged after a barrier by row_merge.
+// ---------------------------------------------------------------------------
+template <typename T, int METHOD>
+__device__ __forceinline__ T row_finalize(const DenseArgs<T>& A, int64_t i, T mx, T s, int* numflag) {
+  if (METHOD == OTG_METHOD_LOG) {
+    return __ldcg(A.loga2 + i) - lse_value(mx, s);
+  } else {
+    T unew = T(1) / ((T(1) / A.a[i]) * s);
+    if (!isfinite(unew)) atomicExch(numflag, 1);
+    return unew;
+  }
+}
+
+template <typename T, int METHOD, bool VEC>
+__device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __restrict__ unew,
+                         long gwarp, long nwarps, int lane) {
+  constexpr int VW = Vec<T>::N;
+  using V = typename Vec<T>::type;
+  const int64_t n = A.n, m = A.m;
+  const int64_t ngroups = (n + RW - 1) / RW;
+  const int64_t units = ngroups * A.Sc;
+  for (int64_t unit = gwarp; unit < units; unit += nwarps) {
+    const int64_t grp = unit % ngroups, cc = unit / ngroups;
+    const int64_t r0 = grp * RW;
+    const int64_t c0 = cc * A.cchunk, c1 = min(m, c0 + A.cchunk);
+    T mx[RW], s[RW];
+#pragma unroll
+    for (int r = 0; r < RW; ++r) { mx[r] = -INFINITY; s[r] = 0; }
+    for (int64_t j = c0 + lane * VW; j < c1; j += 32 * VW) {
+      T vv[VW];
+      if (VEC) {
+        unpack(__ldcg(reinterpret_cast<const V*>(v + j)), vv);
+      } else {
+#pragma unroll
+        for (int k = 0; k < VW; ++k) vv[k] = (j + k < c1) ? __ldcg(v + j + k) : (METHOD == OTG_METHOD_LOG ? T(-INFINITY) : T(0));
+      }
+      T x[RW][VW];
+#pragma unroll
+      for (int r = 0; r < RW; ++r) {
+        const int64_t row = r0 + r;
+        const T* Mrow = A.M + (row < n ? row : n - 1) * A.ldm + j;
+        if (VEC) {
+          V q = ld_stream(reinterpret_cast<const V*>(Mrow));
+          unpack(q, x[r]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < VW; ++k) x[r][k] = (j + k < c1) ? Mrow[k] : T(0);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < RW; ++r) {
+        if (METHOD == OTG_METHOD_LOG) {
+          T t[VW];
+          T gm = -INFINITY;
+#pragma unroll
+          for (int k = 0; k < VW; ++k) { t[k] = fma(x[r][k], A.c, vv[k]); gm = fmax(gm, t[k]); }
+          T nm = fmax(mx[r], gm);
+          if (nm != -INFINITY) {
+            T acc = s[r] * ex2(mx[r] - nm);
+#pragma unroll
+            for (int k = 0; k < VW; ++k) acc += ex2(t[k] - nm);
+            s[r] = acc;
+            mx[r] = nm;
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < VW; ++k) s[r] = fma(ex2(x[r][k] * A.c), vv[k], s[r]);
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RW; ++r) {
+      if (METHOD == OTG_METHOD_LOG) warp_lse(mx[r], s[r]);
+      else s[r] = warp_sum(s[r]);
+    }
+    if (lane < RW) {
+      // lane r publishes row r (registers indexed with a compile-time loop)
+#pragma unroll
+      for (int r = 0; r < RW; ++r) {
+        if (lane == r && r0 + r < n) {
+          const int64_t row = r0 + r;
+          if (A.Sc == 1) unew[row] = row_finalize<T, METHOD>(A, row, mx[r], s[r], A.info + 4);
+          else A.prow[cc * n + row] = Pair<T>{mx[r], s[r]};
+        }
+      }
+    }
+  }
+}
+
+template <typename T, int METHOD>
+__device__ void row_merge(const DenseArgs<T>& A, T* __restrict__ unew, long gtid, long nthreads) {
+  for (int64_t i = gtid; i < A.n; i += nthreads) {
+    T mx = -INFINITY, s = 0;
+    for (int cc = 0; cc < A.Sc; ++cc) {
+      Pair<T> p = ldcg_pair(A.prow + (int64_t)cc * A.n + i);
+      if (METHOD == OTG_METHOD_LOG) lse_merge(mx, s, p.mx, p.s);
+      else s += p.s;
+    }
+    unew[i] = row_finalize<T, METHOD>(A, i, mx, s, A.info + 4);
+  }
+}
+
+// Column merge: combine the Sr partials of column j, update v, and add the
+// squared column-marginal violation of (u_cur, v_cur) when `check`.
+template <typename T, int METHOD>
+__device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* __restrict__ vnxt,
+                          bool check, bool update, double* err_slot, long gtid, long nthreads) {
+  double e2 = 0.0;
+  for (int64_t j = gtid; j < A.m; j += nthreads) {
+    T mx = -INFINITY, s = 0;
+    for (int r = 0; r < A.Sr; ++r) {
+      Pair<T> p = ldcg_pair(A.pcol + (int64_t)r * A.m + j);
+      if (METHOD == OTG_METHOD_LOG) lse_merge(mx, s, p.mx, p.s);
+      else s += p.s;
+    }
+    const T bj = A.b[j];
+    if (METHOD == OTG_METHOD_LOG) {
+      const T L = lse_value(mx, s);
+      if (check) {
+        double cs = (double)ex2(__ldcg(vcur + j) + L);
+        e2 += (cs - (double)bj) * (cs - (double)bj);
+      }
+      if (update) vnxt[j] = __ldcg(A.logb2 + j) - L;
+    } else {
+      if (check) {
+        double cs = (double)(__ldcg(vcur + j) * s);
+        e2 += (cs - (double)bj) * (cs - (double)bj);
+      }
+      if (update) {
+        T vn = bj / s;
+        if (s == T(0) || !isfinite(vn)) atomicExch(A.info + 4, 1);
+        vnxt[j] = vn;
+      }
+    }
+  }
+  if (check) {
+    // block reduction, then one fp64 atomic per CTA
+    __shared__ double red[32];
+    e2 = warp_sum(e2);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+      atomicAdd(err_slot, t);
+    }
+  }
+}
+
+template <typename T> struct BlocksPerSM { static constexpr int value = sizeof(T) == 4 ? 4 : 2; };
+
+template <typename T, int METHOD, bool VEC>
+__global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_kernel(DenseArgs<T> A) {
+  const int lane = threadIdx.x & 31;
+  const long nwb = blockDim.x >> 5;
+  const long gwarp = blockIdx.x * nwb + (threadIdx.x >> 5);
+  const long nwarps = gridDim.x * nwb;
+  const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nthreads = (long)gridDim.x * blockDim.x;
+  int* abort_flag = A.info + 3;
+  const T L2E = T(OTG_LOG2E);
+
+  // Phase 0: initial state.
+  for (int64_t i = gtid; i < A.n; i += nthreads) {
+    if (METHOD == OTG_METHOD_LOG) {
+      A.u0[i] = A.warm_u ? A.warm_u[i] * L2E : T(0);
+      A.loga2[i] = lg2(A.a[i]);
+    } else {
+      A.u0[i] = A.warm_u ? exp(A.warm_u[i]) : T(1) / T(A.n);
+    }
+  }
+  for (int64_t j = gtid; j < A.m; j += nthreads) {
+    if (METHOD == OTG_METHOD_LOG) {
+      A.v0[j] = A.warm_v ? A.warm_v[j] * L2E : T(0);
+      A.logb2[j] = lg2(A.b[j]);
+    } else {
+      A.v0[j] = A.warm_v ? exp(A.warm_v[j]) : T(1) / T(A.m);
+    }
+  }
+  if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+
+  T *ucur = A.u0, *unxt = A.u1, *vcur = A.v0, *vnxt = A.v1;
+  bool prev_check = false;
+  int nchk = 0;
+  int status = OTG_STATUS_MAXITER, niter = A.max_iter - 1;
+  for (int ii = 0;; ++ii) {
+    col_pass<T, METHOD, VEC>(A, ucur, gwarp, nwarps, lane);
+    if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+    const bool update = ii < A.max_iter;
+    double* slot = A.hist + (nchk < A.hist_cap ? nchk : A.hist_cap - 1);
+    col_merge<T, METHOD>(A, vcur, vnxt, prev_check, update, slot, gtid, nthreads);
+    if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+    if (prev_check) {
+      double e2 = *(volatile double*)slot;
+      ++nchk;
+      if (sqrt(e2) < A.stop_thr) { status = OTG_STATUS_CONVERGED; niter = ii - 1; break; }
+    }
+    if (!update) { status = OTG_STATUS_MAXITER; niter = A.max_iter - 1; break; }
+    if (METHOD != OTG_METHOD_LOG && ld_acquire_i(A.info + 4)) {
+      // zero column sum or non-finite v: revert to the previous pair
+      status = OTG_STATUS_NUMERICAL; niter = ii; break;
+    }
+    row_pass<T, METHOD, VEC>(A, vnxt, unxt, gwarp, nwarps, lane);
+    if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+    if (A.Sc > 1) {
+      row_merge<T, METHOD>(A, unxt, gtid, nthreads);
+      if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+    }
+    if (METHOD != OTG_METHOD_LOG && ld_acquire_i(A.info + 4)) {
+      status = OTG_STATUS_NUMERICAL; niter = ii; break;
+    }
+    T* t;
+    t = ucur; ucur = unxt; unxt = t;
+    t = vcur; vcur = vnxt; vnxt = t;
+    prev_check = (ii % 10 == 0);
+  }
+
+  // Final state in natural units.
+  const T LN2 = T(OTG_LN2);
+  for (int64_t i = gtid; i < A.n; i += nthreads)
+    A.out_u[i] = METHOD == OTG_METHOD_LOG ? __ldcg(ucur + i) * LN2 : __ldcg(ucur + i);
+  for (int64_t j = gtid; j < A.m; j += nthreads)
+    A.out_v[j] = METHOD == OTG_METHOD_LOG ? __ldcg(vcur + j) * LN2 : __ldcg(vcur + j);
+  if (gtid == 0) {
+    A.info[0] = status;
+    A.info[1] = niter;
+    A.info[2] = nchk;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plan and loss: P_ij = exp(-M_ij/reg + u_i + v_j) (log form, natural-log
+// potentials) or u_i exp(-M_ij/reg) v_j (scaling form); loss = sum M * P in
+// fp64.  Either output may be null.
+// ---------------------------------------------------------------------------
+template <typename T, int METHOD>
+__global__ void __launch_bounds__(256) dense_plan_kernel(const T* __restrict__ M, int64_t n, int64_t m, int64_t ldm,
+                                                         const T* __restrict__ u, const T* __restrict__ v, T c,
+                                                         T* __restrict__ P, int64_t ldp, double* loss) {
+  const T L2E = T(OTG_LOG2E);
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const T ui = u[i];
+    const T* Mrow = M + i * ldm;
+    for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
+      const T x = Mrow[j];
+      T p;
+      if (METHOD == OTG_METHOD_LOG) p = ex2(fma(x, c, (ui + v[j]) * L2E));
+      else p = ui * ex2(x * c) * v[j];
+      if (P) P[i * ldp + j] = p;
+      if (loss) acc += (double)x * (double)p;
+    }
+  }
+  if (loss) {
+    acc = warp_sum(acc);
+    __shared__ double red[32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) red[w] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+      atomicAdd(loss, t);
+    }
+  }
+}
+
+}  // namespace otg
+
+using namespace otg;
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Layout {
+  int grid, Sr, Sc;
+  int64_t rchunk, cchunk;
+  size_t off_state, off_pcol, off_prow, off_hist, off_ctrl, total;
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Default grid: every SM holds BLOCKS_PER_SM<T> CTAs of 256 threads (the
+// kernels are compiled with matching __launch_bounds__), so the layout does
+// not depend on which template variant runs.
+template <typename T>
+int default_grid() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms * BlocksPerSM<T>::value;
+}
+
+template <typename T>
+int resolve_grid(int requested) {
+  const int g = default_grid<T>();
+  return (requested > 0 && requested < g) ? requested : g;
+}
+
+template <typename T>
+Layout make_layout(int64_t n, int64_t m, int hist_cap, int grid) {
+  constexpr int VW = Vec<T>::N;
+  Layout L{};
+  L.grid = grid;
+  const int64_t W = (int64_t)grid * 8;
+  const int64_t nslabs = (m + 32 * VW - 1) / (32 * VW);
+  int64_t Sr = (2 * W + nslabs - 1) / nslabs;
+  Sr = std::max<int64_t>(1, std::min<int64_t>(Sr, (n + 15) / 16));
+  L.rchunk = (n + Sr - 1) / Sr;
+  L.Sr = (int)((n + L.rchunk - 1) / L.rchunk);
+  const int64_t ngroups = (n + RW - 1) / RW;
+  int64_t Sc = (2 * W + ngroups - 1) / ngroups;
+  Sc = std::max<int64_t>(1, std::min<int64_t>(Sc, (m + 32 * VW * 4 - 1) / (32 * VW * 4)));
+  int64_t cch = (m + Sc - 1) / Sc;
+  cch = (cch + 32 * VW - 1) / (32 * VW) * (32 * VW);
+  L.cchunk = cch;
+  L.Sc = (int)((m + cch - 1) / cch);
+  size_t off = 0;
+  L.off_state = off; off = align_up(off + sizeof(T) * (3 * ((size_t)n + 4) + 3 * ((size_t)m + 4)), 256);
+  L.off_pcol = off; off = align_up(off + sizeof(Pair<T>) * (size_t)L.Sr * m, 256);
+  L.off_prow = off; off = align_up(off + sizeof(Pair<T>) * (size_t)(L.Sc > 1 ? L.Sc : 0) * n, 256);
+  L.off_hist = off; off = align_up(off + sizeof(double) * (size_t)hist_cap, 256);
+  L.off_ctrl = off; off = align_up(off + 64, 256);
+  L.total = off;
+  return L;
+}
+
+template <typename T, int METHOD, bool VEC>
+int launch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
+  const int grid = resolve_grid<T>(p->grid);
+  {
+    int per = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dense_sinkhorn_kernel<T, METHOD, VEC>, 256, 0);
+    if ((int64_t)per * sms < grid) return OTG_ERR_UNSUPPORTED;  // co-residency not possible
+  }
+  Layout L = make_layout<T>(p->n, p->m, p->hist_cap, grid);
+  if (p->workspace_bytes < L.total) return OTG_ERR_WORKSPACE;
+  char* base = static_cast<char*>(ws);
+  DenseArgs<T> A{};
+  A.M = static_cast<const T*>(p->M); A.n = p->n; A.m = p->m; A.ldm = p->ldm;
+  A.a = static_cast<const T*>(p->a); A.b = static_cast<const T*>(p->b);
+  A.warm_u = static_cast<const T*>(p->warm_u); A.warm_v = static_cast<const T*>(p->warm_v);
+  A.c = (T)(-OTG_LOG2E / p->reg);
+  A.max_iter = p->max_iter; A.stop_thr = p->stop_thr;
+  T* st_ = reinterpret_cast<T*>(base + L.off_state);
+  const int64_t n = p->n, m = p->m;
+  // vectors are 16-byte aligned inside the state block
+  auto al = [](int64_t k) { return (k + 3) / 4 * 4; };
+  int64_t o = 0;
+  A.u0 = st_ + o; o += al(n); A.u1 = st_ + o; o += al(n); A.loga2 = st_ + o; o += al(n);
+  A.v0 = st_ + o; o += al(m); A.v1 = st_ + o; o += al(m); A.logb2 = st_ + o; o += al(m);
+  A.pcol = reinterpret_cast<Pair<T>*>(base + L.off_pcol);
+  A.prow = reinterpret_cast<Pair<T>*>(base + L.off_prow);
+  A.Sr = L.Sr; A.Sc = L.Sc; A.rchunk = L.rchunk; A.cchunk = L.cchunk;
+  A.out_u = static_cast<T*>(p->out_u); A.out_v = static_cast<T*>(p->out_v);
+  A.hist = reinterpret_cast<double*>(base + L.off_hist); A.hist_cap = p->hist_cap;
+  A.info = reinterpret_cast<int*>(base + L.off_ctrl);
+  A.bar = reinterpret_cast<unsigned*>(base + L.off_ctrl + 32);
+  A.timeout_ns = p->timeout_ms > 0 ? (uint64_t)p->timeout_ms * 1000000ull : 4000000000ull;
+  cudaError_t e = cudaMemsetAsync(base + L.off_hist, 0, L.total - L.off_hist, st);
+  if (e != cudaSuccess) return OTG_ERR_CUDA;
+  void* args[] = {&A};
+  e = cudaLaunchCooperativeKernel((const void*)dense_sinkhorn_kernel<T, METHOD, VEC>, dim3(grid), dim3(256), args, 0, st);
+  if (e != cudaSuccess) return OTG_ERR_CUDA;
+  return OTG_OK;
+}
+
+template <typename T>
+int dispatch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
+  constexpr int VW = Vec<T>::N;
+  const bool vec = (p->m % VW == 0) && (p->ldm % VW == 0) && ((uintptr_t)p->M % 16 == 0);
+  if (p->method == OTG_METHOD_LOG)
+    return vec ? launch_dense<T, OTG_METHOD_LOG, true>(p, ws, st) : launch_dense<T, OTG_METHOD_LOG, false>(p, ws, st);
+  return vec ? launch_dense<T, OTG_METHOD_KNOPP, true>(p, ws, st) : launch_dense<T, OTG_METHOD_KNOPP, false>(p, ws, st);
+}
+
+int check_problem(const OtgDenseProblem* p) {
+  if (!p || !p->M || !p->a || !p->b || !p->out_u || !p->out_v) return OTG_ERR_ARG;
+  if (p->n < 1 || p->m < 1 || p->ldm < p->m || p->hist_cap < 1) return OTG_ERR_ARG;
+  if (p->dtype != OTG_F32 && p->dtype != OTG_F64) return OTG_ERR_DTYPE;
+  if (p->method != OTG_METHOD_LOG && p->method != OTG_METHOD_KNOPP) return OTG_ERR_ARG;
+  if (p->max_iter < 0) return OTG_ERR_ARG;
+  return OTG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t otg_dense_workspace_bytes(int dtype, int64_t n, int64_t m, int hist_cap, int grid) {
+  if (dtype == OTG_F64) return make_layout<double>(n, m, hist_cap, resolve_grid<double>(grid)).total;
+  return make_layout<float>(n, m, hist_cap, resolve_grid<float>(grid)).total;
+}
+
+size_t otg_dense_info_offset(int dtype, int64_t n, int64_t m, int hist_cap, int grid) {
+  if (dtype == OTG_F64) return make_layout<double>(n, m, hist_cap, resolve_grid<double>(grid)).off_hist;
+  return make_layout<float>(n, m, hist_cap, resolve_grid<float>(grid)).off_hist;
+}
+
+int otg_sinkhorn_dense(const OtgDenseProblem* p, void* workspace, cudaStream_t stream) {
+  int rc = check_problem(p);
+  if (rc != OTG_OK) return rc;
+  if (!workspace) return OTG_ERR_WORKSPACE;
+  if (p->dtype == OTG_F64) return dispatch_dense<double>(p, workspace, stream);
+  return dispatch_dense<float>(p, workspace, stream);
+}
+
+int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, int64_t ldm,
+                   const void* u, const void* v, double reg, void* P, int64_t ldp, double* loss,
+                   cudaStream_t stream) {
+  if (!M || !u || !v || n < 1 || m < 1 || ldm < m || (P && ldp < m)) return OTG_ERR_ARG;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t blocks = std::min<int64_t>(n, (int64_t)sms * 8);
+  if (loss) cudaMemsetAsync(loss, 0, sizeof(double), stream);
+  const double c = -OTG_LOG2E / reg;
+  if (dtype == OTG_F64) {
+    if (method == OTG_METHOD_LOG)
+      dense_plan_kernel<double, OTG_METHOD_LOG><<<blocks, 256, 0, stream>>>((const double*)M, n, m, ldm, (const double*)u, (const double*)v, c, (double*)P, ldp, loss);
+    else
+      dense_plan_kernel<double, OTG_METHOD_KNOPP><<<blocks, 256, 0, stream>>>((const double*)M, n, m, ldm, (const double*)u, (const double*)v, c, (double*)P, ldp, loss);
+  } else if (dtype == OTG_F32) {
+    if (method == OTG_METHOD_LOG)
+      dense_plan_kernel<float, OTG_METHOD_LOG><<<blocks, 256, 0, stream>>>((const float*)M, n, m, ldm, (const float*)u, (const float*)v, (float)c, (float*)P, ldp, loss);
+    else
+      dense_plan_kernel<float, OTG_METHOD_KNOPP><<<blocks, 256, 0, stream>>>((const float*)M, n, m, ldm, (const float*)u, (const float*)v, (float)c, (float*)P, ldp, loss);
+  } else {
+    return OTG_ERR_DTYPE;
+  }
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,160 @@
+"""Parity of the dense GPU Sinkhorn (both forms) with the oracle and with the
+reference's golden vectors.
+
+Tolerances:
+  float64 inputs  -> potentials rtol 1e-8, plan relative L1 1e-9, identical
+                     niter and error history (rtol 1e-6) as the reference.
+  float32 inputs  -> plan relative L1 <= 1e-5 against the float64 oracle and
+                     float64 marginal violation of the returned plan <= 2x
+                     stopThr (the GPU stops on its own fp32 error estimate).
+"""
+import warnings
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import pot_gb300 as pg
+from conftest import golden, golden_names
+
+pytestmark = pytest.mark.gpu
+
+DENSE = golden_names("dense_")
+
+
+def _M(g):
+    if "M" in g:
+        return g["M"]
+    M = oracle.sqeuclidean(g["x"], g["y"])
+    return M / M.max()
+
+
+def rel_l1(P, Q):
+    return float(np.abs(P - Q).sum() / max(np.abs(Q).sum(), 1e-300))
+
+
+def test_doctest_values(cuda):
+    a = [0.5, 0.5]
+    M = [[0.0, 1.0], [1.0, 0.0]]
+    P = pg.sinkhorn(a, a, M, 1)
+    np.testing.assert_allclose(P, [[0.36552929, 0.13447071], [0.13447071, 0.36552929]], atol=1e-8)
+    loss = pg.sinkhorn2(a, a, M, 1)
+    assert abs(float(loss) - 0.26894142136999516) < 1e-14
+
+
+@pytest.mark.parametrize("name", DENSE)
+@pytest.mark.parametrize("tag", ["knopp", "log"])
+def test_dense_f64_golden(cuda, name, tag):
+    g = golden(name)
+    M = _M(g)
+    method = "sinkhorn" if tag == "knopp" else "sinkhorn_log"
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        P, lg = pg.sinkhorn(g["a"], g["b"], M, float(g["reg"]), method=method,
+                            numItermax=int(g["numItermax"]), stopThr=float(g["stopThr"]), log=True)
+    assert lg["niter"] == int(g[tag + "_niter"])
+    np.testing.assert_allclose(np.array(lg["err"], dtype=float), g[tag + "_err"], rtol=1e-6, atol=1e-14)
+    np.testing.assert_allclose(lg["u"], g[tag + "_u"], rtol=1e-8)
+    np.testing.assert_allclose(lg["v"], g[tag + "_v"], rtol=1e-8)
+    Pref, _ = oracle.sinkhorn(g["a"], g["b"], M, float(g["reg"]), method=method,
+                              numItermax=int(g["numItermax"]), stopThr=float(g["stopThr"]))
+    assert rel_l1(P, Pref) < 1e-9
+    loss = pg.sinkhorn2(g["a"], g["b"], M, float(g["reg"]), method=method,
+                        numItermax=int(g["numItermax"]), stopThr=float(g["stopThr"]))
+    assert abs(float(loss) - float(g[tag + "_loss"])) <= 1e-9 * abs(float(g[tag + "_loss"])) + 1e-15
+    nonconv = any("did not converge" in str(x.message) for x in w)
+    assert nonconv == bool(g[tag + "_warn_nonconv"])
+
+
+@pytest.mark.parametrize("name", ["dense_1024_gauss2d", "dense_127x129_reg0.05", "dense_5x300_reg0.5",
+                                  "dense_31x33_reg0.5"])
+@pytest.mark.parametrize("method", ["sinkhorn", "sinkhorn_log"])
+def test_dense_f32_vs_oracle(cuda, name, method):
+    g = golden(name)
+    M = _M(g)
+    stop = 1e-6
+    Pref, _ = oracle.sinkhorn(g["a"], g["b"], M, float(g["reg"]), method=method, numItermax=5000,
+                              stopThr=1e-12)
+    Mt = torch.tensor(M, dtype=torch.float32, device=cuda)
+    at = torch.tensor(g["a"], dtype=torch.float32, device=cuda)
+    bt = torch.tensor(g["b"], dtype=torch.float32, device=cuda)
+    P = pg.sinkhorn(at, bt, Mt, float(g["reg"]), method=method, numItermax=5000, stopThr=stop)
+    assert P.dtype == torch.float32 and P.device.type == "cuda"
+    P = P.double().cpu().numpy()
+    assert rel_l1(P, Pref) <= 1e-5
+    viol = np.linalg.norm(P.sum(0) - g["b"])
+    assert viol <= 2 * stop
+
+
+def test_failure_maxiter_warns(cuda):
+    g = golden("fail_maxiter1")
+    for method in ("sinkhorn", "sinkhorn_log"):
+        with pytest.warns(UserWarning, match="did not converge"):
+            pg.sinkhorn(g["a"], g["b"], g["M"], 1.0, method=method, stopThr=0, numItermax=1)
+        with warnings.catch_warnings():
+            warnings.simplefilter("error")
+            pg.sinkhorn2(g["a"], g["b"], g["M"], 1.0, method=method, stopThr=0, numItermax=1, warn=False)
+
+
+def test_reg0_numerical_error_reverts(cuda):
+    g = golden("fail_reg0_knopp")
+    with pytest.warns(UserWarning, match="numerical errors"):
+        _, lg = pg.sinkhorn(g["a"], g["b"], g["M"], 0.0, method="sinkhorn", warn=False, log=True)
+    assert lg["niter"] == int(g["niter"])
+    np.testing.assert_allclose(lg["u"], g["u"])
+    np.testing.assert_allclose(lg["v"], g["v"])
+
+
+def test_empty_weights_mean_uniform(cuda):
+    rng = np.random.default_rng(1)
+    M = rng.random((20, 30))
+    P1 = pg.sinkhorn([], [], M, 0.5, method="sinkhorn_log")
+    P2 = pg.sinkhorn(np.full(20, 1 / 20), np.full(30, 1 / 30), M, 0.5, method="sinkhorn_log")
+    np.testing.assert_allclose(P1, P2, rtol=1e-12)
+
+
+def test_warmstart_matches_oracle(cuda):
+    g = golden("dense_100x100_reg0.05")
+    rng = np.random.default_rng(2)
+    wu = rng.standard_normal(100) * 0.1
+    wv = rng.standard_normal(100) * 0.1
+    for method in ("sinkhorn", "sinkhorn_log"):
+        Pref, lref = oracle.sinkhorn(g["a"], g["b"], g["M"], 0.05, method=method, warmstart=(wu, wv))
+        P, lg = pg.sinkhorn(g["a"], g["b"], g["M"], 0.05, method=method, warmstart=(wu, wv), log=True)
+        assert lg["niter"] == lref["niter"]
+        assert rel_l1(P, Pref) < 1e-9
+
+
+def test_torch_cuda_in_torch_cuda_out(cuda):
+    M = torch.rand(33, 17, dtype=torch.float64, device=cuda)
+    a = torch.full((33,), 1 / 33, dtype=torch.float64, device=cuda)
+    b = torch.full((17,), 1 / 17, dtype=torch.float64, device=cuda)
+    for method in ("sinkhorn", "sinkhorn_log"):
+        P, lg = pg.sinkhorn(a, b, M, 0.2, method=method, log=True)
+        assert P.device == M.device and P.dtype == M.dtype
+        assert isinstance(lg["err"][0], torch.Tensor)
+        loss = pg.sinkhorn2(a, b, M, 0.2, method=method)
+        assert loss.dim() == 0 and loss.device == M.device
+        Pref, _ = oracle.sinkhorn(a.cpu().numpy(), b.cpu().numpy(), M.cpu().numpy(), 0.2, method=method)
+        assert rel_l1(P.cpu().numpy(), Pref) < 1e-9
+
+
+@pytest.mark.parametrize("method", ["sinkhorn", "sinkhorn_log"])
+def test_sinkhorn2_gradients_shapes(cuda, method):
+    n = 20
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((n, 2))
+    M = torch.tensor(oracle.sqeuclidean(x, x), device=cuda, requires_grad=True)
+    a = torch.full((n,), 1 / n, dtype=torch.float64, device=cuda, requires_grad=True)
+    b = torch.full((n,), 1 / n, dtype=torch.float64, device=cuda, requires_grad=True)
+    loss = pg.sinkhorn2(a, b, M, 1.0, method=method)
+    loss.backward()
+    assert M.grad.shape == M.shape and a.grad.shape == a.shape and b.grad.shape == b.shape
+
+
+def test_log_multi_histogram(cuda):
+    g = golden("multib_31x3")
+    loss, lg = pg.sinkhorn2(g["a"], g["b"], g["M"], 1.0, method="sinkhorn_log", log=True, stopThr=1e-10)
+    np.testing.assert_allclose(loss, g["log_loss"], rtol=1e-9)
+    np.testing.assert_allclose(lg["u"], g["log_u"], rtol=1e-7)
