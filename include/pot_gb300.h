@@ -37,6 +37,7 @@ extern "C" {
 #define OTG_ERR_WORKSPACE -3
 #define OTG_ERR_CUDA -4
 #define OTG_ERR_UNSUPPORTED -5
+#define OTG_ERR_NOALLOC_TOO_LARGE -6 /* needs more scratch than OTG_NOALLOC_SCRATCH_BYTES */
 
 /* solve status written to info[0] */
 #define OTG_STATUS_CONVERGED 0 /* error below stopThr at a check iteration      */
@@ -87,6 +88,32 @@ int otg_sinkhorn_dense(const OtgDenseProblem* p, void* workspace, cudaStream_t s
 int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, int64_t ldm,
                    const void* u, const void* v, double reg, void* P, int64_t ldp, double* loss,
                    cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Allocation-free variant of otg_sinkhorn_dense.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory
+ * when they solve, e.g. a host whose own allocator owns the device pool, or
+ * a latency-bound loop that must not pay cudaMalloc/cudaFree (which can
+ * synchronise the device).  The solver's scratch is one static device array
+ * of OTG_NOALLOC_SCRATCH_BYTES inside this library, held by every GPU that
+ * loads it until the process exits; p->workspace_bytes is ignored.
+ *
+ * The caller still passes all inputs and outputs, plus the result block:
+ * err_hist (device, hist_cap doubles: the squared L2 column-marginal
+ * violation of each check, the same values as the allocating entry point's
+ * history) and info (device, 8 int32, same meaning as there).
+ *
+ * Problems whose scratch exceeds the maximum are rejected with
+ * OTG_ERR_NOALLOC_TOO_LARGE (about n = m = 16384 in float32 with the
+ * default grid fits; a smaller p->grid lowers the need).  The first call on
+ * a device looks up the array's device address; make that first call
+ * before any stream capture.  Every call shares the array and it keeps the
+ * last call's contents: the call clears what must start at zero, and calls
+ * whose kernels overlap on the GPU race, so serialise them.
+ * ---------------------------------------------------------------------- */
+#define OTG_NOALLOC_SCRATCH_BYTES (16u << 20)
+int otg_sinkhorn_dense_noalloc(const OtgDenseProblem* p, double* err_hist, int32_t* info,
+                               cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -14,7 +14,8 @@ OTG_F32, OTG_F64 = 0, 1
 OTG_METHOD_KNOPP, OTG_METHOD_LOG = 0, 1
 STATUS_CONVERGED, STATUS_MAXITER, STATUS_NUMERICAL, STATUS_ABORTED = 0, 1, 2, 3
 _ERRORS = {-1: "invalid argument", -2: "unsupported dtype", -3: "workspace too small",
-           -4: "CUDA launch error", -5: "unsupported configuration"}
+           -4: "CUDA launch error", -5: "unsupported configuration",
+           -6: "problem too large for the static scratch of the allocation-free entry point"}
 
 c_i32, c_i64, c_sz, c_dbl, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t, ctypes.c_double, ctypes.c_void_p
 
@@ -34,6 +35,7 @@ SIGNATURES = {
     "otg_sinkhorn_dense": (ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp]),
     "otg_dense_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp,
                                       c_dbl, c_vp, c_i64, c_vp, c_vp]),
+    "otg_sinkhorn_dense_noalloc": (ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp, c_vp]),
 }
 
 _lib = None

@@ -571,3 +571,70 @@ int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, i
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point.
+//
+// Some callers cannot allocate device memory at solve time: a host program
+// whose own allocator owns the whole device pool and hands out no extra
+// buffers, or a latency-bound loop (a control or serving loop) that must not
+// pay cudaMalloc / cudaFree, which can synchronise the device.  For them the
+// solver's scratch lives in one file-scope device array of fixed size that
+// every GPU loading this library keeps until the process exits.
+//
+// All calls share the array: it keeps the last call's contents (the launch
+// clears the error history and control words that must start at zero), and
+// calls whose kernels overlap on the GPU race on it, so callers serialise
+// them (one stream, or their own ordering).
+// ---------------------------------------------------------------------------
+namespace {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[OTG_NOALLOC_SCRATCH_BYTES];
+
+// Host code cannot use g_noalloc_scratch as a device address (on the host
+// it names a stand-in object), so the address is looked up once per device
+// with that device current and cached here.
+constexpr int kMaxDevices = 64;
+void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return OTG_ERR_CUDA;
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return OTG_ERR_CUDA;
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return OTG_OK;
+}
+
+template <typename T>
+int noalloc_solve(const OtgDenseProblem* p, double* err_hist, int32_t* info, cudaStream_t st) {
+  const Layout L = make_layout<T>(p->n, p->m, p->hist_cap, resolve_grid<T>(p->grid));
+  if (L.total > (size_t)OTG_NOALLOC_SCRATCH_BYTES) return OTG_ERR_NOALLOC_TOO_LARGE;
+  void* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc != OTG_OK) return rc;
+  OtgDenseProblem q = *p;
+  q.workspace_bytes = OTG_NOALLOC_SCRATCH_BYTES;
+  rc = dispatch_dense<T>(&q, scratch, st);
+  if (rc != OTG_OK) return rc;
+  char* base = static_cast<char*>(scratch);
+  if (cudaMemcpyAsync(err_hist, base + L.off_hist, sizeof(double) * (size_t)p->hist_cap,
+                      cudaMemcpyDeviceToDevice, st) != cudaSuccess) return OTG_ERR_CUDA;
+  if (cudaMemcpyAsync(info, base + L.off_ctrl, 8 * sizeof(int32_t), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return OTG_ERR_CUDA;
+  return OTG_OK;
+}
+
+}  // namespace
+
+extern "C" int otg_sinkhorn_dense_noalloc(const OtgDenseProblem* p, double* err_hist, int32_t* info,
+                                          cudaStream_t stream) {
+  int rc = check_problem(p);
+  if (rc != OTG_OK) return rc;
+  if (!err_hist || !info) return OTG_ERR_ARG;
+  if (p->dtype == OTG_F64) return noalloc_solve<double>(p, err_hist, info, stream);
+  return noalloc_solve<float>(p, err_hist, info, stream);
+}
