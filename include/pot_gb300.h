@@ -90,6 +90,91 @@ int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, i
                    cudaStream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Batched dense Sinkhorn: many independent problems of uneven size in ONE
+ * persistent launch, one CTA per problem at a time, each problem stopping on
+ * its own marginal error.  Replaces the loops of ot/batch/_utils.py:268-278
+ * (bregman_log_projection_batch, u_first = 1), :141-149
+ * (bregman_projection_batch, knopp, u_first = 1) and, with u_first = 0, runs
+ * the per-problem order of ot/bregman/_sinkhorn.py:880-899 (sinkhorn_log).
+ * Problem p's cost block is M + m_off[p], rows[p] x cols[p] with row stride
+ * ldm[p] (elements; ldm*elem a multiple of 16 bytes, m_off*elem 16-byte
+ * aligned; padded columns must hold a finite value or +inf).  a/u use
+ * r_off[p], b/v use c_off[p] into the packed vectors.  All table arrays are
+ * device memory.  Limits come from otg_batch_limits.
+ * ---------------------------------------------------------------------- */
+typedef struct OtgBatchProblem {
+  int32_t dtype, method;
+  const void* M;
+  const int64_t* m_off;
+  const int32_t* rows;
+  const int32_t* cols;
+  const int32_t* ldm;
+  const int64_t* r_off;
+  const int64_t* c_off;
+  const void* a;
+  const void* b;
+  const void* warm_u;   /* natural-log warm start (packed like a) or NULL */
+  const void* warm_v;
+  const double* reg;    /* per problem */
+  const int32_t* order; /* processing order, a permutation of 0..nprob-1 */
+  int32_t nprob;
+  int32_t max_iter;
+  double stop_thr;
+  int32_t u_first;
+  int32_t grid;         /* CTAs (0 = one per SM) */
+  void* out_u;          /* log: natural-log potentials; knopp: scalings */
+  void* out_v;
+  int32_t* status;      /* per problem, OTG_STATUS_* */
+  int32_t* niter;       /* per problem, last loop index */
+  double* err;          /* per problem, last logged marginal error (-1 if none) */
+  int32_t* queue;       /* 2 int32 of device scratch (work counter, abort flag) */
+  int32_t timeout_ms;
+} OtgBatchProblem;
+
+int otg_batch_limits(int dtype, int32_t* max_rows, int32_t* max_cols, int32_t* row_bytes_max);
+int otg_sinkhorn_batched(const OtgBatchProblem* q, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Squared-Euclidean cost blocks for a table of point-cloud pairs:
+ * M_p[i, j] = sum_k (X_p[i, k] - Y_p[j, k])^2 for j < cols[p]; padded
+ * columns [cols[p], ldm[p]) are set to +inf.  max_out (optional, one value
+ * per problem) receives max_ij M_p.  Replaces ot/utils.py:400 dist
+ * (sqeuclidean) and ot/batch/_linear.py:178 dist_batch for the batched path.
+ * ---------------------------------------------------------------------- */
+typedef struct OtgCostTable {
+  int32_t dtype;
+  int32_t nprob;
+  const void* X; const void* Y;
+  const int64_t* x_off;  /* element offset of X_p (row-major rows[p] x dim[p]) */
+  const int64_t* y_off;
+  const int32_t* rows; const int32_t* cols; const int32_t* dim;
+  int32_t max_dim;
+  void* M;
+  const int64_t* m_off;
+  const int32_t* ldm;
+  void* max_out;
+} OtgCostTable;
+int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t stream);
+
+/* Plans and values of a batch from its potentials (log: natural-log
+ * potentials; knopp: scalings).  out_vals[3p] = sum M*T, out_vals[3p+1] =
+ * sum T log(T + 1e-16) (kl = 0) or sum T log(T/(a b^T) + 1e-16) (kl = 1),
+ * out_vals[3p+2] = sum T, all fp64.  P may be NULL (values only); it uses
+ * M's layout.  Replaces ot/batch/_linear.py:326-345 and _utils.py:4-21. */
+typedef struct OtgPlanTable {
+  int32_t dtype, method, nprob, kl;
+  const void* M;
+  const int64_t* m_off;
+  const int32_t* rows; const int32_t* cols; const int32_t* ldm;
+  const int64_t* r_off; const int64_t* c_off;
+  const void* u; const void* v; const void* a; const void* b;
+  const double* reg;
+  void* P;
+  double* out_vals;
+} OtgPlanTable;
+int otg_batched_plan(const OtgPlanTable* t, int32_t max_rows, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
  * Allocation-free variant of otg_sinkhorn_dense.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory
  * when they solve, e.g. a host whose own allocator owns the device pool, or

@@ -28,6 +28,27 @@ class OtgDenseProblem(ctypes.Structure):
                 ("timeout_ms", c_i32)]
 
 
+class OtgBatchProblem(ctypes.Structure):
+    _fields_ = [("dtype", c_i32), ("method", c_i32), ("M", c_vp), ("m_off", c_vp), ("rows", c_vp),
+                ("cols", c_vp), ("ldm", c_vp), ("r_off", c_vp), ("c_off", c_vp), ("a", c_vp), ("b", c_vp),
+                ("warm_u", c_vp), ("warm_v", c_vp), ("reg", c_vp), ("order", c_vp), ("nprob", c_i32),
+                ("max_iter", c_i32), ("stop_thr", c_dbl), ("u_first", c_i32), ("grid", c_i32),
+                ("out_u", c_vp), ("out_v", c_vp), ("status", c_vp), ("niter", c_vp), ("err", c_vp),
+                ("queue", c_vp), ("timeout_ms", c_i32)]
+
+
+class OtgCostTable(ctypes.Structure):
+    _fields_ = [("dtype", c_i32), ("nprob", c_i32), ("X", c_vp), ("Y", c_vp), ("x_off", c_vp), ("y_off", c_vp),
+                ("rows", c_vp), ("cols", c_vp), ("dim", c_vp), ("max_dim", c_i32), ("M", c_vp), ("m_off", c_vp),
+                ("ldm", c_vp), ("max_out", c_vp)]
+
+
+class OtgPlanTable(ctypes.Structure):
+    _fields_ = [("dtype", c_i32), ("method", c_i32), ("nprob", c_i32), ("kl", c_i32), ("M", c_vp),
+                ("m_off", c_vp), ("rows", c_vp), ("cols", c_vp), ("ldm", c_vp), ("r_off", c_vp), ("c_off", c_vp),
+                ("u", c_vp), ("v", c_vp), ("a", c_vp), ("b", c_vp), ("reg", c_vp), ("P", c_vp), ("out_vals", c_vp)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "otg_dense_workspace_bytes": (c_sz, [ctypes.c_int, c_i64, c_i64, ctypes.c_int, ctypes.c_int]),
@@ -36,6 +57,11 @@ SIGNATURES = {
     "otg_dense_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp,
                                       c_dbl, c_vp, c_i64, c_vp, c_vp]),
     "otg_sinkhorn_dense_noalloc": (ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp, c_vp]),
+    "otg_batch_limits": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
+                                        ctypes.POINTER(c_i32)]),
+    "otg_sinkhorn_batched": (ctypes.c_int, [ctypes.POINTER(OtgBatchProblem), c_vp]),
+    "otg_batched_sqdist": (ctypes.c_int, [ctypes.POINTER(OtgCostTable), c_i32, c_vp]),
+    "otg_batched_plan": (ctypes.c_int, [ctypes.POINTER(OtgPlanTable), c_i32, c_vp]),
 }
 
 _lib = None

@@ -1,0 +1,320 @@
+"""Batched entropic OT on the GPU: drop-ins for ``ot.batch`` and a native
+ragged-batch API.
+
+``solve_batch`` / ``solve_sample_batch`` / ``bregman_log_projection_batch``
+/ ``bregman_projection_batch`` follow PythonOT/POT ``ot/batch/_linear.py``
+(:236-357, :360-435) and ``ot/batch/_utils.py`` (:46-162, :165-290): same
+arguments, same returned fields.  One design difference: every problem stops
+on its own marginal error (the reference stops the whole batch on the largest
+error), so problems that converge early are not iterated further.
+
+``solve_ragged`` / ``solve_sample_ragged`` take problems of uneven sizes
+directly (no zero-weight padding) and run them in one persistent launch
+(``csrc/batched.cu``).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._arrays import Boundary
+from .utils import OTResult
+
+
+def _vw(dtype):
+    return 4 if dtype == torch.float32 else 2
+
+
+class RaggedLayout:
+    """Packed device layout of B problems with uneven sizes.
+
+    Problem p's cost block is rows[p] x ldm[p] elements starting at m_off[p]
+    (ldm rounded up to 16 bytes; padded columns hold +inf); a/u slices start
+    at r_off[p], b/v slices at c_off[p]."""
+
+    def __init__(self, rows, cols, dtype, device):
+        rows = np.asarray(rows, dtype=np.int64)
+        cols = np.asarray(cols, dtype=np.int64)
+        vw = _vw(dtype)
+        ldm = (cols + vw - 1) // vw * vw
+        sizes = rows * ldm
+        m_off = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+        r_off = np.concatenate([[0], np.cumsum(rows)[:-1]])
+        c_off = np.concatenate([[0], np.cumsum(cols)[:-1]])
+        self.B = len(rows)
+        self.rows_np, self.cols_np, self.ldm_np = rows, cols, ldm
+        self.m_off_np, self.r_off_np, self.c_off_np = m_off, r_off, c_off
+        self.total_m = int(sizes.sum())
+        self.total_r = int(rows.sum())
+        self.total_c = int(cols.sum())
+        self.dtype, self.device = dtype, device
+        dev = device
+        self.rows = torch.tensor(rows, dtype=torch.int32, device=dev)
+        self.cols = torch.tensor(cols, dtype=torch.int32, device=dev)
+        self.ldm = torch.tensor(ldm, dtype=torch.int32, device=dev)
+        self.m_off = torch.tensor(m_off, dtype=torch.int64, device=dev)
+        self.r_off = torch.tensor(r_off, dtype=torch.int64, device=dev)
+        self.c_off = torch.tensor(c_off, dtype=torch.int64, device=dev)
+        order = np.argsort(-(rows * cols), kind="stable").astype(np.int32)  # largest work first
+        self.order = torch.tensor(order, dtype=torch.int32, device=dev)
+
+    def block(self, M_packed, p):
+        o = int(self.m_off_np[p])
+        n, ld, m = int(self.rows_np[p]), int(self.ldm_np[p]), int(self.cols_np[p])
+        return M_packed[o:o + n * ld].view(n, ld)[:, :m]
+
+    def fits_kernel(self):
+        lib = _lib.load()
+        mr, mc, rb = _lib.c_i32(), _lib.c_i32(), _lib.c_i32()
+        lib.otg_batch_limits(_lib.dtype_code(self.dtype), ctypes.byref(mr), ctypes.byref(mc), ctypes.byref(rb))
+        es = 4 if self.dtype == torch.float32 else 8
+        return (self.rows_np.max() <= mr.value and self.cols_np.max() <= mc.value
+                and (self.ldm_np * es).max() <= rb.value)
+
+
+def pack_dense(layout, Ms):
+    """Pack a list of (n_p, m_p) device tensors (or a (B, n, m) tensor) into
+    the layout's buffer, padding columns with +inf."""
+    buf = torch.empty(layout.total_m, dtype=layout.dtype, device=layout.device)
+    for p in range(layout.B):
+        n, ld, m = int(layout.rows_np[p]), int(layout.ldm_np[p]), int(layout.cols_np[p])
+        blk = buf[int(layout.m_off_np[p]):int(layout.m_off_np[p]) + n * ld].view(n, ld)
+        blk[:, :m].copy_(Ms[p])
+        if ld > m:
+            blk[:, m:].fill_(float("inf"))
+    return buf
+
+
+def run_batched(layout, M_packed, a_packed, b_packed, reg, method, max_iter, tol, u_first,
+                warm_u=None, warm_v=None, grid=0, timeout_ms=0):
+    """One persistent launch over the whole table.  Returns (u, v, status,
+    niter, err) as device tensors (u, v packed like a, b)."""
+    lib = _lib.load()
+    dev, dt = layout.device, layout.dtype
+    B = layout.B
+    if not layout.fits_kernel():
+        raise ValueError("pot_gb300 batched kernel: a problem exceeds the per-CTA size limits "
+                         "(otg_batch_limits); solve it with the dense single-problem path")
+    reg_t = torch.as_tensor(reg, dtype=torch.float64, device=dev).reshape(-1)
+    if reg_t.numel() == 1:
+        reg_t = reg_t.expand(B).contiguous()
+    out_u = torch.empty(layout.total_r, dtype=dt, device=dev)
+    out_v = torch.empty(layout.total_c, dtype=dt, device=dev)
+    status = torch.empty(B, dtype=torch.int32, device=dev)
+    niter = torch.empty(B, dtype=torch.int32, device=dev)
+    err = torch.empty(B, dtype=torch.float64, device=dev)
+    queue = torch.zeros(2, dtype=torch.int32, device=dev)
+    q = _lib.OtgBatchProblem(
+        dtype=_lib.dtype_code(dt), method=method, M=M_packed.data_ptr(), m_off=layout.m_off.data_ptr(),
+        rows=layout.rows.data_ptr(), cols=layout.cols.data_ptr(), ldm=layout.ldm.data_ptr(),
+        r_off=layout.r_off.data_ptr(), c_off=layout.c_off.data_ptr(), a=a_packed.data_ptr(),
+        b=b_packed.data_ptr(), warm_u=warm_u.data_ptr() if warm_u is not None else None,
+        warm_v=warm_v.data_ptr() if warm_v is not None else None, reg=reg_t.data_ptr(),
+        order=layout.order.data_ptr(), nprob=B, max_iter=int(max_iter), stop_thr=float(tol),
+        u_first=int(u_first), grid=int(grid), out_u=out_u.data_ptr(), out_v=out_v.data_ptr(),
+        status=status.data_ptr(), niter=niter.data_ptr(), err=err.data_ptr(), queue=queue.data_ptr(),
+        timeout_ms=int(timeout_ms))
+    _lib.check(lib.otg_sinkhorn_batched(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_batched")
+    return out_u, out_v, status, niter, err, reg_t
+
+
+def batched_plan(layout, M_packed, u, v, a_packed, b_packed, reg_t, method, kl=False, want_plan=True):
+    """Plans (packed like M) and per-problem (value_linear, reg term, mass)."""
+    lib = _lib.load()
+    dev = layout.device
+    P = torch.empty_like(M_packed) if want_plan else None
+    vals = torch.empty(3 * layout.B, dtype=torch.float64, device=dev)
+    t = _lib.OtgPlanTable(dtype=_lib.dtype_code(layout.dtype), method=method, nprob=layout.B, kl=int(kl),
+                          M=M_packed.data_ptr(), m_off=layout.m_off.data_ptr(), rows=layout.rows.data_ptr(),
+                          cols=layout.cols.data_ptr(), ldm=layout.ldm.data_ptr(), r_off=layout.r_off.data_ptr(),
+                          c_off=layout.c_off.data_ptr(), u=u.data_ptr(), v=v.data_ptr(), a=a_packed.data_ptr(),
+                          b=b_packed.data_ptr(), reg=reg_t.data_ptr(), P=P.data_ptr() if P is not None else None,
+                          out_vals=vals.data_ptr())
+    _lib.check(lib.otg_batched_plan(ctypes.byref(t), int(layout.rows_np.max()), _lib.stream_handle(dev)),
+               "otg_batched_plan")
+    return P, vals.view(layout.B, 3)
+
+
+def batched_sqdist(layout, X_packed, Y_packed, x_off, y_off, dims, want_max=False):
+    """Cost blocks sum_k (x_ik - y_jk)^2 for every problem of the layout."""
+    lib = _lib.load()
+    dev = layout.device
+    M = torch.empty(layout.total_m, dtype=layout.dtype, device=dev)
+    mx = torch.empty(layout.B, dtype=layout.dtype, device=dev) if want_max else None
+    dims_t = torch.as_tensor(np.asarray(dims, dtype=np.int32), device=dev)
+    xo = torch.as_tensor(np.asarray(x_off, dtype=np.int64), device=dev)
+    yo = torch.as_tensor(np.asarray(y_off, dtype=np.int64), device=dev)
+    t = _lib.OtgCostTable(dtype=_lib.dtype_code(layout.dtype), nprob=layout.B, X=X_packed.data_ptr(),
+                          Y=Y_packed.data_ptr(), x_off=xo.data_ptr(), y_off=yo.data_ptr(),
+                          rows=layout.rows.data_ptr(), cols=layout.cols.data_ptr(), dim=dims_t.data_ptr(),
+                          max_dim=int(np.max(dims)), M=M.data_ptr(), m_off=layout.m_off.data_ptr(),
+                          ldm=layout.ldm.data_ptr(), max_out=mx.data_ptr() if mx is not None else None)
+    _lib.check(lib.otg_batched_sqdist(ctypes.byref(t), int(layout.rows_np.max()), _lib.stream_handle(dev)),
+               "otg_batched_sqdist")
+    return M, mx
+
+
+# ---------------------------------------------------------------------------
+# ot.batch drop-ins
+# ---------------------------------------------------------------------------
+def _uniform_batch(M):
+    layout = RaggedLayout([M.shape[1]] * M.shape[0], [M.shape[2]] * M.shape[0], M.dtype, M.device)
+    if layout.ldm_np[0] == M.shape[2] and M.is_contiguous() and M.data_ptr() % 16 == 0:
+        Mp = M.reshape(-1)
+    else:
+        Mp = pack_dense(layout, M)
+    return layout, Mp
+
+
+def _unpack_rows(layout, packed, width_np, off_np):
+    B = layout.B
+    w = int(width_np[0])
+    return packed.view(B, w)
+
+
+def _solve_uniform(Md, a, b, reg, method, max_iter, tol, kl):
+    layout, Mp = _uniform_batch(Md)
+    ap, bp = a.reshape(-1).contiguous(), b.reshape(-1).contiguous()
+    u, v, status, niter, err, reg_t = run_batched(layout, Mp, ap, bp, reg, method, max_iter, tol, u_first=1)
+    P, vals = batched_plan(layout, Mp, u, v, ap, bp, reg_t, method, kl=kl)
+    B, n, m = Md.shape
+    ld = int(layout.ldm_np[0])
+    T = P.view(B, n, ld)[:, :, :m]
+    if ld != m:
+        T = T.contiguous()
+    return T, u.view(B, n), v.view(B, m), vals, niter, status
+
+
+def solve_batch(M, reg, a=None, b=None, max_iter=1000, tol=1e-5, solver="log_sinkhorn", reg_type="entropy",
+                grad="envelope"):
+    """GPU ``ot.batch.solve_batch`` (``ot/batch/_linear.py:236``)."""
+    if solver not in ("log_sinkhorn", "sinkhorn"):
+        raise ValueError(f"Unknown solver: {solver}")
+    if reg_type.lower() not in ("entropy", "kl"):
+        raise ValueError(f"Unknown reg_type: {reg_type}")
+    bd = Boundary(M, a, b)
+    Md = bd.to_dev(M)
+    B, n, m = Md.shape
+    ad = torch.full((B, n), 1.0 / n, dtype=Md.dtype, device=Md.device) if a is None else bd.to_dev(a, Md.dtype)
+    bv = torch.full((B, m), 1.0 / m, dtype=Md.dtype, device=Md.device) if b is None else bd.to_dev(b, Md.dtype)
+    method = _lib.OTG_METHOD_LOG if solver == "log_sinkhorn" else _lib.OTG_METHOD_KNOPP
+    T, u, v, vals, niter, _ = _solve_uniform(Md, ad, bv, float(reg), method, max_iter, tol,
+                                             reg_type.lower() == "kl")
+    value_linear = vals[:, 0].to(Md.dtype)
+    value = (vals[:, 0] + float(reg) * vals[:, 1]).to(Md.dtype)
+    log = {"n_iter": int(niter.max().item())}
+    return OTResult(value=bd.out(value), value_linear=bd.out(value_linear),
+                    potentials=(bd.out(u), bd.out(v)), plan=bd.out(T), log=log)
+
+
+def dist_batch(X1, X2=None, metric="sqeuclidean", p=2, nx=None):
+    """GPU ``ot.batch.dist_batch`` (``ot/batch/_linear.py:178``) for the
+    'sqeuclidean' and 'euclidean' metrics."""
+    metric = metric.lower()
+    if metric not in ("sqeuclidean", "euclidean"):
+        raise NotImplementedError("pot_gb300 dist_batch: metric '%s' is not on the GPU path" % metric)
+    bd = Boundary(X1, X2)
+    X = bd.to_dev(X1)
+    Y = X if X2 is None else bd.to_dev(X2, X.dtype)
+    B, n, d = X.shape
+    m = Y.shape[1]
+    layout = RaggedLayout([n] * B, [m] * B, X.dtype, X.device)
+    Mp, _ = batched_sqdist(layout, X.reshape(-1).contiguous(), Y.reshape(-1).contiguous(),
+                           np.arange(B) * n * d, np.arange(B) * m * d, [d] * B)
+    ld = int(layout.ldm_np[0])
+    M = Mp.view(B, n, ld)[:, :, :m]
+    if metric == "euclidean":
+        M = torch.sqrt(M)
+    return bd.out(M.contiguous())
+
+
+def solve_sample_batch(X_a, X_b, reg, a=None, b=None, metric="sqeuclidean", p=2, max_iter=1000, tol=1e-5,
+                       solver="log_sinkhorn", reg_type="entropy", grad="envelope"):
+    """GPU ``ot.batch.solve_sample_batch`` (``ot/batch/_linear.py:360``)."""
+    bd = Boundary(X_a, X_b, a, b)
+    M = dist_batch(bd.to_dev(X_a), bd.to_dev(X_b), metric=metric, p=p)
+    res = solve_batch(M, reg, a=None if a is None else bd.to_dev(a, M.dtype),
+                      b=None if b is None else bd.to_dev(b, M.dtype), max_iter=max_iter, tol=tol, solver=solver,
+                      reg_type=reg_type, grad=grad)
+    return OTResult(value=bd.out(res.value), value_linear=bd.out(res.value_linear),
+                    potentials=tuple(bd.out(x) for x in res.potentials), plan=bd.out(res.plan), log=res.log)
+
+
+def bregman_log_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol=1e-5, grad="detach"):
+    """GPU ``ot.batch.bregman_log_projection_batch`` (``_utils.py:165``):
+    ``K = -M/reg`` is solved as cost ``-K`` with unit regularisation."""
+    bd = Boundary(K, a, b)
+    Kd = bd.to_dev(K)
+    B, n, m = Kd.shape
+    ad = torch.ones((B, n), dtype=Kd.dtype, device=Kd.device) / n if a is None else bd.to_dev(a, Kd.dtype)
+    bv = torch.ones((B, m), dtype=Kd.dtype, device=Kd.device) / m if b is None else bd.to_dev(b, Kd.dtype)
+    T, u, v, _, niter, _ = _solve_uniform((-Kd).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_LOG, max_iter, tol, False)
+    log_T = Kd + u[:, :, None] + v[:, None, :]
+    return {"T": bd.out(T), "log_T": bd.out(log_T), "n_iters": int(niter.max().item()),
+            "potentials": (bd.out(u), bd.out(v))}
+
+
+def bregman_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol=1e-5, grad="detach"):
+    """GPU ``ot.batch.bregman_projection_batch`` (``_utils.py:46``): the
+    affinity ``K`` is solved as cost ``-log K`` with unit regularisation."""
+    bd = Boundary(K, a, b)
+    Kd = bd.to_dev(K)
+    B, n, m = Kd.shape
+    ad = torch.ones((B, n), dtype=Kd.dtype, device=Kd.device) / n if a is None else bd.to_dev(a, Kd.dtype)
+    bv = torch.ones((B, m), dtype=Kd.dtype, device=Kd.device) / m if b is None else bd.to_dev(b, Kd.dtype)
+    T, f, g, _, niter, _ = _solve_uniform((-torch.log(Kd)).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_KNOPP,
+                                          max_iter, tol, False)
+    return {"T": bd.out(T), "n_iters": int(niter.max().item()), "potentials": (bd.out(f), bd.out(g))}
+
+
+# ---------------------------------------------------------------------------
+# Native ragged API
+# ---------------------------------------------------------------------------
+class RaggedResult:
+    """Per-problem results of a ragged solve (device tensors)."""
+
+    def __init__(self, layout, u, v, status, niter, err, reg, M=None):
+        self.layout, self.u, self.v = layout, u, v
+        self.status, self.niter, self.err, self.reg, self.M = status, niter, err, reg, M
+
+    def potentials(self, p):
+        L = self.layout
+        return (self.u[int(L.r_off_np[p]):int(L.r_off_np[p] + L.rows_np[p])],
+                self.v[int(L.c_off_np[p]):int(L.c_off_np[p] + L.cols_np[p])])
+
+
+def solve_sample_ragged(Xs, Ys, reg, as_=None, bs=None, reg_relative=False, max_iter=100000, tol=1e-6,
+                        method="sinkhorn_log", warmstart=None, dtype=torch.float32, device=None):
+    """Entropic OT between B point-cloud pairs of uneven sizes and dims, in
+    one persistent launch.  ``reg`` is a scalar or one value per problem; with
+    ``reg_relative`` it multiplies each problem's largest cost.  Per problem
+    the iteration order and stopping test are those of ``ot.sinkhorn(...,
+    method='sinkhorn_log')`` (v first, column-marginal L2 error)."""
+    device = device or torch.device("cuda", torch.cuda.current_device())
+    B = len(Xs)
+    rows = [x.shape[0] for x in Xs]
+    cols = [y.shape[0] for y in Ys]
+    dims = [x.shape[1] for x in Xs]
+    layout = RaggedLayout(rows, cols, dtype, device)
+    X = torch.cat([torch.as_tensor(np.asarray(x), dtype=dtype).reshape(-1) for x in Xs]).to(device)
+    Y = torch.cat([torch.as_tensor(np.asarray(y), dtype=dtype).reshape(-1) for y in Ys]).to(device)
+    x_off = np.concatenate([[0], np.cumsum([r * d for r, d in zip(rows, dims)])[:-1]])
+    y_off = np.concatenate([[0], np.cumsum([c * d for c, d in zip(cols, dims)])[:-1]])
+    M, mx = batched_sqdist(layout, X, Y, x_off, y_off, dims, want_max=reg_relative)
+    reg_t = torch.as_tensor(reg, dtype=torch.float64, device=device).reshape(-1)
+    if reg_t.numel() == 1:
+        reg_t = reg_t.expand(B).contiguous()
+    if reg_relative:
+        reg_t = reg_t * mx.double()
+    ap = (torch.cat([torch.as_tensor(np.asarray(a), dtype=dtype) for a in as_]) if as_ is not None else
+          torch.cat([torch.full((r,), 1.0 / r, dtype=dtype) for r in rows])).to(device)
+    bp = (torch.cat([torch.as_tensor(np.asarray(b), dtype=dtype) for b in bs]) if bs is not None else
+          torch.cat([torch.full((c,), 1.0 / c, dtype=dtype) for c in cols])).to(device)
+    code = _lib.OTG_METHOD_LOG if method == "sinkhorn_log" else _lib.OTG_METHOD_KNOPP
+    wu = wv = None
+    if warmstart is not None:
+        wu, wv = warmstart
+    u, v, status, niter, err, reg_t = run_batched(layout, M, ap, bp, reg_t, code, max_iter, tol, u_first=0,
+                                                  warm_u=wu, warm_v=wv)
+    return RaggedResult(layout, u, v, status, niter, err, reg_t, M)

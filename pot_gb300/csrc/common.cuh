@@ -83,6 +83,13 @@ __device__ __forceinline__ T warp_sum(T x) {
   return x;
 }
 
+template <typename T>
+__device__ __forceinline__ T warp_max(T x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+  return x;
+}
+
 __device__ __forceinline__ int warp_or(int x) { return __any_sync(0xffffffffu, x) ? 1 : 0; }
 
 // ---------------------------------------------------------------------------

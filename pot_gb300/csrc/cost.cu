@@ -1,0 +1,147 @@
+// Squared-Euclidean cost blocks for a table of point-cloud pairs, and the
+// batched plan / value kernel.
+//
+// Reference behaviour: ot/utils.py:270-305 (euclidean_distances, squared) and
+// ot/batch/_linear.py:54-85 (dist_euclidean_batch) compute |x|^2+|y|^2-2x.y;
+// here the cost is formed from coordinate differences, sum_k (x_k - y_k)^2,
+// which has no cancellation and matches a float64 evaluation more closely.
+// Plan and values: ot/batch/_linear.py:326-345 (value_linear = sum M T,
+// value = value_linear + reg * sum T log(T + 1e-16) or the KL form).
+#include <algorithm>
+#include "common.cuh"
+#include "../../include/pot_gb300.h"
+
+namespace otg {
+
+// One CTA per (problem, tile of 32 rows); the tile's points are staged in
+// shared memory; threads sweep the columns.  Padded columns [m, ldm) get +inf.
+template <typename T>
+__global__ void __launch_bounds__(256) batched_sqdist_kernel(OtgCostTable t) {
+  constexpr int TR = 32;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T* xs = reinterpret_cast<T*>(sm_raw);
+  const int p = blockIdx.y;
+  if (p >= t.nprob) return;
+  const int n = t.rows[p], m = t.cols[p], d = t.dim[p], ldm = t.ldm[p];
+  const int r0 = blockIdx.x * TR;
+  if (r0 >= n) return;
+  const int rows = min(TR, n - r0);
+  const T* X = static_cast<const T*>(t.X) + t.x_off[p];
+  const T* Y = static_cast<const T*>(t.Y) + t.y_off[p];
+  T* M = static_cast<T*>(t.M) + t.m_off[p];
+  for (int e = threadIdx.x; e < rows * d; e += blockDim.x) xs[e] = X[(int64_t)r0 * d + e];
+  __syncthreads();
+  T local_max = 0;
+  for (int j = threadIdx.x; j < ldm; j += blockDim.x) {
+    if (j < m) {
+      const T* y = Y + (int64_t)j * d;
+      for (int r = 0; r < rows; ++r) {
+        const T* x = xs + r * d;
+        T acc = 0;
+        for (int k = 0; k < d; ++k) { const T df = x[k] - y[k]; acc = fma(df, df, acc); }
+        M[(int64_t)(r0 + r) * ldm + j] = acc;
+        local_max = fmax(local_max, acc);
+      }
+    } else {
+      for (int r = 0; r < rows; ++r) M[(int64_t)(r0 + r) * ldm + j] = T(INFINITY);
+    }
+  }
+  if (t.max_out) {
+    // non-negative floats order like their bit patterns
+    local_max = warp_max(local_max);
+    if ((threadIdx.x & 31) == 0) {
+      if (sizeof(T) == 4) atomicMax(reinterpret_cast<unsigned int*>(static_cast<T*>(t.max_out) + p), __float_as_uint((float)local_max));
+      else atomicMax(reinterpret_cast<unsigned long long*>(static_cast<T*>(t.max_out) + p), (unsigned long long)__double_as_longlong((double)local_max));
+    }
+  }
+}
+
+// Plan and values per problem.  grid = (row tiles, problems).
+// out_vals[3p+0] = value_linear, [3p+1] = sum T log(T+1e-16) (entropy form)
+// or sum T log(T/(a b) + 1e-16) (KL form), [3p+2] = sum T.
+template <typename T, int METHOD>
+__global__ void __launch_bounds__(256) batched_plan_kernel(OtgPlanTable t) {
+  const int p = blockIdx.y;
+  if (p >= t.nprob) return;
+  const int n = t.rows[p], m = t.cols[p], ldm = t.ldm[p];
+  const T* M = static_cast<const T*>(t.M) + t.m_off[p];
+  const T* u = static_cast<const T*>(t.u) + t.r_off[p];
+  const T* v = static_cast<const T*>(t.v) + t.c_off[p];
+  const T* a = static_cast<const T*>(t.a) + t.r_off[p];
+  const T* b = static_cast<const T*>(t.b) + t.c_off[p];
+  T* P = t.P ? static_cast<T*>(t.P) + t.m_off[p] : nullptr;
+  const T c = (T)(-OTG_LOG2E / t.reg[p]);
+  const T L2E = T(OTG_LOG2E);
+  double lin = 0, reg_term = 0, mass = 0;
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const T ui = u[i];
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+      const T x = M[(int64_t)i * ldm + j];
+      T pij;
+      if (METHOD == OTG_METHOD_LOG) pij = ex2(fma(x, c, (ui + v[j]) * L2E));
+      else pij = ui * ex2(x * c) * v[j];
+      if (P) P[(int64_t)i * ldm + j] = pij;
+      const double pd = (double)pij;
+      lin += (double)x * pd;
+      mass += pd;
+      if (t.kl) reg_term += pd * log(pd / ((double)a[i] * (double)b[j]) + 1e-16);
+      else reg_term += pd * log(pd + 1e-16);
+    }
+  }
+  __shared__ double red[3][8];
+  lin = warp_sum(lin); reg_term = warp_sum(reg_term); mass = warp_sum(mass);
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { red[0][w] = lin; red[1][w] = reg_term; red[2][w] = mass; }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double s = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[threadIdx.x][k];
+    atomicAdd(t.out_vals + 3 * p + threadIdx.x, s);
+  }
+}
+
+}  // namespace otg
+
+using namespace otg;
+
+extern "C" {
+
+int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t stream) {
+  if (!t || !t->X || !t->Y || !t->M || !t->rows || !t->cols || !t->dim || !t->ldm || !t->x_off || !t->y_off ||
+      !t->m_off || t->nprob < 1 || max_rows < 1 || t->max_dim < 1)
+    return OTG_ERR_ARG;
+  if (t->nprob > 65535) return OTG_ERR_UNSUPPORTED;
+  dim3 grid((max_rows + 31) / 32, t->nprob);
+  if (t->max_out) {
+    size_t es = t->dtype == OTG_F64 ? 8 : 4;
+    if (cudaMemsetAsync(t->max_out, 0, es * t->nprob, stream) != cudaSuccess) return OTG_ERR_CUDA;
+  }
+  if (t->dtype == OTG_F64) {
+    batched_sqdist_kernel<double><<<grid, 256, 32 * t->max_dim * sizeof(double), stream>>>(*t);
+  } else if (t->dtype == OTG_F32) {
+    batched_sqdist_kernel<float><<<grid, 256, 32 * t->max_dim * sizeof(float), stream>>>(*t);
+  } else {
+    return OTG_ERR_DTYPE;
+  }
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_batched_plan(const OtgPlanTable* t, int32_t max_rows, cudaStream_t stream) {
+  if (!t || !t->M || !t->u || !t->v || !t->a || !t->b || !t->reg || !t->out_vals || t->nprob < 1 || max_rows < 1)
+    return OTG_ERR_ARG;
+  if (t->nprob > 65535) return OTG_ERR_UNSUPPORTED;
+  if (cudaMemsetAsync(t->out_vals, 0, 3 * sizeof(double) * t->nprob, stream) != cudaSuccess) return OTG_ERR_CUDA;
+  dim3 grid(std::min(max_rows, 64), t->nprob);
+  if (t->dtype == OTG_F64) {
+    if (t->method == OTG_METHOD_LOG) batched_plan_kernel<double, OTG_METHOD_LOG><<<grid, 256, 0, stream>>>(*t);
+    else batched_plan_kernel<double, OTG_METHOD_KNOPP><<<grid, 256, 0, stream>>>(*t);
+  } else if (t->dtype == OTG_F32) {
+    if (t->method == OTG_METHOD_LOG) batched_plan_kernel<float, OTG_METHOD_LOG><<<grid, 256, 0, stream>>>(*t);
+    else batched_plan_kernel<float, OTG_METHOD_KNOPP><<<grid, 256, 0, stream>>>(*t);
+  } else {
+    return OTG_ERR_DTYPE;
+  }
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+}  // extern "C"

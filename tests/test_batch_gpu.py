@@ -1,0 +1,138 @@
+"""Parity of the batched GPU solver with the oracle and the reference goldens.
+
+The GPU stops every problem on its own error, so the exact oracle for a
+batch is the batch projection run one problem at a time; with it, float64
+batches match to 1e-9 and the same iteration index.  Against the reference's
+whole-batch stop (golden fixtures) the plans agree to the stopping tolerance.
+float32 ragged batches: plan relative L1 <= 1e-5 against the float64 oracle
+and a float64 column-marginal violation of at most 2x stopThr.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import pot_gb300 as pg
+from conftest import golden
+from pot_gb300 import batch as pb
+
+pytestmark = pytest.mark.gpu
+
+
+def per_problem_oracle(M, reg, a, b, max_iter, tol, solver):
+    out = []
+    for k in range(M.shape[0]):
+        r = oracle.solve_batch(M[k:k + 1], reg, a[k:k + 1], b[k:k + 1], max_iter, tol, solver)
+        out.append(r)
+    return out
+
+
+@pytest.mark.parametrize("solver", ["log_sinkhorn", "sinkhorn"])
+@pytest.mark.parametrize("reg_type", ["entropy", "kl"])
+def test_solve_batch_f64_exact(cuda, solver, reg_type):
+    g = golden("batch_4x16")
+    M = g["M"]
+    B, n, m = M.shape
+    a = np.full((B, n), 1 / n)
+    b = np.full((B, m), 1 / m)
+    res = pb.solve_batch(M, 0.1, max_iter=10000, tol=1e-5, solver=solver, reg_type=reg_type)
+    ref = per_problem_oracle(M, 0.1, a, b, 10000, 1e-5, solver)
+    for k in range(B):
+        rk = oracle.solve_batch(M[k:k + 1], 0.1, a[k:k + 1], b[k:k + 1], 10000, 1e-5, solver, reg_type)
+        np.testing.assert_allclose(res.plan[k], rk["plan"][0], rtol=1e-9, atol=1e-15)
+        np.testing.assert_allclose(res.value[k], rk["value"][0], rtol=1e-9)
+        np.testing.assert_allclose(res.value_linear[k], rk["value_linear"][0], rtol=1e-9)
+        np.testing.assert_allclose(res.potentials[0][k], rk["potentials"][0][0], rtol=1e-8, atol=1e-12)
+    assert res.log["n_iter"] == max(r["n_iter"] for r in ref)
+    # against the reference's whole-batch stop: within the stopping tolerance
+    tag = "%s_%s" % (solver, reg_type)
+    np.testing.assert_allclose(res.plan, g[tag + "_plan"], atol=1e-5)
+    np.testing.assert_allclose(res.value_linear, g[tag + "_value_linear"], atol=1e-4)
+
+
+def test_solve_batch_padded_ragged(cuda):
+    g = golden("batch_ragged_padded")
+    res = pb.solve_batch(g["M"], float(g["reg"]), a=g["a"], b=g["b"], max_iter=20000, tol=1e-9)
+    assert not np.isnan(res.plan).any()
+    np.testing.assert_allclose(res.plan, g["plan"], atol=1e-8)
+
+
+def test_solve_sample_batch(cuda):
+    g = golden("batch_sample_3x20x25")
+    res = pb.solve_sample_batch(g["X"], g["Y"], float(g["reg"]), max_iter=5000, tol=1e-7)
+    np.testing.assert_allclose(res.plan, g["plan"], atol=1e-7)
+    np.testing.assert_allclose(res.value_linear, g["value_linear"], rtol=1e-6)
+
+
+def test_dist_batch_matches_oracle(cuda):
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((3, 17, 5))
+    Y = rng.standard_normal((3, 22, 5))
+    M = pb.dist_batch(X, Y)
+    for k in range(3):
+        np.testing.assert_allclose(M[k], oracle.sqeuclidean(X[k], Y[k]), rtol=1e-12, atol=1e-12)
+
+
+def test_projection_functions(cuda):
+    rng = np.random.default_rng(1)
+    M = rng.random((3, 10, 12))
+    out = pb.bregman_log_projection_batch(-M / 0.2, max_iter=10000, tol=1e-9)
+    assert out["T"].shape == (3, 10, 12) and out["log_T"].shape == (3, 10, 12)
+    np.testing.assert_allclose(out["T"].sum(2), np.full((3, 10), 0.1), atol=1e-8)
+    out2 = pb.bregman_projection_batch(np.exp(-M / 0.2), max_iter=10000, tol=1e-9)
+    np.testing.assert_allclose(out2["T"], out["T"], atol=1e-8)
+
+
+def _ragged_case(seed, B, lo, hi, dims=(3, 16)):
+    rng = np.random.default_rng(seed)
+    Xs, Ys, As, Bs, regs = [], [], [], [], []
+    for k in range(B):
+        n, m = rng.integers(lo, hi + 1, size=2)
+        d = dims[k % len(dims)]
+        Xs.append(rng.random((n, d)))
+        Ys.append(rng.random((m, d)))
+        As.append(rng.dirichlet(np.ones(n)))
+        Bs.append(rng.dirichlet(np.ones(m)))
+        regs.append(10 ** rng.uniform(-2, -1))
+    return Xs, Ys, As, Bs, regs
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_ragged_vs_oracle(cuda, dtype):
+    Xs, Ys, As, Bs, regs = _ragged_case(3, 24, 2, 300)
+    tol = 1e-9 if dtype == torch.float64 else 1e-6
+    res = pb.solve_sample_ragged(Xs, Ys, regs, As, Bs, reg_relative=True, max_iter=50000, tol=tol, dtype=dtype)
+    torch.cuda.synchronize()
+    st = res.status.cpu().numpy()
+    nit = res.niter.cpu().numpy()
+    for k in range(len(Xs)):
+        M = oracle.sqeuclidean(Xs[k], Ys[k])
+        reg = regs[k] * M.max()
+        P, lg = oracle.sinkhorn_log(As[k], Bs[k], M, reg, numItermax=50000, stopThr=tol if dtype == torch.float64 else 1e-12)
+        u, v = (t.double().cpu().numpy() for t in res.potentials(k))
+        Pg = np.exp(-M / reg + u[:, None] + v[None, :])
+        assert st[k] == 0, (k, st[k])
+        if dtype == torch.float64:
+            assert nit[k] == lg["niter"], (k, nit[k], lg["niter"])
+            assert np.abs(Pg - P).sum() / P.sum() < 1e-9
+        else:
+            assert np.abs(Pg - P).sum() / P.sum() < 1e-5, k
+            assert np.linalg.norm(Pg.sum(0) - Bs[k]) < 2 * tol
+
+
+def test_ragged_sizes_at_the_limits(cuda):
+    # 1x1, thin, wide and the largest column count the kernel takes in one pass
+    rng = np.random.default_rng(4)
+    shapes = [(1, 1), (1, 37), (37, 1), (3, 1024), (1024, 3), (5, 2048), (2048, 7)]
+    Xs = [rng.random((n, 3)) for n, _ in shapes]
+    Ys = [rng.random((m, 3)) for _, m in shapes]
+    res = pb.solve_sample_ragged(Xs, Ys, 0.1, reg_relative=True, max_iter=20000, tol=1e-9, dtype=torch.float64)
+    for k, (n, m) in enumerate(shapes):
+        M = oracle.sqeuclidean(Xs[k], Ys[k])
+        reg = 0.1 * M.max() if M.max() > 0 else 0.1
+        if M.max() == 0:
+            continue
+        P, lg = oracle.sinkhorn_log([], [], M, reg, numItermax=20000, stopThr=1e-9)
+        u, v = (t.cpu().numpy() for t in res.potentials(k))
+        Pg = np.exp(-M / reg + u[:, None] + v[None, :])
+        assert np.abs(Pg - P).sum() / P.sum() < 1e-9, (n, m)
