@@ -2,12 +2,20 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl reference]
 
-Prints ONE JSON line (rank 0).  A step is one full solve of the workload's
-problem(s) to the stated marginal error, on inputs already resident in HBM;
-``e2e`` repeats the measurement through the public API with host (numpy)
-buffers, copies included.  ``--impl reference`` times the reference's CPU
-algorithm (the float64 numpy oracle) on a bounded sample of the same
-workload with all host cores.
+Prints ONE JSON line (rank 0).
+
+Default workload ("warmstart"): learned warm start vs plain zero-initialised
+log-domain Sinkhorn on batches of Gaussian-mixture cloud pairs (n = m = 2048
+points in R^16, 1-6 isotropic components per cloud, uniform weights,
+reg = 0.02 x max cost, marginal error 1e-6).  A step solves the whole batch:
+cost blocks, (warm start,) and the persistent solve; `value` is the warm
+arm's solves/s with the clouds resident in HBM, `plain` the zero-init arm's.
+The cost blocks (16 MiB per pair) exceed L2 many times over.  `e2e` runs the
+public entry point with host (numpy) clouds, copies included.
+
+`--impl reference` times the reference's CPU algorithm (the float64 numpy
+restatement of sinkhorn_log) on a bounded sample of the same workload, over
+all host cores (one process per core).
 """
 import argparse
 import json
@@ -24,6 +32,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 METRIC = "Sinkhorn solves/s at marginal err 1e-6, warm vs plain, 1 GB300; % roofline"
+WS_N, WS_D, WS_REG, WS_TOL = 2048, 16, 0.02, 1e-6
+EVAL_SEED = 10_000_000
 
 
 def peaks():
@@ -83,112 +93,120 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# Workload: dense log-domain Sinkhorn, cost larger than L2
+# warm vs plain (default workload)
 # ---------------------------------------------------------------------------
-def make_dense(n, seed=0):
-    rng = np.random.default_rng(seed)
-    x = rng.standard_normal((n, 2))
-    y = rng.standard_normal((n, 2)) * np.sqrt(0.5) + 1.0
-    M = (x * x).sum(1)[:, None] + (y * y).sum(1)[None, :] - 2 * x @ y.T
-    M = np.maximum(M, 0)
-    M /= M.max()
-    a = np.full(n, 1.0 / n)
-    return a, a.copy(), M
-
-
-def run_dense(args, pk):
+def run_warmstart(args, pk):
     import torch
-    import pot_gb300 as pg
-    from pot_gb300 import bregman, _lib
+    from pot_gb300 import _lib
+    from pot_gb300.warmstart import pipeline as wp
 
-    n = args.n
-    reg, stop = 0.05, 1e-6
-    a, b, M = make_dense(n)
     dev = torch.device("cuda:0")
-    Mt = torch.tensor(M, dtype=torch.float32, device=dev)
-    at = torch.tensor(a, dtype=torch.float32, device=dev)
-    bt = torch.tensor(b, dtype=torch.float32, device=dev)
-    P = torch.empty_like(Mt)
-    lib = _lib.load()
+    B = args.batch
+    X, Y = wp.gen_pairs(EVAL_SEED, B, WS_N, WS_D, dev)
+    net = wp.default_net(dev)
     st = torch.cuda.current_stream()
 
-    def step():
-        r = bregman.solve_dense(Mt, at, bt, reg, _lib.OTG_METHOD_LOG, 10000, stop, read_back=False)
-        lib.otg_dense_plan(_lib.OTG_F32, _lib.OTG_METHOD_LOG, _lib.ptr(Mt), n, n, n, _lib.ptr(r.u),
-                           _lib.ptr(r.v), reg, _lib.ptr(P), n, None, _lib.stream_handle())
-        return r
+    def step(warm, ev=None):
+        ps = wp.PairSolver(X, Y)
+        wu = wp.warm_potential(net, X, Y, ps, WS_REG) if warm else None
+        out = ps.solve(WS_REG, WS_TOL, warm_u=wu, events=ev)
+        return ps, out
 
     for _ in range(args.warmup):
-        r = step()
+        step(True)
+        step(False)
     torch.cuda.synchronize()
-    bregman.read_result(r)
-    iters = r.niter + 1
-    # kernel-only timing of the dominant kernel (solve loop) on the launching stream
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    kev = []
-    torch.cuda.synchronize()
+    res = {}
     with ClockSampler() as cs:
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
-        t0.record(st)
-        for k in range(args.steps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            r = bregman.solve_dense(Mt, at, bt, reg, _lib.OTG_METHOD_LOG, 10000, stop, read_back=False)
-            e1.record(st)
-            lib.otg_dense_plan(_lib.OTG_F32, _lib.OTG_METHOD_LOG, _lib.ptr(Mt), n, n, n, _lib.ptr(r.u),
-                               _lib.ptr(r.v), reg, _lib.ptr(P), n, None, _lib.stream_handle())
-            kev.append((e0, e1))
-        t1.record(st)
-        torch.cuda.synchronize()
-    total_ms = t0.elapsed_time(t1)
-    kern_ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in kev)
-    bregman.read_result(r)
-    ms = total_ms / args.steps
-    passes = (r.niter + 1) * 2 + 1
-    alg_bytes = passes * n * n * 4
-    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
-    # e2e through the public API with host buffers
-    Mf = M.astype(np.float32)
-    af, bf = a.astype(np.float32), b.astype(np.float32)
+        for arm in ("warm", "plain"):
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            kev = []
+            l0 = _lib.LAUNCHES[0]
+            t0.record(st)
+            for _ in range(args.steps):
+                e = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                ps, out = step(arm == "warm", e)
+                kev.append(e)
+            t1.record(st)
+            torch.cuda.synchronize()
+            ms = t0.elapsed_time(t1) / args.steps
+            kms = statistics.mean(a.elapsed_time(b) for a, b in kev)
+            nit = out[3].cpu().numpy().astype(np.int64)
+            stt = out[2].cpu().numpy()
+            err = out[4].cpu().numpy()
+            L = ps.layout
+            passes = (nit + 2) + (nit + 1)  # column passes incl. the final check pass, row passes
+            alg = float((passes * L.rows_np * L.ldm_np * 4).sum())
+            res[arm] = {"ms": ms, "kernel_ms": kms, "alg_bytes": alg, "niter_mean": float(nit.mean()),
+                        "niter_max": int(nit.max()), "converged": int((stt == 0).sum()),
+                        "max_err": float(err.max()), "launches": (_lib.LAUNCHES[0] - l0) // args.steps}
+    w, p = res["warm"], res["plain"]
+    achieved = p["alg_bytes"] / (p["kernel_ms"] * 1e-3) / 1e9
+    # e2e through the public entry point with host clouds
+    Xh, Yh = X.cpu().numpy(), Y.cpu().numpy()
+    e2e_steps = max(1, min(args.steps, 3))
     torch.cuda.synchronize()
     t = time.perf_counter()
-    e2e_steps = max(1, min(args.steps, 3))
     for _ in range(e2e_steps):
-        Pout = pg.sinkhorn_log(af, bf, Mf, reg, numItermax=10000, stopThr=stop)
+        lu, lv, ni = wp.solve_cloud_pairs(Xh, Yh, WS_REG, WS_TOL, warm=True, net=net)
     e2e_s = (time.perf_counter() - t) / e2e_steps
     return {
-        "value": 1000.0 / ms, "unit": "solves/s", "ms_per_step": ms, "dtype": "f32",
-        "config": {"workload": "dense_log_sinkhorn n=m=%d R^2 gauss, reg=0.05, stopThr=1e-6" % n,
-                   "iterations": iters, "l2": "inputs larger than L2 (M = %.2f GiB)" % (n * n * 4 / 2**30)},
+        "value": B / (w["ms"] * 1e-3), "unit": "solves/s", "ms_per_step": w["ms"], "dtype": "f32",
+        "plain": {"value": B / (p["ms"] * 1e-3), "ms_per_step": p["ms"], "niter_mean": p["niter_mean"],
+                  "niter_max": p["niter_max"], "converged": p["converged"], "max_marginal_err": p["max_err"]},
+        "warm": {"niter_mean": w["niter_mean"], "niter_max": w["niter_max"], "converged": w["converged"],
+                 "max_marginal_err": w["max_err"]},
+        "speedup_warm_vs_plain": p["ms"] / w["ms"],
+        "config": {"workload": "learned warm start vs plain log-Sinkhorn, %d GMM cloud pairs n=m=%d d=%d, "
+                               "reg=%.2f x max cost, stopThr=%g, float32" % (B, WS_N, WS_D, WS_REG, WS_TOL),
+                   "pairs_per_step": B, "l2": "inputs larger than L2 (%.1f GiB of cost blocks)" % (
+                       B * WS_N * WS_N * 4 / 2**30),
+                   "held_out_seeds": [EVAL_SEED, EVAL_SEED + B - 1]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "traffic": None,
-                     "kernel": "dense_sinkhorn_kernel", "alg_bytes_per_launch": alg_bytes,
-                     "peak_src": pk["src"]},
-        "e2e": {"value": 1.0 / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(Mf.nbytes + af.nbytes + bf.nbytes),
-                "d2h_bytes_per_step": int(Pout.nbytes)},
-        "gpu_launches": 2 * args.steps,
+                     "frac": achieved / pk["hbm_gbs"], "traffic": None, "kernel": "multi_sinkhorn_kernel (plain arm)",
+                     "alg_bytes_per_launch": p["alg_bytes"], "launch_ms": p["kernel_ms"],
+                     "peak_src": pk["src"] + " (of measured)" if pk["src"] == "measured" else pk["src"]},
+        "e2e": {"value": B / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(Xh.nbytes + Yh.nbytes),
+                "d2h_bytes_per_step": int(lu.nbytes + lv.nbytes + ni.nbytes)},
+        "gpu_launches": int(w["launches"] * args.steps),
         "clocks": cs.summary(),
-        "_sample": (a, b, M, reg, stop, iters),
     }
 
 
-def cpu_dense_baseline(a, b, M, reg, stop, gpu_iters, budget_s=15.0):
-    """Time oracle log-Sinkhorn iterations on a bounded sample and scale to one
-    full solve with the iteration count the GPU needed."""
+def _oracle_pair_solve(args):
+    """One float64 oracle solve of a workload pair (run in a worker process)."""
+    x, y = args
     import oracle
+    M = oracle.sqeuclidean(x, y)
+    reg = WS_REG * M.max()
     t = time.perf_counter()
-    k = 0
-    while True:
-        oracle.sinkhorn_log(a, b, M, reg, numItermax=1, stopThr=0.0)
-        k += 1
-        if time.perf_counter() - t > budget_s or k >= 3:
-            break
-    per_iter = (time.perf_counter() - t) / k
-    per_solve = per_iter * gpu_iters
-    return {"value": 1.0 / per_solve, "unit": "solves/s", "cores": 1, "kind": "port",
-            "sample": "%d single-iteration oracle solves (n=%d, float64) scaled to %d iterations" % (k, len(a), gpu_iters)}
+    _, lg = oracle.sinkhorn_log([], [], M, reg, numItermax=100000, stopThr=WS_TOL)
+    return time.perf_counter() - t, lg["niter"]
+
+
+def cpu_pairs(count, seed):
+    import torch
+    from pot_gb300.warmstart import pipeline as wp
+    X, Y = wp.gen_pairs(seed, count, WS_N, WS_D, torch.device("cpu"))
+    return X.double().numpy(), Y.double().numpy()
+
+
+def cpu_baseline(cores, sample):
+    """Reference CPU algorithm (oracle sinkhorn_log, float64) over `sample`
+    pairs of the workload, `cores` worker processes; solves/s."""
+    import multiprocessing as mp
+    X, Y = cpu_pairs(sample, EVAL_SEED)
+    t = time.perf_counter()
+    if cores > 1:
+        with mp.get_context("spawn").Pool(cores) as pool:
+            out = pool.map(_oracle_pair_solve, [(X[k], Y[k]) for k in range(sample)])
+    else:
+        out = [_oracle_pair_solve((X[k], Y[k])) for k in range(sample)]
+    wall = time.perf_counter() - t
+    return {"value": sample / wall, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": "%d workload pairs (float64 numpy sinkhorn_log restatement, zero init), mean niter %.1f"
+                      % (sample, float(np.mean([o[1] for o in out])))}
 
 
 def main():
@@ -196,8 +214,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="dense")
-    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--workload", default="warmstart")
+    ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -205,24 +223,25 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        a, b, M = make_dense(args.n)
-        cb = cpu_dense_baseline(a, b, M, 0.05, 1e-6, 1000, budget_s=20.0)
+        cores = os.cpu_count() or 1
+        cb = cpu_baseline(cores, max(cores, 4))
         line = {"metric": METRIC, "value": cb["value"], "unit": "solves/s", "impl": "reference",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                 "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "dense_log_sinkhorn n=m=%d" % args.n},
+                "config": {"workload": "plain log-Sinkhorn (reference CPU algorithm), GMM cloud pairs n=m=%d d=%d, "
+                                       "reg=%.2f x max cost, stopThr=%g" % (WS_N, WS_D, WS_REG, WS_TOL)},
                 "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "solves/s",
                                             "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
     pk = peaks()
-    res = run_dense(args, pk)
-    a, b, M, reg, stop, iters = res.pop("_sample")
+    res = run_warmstart(args, pk)
     line = {"metric": METRIC, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic"}
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "data": "synthetic (seeded Gaussian-mixture clouds generated on the device)"}
     line.update(res)
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_dense_baseline(a, b, M, reg, stop, iters)
+        line["cpu_baseline"] = cpu_baseline(1, 3)
     if rank == 0:
         print(json.dumps(line))
 

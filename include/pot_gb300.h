@@ -135,6 +135,49 @@ int otg_batch_limits(int dtype, int32_t* max_rows, int32_t* max_cols, int32_t* r
 int otg_sinkhorn_batched(const OtgBatchProblem* q, cudaStream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Work-balanced batched log-domain Sinkhorn: all SMs work on every active
+ * problem in every half-step (one persistent cooperative launch); problems
+ * leave the active set as they converge.  Per problem the order and stop
+ * test of ot/bregman/_sinkhorn.py:880-899 (sinkhorn_log).  Same packed
+ * layout as otg_sinkhorn_batched; nsr_max[p] (>= 1) bounds the row split of
+ * problem p's column reductions and pc_off[p] places its nsr_max[p] x cols[p]
+ * partial pairs (total_partials in all).  The workspace size comes from
+ * otg_multi_workspace_bytes.
+ * ---------------------------------------------------------------------- */
+typedef struct OtgMultiProblem {
+  int32_t dtype;
+  int32_t nprob;
+  const void* M;
+  const int64_t* m_off;
+  const int32_t* rows;
+  const int32_t* cols;
+  const int32_t* ldm;
+  const int64_t* r_off;
+  const int64_t* c_off;
+  const void* a;
+  const void* b;
+  const void* warm_u;   /* natural-log source warm start or NULL */
+  const double* reg;
+  int32_t max_iter;
+  int32_t grid;
+  double stop_thr;
+  const int32_t* nsr_max;
+  const int64_t* pc_off;
+  int64_t total_rows, total_cols, total_partials;
+  void* out_u;
+  void* out_v;
+  int32_t* status;
+  int32_t* niter;
+  double* err;
+  void* workspace;
+  size_t workspace_bytes;
+  int32_t timeout_ms;
+} OtgMultiProblem;
+size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, int64_t total_cols,
+                                 int64_t total_partials);
+int otg_sinkhorn_multi(const OtgMultiProblem* q, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
  * Squared-Euclidean cost blocks for a table of point-cloud pairs:
  * M_p[i, j] = sum_k (X_p[i, k] - Y_p[j, k])^2 for j < cols[p]; padded
  * columns [cols[p], ldm[p]) are set to +inf.  max_out (optional, one value
@@ -173,6 +216,41 @@ typedef struct OtgPlanTable {
   double* out_vals;
 } OtgPlanTable;
 int otg_batched_plan(const OtgPlanTable* t, int32_t max_rows, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Learned warm start: kernels of the point-cloud network's forward, backward
+ * and AdamW step.  No counterpart in the reference (the network feeds the
+ * warmstart argument of ot/bregman/_sinkhorn.py:864-868).  All fp32.
+ * ---------------------------------------------------------------------- */
+/* Soft-min distances of every source point of every problem to its target
+ * measure, at ntau (<= 8) temperatures relative to scale[p]:
+ * out[(r_off[p]+i)*ntau + k] = -tau_k ln sum_j b_j exp(g_j - M_ij / (scale[p] tau_k)).
+ * g (natural-log target potentials packed like b) may be NULL (zero
+ * potential).  f32 problem table as for otg_sinkhorn_batched. */
+int otg_softmin_features(const float* M, const int64_t* m_off, const int32_t* rows, const int32_t* cols,
+                         const int32_t* ldm, const int64_t* r_off, const int64_t* c_off, const float* b,
+                         const float* scale, const float* taus, int32_t ntau, int32_t nprob, int32_t max_rows,
+                         const float* g, float* out, cudaStream_t stream);
+/* C = alpha op(A) op(B) + beta C (+ bias[N]) (ReLU if relu); op(A) M x K
+ * stored [M,K] (ta=0) or [K,M] (ta=1); op(B) K x N stored [K,N] or [N,K]. */
+int otg_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
+                 const float* B, int64_t ldb, float beta, float* C, int64_t ldc, const float* bias, int relu,
+                 cudaStream_t stream);
+int otg_mlp_relu_bwd(float* dY, const float* Y, int64_t n, cudaStream_t stream);
+int otg_mlp_colsum(const float* X, int64_t R, int64_t C, float* out, cudaStream_t stream);
+int otg_mlp_segment_mean(const float* X, int64_t P, int64_t n, int64_t C, float* out, cudaStream_t stream);
+int otg_mlp_segment_mean_bwd(const float* dS, int64_t P, int64_t n, int64_t C, float* dX, int accumulate,
+                             cudaStream_t stream);
+int otg_mlp_concat3(const float* x, const float* sx, const float* sy, int64_t P, int64_t n, int64_t d, int64_t H,
+                    float* z, cudaStream_t stream);
+int otg_mlp_concat3_bwd(const float* dz, int64_t P, int64_t n, int64_t d, int64_t H, float* dsx, float* dsy,
+                        cudaStream_t stream);
+/* loss (fp64, device) = mean over P segments of sum_r ((f - mean f) - t)^2 / n;
+ * df = its gradient. */
+int otg_mlp_centered_mse(const float* f, const float* t, int64_t P, int64_t n, double* loss, float* df,
+                         cudaStream_t stream);
+int otg_mlp_adamw(float* w, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,
+                  float wd, int step, cudaStream_t stream);
 
 /* ------------------------------------------------------------------------
  * Allocation-free variant of otg_sinkhorn_dense.  No counterpart in the

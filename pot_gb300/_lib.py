@@ -37,6 +37,15 @@ class OtgBatchProblem(ctypes.Structure):
                 ("queue", c_vp), ("timeout_ms", c_i32)]
 
 
+class OtgMultiProblem(ctypes.Structure):
+    _fields_ = [("dtype", c_i32), ("nprob", c_i32), ("M", c_vp), ("m_off", c_vp), ("rows", c_vp), ("cols", c_vp),
+                ("ldm", c_vp), ("r_off", c_vp), ("c_off", c_vp), ("a", c_vp), ("b", c_vp), ("warm_u", c_vp),
+                ("reg", c_vp), ("max_iter", c_i32), ("grid", c_i32), ("stop_thr", c_dbl), ("nsr_max", c_vp),
+                ("pc_off", c_vp), ("total_rows", c_i64), ("total_cols", c_i64), ("total_partials", c_i64),
+                ("out_u", c_vp), ("out_v", c_vp), ("status", c_vp), ("niter", c_vp), ("err", c_vp),
+                ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32)]
+
+
 class OtgCostTable(ctypes.Structure):
     _fields_ = [("dtype", c_i32), ("nprob", c_i32), ("X", c_vp), ("Y", c_vp), ("x_off", c_vp), ("y_off", c_vp),
                 ("rows", c_vp), ("cols", c_vp), ("dim", c_vp), ("max_dim", c_i32), ("M", c_vp), ("m_off", c_vp),
@@ -60,8 +69,23 @@ SIGNATURES = {
     "otg_batch_limits": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
                                         ctypes.POINTER(c_i32)]),
     "otg_sinkhorn_batched": (ctypes.c_int, [ctypes.POINTER(OtgBatchProblem), c_vp]),
+    "otg_multi_workspace_bytes": (c_sz, [ctypes.c_int, c_i32, c_i64, c_i64, c_i64]),
+    "otg_sinkhorn_multi": (ctypes.c_int, [ctypes.POINTER(OtgMultiProblem), c_vp]),
     "otg_batched_sqdist": (ctypes.c_int, [ctypes.POINTER(OtgCostTable), c_i32, c_vp]),
     "otg_batched_plan": (ctypes.c_int, [ctypes.POINTER(OtgPlanTable), c_i32, c_vp]),
+    "otg_softmin_features": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32,
+                                            c_i32, c_vp, c_vp, c_vp]),
+    "otg_gemm_f32": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, ctypes.c_float, c_vp, c_i64,
+                                    c_vp, c_i64, ctypes.c_float, c_vp, c_i64, c_vp, ctypes.c_int, c_vp]),
+    "otg_mlp_relu_bwd": (ctypes.c_int, [c_vp, c_vp, c_i64, c_vp]),
+    "otg_mlp_colsum": (ctypes.c_int, [c_vp, c_i64, c_i64, c_vp, c_vp]),
+    "otg_mlp_segment_mean": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, c_vp]),
+    "otg_mlp_segment_mean_bwd": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, ctypes.c_int, c_vp]),
+    "otg_mlp_concat3": (ctypes.c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp]),
+    "otg_mlp_concat3_bwd": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_vp]),
+    "otg_mlp_centered_mse": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp]),
+    "otg_mlp_adamw": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                     ctypes.c_float, ctypes.c_float, ctypes.c_int, c_vp]),
 }
 
 _lib = None
@@ -90,7 +114,11 @@ def load(build_if_missing=True):
     return lib
 
 
+LAUNCHES = [0]  # C-ABI calls that launched kernels (each call launches its own kernels)
+
+
 def check(rc, what):
+    LAUNCHES[0] += 1
     if rc != 0:
         raise RuntimeError("%s failed: %s (code %d)" % (what, _ERRORS.get(rc, "error"), rc))
 

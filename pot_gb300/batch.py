@@ -119,6 +119,48 @@ def run_batched(layout, M_packed, a_packed, b_packed, reg, method, max_iter, tol
     return out_u, out_v, status, niter, err, reg_t
 
 
+def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
+              events=None):
+    """Work-balanced persistent launch (csrc/multi.cu), log form, per-problem
+    sinkhorn_log order and stop test.  Returns (u, v, status, niter, err, reg)."""
+    lib = _lib.load()
+    dev, dt = layout.device, layout.dtype
+    B = layout.B
+    reg_t = torch.as_tensor(reg, dtype=torch.float64, device=dev).reshape(-1)
+    if reg_t.numel() == 1:
+        reg_t = reg_t.expand(B).contiguous()
+    if not hasattr(layout, "pc_off"):
+        nsr_max = np.maximum(1, np.minimum(64, (layout.rows_np + 15) // 16)).astype(np.int32)
+        sizes = nsr_max.astype(np.int64) * layout.cols_np
+        layout.nsr_max_np = nsr_max
+        layout.total_partials = int(sizes.sum())
+        layout.nsr_max = torch.tensor(nsr_max, dtype=torch.int32, device=dev)
+        layout.pc_off = torch.tensor(np.concatenate([[0], np.cumsum(sizes)[:-1]]), dtype=torch.int64, device=dev)
+    dcode = _lib.dtype_code(dt)
+    wsb = lib.otg_multi_workspace_bytes(dcode, B, layout.total_r, layout.total_c, layout.total_partials)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    out_u = torch.empty(layout.total_r, dtype=dt, device=dev)
+    out_v = torch.empty(layout.total_c, dtype=dt, device=dev)
+    status = torch.empty(B, dtype=torch.int32, device=dev)
+    niter = torch.empty(B, dtype=torch.int32, device=dev)
+    err = torch.empty(B, dtype=torch.float64, device=dev)
+    q = _lib.OtgMultiProblem(
+        dtype=dcode, nprob=B, M=M_packed.data_ptr(), m_off=layout.m_off.data_ptr(), rows=layout.rows.data_ptr(),
+        cols=layout.cols.data_ptr(), ldm=layout.ldm.data_ptr(), r_off=layout.r_off.data_ptr(),
+        c_off=layout.c_off.data_ptr(), a=a_packed.data_ptr(), b=b_packed.data_ptr(),
+        warm_u=warm_u.data_ptr() if warm_u is not None else None, reg=reg_t.data_ptr(), max_iter=int(max_iter),
+        grid=int(grid), stop_thr=float(tol), nsr_max=layout.nsr_max.data_ptr(), pc_off=layout.pc_off.data_ptr(),
+        total_rows=layout.total_r, total_cols=layout.total_c, total_partials=layout.total_partials,
+        out_u=out_u.data_ptr(), out_v=out_v.data_ptr(), status=status.data_ptr(), niter=niter.data_ptr(),
+        err=err.data_ptr(), workspace=ws.data_ptr(), workspace_bytes=wsb, timeout_ms=int(timeout_ms))
+    if events is not None:
+        events[0].record()
+    _lib.check(lib.otg_sinkhorn_multi(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_multi")
+    if events is not None:
+        events[1].record()
+    return out_u, out_v, status, niter, err, reg_t
+
+
 def batched_plan(layout, M_packed, u, v, a_packed, b_packed, reg_t, method, kl=False, want_plan=True):
     """Plans (packed like M) and per-problem (value_linear, reg term, mass)."""
     lib = _lib.load()
@@ -285,7 +327,7 @@ class RaggedResult:
 
 
 def solve_sample_ragged(Xs, Ys, reg, as_=None, bs=None, reg_relative=False, max_iter=100000, tol=1e-6,
-                        method="sinkhorn_log", warmstart=None, dtype=torch.float32, device=None):
+                        method="sinkhorn_log", warmstart=None, dtype=torch.float32, device=None, engine="multi"):
     """Entropic OT between B point-cloud pairs of uneven sizes and dims, in
     one persistent launch.  ``reg`` is a scalar or one value per problem; with
     ``reg_relative`` it multiplies each problem's largest cost.  Per problem
@@ -315,6 +357,9 @@ def solve_sample_ragged(Xs, Ys, reg, as_=None, bs=None, reg_relative=False, max_
     wu = wv = None
     if warmstart is not None:
         wu, wv = warmstart
-    u, v, status, niter, err, reg_t = run_batched(layout, M, ap, bp, reg_t, code, max_iter, tol, u_first=0,
-                                                  warm_u=wu, warm_v=wv)
+    if engine == "multi" and code == _lib.OTG_METHOD_LOG:
+        u, v, status, niter, err, reg_t = run_multi(layout, M, ap, bp, reg_t, max_iter, tol, warm_u=wu)
+    else:
+        u, v, status, niter, err, reg_t = run_batched(layout, M, ap, bp, reg_t, code, max_iter, tol, u_first=0,
+                                                      warm_u=wu, warm_v=wv)
     return RaggedResult(layout, u, v, status, niter, err, reg_t, M)

@@ -100,6 +100,59 @@ __global__ void __launch_bounds__(256) batched_plan_kernel(OtgPlanTable t) {
   }
 }
 
+// Soft-min distances of every source point to the target measure at several
+// temperatures, in units of the problem's cost scale:
+//   out[r_off[p] + i, k] = -tau_k * ln sum_j b_j exp(g_j - M_ij / (scale_p tau_k)).
+// With g = 0 these are c-transforms of the zero potential; with g the
+// (natural-log) target potential of a solved problem on the same target
+// points and tau = reg/scale, it is that potential's c-transform, i.e. the
+// log-domain row update.  One warp per row, all temperatures in one pass.
+constexpr int SM_MAXTAU = 8;
+__global__ void __launch_bounds__(256) softmin_features_kernel(const float* __restrict__ Mall, const int64_t* m_off,
+                                                               const int32_t* rows, const int32_t* cols,
+                                                               const int32_t* ldms, const int64_t* r_off,
+                                                               const int64_t* c_off, const float* __restrict__ ball,
+                                                               const float* scale, const float* taus, int ntau,
+                                                               int nprob, const float* __restrict__ gall,
+                                                               float* out) {
+  const int p = blockIdx.y;
+  if (p >= nprob) return;
+  const int n = rows[p], m = cols[p], ldm = ldms[p];
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= n) return;
+  const float* Mrow = Mall + m_off[p] + (int64_t)row * ldm;
+  const float* b = ball + c_off[p];
+  const float* g = gall ? gall + c_off[p] : nullptr;
+  float ck[SM_MAXTAU], mx[SM_MAXTAU], s[SM_MAXTAU];
+#pragma unroll
+  for (int k = 0; k < SM_MAXTAU; ++k) {
+    ck[k] = k < ntau ? -(float)OTG_LOG2E / (scale[p] * taus[k]) : 0.f;
+    mx[k] = -INFINITY;
+    s[k] = 0.f;
+  }
+  for (int j = lane; j < m; j += 32) {
+    const float x = Mrow[j];
+    const float lb = lg2(b[j]) + (g ? g[j] * (float)OTG_LOG2E : 0.f);
+#pragma unroll
+    for (int k = 0; k < SM_MAXTAU; ++k) {
+      if (k < ntau) {
+        const float t = fmaf(x, ck[k], lb);
+        const float nm = fmaxf(mx[k], t);
+        s[k] = s[k] * ex2(mx[k] - nm) + ex2(t - nm);
+        mx[k] = nm;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < SM_MAXTAU; ++k) {
+    if (k < ntau) {
+      warp_lse(mx[k], s[k]);
+      if (lane == 0) out[(r_off[p] + row) * ntau + k] = -taus[k] * (float)OTG_LN2 * lse_value(mx[k], s[k]);
+    }
+  }
+}
+
 }  // namespace otg
 
 using namespace otg;
@@ -141,6 +194,18 @@ int otg_batched_plan(const OtgPlanTable* t, int32_t max_rows, cudaStream_t strea
   } else {
     return OTG_ERR_DTYPE;
   }
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_softmin_features(const float* M, const int64_t* m_off, const int32_t* rows, const int32_t* cols,
+                         const int32_t* ldm, const int64_t* r_off, const int64_t* c_off, const float* b,
+                         const float* scale, const float* taus, int32_t ntau, int32_t nprob, int32_t max_rows,
+                         const float* g, float* out, cudaStream_t stream) {
+  if (!M || !m_off || !rows || !cols || !ldm || !r_off || !c_off || !b || !scale || !taus || !out) return OTG_ERR_ARG;
+  if (ntau < 1 || ntau > SM_MAXTAU || nprob < 1 || nprob > 65535 || max_rows < 1) return OTG_ERR_ARG;
+  dim3 grid((unsigned)((max_rows + 7) / 8), (unsigned)nprob);
+  softmin_features_kernel<<<grid, 256, 0, stream>>>(M, m_off, rows, cols, ldm, r_off, c_off, b, scale, taus, ntau,
+                                                    nprob, g, out);
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 

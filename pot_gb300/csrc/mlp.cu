@@ -1,0 +1,273 @@
+// Kernels of the learned warm-start network (forward, backward, AdamW).
+//
+// The network (no counterpart in the reference) maps a cloud pair (X, Y) to a
+// source potential f: per-point encoders phi_X, phi_Y, mean pooling into
+// summaries s_X, s_Y, and a per-point head psi([x_i, s_X, s_Y]).  Its layers
+// are dense GEMMs of a few hundred columns over B*n rows; they run as a tiled
+// fp32 GEMM with fused bias and ReLU.  All training arithmetic is fp32 except
+// the loss, which is accumulated in fp64.
+#include <algorithm>
+#include "common.cuh"
+#include "../../include/pot_gb300.h"
+
+namespace otg {
+
+constexpr int GT = 64;      // output tile
+constexpr int GK = 16;      // k tile
+
+// C = alpha * op(A) * op(B) + beta * C (+ bias, ReLU).  op(A) is M x K, op(B)
+// is K x N; ta / tb select the transposed storage of A ([K, M]) / B ([N, K]).
+__global__ void __launch_bounds__(256) gemm_f32_kernel(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha,
+                                                       const float* __restrict__ A, int64_t lda,
+                                                       const float* __restrict__ B, int64_t ldb, float beta,
+                                                       float* __restrict__ C, int64_t ldc,
+                                                       const float* __restrict__ bias, int relu) {
+  __shared__ float As[GK][GT + 4];
+  __shared__ float Bs[GK][GT + 4];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t m0 = (int64_t)blockIdx.y * GT, n0 = (int64_t)blockIdx.x * GT;
+  // split-K: CTA z covers k in [kbeg, kend) and adds its partial product
+  const int64_t kper = ((K + gridDim.z - 1) / gridDim.z + GK - 1) / GK * GK;
+  const int64_t kbeg = (int64_t)blockIdx.z * kper, kend = min(K, kbeg + kper);
+  const bool split = gridDim.z > 1;
+  float acc[4][4] = {};
+  for (int64_t k0 = kbeg; k0 < kend; k0 += GK) {
+    // load A tile (GT x GK) into As[k][m]
+    for (int e = threadIdx.x; e < GT * GK; e += 256) {
+      int mm, kk;
+      if (ta) { kk = e / GT; mm = e % GT; } else { mm = e / GK; kk = e % GK; }
+      const int64_t gm = m0 + mm, gk = k0 + kk;
+      float val = 0.f;
+      if (gm < M && gk < kend) val = ta ? A[gk * lda + gm] : A[gm * lda + gk];
+      As[kk][mm] = val;
+    }
+    for (int e = threadIdx.x; e < GT * GK; e += 256) {
+      int nn, kk;
+      if (tb) { nn = e / GK; kk = e % GK; } else { kk = e / GT; nn = e % GT; }
+      const int64_t gn = n0 + nn, gk = k0 + kk;
+      float val = 0.f;
+      if (gn < N && gk < kend) val = tb ? B[gn * ldb + gk] : B[gk * ldb + gn];
+      Bs[kk][nn] = val;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GK; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t gm = m0 + ty * 4 + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t gn = n0 + tx * 4 + j;
+      if (gn >= N) continue;
+      float r = alpha * acc[i][j];
+      if (split) { atomicAdd(C + gm * ldc + gn, r); continue; }  // C zeroed, no bias/act
+      if (beta != 0.f) r += beta * C[gm * ldc + gn];
+      if (bias) r += bias[gn];
+      if (relu) r = fmaxf(r, 0.f);
+      C[gm * ldc + gn] = r;
+    }
+  }
+}
+
+// dY *= (Y > 0)
+__global__ void relu_bwd_kernel(float* dY, const float* Y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!(Y[i] > 0.f)) dY[i] = 0.f;
+}
+
+// out[c] (+)= sum_r X[r, c]  (bias gradients), X is R x C row-major.
+__global__ void colsum_kernel(const float* X, int64_t R, int64_t C, float* out, int accumulate) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  float s = 0.f;
+  for (int64_t r = blockIdx.y; r < R; r += gridDim.y) s += X[r * C + c];
+  atomicAdd(out + c, s);
+  (void)accumulate;
+}
+
+// Segment mean: out[p, c] = mean_{r in segment p} X[p*n + r, c].
+__global__ void segment_mean_kernel(const float* X, int64_t P, int64_t n, int64_t C, float* out) {
+  const int64_t p = blockIdx.y;
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= C || p >= P) return;
+  float s = 0.f;
+  for (int64_t r = 0; r < n; ++r) s += X[(p * n + r) * C + c];
+  out[p * C + c] = s / (float)n;
+}
+
+// Backward of the segment mean: dX[p*n + r, c] (+)= dS[p, c] / n.
+__global__ void segment_mean_bwd_kernel(const float* dS, int64_t P, int64_t n, int64_t C, float* dX, int accumulate) {
+  const int64_t total = P * n * C;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e % C, row = e / C, p = row / n;
+    const float g = dS[p * C + c] / (float)n;
+    dX[e] = accumulate ? dX[e] + g : g;
+  }
+}
+
+// z[p*n + r] = [x (d), sx[p] (H), sy[p] (H)]
+__global__ void concat3_kernel(const float* x, const float* sx, const float* sy, int64_t P, int64_t n, int64_t d,
+                               int64_t H, float* z) {
+  const int64_t W = d + 2 * H;
+  const int64_t total = P * n * W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e % W, row = e / W, p = row / n;
+    float val;
+    if (c < d) val = x[row * d + c];
+    else if (c < d + H) val = sx[p * H + (c - d)];
+    else val = sy[p * H + (c - d - H)];
+    z[e] = val;
+  }
+}
+
+// Backward of concat3 for the summaries: dsx[p, h] = sum_r dz[p*n+r, d+h], same for dsy.
+__global__ void concat3_bwd_kernel(const float* dz, int64_t P, int64_t n, int64_t d, int64_t H, float* dsx, float* dsy) {
+  const int64_t p = blockIdx.y;
+  const int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (h >= 2 * H || p >= P) return;
+  const int64_t W = d + 2 * H;
+  float s = 0.f;
+  for (int64_t r = 0; r < n; ++r) s += dz[(p * n + r) * W + d + h];
+  if (h < H) dsx[p * H + h] = s;
+  else dsy[p * H + (h - H)] = s;
+}
+
+// Gauge-free loss: per segment, e = (f - mean f) - t (targets already centred);
+// loss += sum e^2 / (P n); df = 2 (e - mean e) / (P n).
+__global__ void centered_mse_kernel(const float* f, const float* t, int64_t P, int64_t n, double* loss, float* df) {
+  const int64_t p = blockIdx.x;
+  __shared__ double red[32];
+  __shared__ float s_mean_f, s_mean_e;
+  double s = 0;
+  for (int64_t r = threadIdx.x; r < n; r += blockDim.x) s += f[p * n + r];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) { double q = 0; for (int w = 0; w < (int)(blockDim.x >> 5); ++w) q += red[w]; s_mean_f = (float)(q / n); }
+  __syncthreads();
+  const float mf = s_mean_f;
+  double se = 0, se2 = 0;
+  for (int64_t r = threadIdx.x; r < n; r += blockDim.x) {
+    const float e = (f[p * n + r] - mf) - t[p * n + r];
+    se += e; se2 += (double)e * e;
+  }
+  se = warp_sum(se); se2 = warp_sum(se2);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = se;
+  __syncthreads();
+  if (threadIdx.x == 0) { double q = 0; for (int w = 0; w < (int)(blockDim.x >> 5); ++w) q += red[w]; s_mean_e = (float)(q / n); }
+  __syncthreads();
+  const double scale = 1.0 / ((double)P * (double)n);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, se2 * scale);
+  const float me = s_mean_e;
+  for (int64_t r = threadIdx.x; r < n; r += blockDim.x) {
+    const float e = (f[p * n + r] - mf) - t[p * n + r];
+    df[p * n + r] = (float)(2.0 * scale) * (e - me);
+  }
+}
+
+// AdamW (decoupled weight decay), bias-corrected.
+__global__ void adamw_kernel(float* w, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2,
+                             float eps, float wd, float bc1, float bc2) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi; v[i] = vi;
+    const float mh = mi / bc1, vh = vi / bc2;
+    w[i] = w[i] - lr * (mh / (sqrtf(vh) + eps) + wd * w[i]);
+  }
+}
+
+inline int blocks_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 152 * 16); }
+
+}  // namespace otg
+
+using namespace otg;
+
+extern "C" {
+
+int otg_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
+                 const float* B, int64_t ldb, float beta, float* C, int64_t ldc, const float* bias, int relu,
+                 cudaStream_t stream) {
+  if (M < 1 || N < 1 || K < 1 || !A || !B || !C) return OTG_ERR_ARG;
+  if ((M + GT - 1) / GT > 65535) return OTG_ERR_UNSUPPORTED;
+  const int64_t tiles = ((N + GT - 1) / GT) * ((M + GT - 1) / GT);
+  int64_t splits = 1;
+  // few output tiles and a long K (weight gradients over many rows): split K
+  if (tiles < 304 && K >= 4096 && beta == 0.f && !bias && !relu) splits = std::min<int64_t>(K / 1024, 608 / tiles + 1);
+  if (splits > 1 && ldc != N) splits = 1;  // split-K accumulates into a zeroed, dense C
+  if (splits > 1 && cudaMemsetAsync(C, 0, sizeof(float) * M * N, stream) != cudaSuccess) return OTG_ERR_CUDA;
+  dim3 grid((unsigned)((N + GT - 1) / GT), (unsigned)((M + GT - 1) / GT), (unsigned)splits);
+  gemm_f32_kernel<<<grid, 256, 0, stream>>>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, bias, relu);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_relu_bwd(float* dY, const float* Y, int64_t n, cudaStream_t stream) {
+  relu_bwd_kernel<<<blocks_for(n), 256, 0, stream>>>(dY, Y, n);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_colsum(const float* X, int64_t R, int64_t C, float* out, cudaStream_t stream) {
+  if (cudaMemsetAsync(out, 0, sizeof(float) * C, stream) != cudaSuccess) return OTG_ERR_CUDA;
+  dim3 grid((unsigned)((C + 127) / 128), (unsigned)std::min<int64_t>(R, 256));
+  colsum_kernel<<<grid, 128, 0, stream>>>(X, R, C, out, 1);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_segment_mean(const float* X, int64_t P, int64_t n, int64_t C, float* out, cudaStream_t stream) {
+  if (P > 65535) return OTG_ERR_UNSUPPORTED;
+  dim3 grid((unsigned)((C + 127) / 128), (unsigned)P);
+  segment_mean_kernel<<<grid, 128, 0, stream>>>(X, P, n, C, out);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_segment_mean_bwd(const float* dS, int64_t P, int64_t n, int64_t C, float* dX, int accumulate,
+                             cudaStream_t stream) {
+  segment_mean_bwd_kernel<<<blocks_for(P * n * C), 256, 0, stream>>>(dS, P, n, C, dX, accumulate);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_concat3(const float* x, const float* sx, const float* sy, int64_t P, int64_t n, int64_t d, int64_t H,
+                    float* z, cudaStream_t stream) {
+  concat3_kernel<<<blocks_for(P * n * (d + 2 * H)), 256, 0, stream>>>(x, sx, sy, P, n, d, H, z);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_concat3_bwd(const float* dz, int64_t P, int64_t n, int64_t d, int64_t H, float* dsx, float* dsy,
+                        cudaStream_t stream) {
+  if (P > 65535) return OTG_ERR_UNSUPPORTED;
+  dim3 grid((unsigned)((2 * H + 127) / 128), (unsigned)P);
+  concat3_bwd_kernel<<<grid, 128, 0, stream>>>(dz, P, n, d, H, dsx, dsy);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_centered_mse(const float* f, const float* t, int64_t P, int64_t n, double* loss, float* df,
+                         cudaStream_t stream) {
+  if (cudaMemsetAsync(loss, 0, sizeof(double), stream) != cudaSuccess) return OTG_ERR_CUDA;
+  centered_mse_kernel<<<(unsigned)P, 256, 0, stream>>>(f, t, P, n, loss, df);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_adamw(float* w, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,
+                  float wd, int step, cudaStream_t stream) {
+  if (step < 1) return OTG_ERR_ARG;
+  const float bc1 = 1.f - powf(b1, (float)step), bc2 = 1.f - powf(b2, (float)step);
+  adamw_kernel<<<blocks_for(n), 256, 0, stream>>>(w, g, m, v, n, lr, b1, b2, eps, wd, bc1, bc2);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,458 @@
+// Work-balanced batched log-domain Sinkhorn: every SM works on every active
+// problem in every half-step, so the time follows the batch's total work and
+// a slow problem is spread over the whole GPU instead of one CTA.
+//
+// Reference behaviour (PythonOT/POT): per problem, the order and stopping test
+// of ot/bregman/_sinkhorn.py:880-899 (sinkhorn_log: v first, then u; L2
+// column-marginal error every 10th iteration); problems stop individually.
+//
+// One persistent cooperative launch.  Each iteration:
+//   column pass : units (problem, row chunk, slab of 32*VW columns) over all
+//                 active problems -> partial (max, sum) per column  | barrier
+//   column merge: per column of every active problem: combine partials, new
+//                 v into the spare buffer, squared marginal error of the
+//                 previous check iteration per problem               | barrier
+//   decision    : (check iterations) converged problems are written out and
+//                 leave the active list                              | barrier
+//   row pass    : units (problem, group of RW rows, column chunk) -> u   | barrier
+// All active problems share the iteration index, so the v buffers swap
+// globally.  Work units map to problems through prefix sums over the active
+// list (binary search).
+#include <algorithm>
+#include "common.cuh"
+#include "../../include/pot_gb300.h"
+
+namespace otg {
+
+constexpr int MT_THREADS = 256;
+constexpr int MT_RW = 4;       // rows per warp in the row pass
+constexpr int MT_GCOL = 4;     // rows folded per max update (column pass)
+
+template <typename T> struct MPair { T mx, s; };
+
+template <typename T>
+struct MultiArgs {
+  const T* M; const int64_t* m_off; const int32_t* rows; const int32_t* cols; const int32_t* ldm;
+  const int64_t* r_off; const int64_t* c_off;
+  const T* a; const T* b; const T* warm_u;
+  const double* reg;
+  int32_t nprob, max_iter;
+  double stop_thr;
+  // per-problem decomposition: partial buffers sized for nsr_max row chunks;
+  // the split in use (nsr, rchunk) is chosen at every rebuild of the active
+  // list from the amount of work left
+  const int32_t* nsr_max;
+  int32_t* nsr;             // row chunks (column pass), device-chosen
+  int32_t* rchunk;          // rows per chunk, device-chosen
+  const int64_t* pc_off;    // offset of problem's partials [nsr_max][m]
+  // state
+  T* u; T* v0; T* v1;       // base-2 potentials, packed like a / b
+  MPair<T>* pcol;
+  double* err2;             // per problem
+  int32_t* active;          // active problem ids [nprob]
+  int64_t* ucol_pre;        // prefix of column-pass units over the active list [nprob+1]
+  int64_t* urow_pre;        // prefix of row-pass units
+  int64_t* colpre;          // prefix of columns (merge) over the active list
+  int32_t* ctl;             // [0] n active, [1] abort
+  unsigned* bar;
+  // outputs
+  T* out_u; T* out_v;
+  int32_t* status; int32_t* niter; double* err;
+  uint64_t timeout_ns;
+};
+
+// Index of the active slot whose prefix range holds `unit` (pre[k] <= unit < pre[k+1]).
+__device__ __forceinline__ int mt_find(const int64_t* pre, int n, int64_t unit) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldcg(pre + mid) <= unit) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <typename T>
+__device__ void mt_col_pass(const MultiArgs<T>& A, int nact, long gwarp, long nwarps, int lane) {
+  constexpr int VW = Vec<T>::N;
+  using V = typename Vec<T>::type;
+  const int64_t total = __ldcg(A.ucol_pre + nact);
+  for (int64_t unit = gwarp; unit < total; unit += nwarps) {
+    const int k = mt_find(A.ucol_pre, nact, unit);
+    const int p = __ldcg(A.active + k);
+    const int64_t local = unit - __ldcg(A.ucol_pre + k);
+    const int n = A.rows[p], m = A.cols[p], ldm = A.ldm[p];
+    const int64_t nslabs = (m + 32 * VW - 1) / (32 * VW);
+    const int64_t slab = local % nslabs, r = local / nslabs;  // r < nsr[p]
+    const int rc = __ldcg(A.rchunk + p);
+    const int i0 = (int)(r * rc), i1 = min(n, i0 + rc);
+    const int j0 = (int)(slab * 32 * VW) + lane * VW;
+    const T* Mp = A.M + A.m_off[p];
+    const T* up = A.u + A.r_off[p];
+    const T c = (T)(-OTG_LOG2E / A.reg[p]);
+    T mx[VW], s[VW];
+#pragma unroll
+    for (int q = 0; q < VW; ++q) { mx[q] = -INFINITY; s[q] = 0; }
+    if (j0 < m) {
+      for (int i = i0; i < i1; i += MT_GCOL) {
+        T x[MT_GCOL][VW], ur[MT_GCOL];
+#pragma unroll
+        for (int g = 0; g < MT_GCOL; ++g) {
+          if (i + g < i1) {
+            unpack(ld_stream(reinterpret_cast<const V*>(Mp + (int64_t)(i + g) * ldm + j0)), x[g]);
+            ur[g] = __ldcg(up + i + g);
+          } else {
+#pragma unroll
+            for (int q = 0; q < VW; ++q) x[g][q] = 0;
+            ur[g] = -INFINITY;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < VW; ++q) {
+          T t[MT_GCOL];
+          T gm = -INFINITY;
+#pragma unroll
+          for (int g = 0; g < MT_GCOL; ++g) { t[g] = fma(x[g][q], c, ur[g]); gm = fmax(gm, t[g]); }
+          const T nm = fmax(mx[q], gm);
+          if (nm != -INFINITY) {
+            T acc = s[q] * ex2(mx[q] - nm);
+#pragma unroll
+            for (int g = 0; g < MT_GCOL; ++g) acc += ex2(t[g] - nm);
+            s[q] = acc;
+            mx[q] = nm;
+          }
+        }
+      }
+      MPair<T>* pc = A.pcol + A.pc_off[p] + r * m;
+#pragma unroll
+      for (int q = 0; q < VW; ++q)
+        if (j0 + q < m) pc[j0 + q] = MPair<T>{mx[q], s[q]};
+    }
+  }
+}
+
+// Column merge over every column of every active problem; per problem the
+// squared marginal error of (u_cur, v_cur) is accumulated when `check`.
+template <typename T>
+__device__ void mt_col_merge(const MultiArgs<T>& A, int nact, const T* vcur, T* vnxt, bool check, bool update,
+                             long gtid, long nthreads) {
+  const int64_t total = __ldcg(A.colpre + nact);
+  for (int64_t e = gtid; e < total; e += nthreads) {
+    const int k = mt_find(A.colpre, nact, e);
+    const int p = __ldcg(A.active + k);
+    const int j = (int)(e - __ldcg(A.colpre + k));
+    const int m = A.cols[p];
+    const MPair<T>* pc = A.pcol + A.pc_off[p];
+    T mx = -INFINITY, s = 0;
+    const int nsr = __ldcg(A.nsr + p);
+    for (int r = 0; r < nsr; ++r) {
+      const T* q = reinterpret_cast<const T*>(pc + (int64_t)r * m + j);
+      lse_merge(mx, s, __ldcg(q), __ldcg(q + 1));
+    }
+    const T L = lse_value(mx, s);
+    const int64_t cj = A.c_off[p] + j;
+    const T bj = A.b[cj];
+    if (check) {
+      double cs = (double)ex2(__ldcg(vcur + cj) + L) - (double)bj;
+      double e2 = cs * cs;
+      // lanes of one problem pre-reduce, one atomic per problem per warp
+      const unsigned act = __activemask();
+      const unsigned same = __match_any_sync(act, p);
+      const int leader = __ffs(same) - 1;
+      for (int o = 16; o > 0; o >>= 1) {
+        const double other = __shfl_down_sync(act, e2, o);
+        const int src_lane = (threadIdx.x & 31) + o;
+        if (src_lane < 32 && ((same >> src_lane) & 1u)) e2 += other;
+      }
+      if ((threadIdx.x & 31) == leader) atomicAdd(A.err2 + p, e2);
+    }
+    if (update) vnxt[cj] = lg2(bj) - L;
+  }
+}
+
+template <typename T>
+__device__ void mt_row_pass(const MultiArgs<T>& A, int nact, const T* v, long gwarp, long nwarps, int lane) {
+  constexpr int VW = Vec<T>::N;
+  using V = typename Vec<T>::type;
+  const int64_t total = __ldcg(A.urow_pre + nact);
+  for (int64_t unit = gwarp; unit < total; unit += nwarps) {
+    const int k = mt_find(A.urow_pre, nact, unit);
+    const int p = __ldcg(A.active + k);
+    const int64_t grp = unit - __ldcg(A.urow_pre + k);
+    const int n = A.rows[p], m = A.cols[p], ldm = A.ldm[p];
+    const int r0 = (int)grp * MT_RW;
+    const T* Mp = A.M + A.m_off[p];
+    const T* vp = v + A.c_off[p];
+    const T c = (T)(-OTG_LOG2E / A.reg[p]);
+    T mx[MT_RW], s[MT_RW];
+#pragma unroll
+    for (int r = 0; r < MT_RW; ++r) { mx[r] = -INFINITY; s[r] = 0; }
+    for (int j = lane * VW; j < m; j += 32 * VW) {
+      T vv[VW];
+      // v beyond m (padding up to ldm) is never read: the vector tail is masked
+#pragma unroll
+      for (int q = 0; q < VW; ++q) vv[q] = (j + q < m) ? __ldcg(vp + j + q) : T(-INFINITY);
+      T x[MT_RW][VW];
+#pragma unroll
+      for (int r = 0; r < MT_RW; ++r) {
+        const int row = min(r0 + r, n - 1);
+        unpack(ld_stream(reinterpret_cast<const V*>(Mp + (int64_t)row * ldm + j)), x[r]);
+      }
+#pragma unroll
+      for (int r = 0; r < MT_RW; ++r) {
+        T t[VW];
+        T gm = -INFINITY;
+#pragma unroll
+        for (int q = 0; q < VW; ++q) { t[q] = fma(x[r][q], c, vv[q]); gm = fmax(gm, t[q]); }
+        const T nm = fmax(mx[r], gm);
+        if (nm != -INFINITY) {
+          T acc = s[r] * ex2(mx[r] - nm);
+#pragma unroll
+          for (int q = 0; q < VW; ++q) acc += ex2(t[q] - nm);
+          s[r] = acc;
+          mx[r] = nm;
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < MT_RW; ++r) warp_lse(mx[r], s[r]);
+#pragma unroll
+    for (int r = 0; r < MT_RW; ++r) {
+      if (lane == r && r0 + r < n) {
+        const int64_t ri = A.r_off[p] + r0 + r;
+        A.u[ri] = lg2(A.a[ri]) - lse_value(mx[r], s[r]);
+      }
+    }
+  }
+}
+
+// Rebuild the active list and its prefix sums (one CTA, block-wide scan).
+// Problems whose flag is set leave the list.
+template <typename T>
+__device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leaving, int* s_scan, int64_t nwarps) {
+  // serial in chunks of blockDim: scan of keep flags
+  __shared__ int s_base;
+  __shared__ int64_t s_ucol, s_urow, s_col;
+  constexpr int VW = Vec<T>::N;
+  if (threadIdx.x == 0) { s_base = 0; s_ucol = 0; s_urow = 0; s_col = 0; }
+  __syncthreads();
+  for (int c0 = 0; c0 < nact; c0 += blockDim.x) {
+    const int k = c0 + threadIdx.x;
+    int p = -1, keep = 0;
+    if (k < nact) { p = __ldcg(A.active + k); keep = leaving[p] ? 0 : 1; }
+    s_scan[threadIdx.x] = keep;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+      const int add = threadIdx.x >= o ? s_scan[threadIdx.x - o] : 0;
+      __syncthreads();
+      s_scan[threadIdx.x] += add;
+      __syncthreads();
+    }
+    const int pos = s_base + s_scan[threadIdx.x] - keep;
+    if (keep) A.active[pos] = p;  // compaction never overtakes the reads of this chunk
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) s_base += s_scan[threadIdx.x];
+    __syncthreads();
+  }
+  // split factor: about 8 column-pass units per warp over the remaining work
+  __shared__ int64_t s_slabs;
+  if (threadIdx.x == 0) s_slabs = 0;
+  __syncthreads();
+  {
+    int64_t part = 0;
+    for (int k = threadIdx.x; k < s_base; k += blockDim.x) {
+      const int m = A.cols[__ldcg(A.active + k)];
+      part += (m + 32 * VW - 1) / (32 * VW);
+    }
+    atomicAdd(reinterpret_cast<unsigned long long*>(&s_slabs), (unsigned long long)part);
+  }
+  __syncthreads();
+  const int64_t S = s_slabs > 0 ? (8 * nwarps + s_slabs - 1) / s_slabs : 1;
+  for (int k = threadIdx.x; k < s_base; k += blockDim.x) {
+    const int p = A.active[k];
+    const int n = A.rows[p];
+    const int ns = (int)(S < (int64_t)A.nsr_max[p] ? S : (int64_t)A.nsr_max[p]);
+    const int rc = (n + ns - 1) / ns;
+    A.rchunk[p] = rc;
+    A.nsr[p] = (n + rc - 1) / rc;
+  }
+  __syncthreads();
+  // prefix sums of units and columns over the new list (serial, one thread)
+  if (threadIdx.x == 0) {
+    const int na = s_base;
+    int64_t uc = 0, ur = 0, cc = 0;
+    for (int k = 0; k < na; ++k) {
+      const int p = A.active[k];
+      const int m = A.cols[p];
+      A.ucol_pre[k] = uc; A.urow_pre[k] = ur; A.colpre[k] = cc;
+      uc += (int64_t)((m + 32 * VW - 1) / (32 * VW)) * A.nsr[p];
+      ur += (A.rows[p] + MT_RW - 1) / MT_RW;
+      cc += m;
+    }
+    A.ucol_pre[na] = uc; A.urow_pre[na] = ur; A.colpre[na] = cc;
+    A.ctl[0] = na;
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(MT_THREADS, 2) multi_sinkhorn_kernel(MultiArgs<T> A, int32_t* leaving) {
+  __shared__ int s_scan[MT_THREADS];
+  const int lane = threadIdx.x & 31;
+  const long nwb = blockDim.x >> 5;
+  const long gwarp = blockIdx.x * nwb + (threadIdx.x >> 5);
+  const long nwarps = gridDim.x * nwb;
+  const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nthreads = (long)gridDim.x * blockDim.x;
+  int* abort_flag = A.ctl + 1;
+  const T L2E = T(OTG_LOG2E), LN2 = T(OTG_LN2);
+  // initial state
+  for (int p = blockIdx.x; p < A.nprob; p += gridDim.x) {
+    const int n = A.rows[p], m = A.cols[p];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int64_t ri = A.r_off[p] + i;
+      A.u[ri] = A.warm_u ? A.warm_u[ri] * L2E : T(0);
+    }
+    for (int j = threadIdx.x; j < m; j += blockDim.x) A.v0[A.c_off[p] + j] = T(0);
+    if (threadIdx.x == 0) { leaving[p] = 0; A.err2[p] = 0.0; }
+  }
+  if (blockIdx.x == 0) {
+    for (int k = threadIdx.x; k < A.nprob; k += blockDim.x) A.active[k] = k;
+  }
+  if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+  if (blockIdx.x == 0) mt_rebuild<T>(A, A.nprob, leaving, s_scan, nwarps);
+  if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+
+  T* vcur = A.v0;
+  T* vnxt = A.v1;
+  bool prev_check = false;
+  for (int ii = 0;; ++ii) {
+    const int nact = ld_acquire_i(A.ctl);
+    if (nact == 0) break;
+    const bool decide = prev_check || ii == A.max_iter;
+    if (ii == A.max_iter && !prev_check) {
+      // every active problem ends without a final check (state of ii-1)
+      for (int k = blockIdx.x; k < nact; k += gridDim.x) {
+        const int p = __ldcg(A.active + k);
+        for (int i = threadIdx.x; i < A.rows[p]; i += blockDim.x) A.out_u[A.r_off[p] + i] = __ldcg(A.u + A.r_off[p] + i) * LN2;
+        for (int j = threadIdx.x; j < A.cols[p]; j += blockDim.x) A.out_v[A.c_off[p] + j] = __ldcg(vcur + A.c_off[p] + j) * LN2;
+        if (threadIdx.x == 0) { A.status[p] = OTG_STATUS_MAXITER; A.niter[p] = A.max_iter - 1; A.err[p] = -1.0; }
+      }
+      break;
+    }
+    mt_col_pass<T>(A, nact, gwarp, nwarps, lane);
+    if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+    mt_col_merge<T>(A, nact, vcur, vnxt, prev_check, ii < A.max_iter, gtid, nthreads);
+    if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+    if (decide) {
+      // decide per problem, write out the leaving ones (state of iteration ii-1)
+      for (int k = blockIdx.x; k < nact; k += gridDim.x) {
+        const int p = __ldcg(A.active + k);
+        const double e = prev_check ? sqrt(__ldcg(A.err2 + p)) : -1.0;
+        const bool conv = prev_check && e < A.stop_thr;
+        const bool leave = conv || ii == A.max_iter;
+        if (leave) {
+          for (int i = threadIdx.x; i < A.rows[p]; i += blockDim.x) A.out_u[A.r_off[p] + i] = __ldcg(A.u + A.r_off[p] + i) * LN2;
+          for (int j = threadIdx.x; j < A.cols[p]; j += blockDim.x) A.out_v[A.c_off[p] + j] = __ldcg(vcur + A.c_off[p] + j) * LN2;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          if (leave) {
+            A.status[p] = conv ? OTG_STATUS_CONVERGED : OTG_STATUS_MAXITER;
+            A.niter[p] = conv ? ii - 1 : A.max_iter - 1;
+            A.err[p] = e;
+          }
+          leaving[p] = leave ? 1 : 0;
+          A.err2[p] = 0.0;
+        }
+      }
+      if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+      if (blockIdx.x == 0) mt_rebuild<T>(A, nact, leaving, s_scan, nwarps);
+      if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+      if (ld_acquire_i(A.ctl) == 0) break;
+    }
+    { T* t = vcur; vcur = vnxt; vnxt = t; }
+    const int nact2 = ld_acquire_i(A.ctl);
+    mt_row_pass<T>(A, nact2, vcur, gwarp, nwarps, lane);
+    if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+    prev_check = (ii % 10 == 0);
+  }
+}
+
+}  // namespace otg
+
+using namespace otg;
+
+namespace {
+template <typename T>
+int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
+  MultiArgs<T> A{};
+  A.M = static_cast<const T*>(q->M); A.m_off = q->m_off; A.rows = q->rows; A.cols = q->cols; A.ldm = q->ldm;
+  A.r_off = q->r_off; A.c_off = q->c_off;
+  A.a = static_cast<const T*>(q->a); A.b = static_cast<const T*>(q->b); A.warm_u = static_cast<const T*>(q->warm_u);
+  A.reg = q->reg; A.nprob = q->nprob; A.max_iter = q->max_iter; A.stop_thr = q->stop_thr;
+  A.nsr_max = q->nsr_max; A.pc_off = q->pc_off;
+  A.out_u = static_cast<T*>(q->out_u); A.out_v = static_cast<T*>(q->out_v);
+  A.status = q->status; A.niter = q->niter; A.err = q->err;
+  A.timeout_ns = q->timeout_ms > 0 ? (uint64_t)q->timeout_ms * 1000000ull : 4000000000ull;
+  // carve the workspace
+  char* w = static_cast<char*>(q->workspace);
+  size_t off = 0;
+  auto take = [&](size_t bytes) { char* p = w + off; off += (bytes + 255) / 256 * 256; return p; };
+  A.u = reinterpret_cast<T*>(take(sizeof(T) * q->total_rows));
+  A.v0 = reinterpret_cast<T*>(take(sizeof(T) * q->total_cols));
+  A.v1 = reinterpret_cast<T*>(take(sizeof(T) * q->total_cols));
+  A.pcol = reinterpret_cast<MPair<T>*>(take(sizeof(MPair<T>) * q->total_partials));
+  A.err2 = reinterpret_cast<double*>(take(sizeof(double) * q->nprob));
+  A.active = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * q->nprob));
+  A.ucol_pre = reinterpret_cast<int64_t*>(take(sizeof(int64_t) * (q->nprob + 1)));
+  A.urow_pre = reinterpret_cast<int64_t*>(take(sizeof(int64_t) * (q->nprob + 1)));
+  A.colpre = reinterpret_cast<int64_t*>(take(sizeof(int64_t) * (q->nprob + 1)));
+  int32_t* leaving = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * q->nprob));
+  A.nsr = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * q->nprob));
+  A.rchunk = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * q->nprob));
+  char* ctlp = take(64);
+  A.ctl = reinterpret_cast<int32_t*>(ctlp);
+  A.bar = reinterpret_cast<unsigned*>(ctlp + 32);
+  if (off > q->workspace_bytes) return OTG_ERR_WORKSPACE;
+  if (cudaMemsetAsync(ctlp, 0, 64, st) != cudaSuccess) return OTG_ERR_CUDA;
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, multi_sinkhorn_kernel<T>, MT_THREADS, 0);
+  int grid = sms * std::min(per, 2);
+  if (q->grid > 0 && q->grid < grid) grid = q->grid;
+  if (grid < 1) return OTG_ERR_UNSUPPORTED;
+  void* args[] = {&A, &leaving};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)multi_sinkhorn_kernel<T>, dim3(grid), dim3(MT_THREADS),
+                                              args, 0, st);
+  return e == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+size_t multi_ws(int dtype, int64_t nprob, int64_t rows, int64_t cols, int64_t partials) {
+  const size_t es = dtype == OTG_F64 ? 8 : 4;
+  auto r = [](size_t b) { return (b + 255) / 256 * 256; };
+  return r(es * rows) + 2 * r(es * cols) + r(2 * es * partials) + r(8 * nprob) + r(4 * nprob) +
+         3 * r(8 * (nprob + 1)) + 3 * r(4 * nprob) + r(64);
+}
+}  // namespace
+
+extern "C" {
+
+size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, int64_t total_cols,
+                                 int64_t total_partials) {
+  return multi_ws(dtype, nprob, total_rows, total_cols, total_partials);
+}
+
+int otg_sinkhorn_multi(const OtgMultiProblem* q, cudaStream_t stream) {
+  if (!q || !q->M || !q->m_off || !q->rows || !q->cols || !q->ldm || !q->r_off || !q->c_off || !q->a || !q->b ||
+      !q->reg || !q->nsr_max || !q->pc_off || !q->out_u || !q->out_v || !q->status || !q->niter ||
+      !q->err || !q->workspace)
+    return OTG_ERR_ARG;
+  if (q->nprob < 1 || q->max_iter < 1) return OTG_ERR_ARG;
+  if (q->dtype == OTG_F64) return launch_multi<double>(q, stream);
+  if (q->dtype == OTG_F32) return launch_multi<float>(q, stream);
+  return OTG_ERR_DTYPE;
+}
+
+}  // extern "C"

@@ -1,0 +1,267 @@
+"""Training data, training loop and warm-started solves for the learned warm
+start.
+
+Workload: pairs of n-point clouds in R^d, each a random 1-6 component
+isotropic Gaussian mixture (means ~ N(0, I), std ~ U[0.1, 0.6]), uniform
+weights, cost = squared distance, reg = reg_rel * max cost (the cost
+normalised by its maximum, as in the plain dense workload).  Targets are the
+converged source log-potentials of the plain log-domain solver; the solver
+itself generates them.
+"""
+import math
+import time
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .. import batch as pb
+from .net import WarmStartNet, normalise_pairs
+
+
+def gen_pairs(seed, count, n=2048, d=16, device=None):
+    """Cloud pairs generated on the device from a seeded generator."""
+    device = device or torch.device("cuda", torch.cuda.current_device())
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+
+    def clouds():
+        k = torch.randint(1, 7, (count, 1), generator=g, device=device)
+        means = torch.randn(count, 6, d, generator=g, device=device)
+        stds = torch.rand(count, 6, generator=g, device=device) * 0.5 + 0.1
+        comp = (torch.rand(count, n, generator=g, device=device) * k).long().clamp_max(5)
+        mu = torch.gather(means, 1, comp[..., None].expand(count, n, d))
+        sd = torch.gather(stds, 1, comp)
+        return mu + sd[..., None] * torch.randn(count, n, d, generator=g, device=device)
+
+    X = clouds()
+    Y = clouds()
+    return X.float().contiguous(), Y.float().contiguous()
+
+
+class PairSolver:
+    """Uniform-size batch of cloud pairs on the device: cost blocks, per-pair
+    max cost, and log-domain solves (zero or warm start)."""
+
+    def __init__(self, X, Y, maxc=None):
+        self.P, self.n, self.d = X.shape
+        self.m = Y.shape[1]
+        self.layout = pb.RaggedLayout([self.n] * self.P, [self.m] * self.P, torch.float32, X.device)
+        xo = np.arange(self.P) * self.n * self.d
+        yo = np.arange(self.P) * self.m * self.d
+        self.M, self.maxc = pb.batched_sqdist(self.layout, X.reshape(-1).contiguous(), Y.reshape(-1).contiguous(),
+                                              xo, yo, [self.d] * self.P, want_max=True)
+        if maxc is not None:  # cost scale of an enclosing problem (sub-sampled clouds)
+            self.maxc = maxc
+        self.a = torch.full((self.P * self.n,), 1.0 / self.n, dtype=torch.float32, device=X.device)
+        self.b = torch.full((self.P * self.m,), 1.0 / self.m, dtype=torch.float32, device=X.device)
+
+    def solve(self, reg_rel, tol, max_iter=100000, warm_u=None, engine="multi", events=None):
+        """Log-domain solve of every pair (sinkhorn_log order and stop test);
+        with `warm_u` the first half-step (the c-transform) derives v from it."""
+        reg = self.maxc.double() * reg_rel
+        if warm_u is not None:
+            warm_u = warm_u.reshape(-1).contiguous()
+        if engine == "multi":
+            u, v, status, niter, err, _ = pb.run_multi(self.layout, self.M, self.a, self.b, reg, max_iter, tol,
+                                                       warm_u=warm_u, events=events)
+        else:
+            wv = None if warm_u is None else torch.zeros(self.P * self.m, dtype=torch.float32, device=self.M.device)
+            u, v, status, niter, err, _ = pb.run_batched(self.layout, self.M, self.a, self.b, reg,
+                                                         _lib.OTG_METHOD_LOG, max_iter, tol, u_first=0,
+                                                         warm_u=warm_u, warm_v=wv)
+        return u.view(self.P, self.n), v.view(self.P, self.m), status, niter, err
+
+
+TAUS = (0.02, 0.05, 0.1, 0.25, 0.6)
+FEATURE_SCALE = 10.0
+
+
+def softmin(ps, taus, g=None):
+    """Soft-min distances (csrc/cost.cu softmin_features_kernel) of the
+    pair solver's source points: (P, n, len(taus)), max-normalised units."""
+    lib = _lib.load()
+    L = ps.layout
+    K = len(taus)
+    out = torch.empty(ps.P * ps.n, K, dtype=torch.float32, device=ps.M.device)
+    tt = torch.tensor(taus, dtype=torch.float32, device=ps.M.device)
+    sc = ps.maxc.float().contiguous()
+    gp = None if g is None else g.reshape(-1).float().contiguous()
+    _lib.check(lib.otg_softmin_features(_lib.ptr(ps.M), _lib.ptr(L.m_off), _lib.ptr(L.rows), _lib.ptr(L.cols),
+                                        _lib.ptr(L.ldm), _lib.ptr(L.r_off), _lib.ptr(L.c_off), _lib.ptr(ps.b),
+                                        _lib.ptr(sc), _lib.ptr(tt), K, ps.P, ps.n, _lib.ptr(gp), _lib.ptr(out),
+                                        _lib.stream_handle(ps.M.device)), "otg_softmin_features")
+    return out.view(ps.P, ps.n, K)
+
+
+def features(ps, taus=TAUS):
+    """Per-point inputs of the head: soft-min distances at several
+    temperatures, centred per pair and scaled to O(1)."""
+    F = softmin(ps, taus)
+    return ((F - F.mean(1, keepdim=True)) * FEATURE_SCALE).contiguous()
+
+
+def coarse_potential(X, Y, maxc, reg_rel=0.02, k=128, tol=1e-5, taus=None):
+    """Multiscale prior: solve the problem on the first k points of each
+    cloud (the points are i.i.d., so this is a random sub-sample) and carry
+    its target potential to every source point with one c-transform (the
+    log-domain row update).  Returns the centred source potential in
+    max-normalised cost units, (P, n), and, if `taus` is given, the soft-min
+    distances of every source point to the k-point target sample at those
+    temperatures, (P, n, len(taus))."""
+    Xs, Ys = X[:, :k].contiguous(), Y[:, :k].contiguous()
+    sub = PairSolver(Xs, Ys, maxc=maxc)
+    _, v, _, _, _ = sub.solve(reg_rel, tol)
+    cross = PairSolver(X, Ys, maxc=maxc)
+    f = softmin(cross, (reg_rel,), g=v)[..., 0]
+    f = (f - f.mean(1, keepdim=True)).contiguous()
+    if taus is None:
+        return f
+    return f, softmin(cross, taus)
+
+
+COARSE_K = 256
+
+
+def inputs(ps, X, Y, reg_rel=0.02, k=COARSE_K):
+    """Per-point head inputs of a pair batch and the coarse prior, all from
+    the source x k-point cross cost (never the full cost): (features
+    (P, n, len(TAUS) + 1), prior (P, n))."""
+    prior, F = coarse_potential(X, Y, ps.maxc, reg_rel, k, taus=TAUS)
+    F = (F - F.mean(1, keepdim=True)) * FEATURE_SCALE
+    return torch.cat([F, prior[..., None] * FEATURE_SCALE], 2).contiguous(), prior
+
+
+def targets(X, Y, reg_rel=0.02, tol=1e-7, chunk=256):
+    """Residual targets (converged centred source potential minus the coarse
+    prior, max-normalised cost units) from the plain solver run to `tol`,
+    with the head inputs; returns (R, F, maxc, niter)."""
+    Ts, Fs, mx, nits = [], [], [], []
+    for s in range(0, X.shape[0], chunk):
+        ps = PairSolver(X[s:s + chunk], Y[s:s + chunk])
+        u, _, status, niter, _ = ps.solve(reg_rel, tol)
+        f = reg_rel * (u - u.mean(1, keepdim=True))
+        F, prior = inputs(ps, X[s:s + chunk], Y[s:s + chunk], reg_rel)
+        Ts.append(f - prior)
+        Fs.append(F)
+        mx.append(ps.maxc)
+        nits.append(niter)
+        del ps
+    return torch.cat(Ts), torch.cat(Fs), torch.cat(mx), torch.cat(nits)
+
+
+def _head_inputs(Xn, F):
+    return torch.cat([Xn, F], 2).contiguous()
+
+
+def predict(net, X, Y, maxc, F, chunk=64):
+    """Network output: the centred residual over the coarse prior
+    (max-normalised cost units)."""
+    out = []
+    for s in range(0, X.shape[0], chunk):
+        Xn, Yn = normalise_pairs(X[s:s + chunk], Y[s:s + chunk], maxc[s:s + chunk])
+        P, n, d = Xn.shape
+        Z = _head_inputs(Xn, F[s:s + chunk])
+        f = net.forward(Xn.view(P * n, d), Yn.view(P * Yn.shape[1], d), P, n, Yn.shape[1],
+                        Z=Z.view(P * n, -1)).view(P, n)
+        out.append(f - f.mean(1, keepdim=True))
+    return torch.cat(out)
+
+
+def new_net(d, device=None, seed=0, taus=TAUS):
+    return WarmStartNet(d, device=device, seed=seed, dz=d + len(taus) + 1)
+
+
+def warm_potential(net, X, Y, ps, reg_rel=0.02):
+    """Warm start of the source log-potential (natural-log units) for the
+    pairs of `ps`: (coarse prior + network residual) / reg_rel."""
+    F, prior = inputs(ps, X, Y, reg_rel)
+    return (prior + predict(net, X, Y, ps.maxc, F)) / reg_rel
+
+
+def train(net, X, Y, T, F, maxc, steps=2000, pairs_per_step=16, lr=2e-3, wd=1e-4, seed=0, log_every=200,
+          verbose=True):
+    """AdamW with cosine decay on the centred-MSE loss; returns the loss
+    history (one value per `log_every` steps)."""
+    N = X.shape[0]
+    g = torch.Generator(device="cpu")
+    g.manual_seed(seed)
+    hist = []
+    t0 = time.perf_counter()
+    for step in range(steps):
+        idx = torch.randint(0, N, (pairs_per_step,), generator=g).to(X.device)
+        Xb, Yb = normalise_pairs(X[idx], Y[idx], maxc[idx])
+        P, n, d = Xb.shape
+        Z = _head_inputs(Xb, F[idx])
+        f = net.forward(Xb.view(P * n, d), Yb.view(P * Yb.shape[1], d), P, n, Yb.shape[1],
+                        Z=Z.view(P * n, -1), keep=True)
+        loss, df = net.loss_and_grad(f, T[idx].reshape(-1).contiguous(), P, n)
+        net.backward(df)
+        cur = lr * 0.5 * (1 + math.cos(math.pi * step / steps))
+        net.adamw(cur, wd=wd)
+        if (step + 1) % log_every == 0 or step == steps - 1:
+            lv = float(loss.item())
+            hist.append(lv)
+            if verbose:
+                print("step %5d  loss %.3e  lr %.2e  %.1fs" % (step + 1, lv, cur, time.perf_counter() - t0), flush=True)
+    return hist
+
+
+def relative_error(F, T):
+    """Per pair ||F - T|| / ||T|| of centred potentials (median over pairs)."""
+    num = torch.linalg.norm(F - T, dim=1)
+    den = torch.linalg.norm(T, dim=1).clamp_min(1e-30)
+    return (num / den)
+
+
+WEIGHTS = "weights_gmm_n2048_d16.npz"
+
+
+def default_net(device=None, train_if_missing=True, verbose=False):
+    """The shipped network for the Gaussian-mixture workload (n = 2048,
+    d = 16, reg = 0.02 x max cost), trained by `train_default`; trained
+    afresh if the weights file is missing."""
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), WEIGHTS)
+    device = device or torch.device("cuda", torch.cuda.current_device())
+    net = new_net(16, device=device)
+    if os.path.exists(path):
+        with np.load(path) as z:
+            net.load({k: z[k] for k in z.files})
+        return net
+    if not train_if_missing:
+        raise FileNotFoundError(path)
+    return train_default(device=device, verbose=verbose)
+
+
+def train_default(device=None, n_train=8192, steps=4000, verbose=True, out=None):
+    """Training recipe of the shipped weights: n_train pairs from seeds
+    1 .. n_train, targets from the plain solver at 1e-7, AdamW 4000 steps of
+    16 pairs, lr 2e-3 cosine."""
+    device = device or torch.device("cuda", torch.cuda.current_device())
+    X, Y = gen_pairs(1, n_train, 2048, 16, device)
+    T, F, maxc, _ = targets(X, Y, 0.02, 1e-7)
+    net = new_net(16, device=device, seed=0)
+    train(net, X, Y, T, F, maxc, steps=steps, pairs_per_step=16, lr=2e-3, verbose=verbose)
+    if out:
+        np.savez(out, **net.state())
+    return net
+
+
+def solve_cloud_pairs(X, Y, reg_rel=0.02, tol=1e-6, max_iter=100000, warm=True, net=None):
+    """Public entry point for batches of equal-size cloud pairs: X (P, n, d),
+    Y (P, m, d) (numpy or torch); returns (log_u, log_v, niter) in the
+    caller's array type.  reg = reg_rel x each pair's max squared distance;
+    sinkhorn_log order and stop test per pair; with `warm` the source
+    potential starts from the learned warm start."""
+    from .._arrays import Boundary
+    bd = Boundary(X, Y)
+    Xd = bd.to_dev(X, torch.float32).contiguous()
+    Yd = bd.to_dev(Y, torch.float32).contiguous()
+    ps = PairSolver(Xd, Yd)
+    wu = None
+    if warm:
+        net = net or default_net(Xd.device)
+        wu = warm_potential(net, Xd, Yd, ps, reg_rel)
+    u, v, status, niter, err = ps.solve(reg_rel, tol, max_iter, warm_u=wu)
+    return bd.out(u), bd.out(v), bd.out(niter)

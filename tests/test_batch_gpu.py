@@ -136,3 +136,32 @@ def test_ragged_sizes_at_the_limits(cuda):
         u, v = (t.cpu().numpy() for t in res.potentials(k))
         Pg = np.exp(-M / reg + u[:, None] + v[None, :])
         assert np.abs(Pg - P).sum() / P.sum() < 1e-9, (n, m)
+
+
+def test_multi_and_per_cta_engines_agree(cuda):
+    """The work-balanced engine and the CTA-per-problem engine run the same
+    per-problem iteration: identical stop index, potentials to 1e-9."""
+    Xs, Ys, As, Bs, regs = _ragged_case(8, 40, 1, 400)
+    r1 = pb.solve_sample_ragged(Xs, Ys, regs, As, Bs, reg_relative=True, max_iter=20000, tol=1e-9,
+                                dtype=torch.float64, engine="multi")
+    r2 = pb.solve_sample_ragged(Xs, Ys, regs, As, Bs, reg_relative=True, max_iter=20000, tol=1e-9,
+                                dtype=torch.float64, engine="cta")
+    np.testing.assert_array_equal(r1.niter.cpu().numpy(), r2.niter.cpu().numpy())
+    np.testing.assert_array_equal(r1.status.cpu().numpy(), r2.status.cpu().numpy())
+    for k in range(len(Xs)):
+        u1, v1 = (t.cpu().numpy() for t in r1.potentials(k))
+        u2, v2 = (t.cpu().numpy() for t in r2.potentials(k))
+        np.testing.assert_allclose(u1, u2, rtol=1e-9, atol=1e-9)
+        np.testing.assert_allclose(v1, v2, rtol=1e-9, atol=1e-9)
+
+
+def test_multi_engine_max_iter_and_single_problem(cuda):
+    rng = np.random.default_rng(12)
+    X = rng.random((700, 3))
+    Y = rng.random((650, 3))
+    r = pb.solve_sample_ragged([X], [Y], 0.003, reg_relative=True, max_iter=25, tol=1e-12, dtype=torch.float64)
+    M = oracle.sqeuclidean(X, Y)
+    P, lg = oracle.sinkhorn_log([], [], M, 0.003 * M.max(), numItermax=25, stopThr=1e-12)
+    assert int(r.status[0]) == 1 and int(r.niter[0]) == lg["niter"] == 24
+    u, v = (t.cpu().numpy() for t in r.potentials(0))
+    np.testing.assert_allclose(u, lg["log_u"], rtol=1e-9, atol=1e-9)

@@ -115,3 +115,32 @@ def test_lazy():
     np.testing.assert_allclose(f, g["f"], rtol=1e-9, atol=1e-12)
     np.testing.assert_allclose(gg, g["g"], rtol=1e-9, atol=1e-12)
     np.testing.assert_allclose(lg["err"], g["err"], rtol=1e-6, atol=1e-15)
+
+
+def test_warmstart_net_gradients_match_finite_differences():
+    """Pins the network oracle: analytic gradients vs central differences."""
+    from oracle import warmstart_net as wn
+    from pot_gb300.warmstart.net import init_params
+    rng = np.random.default_rng(0)
+    d = 3
+    params = {k: v.astype(np.float64) for k, v in init_params(d, seed=1, h1=6, h2=5, h3=7).items()}
+    for k in params:
+        if k.startswith("b"):
+            params[k] = rng.standard_normal(params[k].shape) * 0.1
+    X = rng.standard_normal((2, 9, d))
+    Y = rng.standard_normal((2, 8, d))
+    t = rng.standard_normal((2, 9))
+    t -= t.mean(1, keepdims=True)
+    loss, g, _ = wn.loss_and_grads(params, X, Y, t)
+    h = 1e-6
+    for name in params:
+        flat = params[name].reshape(-1)
+        for idx in rng.choice(flat.size, size=min(4, flat.size), replace=False):
+            old = flat[idx]
+            flat[idx] = old + h
+            lp, _, _ = wn.loss_and_grads(params, X, Y, t)
+            flat[idx] = old - h
+            lm, _, _ = wn.loss_and_grads(params, X, Y, t)
+            flat[idx] = old
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - g[name].reshape(-1)[idx]) <= 1e-6 + 1e-5 * abs(fd), (name, idx, fd, g[name].reshape(-1)[idx])
