@@ -14,7 +14,43 @@
 namespace otg {
 
 // One CTA per (problem, tile of 32 rows); the tile's points are staged in
-// shared memory; threads sweep the columns.  Padded columns [m, ldm) get +inf.
+// shared memory.  With a compile-time dimension D each thread keeps four
+// target points in registers and writes four adjacent costs per row as one
+// 16-byte store; other dimensions take the generic loop.  Padded columns
+// [m, ldm) get +inf.
+template <typename T, int D>
+__device__ __forceinline__ void sqdist_tile_fixed(const T* xs, int rows, const T* Y, int m, int ldm, T* M, int r0,
+                                                  T& local_max) {
+  for (int j0 = threadIdx.x * 4; j0 < ldm; j0 += blockDim.x * 4) {
+    T y[4][D];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int k = 0; k < D; ++k) y[q][k] = (j0 + q < m) ? Y[(int64_t)(j0 + q) * D + k] : T(0);
+    for (int r = 0; r < rows; ++r) {
+      T acc[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        const T xk = xs[r * D + k];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { const T df = xk - y[q][k]; acc[q] = fma(df, df, acc[q]); }
+      }
+      T* dst = M + (int64_t)(r0 + r) * ldm + j0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (j0 + q < m) local_max = fmax(local_max, acc[q]);
+        else acc[q] = T(INFINITY);
+      }
+      if (j0 + 4 <= ldm && sizeof(T) == 4) {
+        *reinterpret_cast<float4*>(dst) = make_float4((float)acc[0], (float)acc[1], (float)acc[2], (float)acc[3]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) if (j0 + q < ldm) dst[q] = acc[q];
+      }
+    }
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) batched_sqdist_kernel(OtgCostTable t) {
   constexpr int TR = 32;
@@ -32,18 +68,25 @@ __global__ void __launch_bounds__(256) batched_sqdist_kernel(OtgCostTable t) {
   for (int e = threadIdx.x; e < rows * d; e += blockDim.x) xs[e] = X[(int64_t)r0 * d + e];
   __syncthreads();
   T local_max = 0;
-  for (int j = threadIdx.x; j < ldm; j += blockDim.x) {
-    if (j < m) {
-      const T* y = Y + (int64_t)j * d;
-      for (int r = 0; r < rows; ++r) {
-        const T* x = xs + r * d;
-        T acc = 0;
-        for (int k = 0; k < d; ++k) { const T df = x[k] - y[k]; acc = fma(df, df, acc); }
-        M[(int64_t)(r0 + r) * ldm + j] = acc;
-        local_max = fmax(local_max, acc);
+  // ldm is a multiple of 16 bytes, so 4-column groups of float rows stay aligned
+  if (d == 16 && ldm % 4 == 0) sqdist_tile_fixed<T, 16>(xs, rows, Y, m, ldm, M, r0, local_max);
+  else if (d == 8 && ldm % 4 == 0) sqdist_tile_fixed<T, 8>(xs, rows, Y, m, ldm, M, r0, local_max);
+  else if (d == 3 && ldm % 4 == 0) sqdist_tile_fixed<T, 3>(xs, rows, Y, m, ldm, M, r0, local_max);
+  else if (d == 2 && ldm % 4 == 0) sqdist_tile_fixed<T, 2>(xs, rows, Y, m, ldm, M, r0, local_max);
+  else {
+    for (int j = threadIdx.x; j < ldm; j += blockDim.x) {
+      if (j < m) {
+        const T* y = Y + (int64_t)j * d;
+        for (int r = 0; r < rows; ++r) {
+          const T* x = xs + r * d;
+          T acc = 0;
+          for (int k = 0; k < d; ++k) { const T df = x[k] - y[k]; acc = fma(df, df, acc); }
+          M[(int64_t)(r0 + r) * ldm + j] = acc;
+          local_max = fmax(local_max, acc);
+        }
+      } else {
+        for (int r = 0; r < rows; ++r) M[(int64_t)(r0 + r) * ldm + j] = T(INFINITY);
       }
-    } else {
-      for (int r = 0; r < rows; ++r) M[(int64_t)(r0 + r) * ldm + j] = T(INFINITY);
     }
   }
   if (t.max_out) {

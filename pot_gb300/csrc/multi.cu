@@ -93,8 +93,8 @@ __device__ void mt_col_pass(const MultiArgs<T>& A, int nact, long gwarp, long nw
 #pragma unroll
     for (int q = 0; q < VW; ++q) { mx[q] = -INFINITY; s[q] = 0; }
     if (j0 < m) {
-      for (int i = i0; i < i1; i += MT_GCOL) {
-        T x[MT_GCOL][VW], ur[MT_GCOL];
+      T xn[MT_GCOL][VW], un[MT_GCOL];
+      auto load_group = [&](int i, T (&x)[MT_GCOL][VW], T (&ur)[MT_GCOL]) {
 #pragma unroll
         for (int g = 0; g < MT_GCOL; ++g) {
           if (i + g < i1) {
@@ -106,6 +106,17 @@ __device__ void mt_col_pass(const MultiArgs<T>& A, int nact, long gwarp, long nw
             ur[g] = -INFINITY;
           }
         }
+      };
+      load_group(i0, xn, un);
+      for (int i = i0; i < i1; i += MT_GCOL) {
+        T x[MT_GCOL][VW], ur[MT_GCOL];
+#pragma unroll
+        for (int g = 0; g < MT_GCOL; ++g) {
+          ur[g] = un[g];
+#pragma unroll
+          for (int q = 0; q < VW; ++q) x[g][q] = xn[g][q];
+        }
+        if (i + MT_GCOL < i1) load_group(i + MT_GCOL, xn, un);
 #pragma unroll
         for (int q = 0; q < VW; ++q) {
           T t[MT_GCOL];
@@ -186,17 +197,28 @@ __device__ void mt_row_pass(const MultiArgs<T>& A, int nact, const T* v, long gw
     T mx[MT_RW], s[MT_RW];
 #pragma unroll
     for (int r = 0; r < MT_RW; ++r) { mx[r] = -INFINITY; s[r] = 0; }
-    for (int j = lane * VW; j < m; j += 32 * VW) {
-      T vv[VW];
-      // v beyond m (padding up to ldm) is never read: the vector tail is masked
+    T xn[MT_RW][VW], vn[VW];
+    auto load_step = [&](int j, T (&x)[MT_RW][VW], T (&vv)[VW]) {
+      // v beyond m (padding up to ldm) is masked to -inf
 #pragma unroll
       for (int q = 0; q < VW; ++q) vv[q] = (j + q < m) ? __ldcg(vp + j + q) : T(-INFINITY);
-      T x[MT_RW][VW];
 #pragma unroll
       for (int r = 0; r < MT_RW; ++r) {
         const int row = min(r0 + r, n - 1);
         unpack(ld_stream(reinterpret_cast<const V*>(Mp + (int64_t)row * ldm + j)), x[r]);
       }
+    };
+    if (lane * VW < m) load_step(lane * VW, xn, vn);
+    for (int j = lane * VW; j < m; j += 32 * VW) {
+      T vv[VW];
+      T x[MT_RW][VW];
+#pragma unroll
+      for (int q = 0; q < VW; ++q) vv[q] = vn[q];
+#pragma unroll
+      for (int r = 0; r < MT_RW; ++r)
+#pragma unroll
+        for (int q = 0; q < VW; ++q) x[r][q] = xn[r][q];
+      if (j + 32 * VW < m) load_step(j + 32 * VW, xn, vn);
 #pragma unroll
       for (int r = 0; r < MT_RW; ++r) {
         T t[VW];
