@@ -253,6 +253,43 @@ int otg_mlp_adamw(float* w, const float* g, float* m, float* v, int64_t n, float
                   float wd, int step, cudaStream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Entropic Gromov-Wasserstein tensor product on the tensor cores.
+ * Replaces the two GEMMs of ot/gromov/_utils.py:244-280 (tensor_product)
+ * used by gwggrad (:323-354) inside entropic_gromov_wasserstein
+ * (ot/gromov/_bregman.py:198-242).
+ *
+ * otg_split_half: half-precision high/low planes hi + lo = scale * X (or
+ * scale * X^T), X rows x cols fp32; out planes have ld_out columns.
+ * otg_gemm_split3: C = A B^T for operands given as high/low half planes
+ * (A: a_rows x lda, B: b_rows x ldb, both K-major, rows and leading dims
+ * multiples of 128, zero-padded beyond the data; K = k_alloc, a multiple of
+ * 64), three tcgen05 MMAs per k-step (Ah Bh + Ah Bl + Al Bh), fp32 TMEM
+ * accumulation.  mode 0 writes scale * C as high/low planes (a_rows x ld_h,
+ * ld_h >= b_rows); mode 1 writes out_ij = s_acc C_ij + s_vec (rowv_i +
+ * colv_j) for i < M, j < N (fp32, ld_o).  abort_flag: one device int32,
+ * zero on entry; set if a bounded wait runs out.
+ * ---------------------------------------------------------------------- */
+typedef struct OtgSplitGemm {
+  const void* a_hi; const void* a_lo; int64_t a_rows, lda;
+  const void* b_hi; const void* b_lo; int64_t b_rows, ldb;
+  int64_t k_alloc;
+  int32_t mode;
+  float scale, s_acc, s_vec;
+  void* out_hi; void* out_lo; int64_t ld_h;
+  float* out; int64_t ld_o;
+  int64_t M, N;
+  const float* rowv; const float* colv;
+  int32_t* abort_flag;
+  int32_t timeout_ms;
+} OtgSplitGemm;
+int otg_split_half(const float* X, int64_t rows, int64_t cols, int64_t ldx, float scale, int transpose, void* hi,
+                   void* lo, int64_t ld_out, cudaStream_t stream);
+int otg_gemm_split3(const OtgSplitGemm* g, cudaStream_t stream);
+/* fp64 tiled GEMM (CUDA cores) for the float64 path: C = alpha op(A) op(B) + beta C. */
+int otg_gemm_f64(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                 const double* B, int64_t ldb, double beta, double* C, int64_t ldc, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
  * Allocation-free variant of otg_sinkhorn_dense.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory
  * when they solve, e.g. a host whose own allocator owns the device pool, or

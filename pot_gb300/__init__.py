@@ -9,5 +9,6 @@ CUDA kernels for sm_103a (``pot_gb300/csrc``) behind the C ABI of
 from .bregman import sinkhorn, sinkhorn2, sinkhorn_knopp, sinkhorn_log  # noqa: F401
 from . import batch  # noqa: F401
 from .batch import solve_batch, solve_sample_batch, dist_batch  # noqa: F401
+from . import gromov  # noqa: F401
 
 __version__ = "0.1.0"

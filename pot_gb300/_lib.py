@@ -58,6 +58,14 @@ class OtgPlanTable(ctypes.Structure):
                 ("u", c_vp), ("v", c_vp), ("a", c_vp), ("b", c_vp), ("reg", c_vp), ("P", c_vp), ("out_vals", c_vp)]
 
 
+class OtgSplitGemm(ctypes.Structure):
+    _fields_ = [("a_hi", c_vp), ("a_lo", c_vp), ("a_rows", c_i64), ("lda", c_i64), ("b_hi", c_vp), ("b_lo", c_vp),
+                ("b_rows", c_i64), ("ldb", c_i64), ("k_alloc", c_i64), ("mode", c_i32), ("scale", ctypes.c_float),
+                ("s_acc", ctypes.c_float), ("s_vec", ctypes.c_float), ("out_hi", c_vp), ("out_lo", c_vp),
+                ("ld_h", c_i64), ("out", c_vp), ("ld_o", c_i64), ("M", c_i64), ("N", c_i64), ("rowv", c_vp),
+                ("colv", c_vp), ("abort_flag", c_vp), ("timeout_ms", c_i32)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "otg_dense_workspace_bytes": (c_sz, [ctypes.c_int, c_i64, c_i64, ctypes.c_int, ctypes.c_int]),
@@ -77,6 +85,11 @@ SIGNATURES = {
                                             c_i32, c_vp, c_vp, c_vp]),
     "otg_gemm_f32": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, ctypes.c_float, c_vp, c_i64,
                                     c_vp, c_i64, ctypes.c_float, c_vp, c_i64, c_vp, ctypes.c_int, c_vp]),
+    "otg_gemm_f64": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, c_dbl, c_vp, c_i64, c_vp, c_i64,
+                                    c_dbl, c_vp, c_i64, c_vp]),
+    "otg_split_half": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, ctypes.c_float, ctypes.c_int, c_vp, c_vp, c_i64,
+                                      c_vp]),
+    "otg_gemm_split3": (ctypes.c_int, [ctypes.POINTER(OtgSplitGemm), c_vp]),
     "otg_mlp_relu_bwd": (ctypes.c_int, [c_vp, c_vp, c_i64, c_vp]),
     "otg_mlp_colsum": (ctypes.c_int, [c_vp, c_i64, c_i64, c_vp, c_vp]),
     "otg_mlp_segment_mean": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, c_vp]),

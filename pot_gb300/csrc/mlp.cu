@@ -17,27 +17,28 @@ constexpr int GK = 16;      // k tile
 
 // C = alpha * op(A) * op(B) + beta * C (+ bias, ReLU).  op(A) is M x K, op(B)
 // is K x N; ta / tb select the transposed storage of A ([K, M]) / B ([N, K]).
-__global__ void __launch_bounds__(256) gemm_f32_kernel(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha,
-                                                       const float* __restrict__ A, int64_t lda,
-                                                       const float* __restrict__ B, int64_t ldb, float beta,
-                                                       float* __restrict__ C, int64_t ldc,
-                                                       const float* __restrict__ bias, int relu) {
-  __shared__ float As[GK][GT + 4];
-  __shared__ float Bs[GK][GT + 4];
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_tiled_kernel(int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha,
+                                                         const T* __restrict__ A, int64_t lda,
+                                                         const T* __restrict__ B, int64_t ldb, T beta,
+                                                         T* __restrict__ C, int64_t ldc,
+                                                         const T* __restrict__ bias, int relu) {
+  __shared__ T As[GK][GT + 4];
+  __shared__ T Bs[GK][GT + 4];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t m0 = (int64_t)blockIdx.y * GT, n0 = (int64_t)blockIdx.x * GT;
   // split-K: CTA z covers k in [kbeg, kend) and adds its partial product
   const int64_t kper = ((K + gridDim.z - 1) / gridDim.z + GK - 1) / GK * GK;
   const int64_t kbeg = (int64_t)blockIdx.z * kper, kend = min(K, kbeg + kper);
   const bool split = gridDim.z > 1;
-  float acc[4][4] = {};
+  T acc[4][4] = {};
   for (int64_t k0 = kbeg; k0 < kend; k0 += GK) {
     // load A tile (GT x GK) into As[k][m]
     for (int e = threadIdx.x; e < GT * GK; e += 256) {
       int mm, kk;
       if (ta) { kk = e / GT; mm = e % GT; } else { mm = e / GK; kk = e % GK; }
       const int64_t gm = m0 + mm, gk = k0 + kk;
-      float val = 0.f;
+      T val = 0;
       if (gm < M && gk < kend) val = ta ? A[gk * lda + gm] : A[gm * lda + gk];
       As[kk][mm] = val;
     }
@@ -45,14 +46,14 @@ __global__ void __launch_bounds__(256) gemm_f32_kernel(int ta, int tb, int64_t M
       int nn, kk;
       if (tb) { nn = e / GK; kk = e % GK; } else { kk = e / GT; nn = e % GT; }
       const int64_t gn = n0 + nn, gk = k0 + kk;
-      float val = 0.f;
+      T val = 0;
       if (gn < N && gk < kend) val = tb ? B[gn * ldb + gk] : B[gk * ldb + gn];
       Bs[kk][nn] = val;
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < GK; ++kk) {
-      float a[4], b[4];
+      T a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
 #pragma unroll
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(256) gemm_f32_kernel(int ta, int tb, int64_t M
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
   }
@@ -72,11 +73,11 @@ __global__ void __launch_bounds__(256) gemm_f32_kernel(int ta, int tb, int64_t M
     for (int j = 0; j < 4; ++j) {
       const int64_t gn = n0 + tx * 4 + j;
       if (gn >= N) continue;
-      float r = alpha * acc[i][j];
+      T r = alpha * acc[i][j];
       if (split) { atomicAdd(C + gm * ldc + gn, r); continue; }  // C zeroed, no bias/act
-      if (beta != 0.f) r += beta * C[gm * ldc + gn];
+      if (beta != T(0)) r += beta * C[gm * ldc + gn];
       if (bias) r += bias[gn];
-      if (relu) r = fmaxf(r, 0.f);
+      if (relu) r = fmax(r, T(0));
       C[gm * ldc + gn] = r;
     }
   }
@@ -198,11 +199,9 @@ inline int blocks_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256
 
 using namespace otg;
 
-extern "C" {
-
-int otg_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
-                 const float* B, int64_t ldb, float beta, float* C, int64_t ldc, const float* bias, int relu,
-                 cudaStream_t stream) {
+template <typename T>
+static int gemm_tiled(int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha, const T* A, int64_t lda, const T* B,
+                      int64_t ldb, T beta, T* C, int64_t ldc, const T* bias, int relu, cudaStream_t stream) {
   if (M < 1 || N < 1 || K < 1 || !A || !B || !C) return OTG_ERR_ARG;
   if ((M + GT - 1) / GT > 65535) return OTG_ERR_UNSUPPORTED;
   const int64_t tiles = ((N + GT - 1) / GT) * ((M + GT - 1) / GT);
@@ -210,10 +209,23 @@ int otg_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, c
   // few output tiles and a long K (weight gradients over many rows): split K
   if (tiles < 304 && K >= 4096 && beta == 0.f && !bias && !relu) splits = std::min<int64_t>(K / 1024, 608 / tiles + 1);
   if (splits > 1 && ldc != N) splits = 1;  // split-K accumulates into a zeroed, dense C
-  if (splits > 1 && cudaMemsetAsync(C, 0, sizeof(float) * M * N, stream) != cudaSuccess) return OTG_ERR_CUDA;
+  if (splits > 1 && cudaMemsetAsync(C, 0, sizeof(T) * M * N, stream) != cudaSuccess) return OTG_ERR_CUDA;
   dim3 grid((unsigned)((N + GT - 1) / GT), (unsigned)((M + GT - 1) / GT), (unsigned)splits);
-  gemm_f32_kernel<<<grid, 256, 0, stream>>>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, bias, relu);
+  gemm_tiled_kernel<T><<<grid, 256, 0, stream>>>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, bias, relu);
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+extern "C" {
+
+int otg_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
+                 const float* B, int64_t ldb, float beta, float* C, int64_t ldc, const float* bias, int relu,
+                 cudaStream_t stream) {
+  return gemm_tiled<float>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, bias, relu, stream);
+}
+
+int otg_gemm_f64(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                 const double* B, int64_t ldb, double beta, double* C, int64_t ldc, cudaStream_t stream) {
+  return gemm_tiled<double>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, nullptr, 0, stream);
 }
 
 int otg_mlp_relu_bwd(float* dY, const float* Y, int64_t n, cudaStream_t stream) {
