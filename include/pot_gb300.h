@@ -178,6 +178,39 @@ size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, i
 int otg_sinkhorn_multi(const OtgMultiProblem* q, cudaStream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Online ("lazy") log-domain Sinkhorn on point clouds with squared-Euclidean
+ * cost that is never stored: cost tiles |x|^2 + |y|^2 - 2 x.y come from
+ * tcgen05 MMAs on high/low half planes of the points (prescaled by the
+ * powers of two scale_x, scale_y), folded into per-row running LSE pairs.
+ * Replaces the blockwise loop of ot/bregman/_empirical.py:205-248
+ * (empirical_sinkhorn, isLazy=True): f first, then g; the L1 row-marginal
+ * error after iterations with (i+1) % 10 == 0, compared with <=.  The host
+ * loop runs inside the call (one synchronisation per check), so the call
+ * returns with the results; info[0] status, info[1] niter, info[2] number
+ * of logged errors (err_hist is HOST memory, hist_cap doubles).  X: n x d,
+ * Y: m x d fp32 row-major, d <= 128; a, b weights; warm_f, warm_g optional
+ * natural-log potentials.
+ * ---------------------------------------------------------------------- */
+typedef struct OtgOnlineProblem {
+  const float* X; const float* Y;
+  int64_t n, m;
+  int32_t d;
+  int32_t max_iter;
+  const float* a; const float* b;
+  const float* warm_f; const float* warm_g;
+  double reg;
+  double stop_thr;
+  float scale_x, scale_y;
+  float* out_f; float* out_g;
+  double* err_hist; int32_t hist_cap;
+  int32_t* info;         /* HOST, 3 ints */
+  void* workspace; size_t workspace_bytes;
+  int32_t timeout_ms;
+} OtgOnlineProblem;
+size_t otg_online_workspace_bytes(int64_t n, int64_t m, int32_t d);
+int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
  * Squared-Euclidean cost blocks for a table of point-cloud pairs:
  * M_p[i, j] = sum_k (X_p[i, k] - Y_p[j, k])^2 for j < cols[p]; padded
  * columns [cols[p], ldm[p]) are set to +inf.  max_out (optional, one value

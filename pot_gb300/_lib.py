@@ -66,6 +66,14 @@ class OtgSplitGemm(ctypes.Structure):
                 ("colv", c_vp), ("abort_flag", c_vp), ("timeout_ms", c_i32)]
 
 
+class OtgOnlineProblem(ctypes.Structure):
+    _fields_ = [("X", c_vp), ("Y", c_vp), ("n", c_i64), ("m", c_i64), ("d", c_i32), ("max_iter", c_i32),
+                ("a", c_vp), ("b", c_vp), ("warm_f", c_vp), ("warm_g", c_vp), ("reg", c_dbl), ("stop_thr", c_dbl),
+                ("scale_x", ctypes.c_float), ("scale_y", ctypes.c_float), ("out_f", c_vp), ("out_g", c_vp),
+                ("err_hist", ctypes.POINTER(c_dbl)), ("hist_cap", c_i32), ("info", ctypes.POINTER(c_i32)),
+                ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "otg_dense_workspace_bytes": (c_sz, [ctypes.c_int, c_i64, c_i64, ctypes.c_int, ctypes.c_int]),
@@ -79,6 +87,8 @@ SIGNATURES = {
     "otg_sinkhorn_batched": (ctypes.c_int, [ctypes.POINTER(OtgBatchProblem), c_vp]),
     "otg_multi_workspace_bytes": (c_sz, [ctypes.c_int, c_i32, c_i64, c_i64, c_i64]),
     "otg_sinkhorn_multi": (ctypes.c_int, [ctypes.POINTER(OtgMultiProblem), c_vp]),
+    "otg_online_workspace_bytes": (c_sz, [c_i64, c_i64, c_i32]),
+    "otg_sinkhorn_online": (ctypes.c_int, [ctypes.POINTER(OtgOnlineProblem), c_vp]),
     "otg_batched_sqdist": (ctypes.c_int, [ctypes.POINTER(OtgCostTable), c_i32, c_vp]),
     "otg_batched_plan": (ctypes.c_int, [ctypes.POINTER(OtgPlanTable), c_i32, c_vp]),
     "otg_softmin_features": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32,
