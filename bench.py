@@ -174,6 +174,176 @@ def run_warmstart(args, pk):
     }
 
 
+# ---------------------------------------------------------------------------
+# other workloads (one JSON line each; not the default)
+# ---------------------------------------------------------------------------
+def _timed(fn, st):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    out = fn()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return out, e0.elapsed_time(e1)
+
+
+def gmm_clouds(n, d, comps, mean_std, std, seed, device):
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    means = torch.randn(comps, d, generator=g, device=device) * mean_std
+    def cloud():
+        c = torch.randint(0, comps, (n,), generator=g, device=device)
+        return (means[c] + torch.randn(n, d, generator=g, device=device) * std).contiguous()
+    return cloud(), cloud(), g
+
+
+def run_online(args, pk):
+    """Online (lazy) log-Sinkhorn: n = m = args.n points in R^64, 8-component
+    mixture (means ~ N(0, 4I), covariance 0.5 I), weights uniform x
+    Dirichlet(50), reg = 0.01 x median cost (4096-point subsample),
+    stopThr 1e-6; cost never stored."""
+    import torch
+    from pot_gb300 import _lib
+    from pot_gb300.empirical import online_sinkhorn
+    dev = torch.device("cuda:0")
+    n, d = args.n, 64
+    X, Y, g = gmm_clouds(n, d, 8, 2.0, 0.5 ** 0.5, 7, dev)
+    gam = torch.distributions.Gamma(torch.full((n,), 50.0, device=dev), torch.ones(n, device=dev))
+    a = gam.sample(); a = (a / a.sum()).float().contiguous()
+    b = gam.sample(); b = (b / b.sum()).float().contiguous()
+    k = min(4096, n)
+    reg = 0.01 * float(torch.cdist(X[:k].double(), Y[:k].double()).pow(2).median())
+    st = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        online_sinkhorn(X, Y, reg, a, b, 2, 0.0)
+    iters = args.iters
+    (res, ms) = _timed(lambda: online_sinkhorn(X, Y, reg, a, b, iters, 0.0), st)
+    per_it = ms / iters
+    flop = 4.0 * n * n * d
+    achieved = flop / (per_it * 1e-3) / 1e12
+    full = None
+    if args.full:
+        (res2, ms2) = _timed(lambda: online_sinkhorn(X, Y, reg, a, b, args.full, 1e-6), st)
+        full = {"ms": ms2, "niter": res2[3], "status": res2[2], "last_err": res2[4][-1] if res2[4] else None}
+    return {"metric": "online log-Sinkhorn iterations/s", "value": 1000.0 / per_it, "unit": "iterations/s",
+            "ms_per_step": per_it, "dtype": "f32 (fp16 hi/lo x3 tensor-core dot products)",
+            "config": {"workload": "online log-Sinkhorn n=m=%d d=64 GMM(8), reg=0.01 x median cost (%.4g)" % (n, reg),
+                       "timed_iterations": iters, "l2": "points %.0f MiB, cost never stored" % (2 * n * d * 4 / 2**20)},
+            "full_solve": full,
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                         "frac": achieved / pk["bf16_tflops"], "issued_multiplier": 3,
+                         "issued_frac": 3 * achieved / pk["bf16_tflops"], "traffic": None,
+                         "kernel": "online_pass_kernel", "alg_flop_per_iteration": flop}}
+
+
+def run_gw(args, pk):
+    """Entropic GW, n = m = args.n: C1 = sqeuclid of N(0, I3) points, C2 of
+    N(0, I8) points, each / max; uniform p, q; square loss; eps = 5e-3;
+    args.outer outer iterations; inner log-Sinkhorn at 1e-7 warm-started
+    from the previous potentials; float32 with tensor-core products."""
+    import torch
+    from pot_gb300 import gromov as pgw
+    dev = torch.device("cuda:0")
+    n = args.n
+    g = torch.Generator(device=dev); g.manual_seed(3)
+    xs = torch.randn(n, 3, generator=g, device=dev, dtype=torch.float64)
+    xt = torch.randn(n, 8, generator=g, device=dev, dtype=torch.float64)
+    C1 = torch.cdist(xs, xs).pow(2); C1 /= C1.max()
+    C2 = torch.cdist(xt, xt).pow(2); C2 /= C2.max()
+    C1, C2 = C1.float().contiguous(), C2.float().contiguous()
+    st = torch.cuda.current_stream()
+    pd = torch.full((n,), 1.0 / n, device=dev)
+    tp = pgw.TensorProduct(C1, C2, pd, pd)
+    T = torch.outer(pd, pd)
+    M = torch.empty(n, n, device=dev)
+    for _ in range(args.warmup):
+        tp.grad(T, M)
+    kms = []
+    for _ in range(max(args.steps, 3)):
+        (_, ms) = _timed(lambda: tp.grad(T, M), st)
+        kms.append(ms)
+    gemm_ms = statistics.median(kms)
+    flop = 4.0 * n ** 3  # two n^3 GEMMs
+    achieved = flop / (gemm_ms * 1e-3) / 1e12
+    (res, ms) = _timed(lambda: pgw.entropic_gromov_wasserstein_log(C1, C2, epsilon=5e-3, max_iter=args.outer,
+                                                                  numItermax=100000, stopThr=1e-7), st)
+    T, lg = res
+    return {"metric": "entropic GW outer iterations/s", "value": args.outer / (ms * 1e-3), "unit": "outer iterations/s",
+            "ms_per_step": ms / args.outer, "dtype": "f32 (fp16 hi/lo x3 tensor-core GEMMs)",
+            "config": {"workload": "entropic GW n=m=%d, eps=5e-3, %d outer iterations, inner log-Sinkhorn 1e-7 warm"
+                                   % (n, args.outer), "inner_niter": lg["inner_niter"], "gw_dist": lg["gw_dist"]},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                         "frac": achieved / pk["bf16_tflops"], "issued_multiplier": 3,
+                         "issued_frac": 3 * achieved / pk["bf16_tflops"], "traffic": None,
+                         "kernel": "gemm_split3_kernel (both GEMMs of one gradient)", "gemm_ms": gemm_ms,
+                         "alg_flop_per_gradient": flop}}
+
+
+def run_ragged(args, pk):
+    """4096 independent problems, n, m ~ U{32..1024}, d in {3, 16}, points ~
+    U[0,1]^d, a, b ~ Dirichlet(1), reg = 10^U[-3,-1] x max cost, stopThr
+    1e-6, float32, one persistent launch."""
+    import torch
+    from pot_gb300 import batch as pb
+    rng = np.random.default_rng(0)
+    B = args.batch
+    Xs, Ys, As, Bs, regs = [], [], [], [], []
+    for k in range(B):
+        n, m = rng.integers(32, 1025, size=2)
+        d = 3 if k % 2 == 0 else 16
+        Xs.append(rng.random((n, d))); Ys.append(rng.random((m, d)))
+        As.append(rng.dirichlet(np.ones(n))); Bs.append(rng.dirichlet(np.ones(m))); regs.append(10 ** rng.uniform(-3, -1))
+    st = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        pb.solve_sample_ragged(Xs[:64], Ys[:64], regs[:64], As[:64], Bs[:64], reg_relative=True, max_iter=1000, tol=1e-6)
+    (res, ms) = _timed(lambda: pb.solve_sample_ragged(Xs, Ys, regs, As, Bs, reg_relative=True, max_iter=100000,
+                                                      tol=1e-6), st)
+    nit = res.niter.cpu().numpy().astype(np.int64)
+    L = res.layout
+    alg = float((((nit + 2) + (nit + 1)) * L.rows_np * L.ldm_np * 4).sum())
+    return {"metric": "batched Sinkhorn solves/s", "value": B / (ms * 1e-3), "unit": "solves/s", "ms_per_step": ms,
+            "dtype": "f32", "config": {"workload": "%d uneven problems n,m~U[32,1024], d in {3,16}, reg=10^U[-3,-1] x "
+                                                   "max cost, stopThr=1e-6" % B,
+                                       "niter_median": float(np.median(nit)), "niter_max": int(nit.max()),
+                                       "status_counts": np.bincount(res.status.cpu().numpy(), minlength=4).tolist()},
+            "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": alg / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], "traffic": None,
+                         "kernel": "multi_sinkhorn_kernel (+ cost build)", "alg_bytes": alg}}
+
+
+def run_dense(args, pk):
+    """One dense log-domain solve: n = m = args.n points in R^2, N(0, I) vs
+    N((1,1), 0.5 I), cost / max, reg = 0.05, stopThr 1e-6, float32 (the
+    plain dense workload scaled up until the cost exceeds L2)."""
+    import torch
+    from pot_gb300 import bregman, _lib
+    dev = torch.device("cuda:0")
+    n = args.n
+    g = torch.Generator(device=dev); g.manual_seed(0)
+    x = torch.randn(n, 2, generator=g, device=dev, dtype=torch.float64)
+    y = torch.randn(n, 2, generator=g, device=dev, dtype=torch.float64) * 0.5 ** 0.5 + 1.0
+    M = torch.cdist(x, y).pow(2); M /= M.max(); M = M.float().contiguous()
+    a = torch.full((n,), 1.0 / n, device=dev)
+    st = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        bregman.solve_dense(M, a, a, 0.05, _lib.OTG_METHOD_LOG, 10000, 1e-6)
+    kms = []
+    for _ in range(args.steps):
+        (r, ms) = _timed(lambda: bregman.solve_dense(M, a, a, 0.05, _lib.OTG_METHOD_LOG, 10000, 1e-6,
+                                                     read_back=False), st)
+        kms.append(ms)
+    bregman.read_result(r)
+    ms = statistics.median(kms)
+    alg = ((r.niter + 2) + (r.niter + 1)) * n * n * 4.0
+    return {"metric": "dense Sinkhorn solves/s", "value": 1000.0 / ms, "unit": "solves/s", "ms_per_step": ms,
+            "dtype": "f32", "config": {"workload": "dense log-Sinkhorn n=m=%d, reg=0.05, stopThr=1e-6" % n,
+                                       "iterations": r.niter + 1, "l2": "M = %.2f GiB" % (n * n * 4 / 2**30)},
+            "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": alg / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], "traffic": None,
+                         "kernel": "dense_sinkhorn_kernel", "alg_bytes_per_launch": alg}}
+
+
 def _oracle_pair_solve(args):
     """One float64 oracle solve of a workload pair (run in a worker process)."""
     x, y = args
@@ -218,6 +388,10 @@ def main():
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--n", type=int, default=65536)
+    ap.add_argument("--iters", type=int, default=20)
+    ap.add_argument("--full", type=int, default=0)
+    ap.add_argument("--outer", type=int, default=50)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
@@ -235,6 +409,13 @@ def main():
         print(json.dumps(line))
         return
     pk = peaks()
+    if args.workload != "warmstart":
+        fn = {"online": run_online, "gw": run_gw, "ragged": run_ragged, "dense": run_dense}[args.workload]
+        line = {"n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "data": "synthetic"}
+        line.update(fn(args, pk))
+        print(json.dumps(line))
+        return
     res = run_warmstart(args, pk)
     line = {"metric": METRIC, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -66,6 +66,37 @@ __device__ __forceinline__ T lse_value(T mx, T s) {
   return mx + lg2(s);
 }
 
+// Merge `cnt` (max, sum) pairs stored as consecutive (mx, s) values at
+// p, p + stride, p + 2 stride, ...  (L2-coherent loads, eight independent
+// loads in flight before the dependent merges).
+template <typename T>
+__device__ __forceinline__ void lse_merge_strided(T& mx, T& s, const T* p, int64_t stride, int cnt) {
+  int r = 0;
+  for (; r + 8 <= cnt; r += 8) {
+    T m8[8], s8[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { m8[k] = __ldcg(p + (r + k) * stride); s8[k] = __ldcg(p + (r + k) * stride + 1); }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) lse_merge(mx, s, m8[k], s8[k]);
+  }
+  for (; r < cnt; ++r) lse_merge(mx, s, __ldcg(p + r * stride), __ldcg(p + r * stride + 1));
+}
+
+template <typename T>
+__device__ __forceinline__ T sum_strided(const T* p, int64_t stride, int cnt) {
+  T acc = 0;
+  int r = 0;
+  for (; r + 8 <= cnt; r += 8) {
+    T v8[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v8[k] = __ldcg(p + (r + k) * stride + 1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc += v8[k];
+  }
+  for (; r < cnt; ++r) acc += __ldcg(p + r * stride + 1);
+  return acc;
+}
+
 template <typename T>
 __device__ __forceinline__ void warp_lse(T& mx, T& s) {
 #pragma unroll

@@ -59,19 +59,26 @@ constexpr int RW = 4;     // rows per warp in the row pass
 constexpr int GCOL = 4;   // rows folded per max update in the column pass
 
 // ---------------------------------------------------------------------------
-// Column pass: one warp-unit = (row chunk r, slab of 32*VW columns).
+// Column pass: one CTA-unit = (row chunk r, slab of 32*VW columns).  The 8
+// warps split the chunk's rows, each lane folds its VW columns, and the 8
+// warp results are merged in shared memory, so each column has one partial
+// pair per row chunk (few chunks: a short merge).
 // ---------------------------------------------------------------------------
 template <typename T, int METHOD, bool VEC>
-__device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, long gwarp, long nwarps, int lane) {
+__device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, int lane) {
   constexpr int VW = Vec<T>::N;
   using V = typename Vec<T>::type;
+  __shared__ T s_mx[8][32 * Vec<T>::N], s_s[8][32 * Vec<T>::N];
+  const int warp = threadIdx.x >> 5;
   const int64_t n = A.n, m = A.m;
   const int64_t slab_w = 32 * VW;
   const int64_t nslabs = (m + slab_w - 1) / slab_w;
   const int64_t units = nslabs * A.Sr;
-  for (int64_t unit = gwarp; unit < units; unit += nwarps) {
+  for (int64_t unit = blockIdx.x; unit < units; unit += gridDim.x) {
     const int64_t slab = unit % nslabs, r = unit / nslabs;
-    const int64_t i0 = r * A.rchunk, i1 = min(n, i0 + A.rchunk);
+    const int64_t c0 = r * A.rchunk, c1 = min(n, c0 + A.rchunk);
+    const int64_t sub = (c1 - c0 + 7) / 8;
+    const int64_t i0 = min(c1, c0 + warp * sub), i1 = min(c1, i0 + sub);
     const int64_t j0 = slab * slab_w + lane * VW;
     T mx[VW], s[VW];
 #pragma unroll
@@ -123,17 +130,31 @@ __device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, long gw
           }
         }
       }
-#pragma unroll
-      for (int k = 0; k < VW; ++k)
-        if (j0 + k < m) A.pcol[r * m + j0 + k] = Pair<T>{mx[k], s[k]};
     }
+#pragma unroll
+    for (int k = 0; k < VW; ++k) { s_mx[warp][lane * VW + k] = mx[k]; s_s[warp][lane * VW + k] = s[k]; }
+    __syncthreads();
+    // threads 0..32*VW-1 merge the 8 warp results of one column each
+    for (int c = threadIdx.x; c < 32 * VW; c += blockDim.x) {
+      const int64_t j = slab * slab_w + c;
+      if (j < m) {
+        T M0 = -INFINITY, S0 = 0;
+        for (int w = 0; w < 8; ++w) {
+          if (METHOD == OTG_METHOD_LOG) lse_merge(M0, S0, s_mx[w][c], s_s[w][c]);
+          else S0 += s_s[w][c];
+        }
+        A.pcol[r * m + j] = Pair<T>{M0, S0};
+      }
+    }
+    __syncthreads();
   }
 }
 
 // ---------------------------------------------------------------------------
-// Row pass: one warp-unit = (group of RW rows, column chunk cc).  With one
-// column chunk the potential update is applied directly; otherwise the
-// partial pairs are merged after a barrier by row_merge.
+// Row pass: one CTA-unit = (group of RW rows, column chunk cc); the 8 warps
+// split the chunk's columns and merge in shared memory.  With one column
+// chunk the potential update is applied directly; otherwise the partial pairs
+// are merged after a barrier by row_merge.
 // ---------------------------------------------------------------------------
 template <typename T, int METHOD>
 __device__ __forceinline__ T row_finalize(const DenseArgs<T>& A, int64_t i, T mx, T s, int* numflag) {
@@ -147,21 +168,22 @@ __device__ __forceinline__ T row_finalize(const DenseArgs<T>& A, int64_t i, T mx
 }
 
 template <typename T, int METHOD, bool VEC>
-__device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __restrict__ unew,
-                         long gwarp, long nwarps, int lane) {
+__device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __restrict__ unew, int lane) {
   constexpr int VW = Vec<T>::N;
   using V = typename Vec<T>::type;
+  __shared__ T r_mx[8][RW], r_s[8][RW];
+  const int warp = threadIdx.x >> 5;
   const int64_t n = A.n, m = A.m;
   const int64_t ngroups = (n + RW - 1) / RW;
   const int64_t units = ngroups * A.Sc;
-  for (int64_t unit = gwarp; unit < units; unit += nwarps) {
+  for (int64_t unit = blockIdx.x; unit < units; unit += gridDim.x) {
     const int64_t grp = unit % ngroups, cc = unit / ngroups;
     const int64_t r0 = grp * RW;
     const int64_t c0 = cc * A.cchunk, c1 = min(m, c0 + A.cchunk);
     T mx[RW], s[RW];
 #pragma unroll
     for (int r = 0; r < RW; ++r) { mx[r] = -INFINITY; s[r] = 0; }
-    for (int64_t j = c0 + lane * VW; j < c1; j += 32 * VW) {
+    for (int64_t j = c0 + (warp * 32 + lane) * VW; j < c1; j += 256 * VW) {
       T vv[VW];
       if (VEC) {
         unpack(__ldcg(reinterpret_cast<const V*>(v + j)), vv);
@@ -208,17 +230,25 @@ __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __re
       if (METHOD == OTG_METHOD_LOG) warp_lse(mx[r], s[r]);
       else s[r] = warp_sum(s[r]);
     }
-    if (lane < RW) {
-      // lane r publishes row r (registers indexed with a compile-time loop)
+    if (lane == 0) {
 #pragma unroll
-      for (int r = 0; r < RW; ++r) {
-        if (lane == r && r0 + r < n) {
-          const int64_t row = r0 + r;
-          if (A.Sc == 1) unew[row] = row_finalize<T, METHOD>(A, row, mx[r], s[r], A.info + 4);
-          else A.prow[cc * n + row] = Pair<T>{mx[r], s[r]};
+      for (int r = 0; r < RW; ++r) { r_mx[warp][r] = mx[r]; r_s[warp][r] = s[r]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < RW) {
+      const int r = threadIdx.x;
+      const int64_t row = r0 + r;
+      if (row < n) {
+        T M0 = -INFINITY, S0 = 0;
+        for (int w = 0; w < 8; ++w) {
+          if (METHOD == OTG_METHOD_LOG) lse_merge(M0, S0, r_mx[w][r], r_s[w][r]);
+          else S0 += r_s[w][r];
         }
+        if (A.Sc == 1) unew[row] = row_finalize<T, METHOD>(A, row, M0, S0, A.info + 4);
+        else A.prow[cc * n + row] = Pair<T>{M0, S0};
       }
     }
+    __syncthreads();
   }
 }
 
@@ -226,11 +256,9 @@ template <typename T, int METHOD>
 __device__ void row_merge(const DenseArgs<T>& A, T* __restrict__ unew, long gtid, long nthreads) {
   for (int64_t i = gtid; i < A.n; i += nthreads) {
     T mx = -INFINITY, s = 0;
-    for (int cc = 0; cc < A.Sc; ++cc) {
-      Pair<T> p = ldcg_pair(A.prow + (int64_t)cc * A.n + i);
-      if (METHOD == OTG_METHOD_LOG) lse_merge(mx, s, p.mx, p.s);
-      else s += p.s;
-    }
+    const T* base = reinterpret_cast<const T*>(A.prow + i);
+    if (METHOD == OTG_METHOD_LOG) lse_merge_strided(mx, s, base, 2 * A.n, A.Sc);
+    else s = sum_strided(base, 2 * A.n, A.Sc);
     unew[i] = row_finalize<T, METHOD>(A, i, mx, s, A.info + 4);
   }
 }
@@ -243,11 +271,9 @@ __device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* 
   double e2 = 0.0;
   for (int64_t j = gtid; j < A.m; j += nthreads) {
     T mx = -INFINITY, s = 0;
-    for (int r = 0; r < A.Sr; ++r) {
-      Pair<T> p = ldcg_pair(A.pcol + (int64_t)r * A.m + j);
-      if (METHOD == OTG_METHOD_LOG) lse_merge(mx, s, p.mx, p.s);
-      else s += p.s;
-    }
+    const T* base = reinterpret_cast<const T*>(A.pcol + j);
+    if (METHOD == OTG_METHOD_LOG) lse_merge_strided(mx, s, base, 2 * A.m, A.Sr);
+    else s = sum_strided(base, 2 * A.m, A.Sr);
     const T bj = A.b[j];
     if (METHOD == OTG_METHOD_LOG) {
       const T L = lse_value(mx, s);
@@ -319,7 +345,7 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
   int nchk = 0;
   int status = OTG_STATUS_MAXITER, niter = A.max_iter - 1;
   for (int ii = 0;; ++ii) {
-    col_pass<T, METHOD, VEC>(A, ucur, gwarp, nwarps, lane);
+    col_pass<T, METHOD, VEC>(A, ucur, lane);
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     const bool update = ii < A.max_iter;
     double* slot = A.hist + (nchk < A.hist_cap ? nchk : A.hist_cap - 1);
@@ -335,7 +361,7 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
       // zero column sum or non-finite v: revert to the previous pair
       status = OTG_STATUS_NUMERICAL; niter = ii; break;
     }
-    row_pass<T, METHOD, VEC>(A, vnxt, unxt, gwarp, nwarps, lane);
+    row_pass<T, METHOD, VEC>(A, vnxt, unxt, lane);
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     if (A.Sc > 1) {
       row_merge<T, METHOD>(A, unxt, gtid, nthreads);
@@ -439,17 +465,19 @@ Layout make_layout(int64_t n, int64_t m, int hist_cap, int grid) {
   constexpr int VW = Vec<T>::N;
   Layout L{};
   L.grid = grid;
-  const int64_t W = (int64_t)grid * 8;
+  // column pass: CTA units (slab, row chunk), about two per CTA, each warp
+  // at least 4 rows; row pass: CTA units (RW rows, column chunk), a column
+  // split only when there are fewer row groups than CTAs
   const int64_t nslabs = (m + 32 * VW - 1) / (32 * VW);
-  int64_t Sr = (2 * W + nslabs - 1) / nslabs;
-  Sr = std::max<int64_t>(1, std::min<int64_t>(Sr, (n + 15) / 16));
+  int64_t Sr = (2 * (int64_t)grid + nslabs - 1) / nslabs;
+  Sr = std::max<int64_t>(1, std::min<int64_t>(Sr, (n + 31) / 32));
   L.rchunk = (n + Sr - 1) / Sr;
   L.Sr = (int)((n + L.rchunk - 1) / L.rchunk);
   const int64_t ngroups = (n + RW - 1) / RW;
-  int64_t Sc = (2 * W + ngroups - 1) / ngroups;
-  Sc = std::max<int64_t>(1, std::min<int64_t>(Sc, (m + 32 * VW * 4 - 1) / (32 * VW * 4)));
+  int64_t Sc = ngroups >= grid ? 1 : (grid + ngroups - 1) / ngroups;
+  Sc = std::max<int64_t>(1, std::min<int64_t>(Sc, (m + 256 * VW - 1) / (256 * VW)));
   int64_t cch = (m + Sc - 1) / Sc;
-  cch = (cch + 32 * VW - 1) / (32 * VW) * (32 * VW);
+  cch = (cch + 256 * VW - 1) / (256 * VW) * (256 * VW);
   L.cchunk = cch;
   L.Sc = (int)((m + cch - 1) / cch);
   size_t off = 0;

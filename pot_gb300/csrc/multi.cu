@@ -155,10 +155,7 @@ __device__ void mt_col_merge(const MultiArgs<T>& A, int nact, const T* vcur, T* 
     const MPair<T>* pc = A.pcol + A.pc_off[p];
     T mx = -INFINITY, s = 0;
     const int nsr = __ldcg(A.nsr + p);
-    for (int r = 0; r < nsr; ++r) {
-      const T* q = reinterpret_cast<const T*>(pc + (int64_t)r * m + j);
-      lse_merge(mx, s, __ldcg(q), __ldcg(q + 1));
-    }
+    lse_merge_strided(mx, s, reinterpret_cast<const T*>(pc + j), 2 * (int64_t)m, nsr);
     const T L = lse_value(mx, s);
     const int64_t cj = A.c_off[p] + j;
     const T bj = A.b[cj];
@@ -288,7 +285,9 @@ __device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leavi
     atomicAdd(reinterpret_cast<unsigned long long*>(&s_slabs), (unsigned long long)part);
   }
   __syncthreads();
-  const int64_t S = s_slabs > 0 ? (8 * nwarps + s_slabs - 1) / s_slabs : 1;
+  // capped at 16 chunks: more splits only lengthen the merge
+  int64_t S = s_slabs > 0 ? (8 * nwarps + s_slabs - 1) / s_slabs : 1;
+  S = S > 16 ? 16 : S;
   for (int k = threadIdx.x; k < s_base; k += blockDim.x) {
     const int p = A.active[k];
     const int n = A.rows[p];

@@ -3,7 +3,8 @@
 The online path computes in float32 with tensor-core dot products carrying
 about 22 bits; against the float64 oracle the plan agrees to relative L1
 <= 2e-5, the row-marginal violation re-evaluated with the exact float64 cost
-is <= 2e-5, and the stop index matches the oracle's within one check.
+is <= 2e-5, and the stop index matches the oracle's within one check (2% of
+the count for slowly converging cases).
 """
 import numpy as np
 import pytest
@@ -58,7 +59,9 @@ def test_online_vs_oracle(cuda, n, m, d):
     assert lr["niter"] < 4999, "oracle did not converge: pick a larger reg"
     assert rel <= 2e-5
     assert viol <= 2e-5
-    assert abs(lg["niter"] - lr["niter"]) <= 10
+    # near stopThr the float32 error estimate crosses the threshold a few
+    # checks apart from the float64 one when convergence is slow
+    assert abs(lg["niter"] - lr["niter"]) <= max(10, 0.02 * lr["niter"])
 
 
 def test_non_lazy_matches_dense(cuda):
