@@ -33,6 +33,10 @@ sys.path.insert(0, HERE)
 
 METRIC = "Sinkhorn solves/s at marginal err 1e-6, warm vs plain, 1 GB300; % roofline"
 WS_N, WS_D, WS_REG, WS_TOL = 2048, 16, 0.02, 1e-6
+# DRAM traffic / algorithmic bytes of multi_sinkhorn_kernel, from one ncu capture of the
+# same workload on 128 pairs (profiles/multi_sinkhorn_warmstart_gmm2048.md); the launch's
+# traffic scales with the problem-iterations it processes
+MULTI_TRAFFIC_RATIO = 132.42 / 133.61
 EVAL_SEED = 10_000_000
 
 
@@ -164,7 +168,9 @@ def run_warmstart(args, pk):
                        B * WS_N * WS_N * 4 / 2**30),
                    "held_out_seeds": [EVAL_SEED, EVAL_SEED + B - 1]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "traffic": None, "kernel": "multi_sinkhorn_kernel (plain arm)",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": p["alg_bytes"] * MULTI_TRAFFIC_RATIO,
+                     "traffic_src": "ncu capture on 128 pairs, scaled by problem-iterations",
+                     "kernel": "multi_sinkhorn_kernel (plain arm)",
                      "alg_bytes_per_launch": p["alg_bytes"], "launch_ms": p["kernel_ms"],
                      "peak_src": pk["src"] + " (of measured)" if pk["src"] == "measured" else pk["src"]},
         "e2e": {"value": B / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(Xh.nbytes + Yh.nbytes),

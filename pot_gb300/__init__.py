@@ -11,5 +11,6 @@ from . import batch  # noqa: F401
 from .batch import solve_batch, solve_sample_batch, dist_batch  # noqa: F401
 from . import gromov  # noqa: F401
 from .empirical import empirical_sinkhorn  # noqa: F401
+from .patch import patch_pot, unpatch_pot  # noqa: F401
 
 __version__ = "0.1.0"

@@ -1,0 +1,90 @@
+"""Route an installed POT (``import ot``) through the GPU implementations.
+
+POT binds the solver functions by name at import time in several modules,
+so rebinding ``ot.sinkhorn`` alone is not enough.  ``patch_pot(ot)``
+replaces the hot-path names in every module that imported them:
+
+    ot/__init__.py:56            sinkhorn, sinkhorn2
+    ot/bregman/__init__.py:13    sinkhorn, sinkhorn2, sinkhorn_knopp, sinkhorn_log, empirical_sinkhorn
+    ot/bregman/_sinkhorn.py      sinkhorn_knopp, sinkhorn_log (the dispatcher's callees)
+    ot/bregman/_empirical.py:18  sinkhorn, sinkhorn2
+    ot/gromov/_bregman.py:17     sinkhorn
+    ot/gromov/__init__.py        entropic_gromov_wasserstein(2)
+    ot/batch/__init__.py         solve_batch, solve_sample_batch, dist_batch,
+                                 bregman_log_projection_batch, bregman_projection_batch
+    ot/batch/_linear.py          the same (module-level callers)
+    ot/batch/_quadratic.py:14    bregman_log_projection_batch
+    ot/solvers.py:14             sinkhorn_log
+
+Calls the GPU path does not cover (other methods, metrics or losses) raise
+NotImplementedError from the GPU function; ``unpatch_pot`` restores the
+original bindings.
+"""
+import importlib
+
+from . import bregman, batch, gromov, empirical
+
+GPU = {
+    "sinkhorn": bregman.sinkhorn,
+    "sinkhorn2": bregman.sinkhorn2,
+    "sinkhorn_knopp": bregman.sinkhorn_knopp,
+    "sinkhorn_log": bregman.sinkhorn_log,
+    "empirical_sinkhorn": empirical.empirical_sinkhorn,
+    "entropic_gromov_wasserstein": gromov.entropic_gromov_wasserstein,
+    "entropic_gromov_wasserstein2": gromov.entropic_gromov_wasserstein2,
+    "solve_batch": batch.solve_batch,
+    "solve_sample_batch": batch.solve_sample_batch,
+    "dist_batch": batch.dist_batch,
+    "bregman_log_projection_batch": batch.bregman_log_projection_batch,
+    "bregman_projection_batch": batch.bregman_projection_batch,
+}
+
+MODULES = {
+    "": ["sinkhorn", "sinkhorn2"],
+    ".bregman": ["sinkhorn", "sinkhorn2", "sinkhorn_knopp", "sinkhorn_log", "empirical_sinkhorn"],
+    ".bregman._sinkhorn": ["sinkhorn_knopp", "sinkhorn_log"],
+    ".bregman._empirical": ["sinkhorn", "sinkhorn2"],
+    ".gromov": ["entropic_gromov_wasserstein", "entropic_gromov_wasserstein2"],
+    ".gromov._bregman": ["sinkhorn"],
+    ".batch": ["solve_batch", "solve_sample_batch", "dist_batch", "bregman_log_projection_batch",
+               "bregman_projection_batch"],
+    ".batch._linear": ["solve_batch", "dist_batch", "bregman_log_projection_batch", "bregman_projection_batch"],
+    ".batch._quadratic": ["bregman_log_projection_batch"],
+    ".solvers": ["sinkhorn_log"],
+}
+
+_saved = {}
+
+
+def _module(root, suffix):
+    name = root.__name__ + suffix
+    try:
+        return importlib.import_module(name)
+    except ImportError:
+        return None
+
+
+def patch_pot(ot_module):
+    """Rebind POT's hot-path names to the GPU implementations; returns the
+    list of (module, name) pairs that were replaced."""
+    done = []
+    for suffix, names in MODULES.items():
+        mod = _module(ot_module, suffix)
+        if mod is None:
+            continue
+        for name in names:
+            if hasattr(mod, name):
+                key = (mod.__name__, name)
+                if key not in _saved:
+                    _saved[key] = getattr(mod, name)
+                setattr(mod, name, GPU[name])
+                done.append(key)
+    return done
+
+
+def unpatch_pot(ot_module):
+    """Restore the bindings replaced by ``patch_pot``."""
+    for (modname, name), fn in list(_saved.items()):
+        mod = importlib.import_module(modname)
+        setattr(mod, name, fn)
+        del _saved[(modname, name)]

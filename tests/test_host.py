@@ -24,3 +24,38 @@ def test_unknown_method_raises_before_any_device_work():
 def test_is_empty():
     assert is_empty([]) and is_empty(np.array([])) and is_empty(torch.tensor([]))
     assert not is_empty([1.0])
+
+
+def test_patch_rebinds_every_importing_module(tmp_path, monkeypatch):
+    """patch_pot replaces the names in all modules that bound them at import
+    (a fake package tree stands in for POT)."""
+    import sys
+    import types
+    from pot_gb300 import patch as pp
+    root = types.ModuleType("fakeot")
+    root.__path__ = []
+    sys.modules["fakeot"] = root
+    made = {}
+    for suffix, names in pp.MODULES.items():
+        if suffix == "":
+            mod = root
+        else:
+            mod = types.ModuleType("fakeot" + suffix)
+            sys.modules["fakeot" + suffix] = mod
+        for nm in names:
+            setattr(mod, nm, ("orig", suffix, nm))
+        made[suffix] = mod
+    try:
+        done = pp.patch_pot(root)
+        assert len(done) == sum(len(v) for v in pp.MODULES.values())
+        for suffix, names in pp.MODULES.items():
+            for nm in names:
+                assert getattr(made[suffix], nm) is pp.GPU[nm]
+        pp.unpatch_pot(root)
+        for suffix, names in pp.MODULES.items():
+            for nm in names:
+                assert getattr(made[suffix], nm) == ("orig", suffix, nm)
+    finally:
+        for k in list(sys.modules):
+            if k == "fakeot" or k.startswith("fakeot."):
+                del sys.modules[k]
