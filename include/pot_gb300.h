@@ -318,6 +318,12 @@ typedef struct OtgSplitGemm {
 int otg_split_half(const float* X, int64_t rows, int64_t cols, int64_t ldx, float scale, int transpose, void* hi,
                    void* lo, int64_t ld_out, cudaStream_t stream);
 int otg_gemm_split3(const OtgSplitGemm* g, cudaStream_t stream);
+/* Batched tiled GEMM (CUDA cores), C_z = alpha op(A_z) op(B_z) + beta C_z for z < batch with
+ * element strides sA, sB, sC between batch members; replaces the einsum chains of
+ * ot/batch/_quadratic.py:535-572 (tensor_product_batch). */
+int otg_gemm_batched(int dtype, int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const void* A,
+                     int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, double beta, void* C,
+                     int64_t ldc, int64_t sC, int64_t batch, cudaStream_t stream);
 /* fp64 tiled GEMM (CUDA cores) for the float64 path: C = alpha op(A) op(B) + beta C. */
 int otg_gemm_f64(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
                  const double* B, int64_t ldb, double beta, double* C, int64_t ldc, cudaStream_t stream);

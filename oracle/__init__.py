@@ -26,4 +26,5 @@ from .entropic import (  # noqa: F401
     entropic_gromov_wasserstein,
     entropic_gw_log_inner,
     empirical_sinkhorn_lazy,
+    solve_gromov_batch,
 )

@@ -413,3 +413,68 @@ def empirical_sinkhorn_lazy(X, Y, reg, a=None, b=None, numIterMax=10000, stopThr
     if not stopped:
         warns.append(NONCONV)
     return f, g, {"err": errs, "u": f, "v": g, "niter": i_ot, "_warnings": warns}
+
+
+def solve_gromov_batch(C1, C2, reg=1e-2, a=None, b=None, symmetric=None, M=None, alpha=None, T_init=None,
+                       max_iter=50, tol=1e-5, max_iter_inner=50, tol_inner=1e-5, per_problem_inner=False):
+    """Batched proximal (fused) Gromov-Wasserstein, squared loss, scalar costs:
+    ``ot/batch/_quadratic.py:269-498`` with ``tensor_batch`` (:17, hC1 = 2 C1,
+    hC2 = C2, f = square; non-symmetric inputs symmetrise f), the outer step
+    ``Mk = (1-alpha) M + 2 alpha (constC - hC1 T hC2^T)`` (averaged with the
+    transposed product when not symmetric), ``K = -Mk/reg + log T`` projected by
+    the batched log Sinkhorn (:458-471), stop on ``max_b mean|T - Tprev| <
+    tol``.  ``per_problem_inner`` runs the inner projection one problem at a
+    time (each problem stops on its own error)."""
+    C1, C2 = _f64(C1), _f64(C2)
+    B, n, m = C1.shape[0], C1.shape[1], C2.shape[1]
+    a = np.ones((B, n)) / n if a is None else _f64(a)
+    b = np.ones((B, m)) / m if b is None else _f64(b)
+    tr = lambda X: np.transpose(X, (0, 2, 1))  # noqa: E731
+    if symmetric is None:
+        symmetric = np.allclose(C1, tr(C1), atol=1e-10) and np.allclose(C2, tr(C2), atol=1e-10)
+    fC1, fC2 = C1 ** 2, C2 ** 2
+    if not symmetric:
+        fC1, fC2 = 0.5 * (fC1 + tr(fC1)), 0.5 * (fC2 + tr(fC2))
+    hC1, hC2 = 2.0 * C1, C2
+    constC = np.einsum("bij,bj->bi", fC1, a)[:, :, None] + np.einsum("bij,bj->bi", fC2, b)[:, None, :]
+    if M is None and alpha is None:
+        M, alpha = np.zeros((B, n, m)), 1.0
+    elif M is None or alpha is None:
+        raise ValueError("M and alpha go together for the fused problem")
+    M = _f64(M)
+
+    def dot(T):
+        d = hC1 @ T @ tr(hC2)
+        if not symmetric:
+            d = 0.5 * (d + tr(hC1) @ T @ hC2)
+        return d
+
+    if T_init is None:
+        const = np.sqrt(a.sum(1) * b.sum(1))
+        T = np.einsum("bi,bj->bij", a, b) / const[:, None, None]
+    else:
+        T = _f64(T_init)
+    with np.errstate(divide="ignore"):
+        log_T = np.log(T + 1e-15)
+    it = 0
+    out = None
+    for it in range(max_iter):
+        T_prev = T
+        Mk = (1 - alpha) * M + 2 * alpha * (constC - dot(T))
+        K = -Mk / reg + log_T
+        if per_problem_inner:
+            parts = [log_projection_batch(K[k:k + 1], a[k:k + 1], b[k:k + 1], max_iter_inner, tol_inner)
+                     for k in range(B)]
+            out = {"T": np.concatenate([p["T"] for p in parts]), "log_T": np.concatenate([p["log_T"] for p in parts]),
+                   "potentials": (np.concatenate([p["potentials"][0] for p in parts]),
+                                  np.concatenate([p["potentials"][1] for p in parts]))}
+        else:
+            out = log_projection_batch(K, a, b, max_iter_inner, tol_inner)
+        T, log_T = out["T"], out["log_T"]
+        if np.max(np.mean(np.abs(T_prev - T), axis=(1, 2))) < tol:
+            break
+    vl = np.sum(M * T, axis=(1, 2))
+    const_rec = np.einsum("bij,bj->bi", fC1, T.sum(2))[:, :, None] + np.einsum("bij,bj->bi", fC2, T.sum(1))[:, None, :]
+    vq = np.sum((const_rec - dot(T)) * T, axis=(1, 2))
+    return {"plan": T, "value": (1 - alpha) * vl + alpha * vq, "value_linear": (1 - alpha) * vl,
+            "value_quad": alpha * vq, "potentials": out["potentials"], "n_iter": it}

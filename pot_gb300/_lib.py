@@ -97,6 +97,8 @@ SIGNATURES = {
                                     c_vp, c_i64, ctypes.c_float, c_vp, c_i64, c_vp, ctypes.c_int, c_vp]),
     "otg_gemm_f64": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, c_dbl, c_vp, c_i64, c_vp, c_i64,
                                     c_dbl, c_vp, c_i64, c_vp]),
+    "otg_gemm_batched": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, c_dbl, c_vp,
+                                        c_i64, c_i64, c_vp, c_i64, c_i64, c_dbl, c_vp, c_i64, c_i64, c_i64, c_vp]),
     "otg_split_half": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, ctypes.c_float, ctypes.c_int, c_vp, c_vp, c_i64,
                                       c_vp]),
     "otg_gemm_split3": (ctypes.c_int, [ctypes.POINTER(OtgSplitGemm), c_vp]),

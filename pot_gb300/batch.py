@@ -363,3 +363,101 @@ def solve_sample_ragged(Xs, Ys, reg, as_=None, bs=None, reg_relative=False, max_
         u, v, status, niter, err, reg_t = run_batched(layout, M, ap, bp, reg_t, code, max_iter, tol, u_first=0,
                                                       warm_u=wu, warm_v=wv)
     return RaggedResult(layout, u, v, status, niter, err, reg_t, M)
+
+
+# ---------------------------------------------------------------------------
+# Batched (fused) Gromov-Wasserstein
+# ---------------------------------------------------------------------------
+def _bgemm(A, B, ta, tb, out, alpha=1.0, beta=0.0):
+    """out_z = alpha op(A_z) op(B_z) + beta out_z over a batch (csrc/mlp.cu)."""
+    lib = _lib.load()
+    Bz = A.shape[0]
+    M = A.shape[2] if ta else A.shape[1]
+    K = A.shape[1] if ta else A.shape[2]
+    N = B.shape[1] if tb else B.shape[2]
+    _lib.check(lib.otg_gemm_batched(_lib.dtype_code(A.dtype), int(ta), int(tb), M, N, K, float(alpha),
+                                    _lib.ptr(A), A.shape[2], A.stride(0), _lib.ptr(B), B.shape[2], B.stride(0),
+                                    float(beta), _lib.ptr(out), out.shape[2], out.stride(0), Bz,
+                                    _lib.stream_handle(A.device)), "otg_gemm_batched")
+    return out
+
+
+def solve_gromov_batch(C1, C2, reg=1e-2, a=None, b=None, loss="sqeuclidean", symmetric=None, M=None, alpha=None,
+                       T_init=None, max_iter=50, tol=1e-5, max_iter_inner=50, tol_inner=1e-5, grad="envelope",
+                       logits=None):
+    """GPU ``ot.batch.solve_gromov_batch`` (``ot/batch/_quadratic.py:269-498``)
+    for the squared loss and scalar costs: per outer step the tensor product
+    ``constC - hC1 T hC2^T`` (batched GEMMs), ``Mk = (1 - alpha) M + 2 alpha
+    L x T``, and the batched log projection of ``-Mk/reg + log T`` (every
+    problem stops on its own inner error)."""
+    if not isinstance(loss, str):
+        raise ValueError(f"Unknown loss function: {loss}")
+    if loss != "sqeuclidean":
+        raise NotImplementedError("pot_gb300 solve_gromov_batch: loss '%s' is not on the GPU path" % loss)
+    bd = Boundary(C1, C2, a, b, M, T_init)
+    C1d = bd.to_dev(C1)
+    C2d = bd.to_dev(C2, C1d.dtype)
+    if C1d.dim() != 3 or C2d.dim() != 3:
+        raise NotImplementedError("pot_gb300 solve_gromov_batch: vector-valued (4-D) costs are not on the GPU path")
+    dt, dev = C1d.dtype, C1d.device
+    B, n, m = C1d.shape[0], C1d.shape[1], C2d.shape[1]
+    ad = torch.ones((B, n), dtype=dt, device=dev) / n if a is None else bd.to_dev(a, dt)
+    bv = torch.ones((B, m), dtype=dt, device=dev) / m if b is None else bd.to_dev(b, dt)
+    tr = lambda X: X.transpose(1, 2).contiguous()  # noqa: E731
+    if symmetric is None:
+        symmetric = bool(torch.allclose(C1d, tr(C1d), atol=1e-10) and torch.allclose(C2d, tr(C2d), atol=1e-10))
+    fC1, fC2 = C1d * C1d, C2d * C2d
+    if not symmetric:
+        fC1, fC2 = 0.5 * (fC1 + tr(fC1)), 0.5 * (fC2 + tr(fC2))
+    hC1, hC2 = (2.0 * C1d).contiguous(), C2d.contiguous()
+    hC1t, hC2t = (tr(hC1), tr(hC2)) if not symmetric else (None, None)
+    if M is None and alpha is None:
+        Md, alpha = torch.zeros((B, n, m), dtype=dt, device=dev), 1.0
+    elif M is not None and alpha is None:
+        raise ValueError("If M is provided, alpha must also be provided for Fused Gromov-Wasserstein problem")
+    elif M is None and alpha is not None:
+        raise ValueError("If alpha is provided, M must also be provided for Fused Gromov-Wasserstein problem")
+    else:
+        Md = bd.to_dev(M, dt).contiguous()
+        if tuple(Md.shape) != (B, n, m):
+            raise ValueError(f"Shape of M {tuple(Md.shape)} does not match the batch size {B} and dimensions {n}, {m}")
+        if alpha < 0 or alpha > 1:
+            raise ValueError("Alpha must be in [0, 1] for Fused Gromov-Wasserstein problem")
+
+    def const_of(p, q):
+        return (torch.einsum("bij,bj->bi", fC1, p)[:, :, None] + torch.einsum("bij,bj->bi", fC2, q)[:, None, :])
+
+    tmp = torch.empty((B, n, m), dtype=dt, device=dev)
+    dotb = torch.empty((B, n, m), dtype=dt, device=dev)
+
+    def dot(T):
+        _bgemm(hC1, T, 0, 0, tmp)
+        _bgemm(tmp, hC2, 0, 1, dotb)                 # hC1 T hC2^T
+        if not symmetric:
+            _bgemm(hC1t, T, 0, 0, tmp)
+            _bgemm(tmp, hC2t, 0, 1, dotb, 0.5, 0.5)  # average with hC1^T T hC2
+        return dotb
+
+    constC = const_of(ad, bv)
+    if T_init is None:
+        const = torch.sqrt(ad.sum(1) * bv.sum(1))
+        T = torch.einsum("bi,bj->bij", ad, bv) / const[:, None, None]
+    else:
+        T = bd.to_dev(T_init, dt).contiguous()
+    log_T = torch.log(T + 1e-15)
+    it = 0
+    u = v = None
+    for it in range(max_iter):
+        T_prev = T
+        Mk = (1 - alpha) * Md + 2 * alpha * (constC - dot(T))
+        K = -Mk / reg + log_T
+        T, u, v, _, _, _ = _solve_uniform((-K).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_LOG, max_iter_inner,
+                                          tol_inner, False)
+        log_T = K + u[:, :, None] + v[:, None, :]
+        if float(torch.amax(torch.mean(torch.abs(T_prev - T), dim=(1, 2)))) < tol:
+            break
+    vl = (Md * T).sum((1, 2))
+    vq = ((const_of(T.sum(2), T.sum(1)) - dot(T)) * T).sum((1, 2))
+    return OTResult(value=bd.out((1 - alpha) * vl + alpha * vq), value_linear=bd.out((1 - alpha) * vl),
+                    value_quad=bd.out(alpha * vq), plan=bd.out(T), potentials=(bd.out(u), bd.out(v)),
+                    log={"n_iter": it})

@@ -214,8 +214,67 @@ def _log_multi(bd, a, B, M, reg, numItermax, stopThr, verbose, log, warmstart):
 
 
 def _knopp_multi(bd, a, B, M, reg, numItermax, stopThr, verbose, log, warn, warmstart):
-    raise NotImplementedError("pot_gb300: scaling-form Sinkhorn with several target histograms "
-                              "is not implemented yet; use method='sinkhorn_log'")
+    """Scaling form with several target histograms (``_sinkhorn.py:600-687``
+    with ``n_hists``): the histograms evolve independently and interact only
+    through the joint stop (Frobenius norm of all column-marginal errors) and
+    the joint revert on numerical errors.  Each histogram is iterated on the
+    GPU with its error history; the joint stop index is found from the
+    histories, and every histogram is re-run to exactly that index."""
+    H = B.shape[1]
+    wu = wv = None
+    if warmstart is not None:
+        wu = bd.to_dev(warmstart[0], M.dtype)
+        wv = bd.to_dev(warmstart[1], M.dtype)
+    warm = lambda k: (None, None) if wu is None else (wu[:, k].contiguous(), wv[:, k].contiguous())  # noqa: E731
+    runs = [solve_dense(M, a, B[:, k].contiguous(), reg, _lib.OTG_METHOD_KNOPP, numItermax, 0.0, *warm(k))
+            for k in range(H)]
+    nan_at = min([r.niter for r in runs if r.status == _lib.STATUS_NUMERICAL], default=None)
+    nchk = min(len(r.errs) for r in runs)
+    joint = [float(np.sqrt(sum(r.errs[k] ** 2 for r in runs))) for k in range(nchk)]
+    stop_ii, errs = None, []
+    for k, e in enumerate(joint):
+        ii = 10 * k
+        if nan_at is not None and ii >= nan_at:
+            break
+        errs.append(e)
+        if e < stopThr:
+            stop_ii = ii
+            break
+    if stop_ii is not None:
+        final_iters, niter, status = stop_ii + 1, stop_ii, _lib.STATUS_CONVERGED
+    elif nan_at is not None:
+        final_iters, niter, status = nan_at, nan_at, _lib.STATUS_NUMERICAL
+    else:
+        final_iters, niter, status = numItermax, numItermax - 1, _lib.STATUS_MAXITER
+    if final_iters == numItermax and nan_at is None:
+        final = runs
+    else:
+        final = [solve_dense(M, a, B[:, k].contiguous(), reg, _lib.OTG_METHOD_KNOPP, final_iters, 0.0, *warm(k))
+                 for k in range(H)] if final_iters > 0 else None
+    if final is None:  # numerical error in the first iteration: the initial scalings
+        n, m = M.shape
+        U = torch.full((n, H), 1.0 / n, dtype=M.dtype, device=M.device) if wu is None else torch.exp(wu)
+        V = torch.full((m, H), 1.0 / m, dtype=M.dtype, device=M.device) if wv is None else torch.exp(wv)
+        losses = []
+        for k in range(H):
+            r = DenseResult()
+            r.u, r.v = U[:, k].contiguous(), V[:, k].contiguous()
+            losses.append(_loss(M, r, reg, _lib.OTG_METHOD_KNOPP))
+    else:
+        U = torch.stack([r.u for r in final], 1)
+        V = torch.stack([r.v for r in final], 1)
+        losses = [_loss(M, r, reg, _lib.OTG_METHOD_KNOPP) for r in final]
+    if status == _lib.STATUS_NUMERICAL:
+        warnings.warn("Warning: numerical errors at iteration %d" % niter)
+    if verbose:
+        _print_errs(np.array(errs[:-1] if status == _lib.STATUS_CONVERGED else errs), False)
+    if status == _lib.STATUS_MAXITER and warn:
+        warnings.warn(NONCONV_MSG)
+    res = torch.stack(losses)
+    if log:
+        return bd.out(res), {"err": _errs_as(bd, np.array(errs), M), "niter": niter, "u": bd.out(U),
+                             "v": bd.out(V)}
+    return bd.out(res)
 
 
 def sinkhorn(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, verbose=False,

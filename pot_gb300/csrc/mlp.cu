@@ -22,15 +22,23 @@ __global__ void __launch_bounds__(256) gemm_tiled_kernel(int ta, int tb, int64_t
                                                          const T* __restrict__ A, int64_t lda,
                                                          const T* __restrict__ B, int64_t ldb, T beta,
                                                          T* __restrict__ C, int64_t ldc,
-                                                         const T* __restrict__ bias, int relu) {
+                                                         const T* __restrict__ bias, int relu,
+                                                         int64_t sA, int64_t sB, int64_t sC, int splitk) {
   __shared__ T As[GK][GT + 4];
   __shared__ T Bs[GK][GT + 4];
+  // gridDim.z is either the split-K factor (splitk = 1) or the batch (strides sA, sB, sC)
+  if (!splitk) {
+    A += blockIdx.z * sA;
+    B += blockIdx.z * sB;
+    C += blockIdx.z * sC;
+  }
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t m0 = (int64_t)blockIdx.y * GT, n0 = (int64_t)blockIdx.x * GT;
   // split-K: CTA z covers k in [kbeg, kend) and adds its partial product
-  const int64_t kper = ((K + gridDim.z - 1) / gridDim.z + GK - 1) / GK * GK;
-  const int64_t kbeg = (int64_t)blockIdx.z * kper, kend = min(K, kbeg + kper);
-  const bool split = gridDim.z > 1;
+  const int64_t nz = splitk ? gridDim.z : 1, z = splitk ? blockIdx.z : 0;
+  const int64_t kper = ((K + nz - 1) / nz + GK - 1) / GK * GK;
+  const int64_t kbeg = z * kper, kend = min(K, kbeg + kper);
+  const bool split = splitk && nz > 1;
   T acc[4][4] = {};
   for (int64_t k0 = kbeg; k0 < kend; k0 += GK) {
     // load A tile (GT x GK) into As[k][m]
@@ -211,7 +219,20 @@ static int gemm_tiled(int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha, 
   if (splits > 1 && ldc != N) splits = 1;  // split-K accumulates into a zeroed, dense C
   if (splits > 1 && cudaMemsetAsync(C, 0, sizeof(T) * M * N, stream) != cudaSuccess) return OTG_ERR_CUDA;
   dim3 grid((unsigned)((N + GT - 1) / GT), (unsigned)((M + GT - 1) / GT), (unsigned)splits);
-  gemm_tiled_kernel<T><<<grid, 256, 0, stream>>>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, bias, relu);
+  gemm_tiled_kernel<T><<<grid, 256, 0, stream>>>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, bias, relu,
+                                                 0, 0, 0, 1);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+template <typename T>
+static int gemm_batched(int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha, const T* A, int64_t lda, int64_t sA,
+                        const T* B, int64_t ldb, int64_t sB, T beta, T* C, int64_t ldc, int64_t sC, int64_t batch,
+                        cudaStream_t stream) {
+  if (M < 1 || N < 1 || K < 1 || batch < 1 || !A || !B || !C) return OTG_ERR_ARG;
+  if ((M + GT - 1) / GT > 65535 || batch > 65535) return OTG_ERR_UNSUPPORTED;
+  dim3 grid((unsigned)((N + GT - 1) / GT), (unsigned)((M + GT - 1) / GT), (unsigned)batch);
+  gemm_tiled_kernel<T><<<grid, 256, 0, stream>>>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, nullptr, 0,
+                                                 sA, sB, sC, 0);
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 
@@ -226,6 +247,18 @@ int otg_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, c
 int otg_gemm_f64(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
                  const double* B, int64_t ldb, double beta, double* C, int64_t ldc, cudaStream_t stream) {
   return gemm_tiled<double>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, nullptr, 0, stream);
+}
+
+int otg_gemm_batched(int dtype, int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const void* A,
+                     int64_t lda, int64_t sA, const void* B, int64_t ldb, int64_t sB, double beta, void* C,
+                     int64_t ldc, int64_t sC, int64_t batch, cudaStream_t stream) {
+  if (dtype == OTG_F64)
+    return gemm_batched<double>(ta, tb, M, N, K, alpha, (const double*)A, lda, sA, (const double*)B, ldb, sB, beta,
+                                (double*)C, ldc, sC, batch, stream);
+  if (dtype == OTG_F32)
+    return gemm_batched<float>(ta, tb, M, N, K, (float)alpha, (const float*)A, lda, sA, (const float*)B, ldb, sB,
+                               (float)beta, (float*)C, ldc, sC, batch, stream);
+  return OTG_ERR_DTYPE;
 }
 
 int otg_mlp_relu_bwd(float* dY, const float* Y, int64_t n, cudaStream_t stream) {

@@ -185,6 +185,29 @@ def main():
                                                   max_iter=10, log=True)
     save("egw_asym_48x40", C1=C1a, C2=C2, T=G, gw=lg["gw_dist"], err=np.array(lg["err"]))
 
+    # 7b. batched (fused) Gromov-Wasserstein (test/batch/test_solve_gromov_batch.py:19 setting)
+    rng = np.random.RandomState(0)
+    X1 = rng.randn(2, 8, 2)
+    C1 = rng.randn(2, 8, 8)
+    perm = np.random.RandomState(1).permutation(8)
+    X2 = X1[:, perm, :] + 0.01 * rng.randn(2, 8, 2)
+    C2 = C1[:, perm, :][:, :, perm] + 0.01 * rng.randn(2, 8, 8)
+    Mb = ot.batch.dist_batch(X1, X2)
+    res = ot.batch.solve_gromov_batch(C1, C2, reg=0.01, M=Mb, alpha=0.5, max_iter=1000, tol=1e-5,
+                                      max_iter_inner=10000, tol_inner=1e-5, symmetric=False)
+    save("gromov_batch_fused", C1=C1, C2=C2, M=Mb, plan=res.plan, value=res.value,
+         value_linear=res.value_linear, value_quad=res.value_quad, n_iter=res.log["n_iter"])
+    rng = np.random.default_rng(8)
+    xs = rng.standard_normal((3, 12, 2))
+    xt = rng.standard_normal((3, 10, 3))
+    C1 = np.stack([ot.dist(x, x) for x in xs])
+    C2 = np.stack([ot.dist(x, x) for x in xt])
+    C1 /= C1.max(axis=(1, 2), keepdims=True)
+    C2 /= C2.max(axis=(1, 2), keepdims=True)
+    res = ot.batch.solve_gromov_batch(C1, C2, reg=0.05, max_iter=50, tol=1e-7, max_iter_inner=2000, tol_inner=1e-9)
+    save("gromov_batch_sym", C1=C1, C2=C2, plan=res.plan, value=res.value, value_quad=res.value_quad,
+         n_iter=res.log["n_iter"])
+
     # 8. lazy empirical Sinkhorn (ot/bregman/_empirical.py:190-263)
     rng = np.random.default_rng(21)
     X = rng.standard_normal((60, 3))

@@ -165,3 +165,23 @@ def test_multi_engine_max_iter_and_single_problem(cuda):
     assert int(r.status[0]) == 1 and int(r.niter[0]) == lg["niter"] == 24
     u, v = (t.cpu().numpy() for t in r.potentials(0))
     np.testing.assert_allclose(u, lg["log_u"], rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", ["gromov_batch_fused", "gromov_batch_sym"])
+def test_solve_gromov_batch(cuda, name):
+    """float64: exact against the oracle with per-problem inner stops; against
+    the reference's whole-batch inner stop within its own tolerances
+    (test/batch/test_solve_gromov_batch.py: plan 1e-5, values 1e-4)."""
+    g = golden(name)
+    if name == "gromov_batch_fused":
+        kw = dict(reg=0.01, M=g["M"], alpha=0.5, max_iter=1000, tol=1e-5, max_iter_inner=10000, tol_inner=1e-5,
+                  symmetric=False)
+    else:
+        kw = dict(reg=0.05, max_iter=50, tol=1e-7, max_iter_inner=2000, tol_inner=1e-9)
+    res = pb.solve_gromov_batch(g["C1"], g["C2"], **kw)
+    ref = oracle.solve_gromov_batch(g["C1"], g["C2"], per_problem_inner=True, **kw)
+    assert res.log["n_iter"] == ref["n_iter"]
+    np.testing.assert_allclose(res.plan, ref["plan"], rtol=1e-7, atol=1e-13)
+    np.testing.assert_allclose(res.value_quad, ref["value_quad"], rtol=1e-7, atol=1e-13)
+    np.testing.assert_allclose(res.plan, g["plan"], atol=1e-5)
+    np.testing.assert_allclose(res.value, g["value"], atol=1e-4)

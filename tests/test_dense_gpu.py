@@ -158,3 +158,14 @@ def test_log_multi_histogram(cuda):
     loss, lg = pg.sinkhorn2(g["a"], g["b"], g["M"], 1.0, method="sinkhorn_log", log=True, stopThr=1e-10)
     np.testing.assert_allclose(loss, g["log_loss"], rtol=1e-9)
     np.testing.assert_allclose(lg["u"], g["log_u"], rtol=1e-7)
+
+
+def test_knopp_multi_histogram(cuda):
+    g = golden("multib_31x3")
+    loss, lg = pg.sinkhorn2(g["a"], g["b"], g["M"], 1.0, method="sinkhorn", log=True, stopThr=1e-10)
+    np.testing.assert_allclose(loss, g["knopp_loss"], rtol=1e-9)
+    np.testing.assert_allclose(lg["u"], g["knopp_u"], rtol=1e-8)
+    np.testing.assert_allclose(lg["v"], g["knopp_v"], rtol=1e-8)
+    lref, lgr = oracle.sinkhorn_knopp(g["a"], g["b"], g["M"], 1.0, stopThr=1e-10)
+    assert lg["niter"] == lgr["niter"]
+    np.testing.assert_allclose(np.array(lg["err"], dtype=float), lgr["err"], rtol=1e-6)

@@ -144,3 +144,19 @@ def test_warmstart_net_gradients_match_finite_differences():
             flat[idx] = old
             fd = (lp - lm) / (2 * h)
             assert abs(fd - g[name].reshape(-1)[idx]) <= 1e-6 + 1e-5 * abs(fd), (name, idx, fd, g[name].reshape(-1)[idx])
+
+
+@pytest.mark.parametrize("name", ["gromov_batch_fused", "gromov_batch_sym"])
+def test_gromov_batch(name):
+    g = golden(name)
+    if name == "gromov_batch_fused":
+        r = oracle.solve_gromov_batch(g["C1"], g["C2"], reg=0.01, M=g["M"], alpha=0.5, max_iter=1000, tol=1e-5,
+                                      max_iter_inner=10000, tol_inner=1e-5, symmetric=False)
+        np.testing.assert_allclose(r["value_linear"], g["value_linear"], rtol=1e-8)
+    else:
+        r = oracle.solve_gromov_batch(g["C1"], g["C2"], reg=0.05, max_iter=50, tol=1e-7, max_iter_inner=2000,
+                                      tol_inner=1e-9)
+    assert r["n_iter"] == int(g["n_iter"])
+    np.testing.assert_allclose(r["plan"], g["plan"], rtol=1e-8, atol=1e-14)
+    np.testing.assert_allclose(r["value"], g["value"], rtol=1e-8)
+    np.testing.assert_allclose(r["value_quad"], g["value_quad"], rtol=1e-8)
