@@ -110,19 +110,23 @@ def run_warmstart(args, pk):
     net = wp.default_net(dev)
     st = torch.cuda.current_stream()
 
-    def step(warm, ev=None):
+    def step(arm, ev=None):
         ps = wp.PairSolver(X, Y)
-        wu = wp.warm_potential(net, X, Y, ps, WS_REG) if warm else None
+        wu = None
+        if arm == "warm":
+            wu = wp.warm_potential(net, X, Y, ps, WS_REG)
+        elif arm == "prior":
+            wu = wp.coarse_potential(X, Y, ps.maxc, WS_REG, wp.COARSE_K) / WS_REG
         out = ps.solve(WS_REG, WS_TOL, warm_u=wu, events=ev)
         return ps, out
 
     for _ in range(args.warmup):
-        step(True)
-        step(False)
+        for arm in ("warm", "plain", "prior"):
+            step(arm)
     torch.cuda.synchronize()
     res = {}
     with ClockSampler() as cs:
-        for arm in ("warm", "plain"):
+        for arm in ("warm", "plain", "prior"):
             t0 = torch.cuda.Event(enable_timing=True)
             t1 = torch.cuda.Event(enable_timing=True)
             kev = []
@@ -130,7 +134,7 @@ def run_warmstart(args, pk):
             t0.record(st)
             for _ in range(args.steps):
                 e = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-                ps, out = step(arm == "warm", e)
+                ps, out = step(arm, e)
                 kev.append(e)
             t1.record(st)
             torch.cuda.synchronize()
@@ -162,6 +166,8 @@ def run_warmstart(args, pk):
         "warm": {"niter_mean": w["niter_mean"], "niter_max": w["niter_max"], "converged": w["converged"],
                  "max_marginal_err": w["max_err"]},
         "speedup_warm_vs_plain": p["ms"] / w["ms"],
+        "prior_only": {"value": B / (res["prior"]["ms"] * 1e-3), "niter_mean": res["prior"]["niter_mean"],
+                       "note": "coarse multiscale prior without the network"},
         "config": {"workload": "learned warm start vs plain log-Sinkhorn, %d GMM cloud pairs n=m=%d d=%d, "
                                "reg=%.2f x max cost, stopThr=%g, float32" % (B, WS_N, WS_D, WS_REG, WS_TOL),
                    "pairs_per_step": B, "l2": "inputs larger than L2 (%.1f GiB of cost blocks)" % (

@@ -255,6 +255,11 @@ int otg_batched_plan(const OtgPlanTable* t, int32_t max_rows, cudaStream_t strea
  * and AdamW step.  No counterpart in the reference (the network feeds the
  * warmstart argument of ot/bregman/_sinkhorn.py:864-868).  All fp32.
  * ---------------------------------------------------------------------- */
+/* Voronoi cell masses for the learned warm start's coarse problem: w[p*k + c] = fraction of
+ * the n points of X_p (row-major n x d, problem stride sx elements) whose nearest of the k
+ * centres C_p (k x d, stride sc) is centre c.  d in {2, 3, 8, 16}. */
+int otg_nearest_mass(const float* X, const float* C, int32_t nprob, int32_t n, int32_t k, int32_t d, int64_t sx,
+                     int64_t sc, float* w, cudaStream_t stream);
 /* Soft-min distances of every source point of every problem to its target
  * measure, at ntau (<= 8) temperatures relative to scale[p]:
  * out[(r_off[p]+i)*ntau + k] = -tau_k ln sum_j b_j exp(g_j - M_ij / (scale[p] tau_k)).

@@ -91,6 +91,7 @@ SIGNATURES = {
     "otg_sinkhorn_online": (ctypes.c_int, [ctypes.POINTER(OtgOnlineProblem), c_vp]),
     "otg_batched_sqdist": (ctypes.c_int, [ctypes.POINTER(OtgCostTable), c_i32, c_vp]),
     "otg_batched_plan": (ctypes.c_int, [ctypes.POINTER(OtgPlanTable), c_i32, c_vp]),
+    "otg_nearest_mass": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i64, c_i64, c_vp, c_vp]),
     "otg_softmin_features": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32,
                                             c_i32, c_vp, c_vp, c_vp]),
     "otg_gemm_f32": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, ctypes.c_float, c_vp, c_i64,

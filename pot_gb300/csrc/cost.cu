@@ -196,6 +196,33 @@ __global__ void __launch_bounds__(256) softmin_features_kernel(const float* __re
   }
 }
 
+// Voronoi cell masses: for every point of cloud p (n points, rows of X), the
+// nearest of its k centres (the first k points of the paired centre cloud)
+// gains weight 1/n.  Centres are staged in shared memory; one thread per point.
+template <int D>
+__global__ void __launch_bounds__(256) nearest_mass_kernel(const float* __restrict__ X, const float* __restrict__ Cc,
+                                                           int n, int k, int64_t sx, int64_t sc, float* w) {
+  extern __shared__ float cs[];
+  const int p = blockIdx.y;
+  const float* C = Cc + p * sc;
+  for (int e = threadIdx.x; e < k * D; e += blockDim.x) cs[e] = C[e];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float x[D];
+#pragma unroll
+  for (int q = 0; q < D; ++q) x[q] = X[p * sx + (int64_t)i * D + q];
+  float best = INFINITY;
+  int arg = 0;
+  for (int c = 0; c < k; ++c) {
+    float d2 = 0.f;
+#pragma unroll
+    for (int q = 0; q < D; ++q) { const float df = x[q] - cs[c * D + q]; d2 = fmaf(df, df, d2); }
+    if (d2 < best) { best = d2; arg = c; }
+  }
+  atomicAdd(w + (int64_t)p * k + arg, 1.0f / (float)n);
+}
+
 }  // namespace otg
 
 using namespace otg;
@@ -237,6 +264,21 @@ int otg_batched_plan(const OtgPlanTable* t, int32_t max_rows, cudaStream_t strea
   } else {
     return OTG_ERR_DTYPE;
   }
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_nearest_mass(const float* X, const float* C, int32_t nprob, int32_t n, int32_t k, int32_t d, int64_t sx,
+                     int64_t sc, float* w, cudaStream_t stream) {
+  if (!X || !C || !w || nprob < 1 || nprob > 65535 || n < 1 || k < 1) return OTG_ERR_ARG;
+  if (cudaMemsetAsync(w, 0, sizeof(float) * (size_t)nprob * k, stream) != cudaSuccess) return OTG_ERR_CUDA;
+  dim3 grid((unsigned)((n + 255) / 256), (unsigned)nprob);
+  const size_t sm = sizeof(float) * (size_t)k * d;
+  if (sm > 48 * 1024) return OTG_ERR_UNSUPPORTED;
+  if (d == 16) nearest_mass_kernel<16><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, w);
+  else if (d == 8) nearest_mass_kernel<8><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, w);
+  else if (d == 3) nearest_mass_kernel<3><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, w);
+  else if (d == 2) nearest_mass_kernel<2><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, w);
+  else return OTG_ERR_UNSUPPORTED;
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 

@@ -43,7 +43,7 @@ class PairSolver:
     """Uniform-size batch of cloud pairs on the device: cost blocks, per-pair
     max cost, and log-domain solves (zero or warm start)."""
 
-    def __init__(self, X, Y, maxc=None):
+    def __init__(self, X, Y, maxc=None, a=None, b=None):
         self.P, self.n, self.d = X.shape
         self.m = Y.shape[1]
         self.layout = pb.RaggedLayout([self.n] * self.P, [self.m] * self.P, torch.float32, X.device)
@@ -53,8 +53,10 @@ class PairSolver:
                                               xo, yo, [self.d] * self.P, want_max=True)
         if maxc is not None:  # cost scale of an enclosing problem (sub-sampled clouds)
             self.maxc = maxc
-        self.a = torch.full((self.P * self.n,), 1.0 / self.n, dtype=torch.float32, device=X.device)
-        self.b = torch.full((self.P * self.m,), 1.0 / self.m, dtype=torch.float32, device=X.device)
+        self.a = (torch.full((self.P * self.n,), 1.0 / self.n, dtype=torch.float32, device=X.device) if a is None
+                  else a.reshape(-1).float().contiguous())
+        self.b = (torch.full((self.P * self.m,), 1.0 / self.m, dtype=torch.float32, device=X.device) if b is None
+                  else b.reshape(-1).float().contiguous())
 
     def solve(self, reg_rel, tol, max_iter=100000, warm_u=None, engine="multi", events=None):
         """Log-domain solve of every pair (sinkhorn_log order and stop test);
@@ -101,18 +103,32 @@ def features(ps, taus=TAUS):
     return ((F - F.mean(1, keepdim=True)) * FEATURE_SCALE).contiguous()
 
 
+def cell_masses(X, centres):
+    """Voronoi cell masses of each cloud of X over its centres (csrc/cost.cu
+    nearest_mass_kernel): (P, k), rows summing to one."""
+    lib = _lib.load()
+    P, n, d = X.shape
+    k = centres.shape[1]
+    w = torch.empty(P, k, dtype=torch.float32, device=X.device)
+    _lib.check(lib.otg_nearest_mass(_lib.ptr(X), _lib.ptr(centres), P, n, k, d, X.stride(0), centres.stride(0),
+                                    _lib.ptr(w), _lib.stream_handle(X.device)), "otg_nearest_mass")
+    return w
+
+
 def coarse_potential(X, Y, maxc, reg_rel=0.02, k=128, tol=1e-5, taus=None):
-    """Multiscale prior: solve the problem on the first k points of each
-    cloud (the points are i.i.d., so this is a random sub-sample) and carry
-    its target potential to every source point with one c-transform (the
-    log-domain row update).  Returns the centred source potential in
+    """Multiscale prior: the first k points of each cloud (the points are
+    i.i.d., so a random sample) become atoms weighted by the exact mass of
+    their Voronoi cells in the full cloud; that coarse problem is solved and
+    its target potential is carried to every source point with one c-transform
+    (the log-domain row update).  Returns the centred source potential in
     max-normalised cost units, (P, n), and, if `taus` is given, the soft-min
-    distances of every source point to the k-point target sample at those
+    distances of every source point to the weighted target atoms at those
     temperatures, (P, n, len(taus))."""
     Xs, Ys = X[:, :k].contiguous(), Y[:, :k].contiguous()
-    sub = PairSolver(Xs, Ys, maxc=maxc)
+    wa, wb = cell_masses(X, Xs), cell_masses(Y, Ys)
+    sub = PairSolver(Xs, Ys, maxc=maxc, a=wa, b=wb)
     _, v, _, _, _ = sub.solve(reg_rel, tol)
-    cross = PairSolver(X, Ys, maxc=maxc)
+    cross = PairSolver(X, Ys, maxc=maxc, b=wb)
     f = softmin(cross, (reg_rel,), g=v)[..., 0]
     f = (f - f.mean(1, keepdim=True)).contiguous()
     if taus is None:
