@@ -29,6 +29,8 @@ extern "C" {
 /* Sinkhorn forms */
 #define OTG_METHOD_KNOPP 0 /* scaling form,  ot/bregman/_sinkhorn.py:487 sinkhorn_knopp */
 #define OTG_METHOD_LOG 1   /* log form,      ot/bregman/_sinkhorn.py:690 sinkhorn_log   */
+#define OTG_METHOD_STAB 2  /* log-stabilised scaling form with absorption,
+                              ot/bregman/_sinkhorn.py:1105 sinkhorn_stabilized       */
 
 /* return codes */
 #define OTG_OK 0
@@ -48,19 +50,30 @@ extern "C" {
 /* ------------------------------------------------------------------------
  * Dense-cost Sinkhorn, one problem, the whole iteration loop in one
  * persistent cooperative launch.
- * Replaces the loops of ot/bregman/_sinkhorn.py:626-663 (sinkhorn_knopp) and
- * :880-899 (sinkhorn_log) behind ot.sinkhorn / ot.sinkhorn2
- * (ot/bregman/_sinkhorn.py:21, :237).
+ * Replaces the loops of ot/bregman/_sinkhorn.py:626-663 (sinkhorn_knopp),
+ * :880-899 (sinkhorn_log) and :1272-1327 (sinkhorn_stabilized) behind
+ * ot.sinkhorn / ot.sinkhorn2 (ot/bregman/_sinkhorn.py:21, :237).
+ *
+ * OTG_METHOD_STAB runs the log iteration on F = alpha/reg + log u,
+ * G = beta/reg + log v in the gauge of a run without absorptions, started
+ * from F0 = alpha0/reg - log n, and reproduces the reference's absorption
+ * decisions (max u or max v above tau) and the check-iteration errors they
+ * affect.  out_u, out_v receive F, G in that gauge; info[5] counts the
+ * absorptions up to the returned iteration and info[6] says whether that
+ * iteration absorbed.  The reference's own values are then
+ *   logu = F - k log n,  logv = G + k log n                (info[6] == 0)
+ *   logu = F - k log n,  logv = G + (k-1) log n - log m    (info[6] == 1)
+ * with k = info[5]; alpha = reg logu, beta = reg logv.
  * ---------------------------------------------------------------------- */
 typedef struct OtgDenseProblem {
   int32_t dtype;      /* OTG_F32 or OTG_F64: type of M, a, b, warm_*, out_* */
-  int32_t method;     /* OTG_METHOD_KNOPP or OTG_METHOD_LOG                  */
+  int32_t method;     /* OTG_METHOD_KNOPP, OTG_METHOD_LOG or OTG_METHOD_STAB */
   const void* M;      /* n x m cost, row-major, leading dimension ldm        */
   int64_t n, m, ldm;
   const void* a;      /* source weights (n)                                  */
   const void* b;      /* target weights (m)                                  */
-  const void* warm_u; /* optional natural-log warm start (n) or NULL         */
-  const void* warm_v; /* optional natural-log warm start (m) or NULL         */
+  const void* warm_u; /* optional natural-log warm start (n) or NULL; STAB:  */
+  const void* warm_v; /* alpha0/reg and beta0/reg                           */
   double reg;         /* entropic regularisation (> 0)                       */
   int32_t max_iter;   /* numItermax                                          */
   int32_t hist_cap;   /* capacity of the error history (>= max_iter/10 + 2)  */
@@ -70,6 +83,9 @@ typedef struct OtgDenseProblem {
   size_t workspace_bytes;
   int32_t grid;       /* CTAs (0 = all co-resident CTAs); tuning knob        */
   int32_t timeout_ms; /* bound on any single device wait (0 = 4000 ms)       */
+  double tau;         /* STAB: absorption threshold on the scalings (> 0)    */
+  int32_t check_period; /* STAB: iterations between marginal checks (>= 1) */
+  int32_t reserved;
 } OtgDenseProblem;
 
 /* Workspace size for otg_sinkhorn_dense (device bytes, 256-byte aligned). */
@@ -77,17 +93,59 @@ size_t otg_dense_workspace_bytes(int dtype, int64_t n, int64_t m, int hist_cap, 
 /* Byte offset inside the workspace of the result block:
  *   double err_hist[hist_cap]; then int32 info[8] 256-byte aligned after it
  *   (info[0] status, info[1] niter = last loop index, info[2] number of
- *   logged errors, info[3] abort flag). */
+ *   logged errors, info[3] abort flag, info[5] and info[6] the absorption
+ *   count and last-iteration flag of OTG_METHOD_STAB). */
 size_t otg_dense_info_offset(int dtype, int64_t n, int64_t m, int hist_cap, int grid);
 int otg_sinkhorn_dense(const OtgDenseProblem* p, void* workspace, cudaStream_t stream);
 
 /* Plan and/or loss from potentials: P = exp(-M/reg + u + v) (log form) or
  * diag(u) exp(-M/reg) diag(v) (scaling form); *loss = sum(M * P) in fp64.
- * P or loss may be NULL.  Replaces the returns of ot/bregman/_sinkhorn.py:
- * 681-687 and :915-918 and the loss of sinkhorn2 :435-438. */
+ * P or loss may be NULL; OTG_METHOD_STAB takes natural-log potentials like
+ * the log form.  Replaces the returns of ot/bregman/_sinkhorn.py:681-687,
+ * :915-918 and :1340-1368 and the loss of sinkhorn2 :435-438. */
 int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, int64_t ldm,
                    const void* u, const void* v, double reg, void* P, int64_t ldp, double* loss,
                    cudaStream_t stream);
+
+/* Row and column sums of P = exp(-M/reg + u + v) (natural-log potentials),
+ * accumulated in fp64 (rowsum: n, colsum: m).  The marginal error of the
+ * epsilon-scaling loop, ot/bregman/_sinkhorn.py:1534-1542. */
+int otg_dense_marginals(int dtype, const void* M, int64_t n, int64_t m, int64_t ldm, const void* u, const void* v,
+                        double reg, double* rowsum, double* colsum, cudaStream_t stream);
+
+/* Loss of a lazy plan, sum_ij C_ij exp(f_i + g_j - C_ij/reg) with
+ * C_ij = |x_i - y_j|^2 (X: n x d, Y: m x d row-major; f, g natural-log
+ * potentials), fp64 accumulation.  Replaces the block loop of
+ * ot/bregman/_empirical.py:470-478 (empirical_sinkhorn2, isLazy=True). */
+int otg_lazy_loss(int dtype, const void* X, const void* Y, int64_t n, int64_t m, int32_t d, const void* f,
+                  const void* g, double reg, double* out, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Entropic Wasserstein barycenter of n_hists histograms on one support of
+ * size dim (cost M: dim x dim), the iteration loop driven natively with one
+ * host synchronisation per error check.  Replaces
+ * ot/bregman/_barycenter.py:141-259 (barycenter_sinkhorn, OTG_METHOD_KNOPP)
+ * and :403-473 (_barycenter_sinkhorn_log, OTG_METHOD_LOG) behind
+ * ot.bregman.barycenter (:23).
+ * ---------------------------------------------------------------------- */
+typedef struct OtgBaryProblem {
+  int32_t dtype, method;   /* OTG_F32/OTG_F64; OTG_METHOD_KNOPP or OTG_METHOD_LOG */
+  const void* M;           /* dim x dim cost, leading dimension ldm               */
+  int64_t dim, ldm;
+  const void* A;           /* dim x n_hists histograms, row-major                 */
+  int32_t n_hists;
+  int32_t max_iter;        /* numItermax (>= 1)                                   */
+  const void* weights;     /* n_hists barycentric weights                         */
+  double reg, stop_thr;
+  void* out_bar;           /* dim: the barycenter                                 */
+  double* err_hist;        /* HOST: errors of the check iterations (ii % 10 == 1) */
+  int32_t hist_cap;
+  int32_t* info;           /* HOST int32[3]: status, niter (last loop index), checks */
+  void* workspace; size_t workspace_bytes;
+} OtgBaryProblem;
+
+size_t otg_barycenter_workspace_bytes(int dtype, int method, int64_t dim, int32_t n_hists);
+int otg_barycenter(const OtgBaryProblem* p, cudaStream_t stream);
 
 /* ------------------------------------------------------------------------
  * Batched dense Sinkhorn: many independent problems of uneven size in ONE
@@ -319,6 +377,10 @@ typedef struct OtgSplitGemm {
   const float* rowv; const float* colv;
   int32_t* abort_flag;
   int32_t timeout_ms;
+  /* mode 1, optional: out += s_add * addend (M x N, leading dimension
+   * ld_add; may alias out) -- the (1 - alpha) M term of fused GW,
+   * ot/gromov/_bregman.py:1184-1190 */
+  const float* addend; int64_t ld_add; float s_add;
 } OtgSplitGemm;
 int otg_split_half(const float* X, int64_t rows, int64_t cols, int64_t ldx, float scale, int transpose, void* hi,
                    void* lo, int64_t ld_out, cudaStream_t stream);

@@ -11,6 +11,7 @@ the reference itself (PythonOT/POT 0.9.7.dev0, imported in the build container
 by ``tests/golden/gen_golden.py``) and against the reference's own doctest
 values; see ``tests/test_oracle.py``.
 """
+from .entropic import NONCONV, NUMERR, NUMERR_STAB  # noqa: F401
 from .entropic import (  # noqa: F401
     sqeuclidean,
     logsumexp,
@@ -18,12 +19,19 @@ from .entropic import (  # noqa: F401
     sinkhorn_log,
     sinkhorn,
     sinkhorn2,
+    sinkhorn_stabilized,
+    sinkhorn_epsilon_scaling,
+    barycenter_sinkhorn,
+    barycenter_sinkhorn_log,
+    solve_entropic,
+    empirical_sinkhorn2_lazy,
     log_projection_batch,
     scaling_projection_batch,
     solve_batch,
     init_matrix_square_loss,
     tensor_product,
     entropic_gromov_wasserstein,
+    entropic_fused_gromov_wasserstein,
     entropic_gw_log_inner,
     empirical_sinkhorn_lazy,
     solve_gromov_batch,

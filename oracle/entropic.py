@@ -13,6 +13,7 @@ import numpy as np
 
 NONCONV = "Sinkhorn did not converge"
 NUMERR = "numerical errors at iteration"
+NUMERR_STAB = "Numerical errors at iteration %d"
 
 
 def _f64(x):
@@ -179,6 +180,10 @@ def sinkhorn(a, b, M, reg, method="sinkhorn", **kw):
         return sinkhorn_knopp(a, b, M, reg, **kw)
     if method.lower() == "sinkhorn_log":
         return sinkhorn_log(a, b, M, reg, **kw)
+    if method.lower() == "sinkhorn_stabilized":
+        return sinkhorn_stabilized(a, b, M, reg, **kw)
+    if method.lower() == "sinkhorn_epsilon_scaling":
+        return sinkhorn_epsilon_scaling(a, b, M, reg, **kw)
     raise ValueError("Unknown method '%s'." % method)
 
 
@@ -189,6 +194,217 @@ def sinkhorn2(a, b, M, reg, method="sinkhorn", **kw):
     if _f64(b).ndim < 2:
         return float(np.sum(_f64(M) * res)), log
     return res, log
+
+
+def sinkhorn_stabilized(a, b, M, reg, numItermax=1000, tau=1e3, stopThr=1e-9, warmstart=None,
+                        print_period=20):
+    """Log-stabilised scaling Sinkhorn, ``ot/bregman/_sinkhorn.py:1105-1368``
+    (1-D ``b``).
+
+    Scalings start at ``u = 1/n, v = 1/m`` (``:1250-1256``) over the absorbed
+    potentials ``alpha, beta`` (zero or the warm start); per iteration
+    ``v = b / K^T u`` then ``u = a / K v`` (``:1277-1279``) with
+    ``K = exp(-(M - alpha - beta)/reg)``; when ``max |u|`` or ``max |v|``
+    exceeds ``tau`` the scalings are absorbed (``alpha += reg log u``, ...)
+    and reset to ``1/n, 1/m`` (``:1282-1296``); every ``print_period``
+    iterations the L2 column-marginal violation of the current plan is
+    recorded (``:1298-1310``) and the loop stops once it is ``<= stopThr``
+    (``:1318``); a NaN scaling reverts to the previous pair (``:1321-1327``).
+    """
+    M = _f64(M)
+    a, b = _uniform_if_empty(a, b, M)
+    if b.ndim > 1:
+        raise NotImplementedError("several target histograms")
+    n, m = M.shape
+    if warmstart is None:
+        alpha, beta = np.zeros(n), np.zeros(m)
+    else:
+        alpha, beta = _f64(warmstart[0]).copy(), _f64(warmstart[1]).copy()
+    u, v = np.full(n, 1.0 / n), np.full(m, 1.0 / m)
+
+    def kernel(al, be):
+        return np.exp(-(M - al[:, None] - be[None, :]) / reg)
+
+    def gamma(al, be, uu, vv):
+        return np.exp(-(M - al[:, None] - be[None, :]) / reg + np.log(uu)[:, None] + np.log(vv)[None, :])
+
+    K = kernel(alpha, beta)
+    errs, warns = [], []
+    err = 1.0
+    ii = 0
+    stopped = False
+    with np.errstate(all="ignore"):
+        for ii in range(numItermax):
+            uprev, vprev = u, v
+            v = b / (K.T @ u)
+            u = a / (K @ v)
+            if np.max(np.abs(u)) > tau or np.max(np.abs(v)) > tau:
+                alpha, beta = alpha + reg * np.log(u), beta + reg * np.log(v)
+                u, v = np.full(n, 1.0 / n), np.full(m, 1.0 / m)
+                K = kernel(alpha, beta)
+            if ii % print_period == 0:
+                err = float(np.linalg.norm(np.sum(gamma(alpha, beta, u, v), 0) - b))
+                errs.append(err)
+            if err <= stopThr:
+                stopped = True
+                break
+            if np.any(np.isnan(u)) or np.any(np.isnan(v)):
+                warns.append(NUMERR_STAB % ii)
+                u, v = uprev, vprev
+                stopped = True
+                break
+        P = gamma(alpha, beta, u, v)
+        logu = alpha / reg + np.log(u)
+        logv = beta / reg + np.log(v)
+    if not stopped:
+        warns.append(NONCONV)
+    al, be = alpha + reg * np.log(u), beta + reg * np.log(v)
+    return P, {"err": errs, "n_iter": ii, "logu": logu, "logv": logv, "alpha": al, "beta": be,
+               "warmstart": (al, be), "_warnings": warns}
+
+
+def sinkhorn_epsilon_scaling(a, b, M, reg, numItermax=100, epsilon0=1e4, numInnerItermax=100, tau=1e3,
+                             stopThr=1e-9, warmstart=None, print_period=10):
+    """Epsilon scaling over the stabilised solver,
+    ``ot/bregman/_sinkhorn.py:1371-1575``: at least 35 outer steps
+    (``:1495-1496``), ``reg_k = (epsilon0 - reg) exp(-k) + reg``, each a
+    stabilised solve of ``numInnerItermax`` iterations warm-started from the
+    previous ``(alpha, beta)`` (whose own non-convergence warnings are kept);
+    every ``print_period`` steps ``|G^T 1 - b|^2 + |G 1 - a|^2`` is recorded
+    and the loop stops once it is ``<= stopThr`` after step 35."""
+    M = _f64(M)
+    a, b = _uniform_if_empty(a, b, M)
+    n, m = M.shape
+    numItermin = 35
+    numItermax = max(numItermin, numItermax)
+    if warmstart is None:
+        alpha, beta = np.zeros(n), np.zeros(m)
+    else:
+        alpha, beta = _f64(warmstart[0]).copy(), _f64(warmstart[1]).copy()
+    errs, warns = [], []
+    err = 1.0
+    ii = 0
+    stopped = False
+    G = None
+    for ii in range(numItermax):
+        regi = (epsilon0 - reg) * np.exp(-ii) + reg
+        G, lg = sinkhorn_stabilized(a, b, M, regi, numItermax=numInnerItermax, tau=tau, stopThr=stopThr,
+                                    warmstart=(alpha, beta), print_period=20)
+        warns += lg["_warnings"]
+        alpha, beta = lg["alpha"], lg["beta"]
+        if ii % print_period == 0:
+            err = float(np.linalg.norm(G.sum(0) - b) ** 2 + np.linalg.norm(G.sum(1) - a) ** 2)
+            errs.append(err)
+        if err <= stopThr and ii > numItermin:
+            stopped = True
+            break
+    if not stopped:
+        warns.append(NONCONV)
+    return G, {"err": errs, "alpha": alpha, "beta": beta, "warmstart": (alpha, beta), "niter": ii,
+               "_warnings": warns}
+
+
+def solve_entropic(M, a=None, b=None, reg=1.0, reg_type="KL", max_iter=None, tol=None):
+    """The regularised balanced branch of ``ot.solve`` for ``reg_type`` in
+    ``{"KL", "entropy"}`` (``ot/solvers.py:428-494``): ``sinkhorn_log`` with
+    ``max_iter = 1000, tol = 1e-9`` by default; potentials are the log
+    scalings; ``value_linear = <M, P>`` and ``value`` adds
+    ``reg * sum P log(P + 1e-16)`` (entropy) or
+    ``reg * sum P log(P / (a b^T) + 1e-16)`` (KL, ``ot/backend.py:1542``)."""
+    M = _f64(M)
+    n, m = M.shape
+    a = np.full(n, 1.0 / n) if a is None else _f64(a)
+    b = np.full(m, 1.0 / m) if b is None else _f64(b)
+    P, lg = sinkhorn_log(a, b, M, reg, numItermax=1000 if max_iter is None else max_iter,
+                         stopThr=1e-9 if tol is None else tol)
+    vlin = float(np.sum(M * P))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        if reg_type.lower() == "entropy":
+            value = vlin + reg * float(np.sum(P * np.log(P + 1e-16)))
+        else:
+            value = vlin + reg * float(np.sum(P * np.log(P / (a[:, None] * b[None, :]) + 1e-16)))
+    return {"plan": P, "value": value, "value_linear": vlin, "potentials": (lg["log_u"], lg["log_v"]),
+            "log": lg}
+
+
+def empirical_sinkhorn2_lazy(X, Y, reg, a=None, b=None, numIterMax=10000, stopThr=1e-9, batchSize=100,
+                             warmstart=None):
+    """``ot/bregman/_empirical.py:430-481`` with ``isLazy=True``: the lazy
+    solve, then ``sum_ij C_ij exp(f_i + g_j - C_ij/reg)`` accumulated over row
+    blocks of ``batchSize``."""
+    f, g, lg = empirical_sinkhorn_lazy(X, Y, reg, a, b, numIterMax, stopThr, batchSize, warmstart)
+    X, Y = _f64(X), _f64(Y)
+    bs = batchSize if isinstance(batchSize, int) else batchSize[0]
+    loss = 0.0
+    for i in range(0, X.shape[0], bs):
+        C = sqeuclidean(X[i:i + bs], Y)
+        loss += float(np.sum(C * np.exp(f[i:i + bs, None] + g[None, :] - C / reg)))
+    return loss, lg
+
+
+def barycenter_sinkhorn(A, M, reg, weights=None, numItermax=1000, stopThr=1e-4):
+    """Entropic Wasserstein barycenter, scaling form,
+    ``ot/bregman/_barycenter.py:141-259``: ``K = exp(-M/reg)``;
+    ``UKv = K (A^T / K^T 1)^T``, ``u = geomMean(UKv) / UKv``; per iteration
+    ``UKv = u * K^T (A / K u)``, ``u = u * geomBar(w, UKv) / UKv``; at
+    ``ii % 10 == 1`` the error ``sum_i std_k UKv_ik`` stops the loop when
+    ``< stopThr``.  Returns ``geomBar(w, UKv)`` and ``{"err", "niter"}``."""
+    A, M = _f64(A), _f64(M)
+    dim, H = A.shape
+    w = np.full(H, 1.0 / H) if weights is None else _f64(weights)
+    K = np.exp(-M / reg)
+    UKv = K @ (A.T / np.sum(K, axis=0)).T
+    u = (np.exp(np.mean(np.log(UKv), axis=1)) / UKv.T).T
+    errs, warns = [], []
+    ii = 0
+    stopped = False
+    for ii in range(numItermax):
+        UKv = u * (K.T @ (A / (K @ u)))
+        u = (u.T * np.exp(np.log(UKv) @ w)).T / UKv
+        if ii % 10 == 1:
+            err = float(np.sum(np.std(UKv, axis=1)))
+            errs.append(err)
+            if err < stopThr:
+                stopped = True
+                break
+    if not stopped:
+        warns.append(NONCONV)
+    return np.exp(np.log(UKv) @ w), {"err": errs, "niter": ii, "_warnings": warns}
+
+
+def barycenter_sinkhorn_log(A, M, reg, weights=None, numItermax=1000, stopThr=1e-4):
+    """Entropic Wasserstein barycenter, log domain,
+    ``ot/bregman/_barycenter.py:403-473``: per iteration and histogram
+    ``f_k = log A_k - LSE_j(-M/reg + G_k)``, ``log KU_k = LSE_i(-M/reg + f_k)``,
+    ``log bar = sum_k w_k log KU_k``; at ``ii % 10 == 1`` the error
+    ``sum_i std_k exp(G + log KU)``; then ``G = log bar - log KU``."""
+    A, M = _f64(A), _f64(M)
+    dim, H = A.shape
+    w = np.full(H, 1.0 / H) if weights is None else _f64(weights)
+    Mr = -M / reg
+    logA = np.log(A + 1e-16)
+    log_KU = np.zeros_like(logA)
+    G = np.zeros_like(logA)
+    errs, warns = [], []
+    ii = 0
+    stopped = False
+    log_bar = np.zeros(dim)
+    for ii in range(numItermax):
+        log_bar = np.zeros(dim)
+        for k in range(H):
+            f = logA[:, k] - logsumexp(Mr + G[None, :, k], 1)
+            log_KU[:, k] = logsumexp(Mr + f[:, None], 0)
+            log_bar = log_bar + w[k] * log_KU[:, k]
+        if ii % 10 == 1:
+            err = float(np.exp(G + log_KU).std(axis=1).sum())
+            errs.append(err)
+            if err < stopThr:
+                stopped = True
+                break
+        G = log_bar[:, None] - log_KU
+    if not stopped:
+        warns.append(NONCONV)
+    return np.exp(log_bar), {"err": errs, "niter": ii, "_warnings": warns}
 
 
 def log_projection_batch(K, a=None, b=None, max_iter=10000, tol=1e-5):
@@ -301,6 +517,27 @@ def entropic_gromov_wasserstein(C1, C2, p=None, q=None, epsilon=0.1, symmetric=N
     reads as ``log u``.  Every 10th outer iteration logs ``||T - Tprev||_F``.
     Returns ``(T, log)`` with ``log = {"err", "gw_dist"}``.
     """
+    T, lg = _entropic_gw(None, C1, C2, p, q, epsilon, symmetric, 1.0, G0, max_iter, tol, solver, warmstart,
+                         numItermax, stopThr)
+    lg["gw_dist"] = lg.pop("dist")
+    return T, lg
+
+
+def entropic_fused_gromov_wasserstein(M, C1, C2, p=None, q=None, epsilon=0.1, symmetric=None, alpha=0.5,
+                                      G0=None, max_iter=1000, tol=1e-9, solver="PGD", warmstart=False,
+                                      numItermax=1000, stopThr=1e-9):
+    """Entropic fused GW with square loss, ``ot/gromov/_bregman.py:997-1241``:
+    the loop above with ``tens = alpha gwggrad(T) + (1 - alpha) M``
+    (``:1184-1192``) and ``fgw_dist = (1 - alpha) <M, T> + alpha gwloss(T)``
+    (``:1235-1238``)."""
+    T, lg = _entropic_gw(M, C1, C2, p, q, epsilon, symmetric, alpha, G0, max_iter, tol, solver, warmstart,
+                         numItermax, stopThr)
+    lg["fgw_dist"] = lg.pop("dist")
+    return T, lg
+
+
+def _entropic_gw(M, C1, C2, p, q, epsilon, symmetric, alpha, G0, max_iter, tol, solver, warmstart, numItermax,
+                 stopThr):
     C1, C2 = _f64(C1), _f64(C2)
     n1, n2 = C1.shape[0], C2.shape[0]
     p = np.full(n1, 1.0 / n1) if p is None else _f64(p)
@@ -322,6 +559,8 @@ def entropic_gromov_wasserstein(C1, C2, p=None, q=None, epsilon=0.1, symmetric=N
         else:
             tens = 0.5 * (2.0 * tensor_product(constC, hC1, hC2, T)
                           + 2.0 * tensor_product(constCt, hC1t, hC2t, T))
+        if M is not None:
+            tens = alpha * tens + (1 - alpha) * _f64(M)
         if solver == "PPA":
             with np.errstate(divide="ignore"):
                 tens = tens - epsilon * np.log(T)
@@ -340,7 +579,8 @@ def entropic_gromov_wasserstein(C1, C2, p=None, q=None, epsilon=0.1, symmetric=N
     if abs(np.sum(T) - 1) > 1e-5:
         warns.append("Solver failed to produce a transport plan")
     gw = float(np.sum(tensor_product(constC, hC1, hC2, T) * T))
-    return T, {"err": errs, "gw_dist": gw, "_warnings": warns, "n_outer": cpt}
+    dist = gw if M is None else (1 - alpha) * float(np.sum(_f64(M) * T)) + alpha * gw
+    return T, {"err": errs, "dist": dist, "_warnings": warns, "n_outer": cpt}
 
 
 def entropic_gw_log_inner(C1, C2, p=None, q=None, epsilon=0.1, max_iter=50, tol=0.0,

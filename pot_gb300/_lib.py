@@ -11,7 +11,7 @@ import torch
 from . import _build
 
 OTG_F32, OTG_F64 = 0, 1
-OTG_METHOD_KNOPP, OTG_METHOD_LOG = 0, 1
+OTG_METHOD_KNOPP, OTG_METHOD_LOG, OTG_METHOD_STAB = 0, 1, 2
 STATUS_CONVERGED, STATUS_MAXITER, STATUS_NUMERICAL, STATUS_ABORTED = 0, 1, 2, 3
 _ERRORS = {-1: "invalid argument", -2: "unsupported dtype", -3: "workspace too small",
            -4: "CUDA launch error", -5: "unsupported configuration",
@@ -25,7 +25,7 @@ class OtgDenseProblem(ctypes.Structure):
                 ("ldm", c_i64), ("a", c_vp), ("b", c_vp), ("warm_u", c_vp), ("warm_v", c_vp),
                 ("reg", c_dbl), ("max_iter", c_i32), ("hist_cap", c_i32), ("stop_thr", c_dbl),
                 ("out_u", c_vp), ("out_v", c_vp), ("workspace_bytes", c_sz), ("grid", c_i32),
-                ("timeout_ms", c_i32)]
+                ("timeout_ms", c_i32), ("tau", c_dbl), ("check_period", c_i32), ("reserved", c_i32)]
 
 
 class OtgBatchProblem(ctypes.Structure):
@@ -63,7 +63,15 @@ class OtgSplitGemm(ctypes.Structure):
                 ("b_rows", c_i64), ("ldb", c_i64), ("k_alloc", c_i64), ("mode", c_i32), ("scale", ctypes.c_float),
                 ("s_acc", ctypes.c_float), ("s_vec", ctypes.c_float), ("out_hi", c_vp), ("out_lo", c_vp),
                 ("ld_h", c_i64), ("out", c_vp), ("ld_o", c_i64), ("M", c_i64), ("N", c_i64), ("rowv", c_vp),
-                ("colv", c_vp), ("abort_flag", c_vp), ("timeout_ms", c_i32)]
+                ("colv", c_vp), ("abort_flag", c_vp), ("timeout_ms", c_i32), ("addend", c_vp), ("ld_add", c_i64),
+                ("s_add", ctypes.c_float)]
+
+
+class OtgBaryProblem(ctypes.Structure):
+    _fields_ = [("dtype", c_i32), ("method", c_i32), ("M", c_vp), ("dim", c_i64), ("ldm", c_i64), ("A", c_vp),
+                ("n_hists", c_i32), ("max_iter", c_i32), ("weights", c_vp), ("reg", c_dbl), ("stop_thr", c_dbl),
+                ("out_bar", c_vp), ("err_hist", ctypes.POINTER(c_dbl)), ("hist_cap", c_i32),
+                ("info", ctypes.POINTER(c_i32)), ("workspace", c_vp), ("workspace_bytes", c_sz)]
 
 
 class OtgOnlineProblem(ctypes.Structure):
@@ -81,6 +89,11 @@ SIGNATURES = {
     "otg_sinkhorn_dense": (ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp]),
     "otg_dense_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp,
                                       c_dbl, c_vp, c_i64, c_vp, c_vp]),
+    "otg_barycenter_workspace_bytes": (c_sz, [ctypes.c_int, ctypes.c_int, c_i64, c_i32]),
+    "otg_barycenter": (ctypes.c_int, [ctypes.POINTER(OtgBaryProblem), c_vp]),
+    "otg_lazy_loss": (ctypes.c_int, [ctypes.c_int, c_vp, c_vp, c_i64, c_i64, c_i32, c_vp, c_vp, c_dbl, c_vp, c_vp]),
+    "otg_dense_marginals": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_dbl, c_vp, c_vp,
+                                           c_vp]),
     "otg_sinkhorn_dense_noalloc": (ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp, c_vp]),
     "otg_batch_limits": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
                                         ctypes.POINTER(c_i32)]),

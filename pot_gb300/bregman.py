@@ -1,13 +1,17 @@
 """Drop-in replacements for ``ot.sinkhorn``, ``ot.sinkhorn2``,
-``ot.bregman.sinkhorn_knopp`` and ``ot.bregman.sinkhorn_log``.
+``ot.bregman.sinkhorn_knopp``, ``ot.bregman.sinkhorn_log``,
+``ot.bregman.sinkhorn_stabilized`` and ``ot.bregman.sinkhorn_epsilon_scaling``.
 
 Signatures, defaults, return values, log-dict keys and warnings follow
 PythonOT/POT ``ot/bregman/_sinkhorn.py`` (``sinkhorn`` :21-234, ``sinkhorn2``
-:237-484, ``sinkhorn_knopp`` :487-687, ``sinkhorn_log`` :690-918).  The
+:237-484, ``sinkhorn_knopp`` :487-687, ``sinkhorn_log`` :690-918,
+``sinkhorn_stabilized`` :1105-1368, ``sinkhorn_epsilon_scaling``
+:1371-1575).  The
 iteration loop runs on the GPU in one persistent kernel
 (``csrc/dense.cu``); the host only reads the result block once per solve.
 """
 import ctypes
+import math
 import warnings
 
 import numpy as np
@@ -26,7 +30,7 @@ def _hist_cap(max_iter):
 
 
 class DenseResult:
-    __slots__ = ("u", "v", "status", "niter", "errs", "workspace", "layout")
+    __slots__ = ("u", "v", "status", "niter", "errs", "workspace", "layout", "nabs", "absorbed_last")
 
 
 def default_grid(n, m):
@@ -39,7 +43,7 @@ def default_grid(n, m):
 
 
 def solve_dense(M, a, b, reg, method, max_iter, stop_thr, warm_u=None, warm_v=None, grid=None,
-                timeout_ms=0, read_back=True):
+                timeout_ms=0, read_back=True, tau=0.0, check_period=10):
     """Run one dense solve on device tensors (contiguous rows, same dtype).
 
     Returns a DenseResult whose ``u, v`` are scalings (knopp) or natural-log
@@ -50,7 +54,7 @@ def solve_dense(M, a, b, reg, method, max_iter, stop_thr, warm_u=None, warm_v=No
     if grid is None:
         grid = default_grid(n, m)
     dt = _lib.dtype_code(M.dtype)
-    cap = _hist_cap(max_iter)
+    cap = max(2, max_iter // check_period + 2)
     wsb = lib.otg_dense_workspace_bytes(dt, n, m, cap, grid)
     ws = torch.empty(wsb, dtype=torch.uint8, device=M.device)
     out_u = torch.empty(n, dtype=M.dtype, device=M.device)
@@ -62,7 +66,7 @@ def solve_dense(M, a, b, reg, method, max_iter, stop_thr, warm_u=None, warm_v=No
         warm_v=warm_v.data_ptr() if warm_v is not None else None,
         reg=float(reg), max_iter=int(max_iter), hist_cap=cap, stop_thr=float(stop_thr),
         out_u=out_u.data_ptr(), out_v=out_v.data_ptr(), workspace_bytes=wsb, grid=grid,
-        timeout_ms=timeout_ms)
+        timeout_ms=timeout_ms, tau=float(tau), check_period=int(check_period))
     _lib.check(lib.otg_sinkhorn_dense(ctypes.byref(p), ctypes.c_void_p(ws.data_ptr()),
                                       _lib.stream_handle(M.device)), "otg_sinkhorn_dense")
     r = DenseResult()
@@ -84,6 +88,7 @@ def read_result(r):
     info = blk[ctrl - off:ctrl - off + 32].view(np.int32)
     r.status, r.niter = int(info[0]), int(info[1])
     nchk = int(info[2])
+    r.nabs, r.absorbed_last = int(info[5]), bool(info[6])
     if int(info[3]) != 0:
         r.status = _lib.STATUS_ABORTED
     r.errs = np.sqrt(hist[:nchk])
@@ -277,6 +282,122 @@ def _knopp_multi(bd, a, B, M, reg, numItermax, stopThr, verbose, log, warn, warm
     return bd.out(res)
 
 
+def _stab_solve(bd, a, b, M, reg, numItermax, tau, stopThr, warmstart, print_period):
+    """One stabilised solve (``OTG_METHOD_STAB``); returns the result and the
+    reference's ``logu, logv`` (its gauge: shifted by the absorptions)."""
+    wu = wv = None
+    if warmstart is not None:
+        al, be = _warm(bd, warmstart, M.dtype)
+        wu, wv = (al / reg).contiguous(), (be / reg).contiguous()
+    r = solve_dense(M, a, b, reg, _lib.OTG_METHOD_STAB, numItermax, stopThr, wu, wv, tau=tau,
+                    check_period=print_period)
+    n, m = M.shape
+    k = r.nabs
+    logu = r.u - k * math.log(n)
+    logv = r.v + (((k - 1) * math.log(n) - math.log(m)) if r.absorbed_last else k * math.log(n))
+    return r, logu, logv
+
+
+def _plan_from_logs(M, logu, logv, reg):
+    lib = _lib.load()
+    P = torch.empty_like(M)
+    _lib.check(lib.otg_dense_plan(_lib.dtype_code(M.dtype), _lib.OTG_METHOD_LOG, ctypes.c_void_p(M.data_ptr()),
+                                  M.shape[0], M.shape[1], M.stride(0), _lib.ptr(logu), _lib.ptr(logv), float(reg),
+                                  _lib.ptr(P), P.stride(0), None, _lib.stream_handle(M.device)), "otg_dense_plan")
+    return P
+
+
+def sinkhorn_stabilized(a, b, M, reg, numItermax=1000, tau=1e3, stopThr=1e-9, warmstart=None, verbose=False,
+                        print_period=20, log=False, warn=True, **kwargs):
+    """GPU ``ot.bregman.sinkhorn_stabilized`` (``_sinkhorn.py:1105-1368``),
+    1-D ``b``.  ``warmstart`` is ``(alpha, beta)`` in cost units, as in the
+    reference.  The iteration runs in the log domain on the GPU and
+    reproduces the reference's absorptions, error history and stop index;
+    the log holds ``err, n_iter, logu, logv, alpha, beta, warmstart``."""
+    bd, Md, ad, bdv = _prep(a, b, M)
+    if bdv.dim() > 1:
+        raise NotImplementedError("pot_gb300 sinkhorn_stabilized: several target histograms are not on the GPU path")
+    r, logu, logv, lg = _stabilized(bd, ad, bdv, Md, reg, numItermax, stopThr, warmstart, verbose, warn, log,
+                                    tau, print_period)
+    P = _plan_from_logs(Md, logu, logv, reg)
+    return (bd.out(P), lg) if log else bd.out(P)
+
+
+def _stabilized(bd, ad, bdv, Md, reg, numItermax, stopThr, warmstart, verbose, warn, log, tau=1e3,
+                print_period=20):
+    r, logu, logv = _stab_solve(bd, ad, bdv, Md, reg, numItermax, tau, stopThr, warmstart, print_period)
+    if verbose:
+        for k, e in enumerate(r.errs):
+            ii = k * print_period
+            if ii % (print_period * 20) == 0:
+                print("{:5s}|{:12s}".format("It.", "Err") + "\n" + "-" * 19)
+            print("{:5d}|{:8e}|".format(ii, e))
+    if r.status == _lib.STATUS_NUMERICAL:
+        warnings.warn("Numerical errors at iteration %d" % r.niter)
+    elif r.status == _lib.STATUS_MAXITER and warn:
+        warnings.warn(NONCONV_MSG)
+    lg = None
+    if log:
+        alpha, beta = reg * logu, reg * logv
+        lg = {"err": _errs_as(bd, r.errs, Md), "n_iter": r.niter, "logu": bd.out(logu), "logv": bd.out(logv),
+              "alpha": bd.out(alpha), "beta": bd.out(beta), "warmstart": (bd.out(alpha), bd.out(beta))}
+    return r, logu, logv, lg
+
+
+def sinkhorn_epsilon_scaling(a, b, M, reg, numItermax=100, epsilon0=1e4, numInnerItermax=100, tau=1e3,
+                             stopThr=1e-9, warmstart=None, verbose=False, print_period=10, log=False, warn=True,
+                             **kwargs):
+    """GPU ``ot.bregman.sinkhorn_epsilon_scaling`` (``_sinkhorn.py:1371-1575``):
+    at least 35 outer steps with ``reg_k = (epsilon0 - reg) exp(-k) + reg``,
+    each a stabilised GPU solve warm-started from the previous
+    ``(alpha, beta)``; every ``print_period`` steps the squared marginal
+    errors of the inner plan (``otg_dense_marginals``) are logged."""
+    bd, Md, ad, bdv = _prep(a, b, M)
+    lib = _lib.load()
+    n, m = Md.shape
+    numItermax = max(35, numItermax)
+    ws = None if warmstart is None else _warm(bd, warmstart, Md.dtype)
+    rows = torch.empty(n, dtype=torch.float64, device=Md.device)
+    cols = torch.empty(m, dtype=torch.float64, device=Md.device)
+    a64, b64 = ad.double(), bdv.double()
+    errs = []
+    err = 1.0
+    stopped = False
+    ii = 0
+    logu = logv = regi = None
+    for ii in range(numItermax):
+        regi = (epsilon0 - reg) * math.exp(-ii) + reg
+        r, logu, logv = _stab_solve(bd, ad, bdv, Md, regi, numInnerItermax, tau, stopThr, ws, 20)
+        if r.status == _lib.STATUS_NUMERICAL:
+            warnings.warn("Numerical errors at iteration %d" % r.niter)
+        elif r.status == _lib.STATUS_MAXITER:
+            warnings.warn(NONCONV_MSG)
+        ws = (regi * logu, regi * logv)
+        if ii % print_period == 0:
+            _lib.check(lib.otg_dense_marginals(_lib.dtype_code(Md.dtype), ctypes.c_void_p(Md.data_ptr()), n, m,
+                                               Md.stride(0), _lib.ptr(logu), _lib.ptr(logv), float(regi),
+                                               _lib.ptr(rows), _lib.ptr(cols), _lib.stream_handle(Md.device)),
+                       "otg_dense_marginals")
+            err = float(torch.linalg.vector_norm(cols - b64) ** 2 + torch.linalg.vector_norm(rows - a64) ** 2)
+            errs.append(err)
+            if verbose:
+                if ii % (print_period * 10) == 0:
+                    print("{:5s}|{:12s}".format("It.", "Err") + "\n" + "-" * 19)
+                print("{:5d}|{:8e}|".format(ii, err))
+        if err <= stopThr and ii > 35:
+            stopped = True
+            break
+    if not stopped and warn:
+        warnings.warn(NONCONV_MSG)
+    P = _plan_from_logs(Md, logu, logv, regi)
+    if log:
+        alpha, beta = bd.out(ws[0]), bd.out(ws[1])
+        lg = {"err": _errs_as(bd, np.asarray(errs), Md), "alpha": alpha, "beta": beta, "warmstart": (alpha, beta),
+              "niter": ii}
+        return bd.out(P), lg
+    return bd.out(P)
+
+
 def sinkhorn(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, verbose=False,
              log=False, warn=True, warmstart=None, **kwargs):
     """GPU ``ot.sinkhorn``: dispatch on ``method`` (``_sinkhorn.py:164-234``)."""
@@ -287,9 +408,14 @@ def sinkhorn(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, ver
     if meth == "sinkhorn_log":
         return sinkhorn_log(a, b, M, reg, numItermax=numItermax, stopThr=stopThr, verbose=verbose,
                             log=log, warn=warn, warmstart=warmstart, **kwargs)
-    if meth in ("greenkhorn", "sinkhorn_stabilized", "sinkhorn_epsilon_scaling"):
-        raise NotImplementedError("pot_gb300 implements method='sinkhorn' and 'sinkhorn_log'; "
-                                  "'%s' is not on the GPU path" % method)
+    if meth == "sinkhorn_stabilized":
+        return sinkhorn_stabilized(a, b, M, reg, numItermax=numItermax, stopThr=stopThr, warmstart=warmstart,
+                                   verbose=verbose, log=log, warn=warn, **kwargs)
+    if meth == "sinkhorn_epsilon_scaling":
+        return sinkhorn_epsilon_scaling(a, b, M, reg, numItermax=numItermax, stopThr=stopThr,
+                                        warmstart=warmstart, verbose=verbose, log=log, warn=warn, **kwargs)
+    if meth == "greenkhorn":
+        raise NotImplementedError("pot_gb300: method='greenkhorn' is not on the GPU path")
     raise ValueError("Unknown method '%s'." % method)
 
 
@@ -298,9 +424,19 @@ def sinkhorn2(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, ve
     """GPU ``ot.sinkhorn2``: the loss ``<P, M>`` (fp64 accumulation) for 1-D
     ``b``; the per-histogram losses for 2-D ``b`` (``_sinkhorn.py:435-484``)."""
     meth = method.lower()
+    if meth == "sinkhorn_stabilized":
+        bd, Md, ad, bdv = _prep(a, b, M)
+        if bdv.dim() > 1:
+            raise NotImplementedError("pot_gb300 sinkhorn_stabilized: several target histograms are not on "
+                                      "the GPU path")
+        kw = {k: kwargs[k] for k in ("tau", "print_period") if k in kwargs}
+        r, logu, logv, lg = _stabilized(bd, ad, bdv, Md, reg, numItermax, stopThr, warmstart, verbose, warn,
+                                        log, **kw)
+        rr = DenseResult()
+        rr.u, rr.v = logu, logv
+        out = bd.scalar(_loss(Md, rr, reg, _lib.OTG_METHOD_LOG))
+        return (out, lg) if log else out
     if meth not in ("sinkhorn", "sinkhorn_log"):
-        if meth == "sinkhorn_stabilized":
-            raise NotImplementedError("pot_gb300: method='sinkhorn_stabilized' is not on the GPU path")
         raise ValueError("Unknown method '%s'." % method)
     bd, Md, ad, bdv = _prep(a, b, M)
     code = _lib.OTG_METHOD_KNOPP if meth == "sinkhorn" else _lib.OTG_METHOD_LOG

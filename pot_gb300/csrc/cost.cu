@@ -223,6 +223,48 @@ __global__ void __launch_bounds__(256) nearest_mass_kernel(const float* __restri
   atomicAdd(w + (int64_t)p * k + arg, 1.0f / (float)n);
 }
 
+// Loss of a lazy plan: sum_ij C_ij exp(f_i + g_j - C_ij / reg) with C the
+// squared distance of points x_i, y_j (natural-log potentials f, g), the
+// value ot/bregman/_empirical.py:470-478 accumulates block by block.  One CTA
+// per tile of LL_ROWS points (staged in shared memory); each thread walks
+// columns; fp64 accumulation, one atomic per CTA.
+constexpr int LL_ROWS = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(256) lazy_loss_kernel(const T* __restrict__ X, const T* __restrict__ Y, int64_t n,
+                                                        int64_t m, int d, const T* __restrict__ f,
+                                                        const T* __restrict__ g, T c, double* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char ll_raw[];
+  T* xs = reinterpret_cast<T*>(ll_raw);
+  T* fs = xs + LL_ROWS * d;
+  const int64_t r0 = (int64_t)blockIdx.x * LL_ROWS;
+  const int rows = (n - r0) < LL_ROWS ? (int)(n - r0) : LL_ROWS;
+  const T L2E = T(OTG_LOG2E);
+  for (int e = threadIdx.x; e < rows * d; e += blockDim.x) xs[e] = X[r0 * d + e];
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) fs[r] = f[r0 + r] * L2E;
+  __syncthreads();
+  double acc = 0.0;
+  for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
+    const T* y = Y + j * d;
+    const T gj = g[j] * L2E;
+    for (int r = 0; r < rows; ++r) {
+      const T* x = xs + r * d;
+      T cij = 0;
+      for (int k = 0; k < d; ++k) { const T df = x[k] - y[k]; cij = fma(df, df, cij); }
+      acc += (double)cij * (double)ex2(fma(cij, c, fs[r] + gj));
+    }
+  }
+  __shared__ double red[8];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    atomicAdd(out, t);
+  }
+}
+
 }  // namespace otg
 
 using namespace otg;
@@ -291,6 +333,33 @@ int otg_softmin_features(const float* M, const int64_t* m_off, const int32_t* ro
   dim3 grid((unsigned)((max_rows + 7) / 8), (unsigned)nprob);
   softmin_features_kernel<<<grid, 256, 0, stream>>>(M, m_off, rows, cols, ldm, r_off, c_off, b, scale, taus, ntau,
                                                     nprob, g, out);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_lazy_loss(int dtype, const void* X, const void* Y, int64_t n, int64_t m, int32_t d, const void* f,
+                  const void* g, double reg, double* out, cudaStream_t stream) {
+  if (!X || !Y || !f || !g || !out || n < 1 || m < 1 || d < 1 || !(reg > 0)) return OTG_ERR_ARG;
+  const size_t esz = dtype == OTG_F64 ? 8 : 4;
+  const size_t smem = esz * (size_t)LL_ROWS * (size_t)(d + 1);
+  if (smem > 96 * 1024) return OTG_ERR_UNSUPPORTED;
+  if (cudaMemsetAsync(out, 0, sizeof(double), stream) != cudaSuccess) return OTG_ERR_CUDA;
+  const unsigned blocks = (unsigned)((n + LL_ROWS - 1) / LL_ROWS);
+  const double c = -OTG_LOG2E / reg;
+  if (dtype == OTG_F64) {
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(lazy_loss_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return OTG_ERR_CUDA;
+    lazy_loss_kernel<double><<<blocks, 256, smem, stream>>>((const double*)X, (const double*)Y, n, m, d,
+                                                            (const double*)f, (const double*)g, c, out);
+  } else if (dtype == OTG_F32) {
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(lazy_loss_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return OTG_ERR_CUDA;
+    lazy_loss_kernel<float><<<blocks, 256, smem, stream>>>((const float*)X, (const float*)Y, n, m, d,
+                                                           (const float*)f, (const float*)g, (float)c, out);
+  } else {
+    return OTG_ERR_DTYPE;
+  }
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 

@@ -7,6 +7,8 @@
 //                              10th iteration :646-658)
 //   sinkhorn_log    :690-918  (v = log b - LSE_i(Mr + u) ; u = log a - LSE_j(Mr + v),
 //                              same check :884-899)
+//   sinkhorn_stabilized :1105-1368 (scalings over absorbed potentials; see
+//                              "Stabilised form" below)
 //
 // One iteration is one COLUMN pass and one ROW pass over M:
 //   column pass  : partial column reductions over row chunks      -> barrier
@@ -21,7 +23,27 @@
 //
 // Log-domain arithmetic runs in base 2: x = M * c with c = -log2(e)/reg,
 // potentials are kept as log2 values, and exp is the MUFU ex2 instruction.
+//
+// Stabilised form.  The reference keeps scalings u = exp(F - alpha/reg),
+// v = exp(G - beta/reg) over absorbed potentials and, whenever max u or max v
+// exceeds tau, moves them into alpha, beta and resets u = 1/n, v = 1/m
+// (:1282-1296).  In exact arithmetic F + G follows the log-domain v-first
+// iteration started from F0 = alpha0/reg - log n; an absorption only shifts
+// the gauge: F by -log n and G by -log m at the absorbing iteration, after
+// which G carries +log n per absorption.  The kernel therefore runs the log
+// iteration on (F, G) in that standard gauge and tracks, per row and column,
+// the reference point SA, SB of the last absorption, so that
+// u = exp(F - SA), v = exp(G - SB) exactly as the reference sees them:
+//   start          SA = alpha0/reg, SB = beta0/reg
+//   absorption     SA = F + log n,  SB = G - log n
+// The absorption test max(F - SA) > log tau, max(G - SB) > log tau is a
+// grid-wide max folded into the column merge and the row pass.  A check
+// iteration that absorbed measures the plan of the shifted gauge, i.e. the
+// column sums divided by n m (:1298-1306).  The host turns (F, G), the
+// absorption count and the last-iteration flag back into the reference's
+// logu, logv, alpha, beta.
 #include <algorithm>
+#include <cmath>
 #include "common.cuh"
 #include "../../include/pot_gb300.h"
 
@@ -53,7 +75,39 @@ struct DenseArgs {
   int* info;                            // status, niter, nchecks, abort, numflag
   unsigned* bar;
   uint64_t timeout_ns;
+  // stabilised form only
+  T *sa, *sb;                           // absorption reference points (base 2)
+  T log2n, log2m, log2tau;
+  int period;                           // iterations between marginal checks
+  unsigned long long* mslot;            // [2] max(F - SA), [2] max(G - SB), ordered keys
 };
+
+template <int METHOD> struct LogDomain { static constexpr bool value = METHOD != OTG_METHOD_KNOPP; };
+
+// Order-preserving map of doubles to unsigned keys (atomicMax on keys = max
+// on values; key 0 is below every value).
+__device__ __forceinline__ unsigned long long order_key(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double key_value(unsigned long long k) {
+  return (k >> 63) ? __longlong_as_double((long long)(k & 0x7fffffffffffffffull)) : __longlong_as_double((long long)~k);
+}
+
+// Block-wide max of one value per thread, then one atomicMax per CTA.  All
+// threads of the block call it.
+__device__ void block_max_atomic(double x, unsigned long long* slot) {
+  __shared__ double red[32];
+  x = warp_max(x);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = -INFINITY;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t = fmax(t, red[k]);
+    if (t != -INFINITY) atomicMax(slot, order_key(t));
+  }
+  __syncthreads();
+}
 
 constexpr int RW = 4;     // rows per warp in the row pass
 constexpr int GCOL = 4;   // rows folded per max update in the column pass
@@ -103,10 +157,10 @@ __device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, int lan
           } else {
 #pragma unroll
             for (int k = 0; k < VW; ++k) x[g][k] = T(0);
-            ur[g] = METHOD == OTG_METHOD_LOG ? T(-INFINITY) : T(0);
+            ur[g] = LogDomain<METHOD>::value ? T(-INFINITY) : T(0);
           }
         }
-        if (METHOD == OTG_METHOD_LOG) {
+        if (LogDomain<METHOD>::value) {
 #pragma unroll
           for (int k = 0; k < VW; ++k) {
             T t[GCOL];
@@ -140,7 +194,7 @@ __device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, int lan
       if (j < m) {
         T M0 = -INFINITY, S0 = 0;
         for (int w = 0; w < 8; ++w) {
-          if (METHOD == OTG_METHOD_LOG) lse_merge(M0, S0, s_mx[w][c], s_s[w][c]);
+          if (LogDomain<METHOD>::value) lse_merge(M0, S0, s_mx[w][c], s_s[w][c]);
           else S0 += s_s[w][c];
         }
         A.pcol[r * m + j] = Pair<T>{M0, S0};
@@ -158,8 +212,10 @@ __device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, int lan
 // ---------------------------------------------------------------------------
 template <typename T, int METHOD>
 __device__ __forceinline__ T row_finalize(const DenseArgs<T>& A, int64_t i, T mx, T s, int* numflag) {
-  if (METHOD == OTG_METHOD_LOG) {
-    return __ldcg(A.loga2 + i) - lse_value(mx, s);
+  if (LogDomain<METHOD>::value) {
+    const T unew = __ldcg(A.loga2 + i) - lse_value(mx, s);
+    if (METHOD == OTG_METHOD_STAB && isnan(unew)) atomicExch(numflag, 1);
+    return unew;
   } else {
     T unew = T(1) / ((T(1) / A.a[i]) * s);
     if (!isfinite(unew)) atomicExch(numflag, 1);
@@ -168,7 +224,8 @@ __device__ __forceinline__ T row_finalize(const DenseArgs<T>& A, int64_t i, T mx
 }
 
 template <typename T, int METHOD, bool VEC>
-__device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __restrict__ unew, int lane) {
+__device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __restrict__ unew, int lane,
+                         double& umax) {
   constexpr int VW = Vec<T>::N;
   using V = typename Vec<T>::type;
   __shared__ T r_mx[8][RW], r_s[8][RW];
@@ -189,7 +246,7 @@ __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __re
         unpack(__ldcg(reinterpret_cast<const V*>(v + j)), vv);
       } else {
 #pragma unroll
-        for (int k = 0; k < VW; ++k) vv[k] = (j + k < c1) ? __ldcg(v + j + k) : (METHOD == OTG_METHOD_LOG ? T(-INFINITY) : T(0));
+        for (int k = 0; k < VW; ++k) vv[k] = (j + k < c1) ? __ldcg(v + j + k) : (LogDomain<METHOD>::value ? T(-INFINITY) : T(0));
       }
       T x[RW][VW];
 #pragma unroll
@@ -206,7 +263,7 @@ __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __re
       }
 #pragma unroll
       for (int r = 0; r < RW; ++r) {
-        if (METHOD == OTG_METHOD_LOG) {
+        if (LogDomain<METHOD>::value) {
           T t[VW];
           T gm = -INFINITY;
 #pragma unroll
@@ -227,7 +284,7 @@ __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __re
     }
 #pragma unroll
     for (int r = 0; r < RW; ++r) {
-      if (METHOD == OTG_METHOD_LOG) warp_lse(mx[r], s[r]);
+      if (LogDomain<METHOD>::value) warp_lse(mx[r], s[r]);
       else s[r] = warp_sum(s[r]);
     }
     if (lane == 0) {
@@ -241,11 +298,16 @@ __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __re
       if (row < n) {
         T M0 = -INFINITY, S0 = 0;
         for (int w = 0; w < 8; ++w) {
-          if (METHOD == OTG_METHOD_LOG) lse_merge(M0, S0, r_mx[w][r], r_s[w][r]);
+          if (LogDomain<METHOD>::value) lse_merge(M0, S0, r_mx[w][r], r_s[w][r]);
           else S0 += r_s[w][r];
         }
-        if (A.Sc == 1) unew[row] = row_finalize<T, METHOD>(A, row, M0, S0, A.info + 4);
-        else A.prow[cc * n + row] = Pair<T>{M0, S0};
+        if (A.Sc == 1) {
+          const T un = row_finalize<T, METHOD>(A, row, M0, S0, A.info + 4);
+          unew[row] = un;
+          if (METHOD == OTG_METHOD_STAB) umax = fmax(umax, (double)(un - __ldcg(A.sa + row)));
+        } else {
+          A.prow[cc * n + row] = Pair<T>{M0, S0};
+        }
       }
     }
     __syncthreads();
@@ -253,35 +315,47 @@ __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __re
 }
 
 template <typename T, int METHOD>
-__device__ void row_merge(const DenseArgs<T>& A, T* __restrict__ unew, long gtid, long nthreads) {
+__device__ void row_merge(const DenseArgs<T>& A, T* __restrict__ unew, long gtid, long nthreads, double& umax) {
   for (int64_t i = gtid; i < A.n; i += nthreads) {
     T mx = -INFINITY, s = 0;
     const T* base = reinterpret_cast<const T*>(A.prow + i);
-    if (METHOD == OTG_METHOD_LOG) lse_merge_strided(mx, s, base, 2 * A.n, A.Sc);
+    if (LogDomain<METHOD>::value) lse_merge_strided(mx, s, base, 2 * A.n, A.Sc);
     else s = sum_strided(base, 2 * A.n, A.Sc);
-    unew[i] = row_finalize<T, METHOD>(A, i, mx, s, A.info + 4);
+    const T un = row_finalize<T, METHOD>(A, i, mx, s, A.info + 4);
+    unew[i] = un;
+    if (METHOD == OTG_METHOD_STAB) umax = fmax(umax, (double)(un - __ldcg(A.sa + i)));
   }
 }
 
 // Column merge: combine the Sr partials of column j, update v, and add the
-// squared column-marginal violation of (u_cur, v_cur) when `check`.
+// squared column-marginal violation of (u_cur, v_cur) when `check` (with the
+// plan scaled by 2^err_shift).  The stabilised form also returns the
+// thread's max of v_new - SB.
 template <typename T, int METHOD>
 __device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* __restrict__ vnxt,
-                          bool check, bool update, double* err_slot, long gtid, long nthreads) {
+                          bool check, bool update, double* err_slot, long gtid, long nthreads, T err_shift,
+                          double& vmax) {
   double e2 = 0.0;
   for (int64_t j = gtid; j < A.m; j += nthreads) {
     T mx = -INFINITY, s = 0;
     const T* base = reinterpret_cast<const T*>(A.pcol + j);
-    if (METHOD == OTG_METHOD_LOG) lse_merge_strided(mx, s, base, 2 * A.m, A.Sr);
+    if (LogDomain<METHOD>::value) lse_merge_strided(mx, s, base, 2 * A.m, A.Sr);
     else s = sum_strided(base, 2 * A.m, A.Sr);
     const T bj = A.b[j];
-    if (METHOD == OTG_METHOD_LOG) {
+    if (LogDomain<METHOD>::value) {
       const T L = lse_value(mx, s);
       if (check) {
-        double cs = (double)ex2(__ldcg(vcur + j) + L);
+        double cs = (double)ex2(__ldcg(vcur + j) + L + err_shift);
         e2 += (cs - (double)bj) * (cs - (double)bj);
       }
-      if (update) vnxt[j] = __ldcg(A.logb2 + j) - L;
+      if (update) {
+        const T vn = __ldcg(A.logb2 + j) - L;
+        vnxt[j] = vn;
+        if (METHOD == OTG_METHOD_STAB) {
+          if (isnan(vn)) atomicExch(A.info + 4, 1);
+          vmax = fmax(vmax, (double)(vn - __ldcg(A.sb + j)));
+        }
+      }
     } else {
       if (check) {
         double cs = (double)(__ldcg(vcur + j) * s);
@@ -323,7 +397,12 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
 
   // Phase 0: initial state.
   for (int64_t i = gtid; i < A.n; i += nthreads) {
-    if (METHOD == OTG_METHOD_LOG) {
+    if (METHOD == OTG_METHOD_STAB) {
+      const T s0 = A.warm_u ? A.warm_u[i] * L2E : T(0);
+      A.sa[i] = s0;
+      A.u0[i] = s0 - A.log2n;
+      A.loga2[i] = lg2(A.a[i]);
+    } else if (LogDomain<METHOD>::value) {
       A.u0[i] = A.warm_u ? A.warm_u[i] * L2E : T(0);
       A.loga2[i] = lg2(A.a[i]);
     } else {
@@ -331,7 +410,12 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
     }
   }
   for (int64_t j = gtid; j < A.m; j += nthreads) {
-    if (METHOD == OTG_METHOD_LOG) {
+    if (METHOD == OTG_METHOD_STAB) {
+      const T s0 = A.warm_v ? A.warm_v[j] * L2E : T(0);
+      A.sb[j] = s0;
+      A.v0[j] = s0 - A.log2m;
+      A.logb2[j] = lg2(A.b[j]);
+    } else if (LogDomain<METHOD>::value) {
       A.v0[j] = A.warm_v ? A.warm_v[j] * L2E : T(0);
       A.logb2[j] = lg2(A.b[j]);
     } else {
@@ -342,6 +426,8 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
 
   T *ucur = A.u0, *unxt = A.u1, *vcur = A.v0, *vnxt = A.v1;
   bool prev_check = false;
+  bool absorbed = false;  // stabilised form: the last completed iteration absorbed
+  int nabs = 0;
   int nchk = 0;
   int status = OTG_STATUS_MAXITER, niter = A.max_iter - 1;
   for (int ii = 0;; ++ii) {
@@ -349,43 +435,65 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     const bool update = ii < A.max_iter;
     double* slot = A.hist + (nchk < A.hist_cap ? nchk : A.hist_cap - 1);
-    col_merge<T, METHOD>(A, vcur, vnxt, prev_check, update, slot, gtid, nthreads);
+    double vmax = -INFINITY;
+    const T shift = (METHOD == OTG_METHOD_STAB && absorbed) ? -(A.log2n + A.log2m) : T(0);
+    col_merge<T, METHOD>(A, vcur, vnxt, prev_check, update, slot, gtid, nthreads, shift, vmax);
+    if (METHOD == OTG_METHOD_STAB && update) block_max_atomic(vmax, A.mslot + 2 + (ii & 1));
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     if (prev_check) {
       double e2 = *(volatile double*)slot;
       ++nchk;
-      if (sqrt(e2) < A.stop_thr) { status = OTG_STATUS_CONVERGED; niter = ii - 1; break; }
+      const bool stop = METHOD == OTG_METHOD_STAB ? sqrt(e2) <= A.stop_thr : sqrt(e2) < A.stop_thr;
+      if (stop) { status = OTG_STATUS_CONVERGED; niter = ii - 1; break; }
     }
     if (!update) { status = OTG_STATUS_MAXITER; niter = A.max_iter - 1; break; }
-    if (METHOD != OTG_METHOD_LOG && ld_acquire_i(A.info + 4)) {
+    if (!LogDomain<METHOD>::value && ld_acquire_i(A.info + 4)) {
       // zero column sum or non-finite v: revert to the previous pair
       status = OTG_STATUS_NUMERICAL; niter = ii; break;
     }
-    row_pass<T, METHOD, VEC>(A, vnxt, unxt, lane);
+    double umax = -INFINITY;
+    row_pass<T, METHOD, VEC>(A, vnxt, unxt, lane, umax);
+    if (METHOD == OTG_METHOD_STAB && A.Sc == 1) block_max_atomic(umax, A.mslot + (ii & 1));
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     if (A.Sc > 1) {
-      row_merge<T, METHOD>(A, unxt, gtid, nthreads);
+      row_merge<T, METHOD>(A, unxt, gtid, nthreads, umax);
+      if (METHOD == OTG_METHOD_STAB) block_max_atomic(umax, A.mslot + (ii & 1));
       if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     }
     if (METHOD != OTG_METHOD_LOG && ld_acquire_i(A.info + 4)) {
       status = OTG_STATUS_NUMERICAL; niter = ii; break;
     }
+    if (METHOD == OTG_METHOD_STAB) {
+      // absorption test on u = 2^(F - SA), v = 2^(G - SB) of this iteration;
+      // the slots of the other parity were last read one iteration ago
+      const double mu = key_value(__ldcg(A.mslot + (ii & 1)));
+      const double mv = key_value(__ldcg(A.mslot + 2 + (ii & 1)));
+      absorbed = mu > (double)A.log2tau || mv > (double)A.log2tau;
+      if (absorbed) {
+        ++nabs;
+        for (int64_t i = gtid; i < A.n; i += nthreads) A.sa[i] = __ldcg(unxt + i) + A.log2n;
+        for (int64_t j = gtid; j < A.m; j += nthreads) A.sb[j] = __ldcg(vnxt + j) - A.log2n;
+      }
+      if (gtid == 0) { A.mslot[(ii + 1) & 1] = 0ull; A.mslot[2 + ((ii + 1) & 1)] = 0ull; }
+    }
     T* t;
     t = ucur; ucur = unxt; unxt = t;
     t = vcur; vcur = vnxt; vnxt = t;
-    prev_check = (ii % 10 == 0);
+    prev_check = (ii % A.period == 0);
   }
 
   // Final state in natural units.
   const T LN2 = T(OTG_LN2);
   for (int64_t i = gtid; i < A.n; i += nthreads)
-    A.out_u[i] = METHOD == OTG_METHOD_LOG ? __ldcg(ucur + i) * LN2 : __ldcg(ucur + i);
+    A.out_u[i] = LogDomain<METHOD>::value ? __ldcg(ucur + i) * LN2 : __ldcg(ucur + i);
   for (int64_t j = gtid; j < A.m; j += nthreads)
-    A.out_v[j] = METHOD == OTG_METHOD_LOG ? __ldcg(vcur + j) * LN2 : __ldcg(vcur + j);
+    A.out_v[j] = LogDomain<METHOD>::value ? __ldcg(vcur + j) * LN2 : __ldcg(vcur + j);
   if (gtid == 0) {
     A.info[0] = status;
     A.info[1] = niter;
     A.info[2] = nchk;
+    A.info[5] = nabs;
+    A.info[6] = absorbed ? 1 : 0;
   }
 }
 
@@ -406,7 +514,7 @@ __global__ void __launch_bounds__(256) dense_plan_kernel(const T* __restrict__ M
     for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
       const T x = Mrow[j];
       T p;
-      if (METHOD == OTG_METHOD_LOG) p = ex2(fma(x, c, (ui + v[j]) * L2E));
+      if (LogDomain<METHOD>::value) p = ex2(fma(x, c, (ui + v[j]) * L2E));
       else p = ui * ex2(x * c) * v[j];
       if (P) P[i * ldp + j] = p;
       if (loss) acc += (double)x * (double)p;
@@ -424,6 +532,40 @@ __global__ void __launch_bounds__(256) dense_plan_kernel(const T* __restrict__ M
       atomicAdd(loss, t);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Marginals of the plan exp(-M_ij/reg + u_i + v_j) (natural-log potentials),
+// accumulated in fp64: one warp per row for the row sums; column sums from
+// CTAs of 256 columns x 64 rows, one atomic per column per CTA.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) dense_rowsum_kernel(const T* __restrict__ M, int64_t n, int64_t m, int64_t ldm,
+                                                           const T* __restrict__ u, const T* __restrict__ v, T c,
+                                                           double* __restrict__ rows) {
+  const T L2E = T(OTG_LOG2E);
+  const int64_t i = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const T ui = u[i] * L2E;
+  double acc = 0.0;
+  for (int64_t j = lane; j < m; j += 32) acc += (double)ex2(fma(M[i * ldm + j], c, ui + v[j] * L2E));
+  acc = warp_sum(acc);
+  if (lane == 0) rows[i] = acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) dense_colsum_kernel(const T* __restrict__ M, int64_t n, int64_t m, int64_t ldm,
+                                                           const T* __restrict__ u, const T* __restrict__ v, T c,
+                                                           double* __restrict__ cols) {
+  const T L2E = T(OTG_LOG2E);
+  const int64_t j = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  const int64_t i0 = (int64_t)blockIdx.y * 64, i1 = min(n, i0 + 64);
+  if (j >= m) return;
+  const T vj = v[j] * L2E;
+  double acc = 0.0;
+  for (int64_t i = i0; i < i1; ++i) acc += (double)ex2(fma(M[i * ldm + j], c, u[i] * L2E + vj));
+  atomicAdd(cols + j, acc);
 }
 
 }  // namespace otg
@@ -481,11 +623,11 @@ Layout make_layout(int64_t n, int64_t m, int hist_cap, int grid) {
   L.cchunk = cch;
   L.Sc = (int)((m + cch - 1) / cch);
   size_t off = 0;
-  L.off_state = off; off = align_up(off + sizeof(T) * (3 * ((size_t)n + 4) + 3 * ((size_t)m + 4)), 256);
+  L.off_state = off; off = align_up(off + sizeof(T) * (4 * ((size_t)n + 4) + 4 * ((size_t)m + 4)), 256);
   L.off_pcol = off; off = align_up(off + sizeof(Pair<T>) * (size_t)L.Sr * m, 256);
   L.off_prow = off; off = align_up(off + sizeof(Pair<T>) * (size_t)(L.Sc > 1 ? L.Sc : 0) * n, 256);
   L.off_hist = off; off = align_up(off + sizeof(double) * (size_t)hist_cap, 256);
-  L.off_ctrl = off; off = align_up(off + 64, 256);
+  L.off_ctrl = off; off = align_up(off + 128, 256);
   L.total = off;
   return L;
 }
@@ -516,6 +658,7 @@ int launch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
   int64_t o = 0;
   A.u0 = st_ + o; o += al(n); A.u1 = st_ + o; o += al(n); A.loga2 = st_ + o; o += al(n);
   A.v0 = st_ + o; o += al(m); A.v1 = st_ + o; o += al(m); A.logb2 = st_ + o; o += al(m);
+  A.sa = st_ + o; o += al(n); A.sb = st_ + o; o += al(m);
   A.pcol = reinterpret_cast<Pair<T>*>(base + L.off_pcol);
   A.prow = reinterpret_cast<Pair<T>*>(base + L.off_prow);
   A.Sr = L.Sr; A.Sc = L.Sc; A.rchunk = L.rchunk; A.cchunk = L.cchunk;
@@ -524,6 +667,11 @@ int launch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
   A.info = reinterpret_cast<int*>(base + L.off_ctrl);
   A.bar = reinterpret_cast<unsigned*>(base + L.off_ctrl + 32);
   A.timeout_ns = p->timeout_ms > 0 ? (uint64_t)p->timeout_ms * 1000000ull : 4000000000ull;
+  A.log2n = (T)std::log2((double)n);
+  A.log2m = (T)std::log2((double)m);
+  A.log2tau = (T)(METHOD == OTG_METHOD_STAB ? std::log2(p->tau) : 0.0);
+  A.period = METHOD == OTG_METHOD_STAB ? p->check_period : 10;
+  A.mslot = reinterpret_cast<unsigned long long*>(base + L.off_ctrl + 64);
   cudaError_t e = cudaMemsetAsync(base + L.off_hist, 0, L.total - L.off_hist, st);
   if (e != cudaSuccess) return OTG_ERR_CUDA;
   void* args[] = {&A};
@@ -538,6 +686,8 @@ int dispatch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
   const bool vec = (p->m % VW == 0) && (p->ldm % VW == 0) && ((uintptr_t)p->M % 16 == 0);
   if (p->method == OTG_METHOD_LOG)
     return vec ? launch_dense<T, OTG_METHOD_LOG, true>(p, ws, st) : launch_dense<T, OTG_METHOD_LOG, false>(p, ws, st);
+  if (p->method == OTG_METHOD_STAB)
+    return vec ? launch_dense<T, OTG_METHOD_STAB, true>(p, ws, st) : launch_dense<T, OTG_METHOD_STAB, false>(p, ws, st);
   return vec ? launch_dense<T, OTG_METHOD_KNOPP, true>(p, ws, st) : launch_dense<T, OTG_METHOD_KNOPP, false>(p, ws, st);
 }
 
@@ -545,7 +695,9 @@ int check_problem(const OtgDenseProblem* p) {
   if (!p || !p->M || !p->a || !p->b || !p->out_u || !p->out_v) return OTG_ERR_ARG;
   if (p->n < 1 || p->m < 1 || p->ldm < p->m || p->hist_cap < 1) return OTG_ERR_ARG;
   if (p->dtype != OTG_F32 && p->dtype != OTG_F64) return OTG_ERR_DTYPE;
-  if (p->method != OTG_METHOD_LOG && p->method != OTG_METHOD_KNOPP) return OTG_ERR_ARG;
+  if (p->method != OTG_METHOD_LOG && p->method != OTG_METHOD_KNOPP && p->method != OTG_METHOD_STAB)
+    return OTG_ERR_ARG;
+  if (p->method == OTG_METHOD_STAB && (p->check_period < 1 || !(p->tau > 0))) return OTG_ERR_ARG;
   if (p->max_iter < 0) return OTG_ERR_ARG;
   return OTG_OK;
 }
@@ -582,6 +734,7 @@ int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, i
   int64_t blocks = std::min<int64_t>(n, (int64_t)sms * 8);
   if (loss) cudaMemsetAsync(loss, 0, sizeof(double), stream);
   const double c = -OTG_LOG2E / reg;
+  if (method == OTG_METHOD_STAB) method = OTG_METHOD_LOG;  // plan of natural-log potentials
   if (dtype == OTG_F64) {
     if (method == OTG_METHOD_LOG)
       dense_plan_kernel<double, OTG_METHOD_LOG><<<blocks, 256, 0, stream>>>((const double*)M, n, m, ldm, (const double*)u, (const double*)v, c, (double*)P, ldp, loss);
@@ -592,6 +745,24 @@ int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, i
       dense_plan_kernel<float, OTG_METHOD_LOG><<<blocks, 256, 0, stream>>>((const float*)M, n, m, ldm, (const float*)u, (const float*)v, (float)c, (float*)P, ldp, loss);
     else
       dense_plan_kernel<float, OTG_METHOD_KNOPP><<<blocks, 256, 0, stream>>>((const float*)M, n, m, ldm, (const float*)u, (const float*)v, (float)c, (float*)P, ldp, loss);
+  } else {
+    return OTG_ERR_DTYPE;
+  }
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_dense_marginals(int dtype, const void* M, int64_t n, int64_t m, int64_t ldm, const void* u, const void* v,
+                        double reg, double* rowsum, double* colsum, cudaStream_t stream) {
+  if (!M || !u || !v || !rowsum || !colsum || n < 1 || m < 1 || ldm < m || !(reg > 0)) return OTG_ERR_ARG;
+  if (cudaMemsetAsync(colsum, 0, sizeof(double) * (size_t)m, stream) != cudaSuccess) return OTG_ERR_CUDA;
+  const double c = -OTG_LOG2E / reg;
+  const dim3 rg((unsigned)((n + 7) / 8)), cg((unsigned)((m + 255) / 256), (unsigned)((n + 63) / 64));
+  if (dtype == OTG_F64) {
+    dense_rowsum_kernel<double><<<rg, 256, 0, stream>>>((const double*)M, n, m, ldm, (const double*)u, (const double*)v, c, rowsum);
+    dense_colsum_kernel<double><<<cg, 256, 0, stream>>>((const double*)M, n, m, ldm, (const double*)u, (const double*)v, c, colsum);
+  } else if (dtype == OTG_F32) {
+    dense_rowsum_kernel<float><<<rg, 256, 0, stream>>>((const float*)M, n, m, ldm, (const float*)u, (const float*)v, (float)c, rowsum);
+    dense_colsum_kernel<float><<<cg, 256, 0, stream>>>((const float*)M, n, m, ldm, (const float*)u, (const float*)v, (float)c, colsum);
   } else {
     return OTG_ERR_DTYPE;
   }

@@ -14,8 +14,11 @@
 // epilogue:
 //   mode 0: write the scaled result again as high/low half planes (the next
 //           product's operand);
-//   mode 1: out_ij = s_acc * acc_ij + s_vec * (rowv_i + colv_j)  (the cost of
-//           the inner Sinkhorn, 2 constC - 2 hC1 T hC2^T, in fp32).
+//   mode 1: out_ij = s_acc * acc_ij + s_vec * (rowv_i + colv_j)
+//           [+ s_add * addend_ij]  (the cost of the inner Sinkhorn,
+//           2 constC - 2 hC1 T hC2^T, in fp32, optionally weighted and with
+//           the linear term of fused GW or the other half of an asymmetric
+//           gradient added).
 // The tensor-core accumulator is not a round-to-nearest fp32 sum over long K
 // (measured error grows like 2^-24 per accumulation step), so every 4
 // k-tiles the tile is moved out of TMEM (two buffers, alternating) and added
@@ -49,6 +52,7 @@ struct GemmEpi {
   __half* out_hi; __half* out_lo; int64_t ld_h;
   float* out; int64_t ld_o;
   const float* rowv; const float* colv;
+  const float* addend; int64_t ld_add; float s_add;  // mode 1, optional
   int k_tiles;
   int* abort_flag;
   uint64_t timeout_ns;
@@ -194,10 +198,20 @@ gemm_split3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
         } else if (row < ep.M) {
           const float rv = ep.rowv[row];
           float* dst = ep.out + row * ep.ld_o;
+          if (ep.addend) {
+            const float* add = ep.addend + row * ep.ld_add;
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            const int64_t col = col0 + i;
-            if (col < ep.N) dst[col] = ep.s_acc * acc[c0 + i] + ep.s_vec * (rv + ep.colv[col]);
+            for (int i = 0; i < 32; ++i) {
+              const int64_t col = col0 + i;
+              if (col < ep.N)
+                dst[col] = fmaf(ep.s_add, add[col], ep.s_acc * acc[c0 + i] + ep.s_vec * (rv + ep.colv[col]));
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              const int64_t col = col0 + i;
+              if (col < ep.N) dst[col] = ep.s_acc * acc[c0 + i] + ep.s_vec * (rv + ep.colv[col]);
+            }
           }
         }
       }
@@ -302,6 +316,7 @@ int otg_gemm_split3(const OtgSplitGemm* g, cudaStream_t stream) {
   ep.scale = g->scale; ep.s_acc = g->s_acc; ep.s_vec = g->s_vec;
   ep.out_hi = static_cast<__half*>(g->out_hi); ep.out_lo = static_cast<__half*>(g->out_lo); ep.ld_h = g->ld_h;
   ep.out = g->out; ep.ld_o = g->ld_o; ep.rowv = g->rowv; ep.colv = g->colv;
+  ep.addend = g->addend; ep.ld_add = g->ld_add; ep.s_add = g->s_add;
   ep.k_tiles = (int)(g->k_alloc / GB_K);
   ep.abort_flag = g->abort_flag;
   ep.timeout_ns = g->timeout_ms > 0 ? (uint64_t)g->timeout_ms * 1000000ull : 4000000000ull;
@@ -311,6 +326,7 @@ int otg_gemm_split3(const OtgSplitGemm* g, cudaStream_t stream) {
       return OTG_ERR_ARG;
   } else {
     if (!ep.out || !ep.rowv || !ep.colv || ep.ld_o < ep.N || ep.M > g->a_rows || ep.N > g->b_rows) return OTG_ERR_ARG;
+    if (ep.addend && ep.ld_add < ep.N) return OTG_ERR_ARG;
   }
   CUtensorMap mah, mal, mbh, mbl;
   if (!make_plane_map(&mah, g->a_hi, g->a_rows, g->lda) || !make_plane_map(&mal, g->a_lo, g->a_rows, g->lda) ||

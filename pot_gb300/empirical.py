@@ -70,6 +70,25 @@ def online_sinkhorn(X, Y, reg, a, b, numIterMax, stopThr, warm_f=None, warm_g=No
     return f, g, info[0], info[1], [hist[k] for k in range(min(info[2], cap))]
 
 
+def lazy_loss(X_s, X_t, f, g, reg):
+    """``sum_ij C_ij exp(f_i + g_j - C_ij / reg)`` over squared distances,
+    the loss of ``empirical_sinkhorn2(isLazy=True)``
+    (``ot/bregman/_empirical.py:470-478``), in one kernel
+    (``otg_lazy_loss``, fp64 accumulation)."""
+    bd = Boundary(X_s, X_t, f, g)
+    X = bd.to_dev(X_s)
+    dt = X.dtype
+    X = X.contiguous()
+    Y = bd.to_dev(X_t, dt).contiguous()
+    fd, gd = bd.to_dev(f, dt).contiguous(), bd.to_dev(g, dt).contiguous()
+    out = torch.empty(1, dtype=torch.float64, device=X.device)
+    lib = _lib.load()
+    _lib.check(lib.otg_lazy_loss(_lib.dtype_code(dt), _lib.ptr(X), _lib.ptr(Y), X.shape[0], Y.shape[0], X.shape[1],
+                                 _lib.ptr(fd), _lib.ptr(gd), float(reg), _lib.ptr(out), _lib.stream_handle(X.device)),
+               "otg_lazy_loss")
+    return bd.scalar(out[0].to(dt))
+
+
 def empirical_sinkhorn(X_s, X_t, reg, a=None, b=None, metric="sqeuclidean", numIterMax=10000, stopThr=1e-9,
                        isLazy=False, batchSize=100, verbose=False, log=False, warn=True, warmstart=None, **kwargs):
     """GPU ``ot.bregman.empirical_sinkhorn`` (squared-Euclidean metric)."""

@@ -1,8 +1,9 @@
 """GPU entropic Gromov-Wasserstein: drop-ins for
 ``ot.gromov.entropic_gromov_wasserstein`` / ``entropic_gromov_wasserstein2``
-(PythonOT/POT ``ot/gromov/_bregman.py:25-253``, ``:256-400``) with the
-square loss, plus the log-domain inner-solver variant used for large
-problems.
+(PythonOT/POT ``ot/gromov/_bregman.py:25-253``, ``:256-400``) and the fused
+variants ``entropic_fused_gromov_wasserstein`` / ``...2`` (``:997-1241``,
+``:1244-1403``) with the square loss, plus the log-domain inner-solver
+variant used for large problems.
 
 Per outer iteration: the gradient ``2 (constC - C1 T (2 C2)^T)`` comes from
 two GEMMs (``csrc/gw.cu``: tcgen05 tensor cores with a high/low half split
@@ -84,8 +85,9 @@ class TensorProduct:
             self.P1 = _Planes(n, m, self.device)
             self.flag = torch.zeros(1, dtype=torch.int32, device=self.device)
 
-    def grad(self, T, out=None):
-        """2 (constC - C1 T hC2^T) as an (n, m) tensor of the input dtype."""
+    def grad(self, T, out=None, w=1.0, addend=None, s_add=0.0):
+        """``w * 2 (constC - C1 T hC2^T) [+ s_add * addend]`` as an (n, m)
+        tensor of the input dtype (``addend`` may be ``out``)."""
         n, m = self.n, self.m
         st = _lib.stream_handle(self.device)
         if out is None:
@@ -94,8 +96,11 @@ class TensorProduct:
             A1 = torch.empty(n, m, dtype=torch.float64, device=self.device)
             _lib.check(self.lib.otg_gemm_f64(0, 0, n, m, n, 1.0, _lib.ptr(self.C1), n, _lib.ptr(T), T.stride(0),
                                              0.0, _lib.ptr(A1), m, st), "otg_gemm_f64")
-            out.copy_(2.0 * (self.alpha[:, None] + self.beta[None, :]))
-            _lib.check(self.lib.otg_gemm_f64(0, 1, n, m, m, -2.0, _lib.ptr(A1), m, _lib.ptr(self.hC2), m, 1.0,
+            base = (2.0 * w) * (self.alpha[:, None] + self.beta[None, :])
+            if addend is not None:
+                base = base + s_add * addend
+            out.copy_(base)
+            _lib.check(self.lib.otg_gemm_f64(0, 1, n, m, m, -2.0 * w, _lib.ptr(A1), m, _lib.ptr(self.hC2), m, 1.0,
                                              _lib.ptr(out), m, st), "otg_gemm_f64")
             return out
         Tc = T.contiguous()
@@ -110,10 +115,12 @@ class TensorProduct:
         g2 = _lib.OtgSplitGemm(a_hi=_lib.ptr(self.P1.hi), a_lo=_lib.ptr(self.P1.lo), a_rows=self.P1.rows,
                                lda=self.P1.cols, b_hi=_lib.ptr(self.B2.hi), b_lo=_lib.ptr(self.B2.lo),
                                b_rows=self.B2.rows, ldb=self.B2.cols, k_alloc=self.P1.cols, mode=1, scale=1.0,
-                               s_acc=-2.0 / (self.s1 * self.sT * self.e1 * self.s2), s_vec=2.0, out_hi=None,
+                               s_acc=-2.0 * w / (self.s1 * self.sT * self.e1 * self.s2), s_vec=2.0 * w, out_hi=None,
                                out_lo=None, ld_h=0, out=_lib.ptr(out),
                                ld_o=out.stride(0), M=n, N=m, rowv=_lib.ptr(self.alpha), colv=_lib.ptr(self.beta),
-                               abort_flag=_lib.ptr(self.flag), timeout_ms=0)
+                               abort_flag=_lib.ptr(self.flag), timeout_ms=0,
+                               addend=_lib.ptr(addend) if addend is not None else None,
+                               ld_add=addend.stride(0) if addend is not None else 0, s_add=float(s_add))
         _lib.check(self.lib.otg_gemm_split3(ctypes.byref(g2), st), "otg_gemm_split3")
         return out
 
@@ -135,14 +142,60 @@ def entropic_gromov_wasserstein(C1, C2, p=None, q=None, loss_fun="square_loss", 
                                 G0=None, max_iter=1000, tol=1e-9, solver="PGD", warmstart=False, verbose=False,
                                 log=False, **kwargs):
     """GPU ``ot.gromov.entropic_gromov_wasserstein`` (square loss)."""
+    T, lg = _entropic_gw(None, C1, C2, p, q, loss_fun, epsilon, symmetric, 1.0, G0, max_iter, tol, solver,
+                         warmstart, verbose, kwargs)
+    if log:
+        return T, {"err": lg["err"], "gw_dist": lg["dist"]}
+    return T
+
+
+def entropic_fused_gromov_wasserstein(M, C1, C2, p=None, q=None, loss_fun="square_loss", epsilon=0.1,
+                                      symmetric=None, alpha=0.5, G0=None, max_iter=1000, tol=1e-9, solver="PGD",
+                                      warmstart=False, verbose=False, log=False, **kwargs):
+    """GPU ``ot.gromov.entropic_fused_gromov_wasserstein``
+    (``ot/gromov/_bregman.py:997-1241``, square loss): the entropic GW loop
+    with the inner cost ``alpha * gwggrad(T) + (1 - alpha) M``, the linear
+    term added in the GEMM epilogue; ``log`` holds ``err`` and ``fgw_dist``."""
+    T, lg = _entropic_gw(M, C1, C2, p, q, loss_fun, epsilon, symmetric, alpha, G0, max_iter, tol, solver,
+                         warmstart, verbose, kwargs)
+    if log:
+        return T, {"err": lg["err"], "fgw_dist": lg["dist"]}
+    return T
+
+
+def entropic_fused_gromov_wasserstein2(M, C1, C2, p=None, q=None, loss_fun="square_loss", epsilon=0.1,
+                                       symmetric=None, alpha=0.5, G0=None, max_iter=1000, tol=1e-9, solver="PGD",
+                                       warmstart=False, verbose=False, log=False, **kwargs):
+    """GPU ``ot.gromov.entropic_fused_gromov_wasserstein2``
+    (``ot/gromov/_bregman.py:1244-1403``): the FGW loss; the log adds ``T``,
+    ``quad_loss`` and ``lin_loss``."""
+    T, lg = _entropic_gw(M, C1, C2, p, q, loss_fun, epsilon, symmetric, alpha, G0, max_iter, tol, solver,
+                         warmstart, verbose, kwargs, keep_device=True)
+    bd = lg["bd"]
+    lin = lg["lin"]
+    logv = {"err": lg["err"], "fgw_dist": lg["dist"], "T": bd.out(T),
+            "quad_loss": bd.scalar(torch.tensor(lg["dist_f"] - (1 - alpha) * lin, dtype=T.dtype, device=T.device)),
+            "lin_loss": bd.scalar(torch.tensor(lin * (1 - alpha), dtype=T.dtype, device=T.device))}
+    if log:
+        return logv["fgw_dist"], logv
+    return logv["fgw_dist"]
+
+
+def _entropic_gw(Mf, C1, C2, p, q, loss_fun, epsilon, symmetric, alpha, G0, max_iter, tol, solver, warmstart,
+                 verbose, kwargs, keep_device=False):
+    """Outer loop of ``ot/gromov/_bregman.py:150-253`` (GW) and
+    ``:1140-1241`` (fused GW with ``Mf``): gradient by tensor-core GEMMs,
+    scaling-form inner Sinkhorn, ``||T - Tprev||_F`` every 10th iteration."""
     _validate(loss_fun, solver)
     if "method" in kwargs:
         raise TypeError("sinkhorn() got multiple values for keyword argument 'method'")
-    bd = Boundary(C1, C2, p, q, G0)
+    kwargs = dict(kwargs)
+    bd = Boundary(C1, C2, p, q, G0, Mf)
     C1d = bd.to_dev(C1)
     C2d = bd.to_dev(C2, C1d.dtype)
     dt, dev = C1d.dtype, C1d.device
     n, m = C1d.shape[0], C2d.shape[0]
+    Mfd = None if Mf is None else bd.to_dev(Mf, dt).contiguous()
     pd = torch.full((n,), 1.0 / n, dtype=dt, device=dev) if p is None else bd.to_dev(p, dt)
     qd = torch.full((m,), 1.0 / m, dtype=dt, device=dev) if q is None else bd.to_dev(q, dt)
     T = torch.outer(pd, qd) if G0 is None else bd.to_dev(G0, dt).contiguous()
@@ -155,23 +208,28 @@ def entropic_gromov_wasserstein(C1, C2, p=None, q=None, loss_fun="square_loss", 
     if warmstart:
         mu = torch.full((n,), -float(torch.log(torch.tensor(float(n)))), dtype=dt, device=dev)
         nu = torch.full((m,), -float(torch.log(torch.tensor(float(m)))), dtype=dt, device=dev)
+    lin_w = 0.0 if Mfd is None else 1.0 - alpha
     cpt, err = 0, 1.0
     errs = []
     M = torch.empty(n, m, dtype=dt, device=dev)
     while err > tol and cpt < max_iter:
         Tprev = T
-        tp.grad(T, M)
-        if not symmetric:
-            M = 0.5 * (M + tpt.grad(T))
+        if symmetric:
+            tp.grad(T, M, w=alpha, addend=Mfd, s_add=lin_w)
+        else:
+            # alpha/2 (G(T) + G^t(T)) + (1 - alpha) Mf, the second GEMM adding onto the first
+            tp.grad(T, M, w=0.5 * alpha, addend=Mfd, s_add=lin_w)
+            tpt.grad(T, M, w=0.5 * alpha, addend=M, s_add=1.0)
+        tens = M
         if solver == "PPA":
-            M = M - epsilon * torch.log(T)
+            tens = M - epsilon * torch.log(T)
         if warmstart:
-            T, lg = bregman.sinkhorn_knopp(pd, qd, M, epsilon, numItermax=numItermax, stopThr=stopThr, log=True,
+            T, lg = bregman.sinkhorn_knopp(pd, qd, tens, epsilon, numItermax=numItermax, stopThr=stopThr, log=True,
                                            warmstart=(mu, nu), **kwargs)
             mu = epsilon * torch.log(lg["u"])
             nu = epsilon * torch.log(lg["v"])
         else:
-            T = bregman.sinkhorn_knopp(pd, qd, M, epsilon, numItermax=numItermax, stopThr=stopThr, **kwargs)
+            T = bregman.sinkhorn_knopp(pd, qd, tens, epsilon, numItermax=numItermax, stopThr=stopThr, **kwargs)
         if cpt % 10 == 0:
             err = float(torch.linalg.norm(T - Tprev))
             errs.append(err)
@@ -180,17 +238,16 @@ def entropic_gromov_wasserstein(C1, C2, p=None, q=None, loss_fun="square_loss", 
                     print("{:5s}|{:12s}".format("It.", "Err") + "\n" + "-" * 19)
                 print("{:5d}|{:8e}|".format(cpt, err))
         cpt += 1
-        if M is not None and not symmetric:
-            M = torch.empty(n, m, dtype=dt, device=dev)
     tp.check_abort()
     if abs(float(T.sum()) - 1) > 1e-5:
         warnings.warn("Solver failed to produce a transport plan. You might "
                       "want to increase the regularization parameter `epsilon`.")
-    if log:
-        gw = 0.5 * float((tp.grad(T) * T).sum())
-        return bd.out(T), {"err": [torch.tensor(e) for e in errs] if bd.kind == "torch" else errs,
-                           "gw_dist": bd.scalar(torch.tensor(gw, dtype=dt, device=dev))}
-    return bd.out(T)
+    quad = 0.5 * float((tp.grad(T) * T).sum())
+    lin = 0.0 if Mfd is None else float((Mfd * T).sum())
+    dist = (1.0 - alpha) * lin + alpha * quad if Mfd is not None else quad
+    out = {"err": [torch.tensor(e) for e in errs] if bd.kind == "torch" else errs,
+           "dist": bd.scalar(torch.tensor(dist, dtype=dt, device=dev)), "dist_f": dist, "lin": lin, "bd": bd}
+    return (T if keep_device else bd.out(T)), out
 
 
 def entropic_gromov_wasserstein2(C1, C2, p=None, q=None, loss_fun="square_loss", epsilon=0.1, symmetric=None,

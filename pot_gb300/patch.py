@@ -5,16 +5,20 @@ so rebinding ``ot.sinkhorn`` alone is not enough.  ``patch_pot(ot)``
 replaces the hot-path names in every module that imported them:
 
     ot/__init__.py:56            sinkhorn, sinkhorn2
-    ot/bregman/__init__.py:13    sinkhorn, sinkhorn2, sinkhorn_knopp, sinkhorn_log, empirical_sinkhorn
-    ot/bregman/_sinkhorn.py      sinkhorn_knopp, sinkhorn_log (the dispatcher's callees)
+    ot/bregman/__init__.py:13    sinkhorn, sinkhorn2, sinkhorn_knopp, sinkhorn_log, sinkhorn_stabilized,
+                                 sinkhorn_epsilon_scaling, empirical_sinkhorn, empirical_sinkhorn2,
+                                 barycenter, barycenter_sinkhorn
+    ot/bregman/_sinkhorn.py      sinkhorn_knopp, sinkhorn_log, sinkhorn_stabilized,
+                                 sinkhorn_epsilon_scaling (the dispatcher's callees)
     ot/bregman/_empirical.py:18  sinkhorn, sinkhorn2
     ot/gromov/_bregman.py:17     sinkhorn
-    ot/gromov/__init__.py        entropic_gromov_wasserstein(2)
+    ot/gromov/__init__.py        entropic_gromov_wasserstein(2), entropic_fused_gromov_wasserstein(2)
     ot/batch/__init__.py         solve_batch, solve_sample_batch, dist_batch,
                                  bregman_log_projection_batch, bregman_projection_batch
     ot/batch/_linear.py          the same (module-level callers)
     ot/batch/_quadratic.py:14    bregman_log_projection_batch
-    ot/solvers.py:14             sinkhorn_log
+    ot/solvers.py:14             sinkhorn_log, empirical_sinkhorn2 (the entropic branches of
+                                 ot.solve / ot.solve_sample)
 
 Calls the GPU path does not cover (other methods, metrics or losses) raise
 NotImplementedError from the GPU function; ``unpatch_pot`` restores the
@@ -22,16 +26,23 @@ original bindings.
 """
 import importlib
 
-from . import bregman, batch, gromov, empirical
+from . import bregman, batch, gromov, empirical, solvers, barycenters
 
 GPU = {
     "sinkhorn": bregman.sinkhorn,
     "sinkhorn2": bregman.sinkhorn2,
     "sinkhorn_knopp": bregman.sinkhorn_knopp,
     "sinkhorn_log": bregman.sinkhorn_log,
+    "sinkhorn_stabilized": bregman.sinkhorn_stabilized,
+    "sinkhorn_epsilon_scaling": bregman.sinkhorn_epsilon_scaling,
+    "empirical_sinkhorn2": solvers.empirical_sinkhorn2,
+    "barycenter": barycenters.barycenter,
+    "barycenter_sinkhorn": barycenters.barycenter_sinkhorn,
     "empirical_sinkhorn": empirical.empirical_sinkhorn,
     "entropic_gromov_wasserstein": gromov.entropic_gromov_wasserstein,
     "entropic_gromov_wasserstein2": gromov.entropic_gromov_wasserstein2,
+    "entropic_fused_gromov_wasserstein": gromov.entropic_fused_gromov_wasserstein,
+    "entropic_fused_gromov_wasserstein2": gromov.entropic_fused_gromov_wasserstein2,
     "solve_batch": batch.solve_batch,
     "solve_sample_batch": batch.solve_sample_batch,
     "dist_batch": batch.dist_batch,
@@ -41,16 +52,19 @@ GPU = {
 
 MODULES = {
     "": ["sinkhorn", "sinkhorn2"],
-    ".bregman": ["sinkhorn", "sinkhorn2", "sinkhorn_knopp", "sinkhorn_log", "empirical_sinkhorn"],
-    ".bregman._sinkhorn": ["sinkhorn_knopp", "sinkhorn_log"],
+    ".bregman": ["sinkhorn", "sinkhorn2", "sinkhorn_knopp", "sinkhorn_log", "sinkhorn_stabilized",
+                 "sinkhorn_epsilon_scaling", "empirical_sinkhorn", "empirical_sinkhorn2", "barycenter",
+                 "barycenter_sinkhorn"],
+    ".bregman._sinkhorn": ["sinkhorn_knopp", "sinkhorn_log", "sinkhorn_stabilized", "sinkhorn_epsilon_scaling"],
     ".bregman._empirical": ["sinkhorn", "sinkhorn2"],
-    ".gromov": ["entropic_gromov_wasserstein", "entropic_gromov_wasserstein2"],
+    ".gromov": ["entropic_gromov_wasserstein", "entropic_gromov_wasserstein2", "entropic_fused_gromov_wasserstein",
+                "entropic_fused_gromov_wasserstein2"],
     ".gromov._bregman": ["sinkhorn"],
     ".batch": ["solve_batch", "solve_sample_batch", "dist_batch", "bregman_log_projection_batch",
                "bregman_projection_batch"],
     ".batch._linear": ["solve_batch", "dist_batch", "bregman_log_projection_batch", "bregman_projection_batch"],
     ".batch._quadratic": ["bregman_log_projection_batch"],
-    ".solvers": ["sinkhorn_log"],
+    ".solvers": ["sinkhorn_log", "empirical_sinkhorn2"],
 }
 
 _saved = {}

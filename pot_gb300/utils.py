@@ -1,7 +1,19 @@
-"""Result container of the batch API, after ``ot.utils.OTResult``
-(``ot/utils.py:1127``): the fields the batch solvers fill (``plan``,
-``value``, ``value_linear``, ``potentials``, ``log``) and the derived
-properties users read from them."""
+"""``ot.utils`` pieces on the path: ``dist`` for the squared-Euclidean and
+Euclidean metrics (``ot/utils.py:400``), and the result container
+``OTResult`` (``ot/utils.py:1127``) with the fields the solvers fill
+(``plan``, ``value``, ``value_linear``, ``potentials``, ``log``, ``lazy_plan``)
+and the derived properties users read from them."""
+
+
+def dist(x1, x2=None, metric="sqeuclidean", p=2, w=None, backend="auto", nx=None, use_tensor=False):
+    """GPU ``ot.dist`` for 'sqeuclidean' and 'euclidean' (``ot/utils.py:400-470``):
+    the cost kernel of the batch path with one problem.  ``x2=None`` means
+    ``x2 = x1`` (zero diagonal); other metrics raise NotImplementedError."""
+    from . import batch as pb
+    X1 = x1[None] if hasattr(x1, "shape") else [x1]
+    X2 = None if x2 is None else (x2[None] if hasattr(x2, "shape") else [x2])
+    M = pb.dist_batch(X1, X2, metric=metric, p=p)
+    return M[0]
 
 
 class OTResult:

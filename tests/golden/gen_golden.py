@@ -5,7 +5,8 @@ through ``ref_import.py``); the GPU machine never runs this script, it only reads
 the ``.npz`` files it writes.  Every case records its inputs, the reference's
 outputs and, where the reference warns, the warnings it raised.
 
-    python tests/golden/gen_golden.py
+    python tests/golden/gen_golden.py            # every section
+    python tests/golden/gen_golden.py next       # one section
 """
 import os
 import sys
@@ -51,7 +52,7 @@ def dense_case(name, a, b, M, reg, numItermax=1000, stopThr=1e-9):
     save(name, **out)
 
 
-def main():
+def core():
     # 1. reference doctest (ot/bregman/_sinkhorn.py:123-129, 342-347)
     a = np.array([0.5, 0.5])
     M = np.array([[0.0, 1.0], [1.0, 0.0]])
@@ -217,5 +218,167 @@ def main():
     save("lazy_60x50", X=X, Y=Y, reg=1.0, f=f, g=g, err=np.array(lg["err"]), niter=lg["niter"])
 
 
+def stab_case(name, a, b, x, y, reg, **kw):
+    """sinkhorn_stabilized (ot/bregman/_sinkhorn.py:1105) on one dense problem
+    with M = dist(x, y) / max; M and the plan are stored for small cases."""
+    M = ot.dist(x, y)
+    M /= M.max()
+    (P, lg), w = call_warn(ot.bregman.sinkhorn_stabilized, a, b, M, reg, log=True, **kw)
+    out = dict(a=a, b=b, x=x, y=y, reg=reg, loss=float(np.sum(M * P)), n_iter=lg["n_iter"],
+               err=np.array(lg["err"], dtype=np.float64), logu=lg["logu"], logv=lg["logv"],
+               alpha=lg["alpha"], beta=lg["beta"],
+               warn_nonconv=int(any("did not converge" in x for x in w)),
+               warn_numerr=int(any("Numerical errors" in x for x in w)),
+               **{"kw_" + k: v for k, v in kw.items() if k != "warmstart"})
+    if "warmstart" in kw:
+        out["ws_alpha"], out["ws_beta"] = kw["warmstart"]
+    if M.size <= 5000:
+        out["M"] = M
+        out["plan"] = P
+    save(name, **out)
+
+
+def next_rows():
+    # 9. stabilised Sinkhorn (ot/bregman/_sinkhorn.py:1105-1368): absorptions,
+    # warm start, an exit at numItermax right after an absorption
+    rng = np.random.default_rng(31)
+    for (n, m) in [(31, 33), (127, 129)]:
+        x = rng.standard_normal((n, 2))
+        y = rng.standard_normal((m, 2)) + 0.5
+        a = rng.random(n) + 0.1
+        a /= a.sum()
+        b = rng.random(m) + 0.1
+        b /= b.sum()
+        for reg in (0.5, 0.02, 0.002):
+            stab_case("stab_%dx%d_reg%g" % (n, m, reg), a, b, x, y, reg, numItermax=2000)
+    rng = np.random.default_rng(32)
+    x = rng.standard_normal((40, 3))
+    y = rng.standard_normal((50, 3))
+    a, b = ot.unif(40), ot.unif(50)
+    stab_case("stab_warm_40x50", a, b, x, y, 0.01,
+              warmstart=(rng.standard_normal(40) * 0.01, rng.standard_normal(50) * 0.01), numItermax=3000)
+    stab_case("stab_maxiter1_40x50", a, b, x, y, 0.01, numItermax=1)
+    stab_case("stab_tau10_40x50", a, b, x, y, 0.05, tau=10.0, print_period=7, stopThr=1e-11)
+    g = dict(np.load(os.path.join(HERE, "dense_1024_gauss2d.npz")))
+    stab_case("stab_1024_gauss2d", g["a"], g["b"], g["x"], g["y"], 0.01, numItermax=1000)
+
+    # 10. epsilon scaling (ot/bregman/_sinkhorn.py:1371-1575)
+    rng = np.random.default_rng(33)
+    x = rng.standard_normal((31, 2))
+    y = rng.standard_normal((33, 2)) + 0.5
+    M = ot.dist(x, y)
+    M /= M.max()
+    a, b = ot.unif(31), ot.unif(33)
+    for reg, kw in ((0.01, {}), (0.05, dict(numItermax=60, epsilon0=10.0, numInnerItermax=30, print_period=5))):
+        (G, lg), w = call_warn(ot.bregman.sinkhorn_epsilon_scaling, a, b, M, reg, log=True, **kw)
+        save("epsscale_31x33_reg%g" % reg, a=a, b=b, M=M, reg=reg, plan=G, alpha=lg["alpha"], beta=lg["beta"],
+             err=np.array(lg["err"], dtype=np.float64), niter=lg["niter"], nwarn=len(w),
+             warn_nonconv=sum("did not converge" in x for x in w),
+             **{"kw_" + k: v for k, v in kw.items()})
+
+    # 11. ot.solve / ot.solve_sample entropic branches (ot/solvers.py:428-494, 1765-1877)
+    rng = np.random.default_rng(34)
+    x = rng.standard_normal((40, 3))
+    y = rng.standard_normal((30, 3)) + 0.3
+    a = rng.random(40) + 0.2
+    a /= a.sum()
+    b = rng.random(30) + 0.2
+    b /= b.sum()
+    M = ot.dist(x, y)
+    for reg_type in ("KL", "entropy"):
+        res = ot.solve(M, a, b, reg=0.5, reg_type=reg_type)
+        save("solve_40x30_%s" % reg_type, x=x, y=y, a=a, b=b, M=M, reg=0.5, plan=res.plan, value=res.value,
+             value_linear=res.value_linear, pa=res.potentials[0], pb=res.potentials[1])
+    res = ot.solve(M, a, b, reg=0.5, max_iter=7, tol=0.0)
+    save("solve_40x30_iter7", M=M, a=a, b=b, reg=0.5, plan=res.plan, value=res.value,
+         value_linear=res.value_linear, pa=res.potentials[0], pb=res.potentials[1])
+    res = ot.solve_sample(x, y, a, b, reg=0.5)
+    save("solve_sample_40x30", x=x, y=y, a=a, b=b, reg=0.5, plan=res.plan, value=res.value,
+         value_linear=res.value_linear, pa=res.potentials[0], pb=res.potentials[1])
+    res = ot.solve_sample(x, y, a, b, reg=0.5, lazy=True, batch_size=7, tol=1e-10)
+    save("solve_sample_lazy_40x30", x=x, y=y, a=a, b=b, reg=0.5, value_linear=res.value_linear,
+         pa=res.potentials[0], pb=res.potentials[1], err=np.array(res.log["err"]), niter=res.log["niter"])
+    loss, lg = ot.bregman.empirical_sinkhorn2(x, y, 0.5, a, b, isLazy=True, batchSize=11, numIterMax=300,
+                                              stopThr=1e-9, log=True)
+    save("emp2_lazy_40x30", x=x, y=y, a=a, b=b, reg=0.5, loss=float(loss), f=lg["u"], g=lg["v"],
+         niter=lg["niter"], err=np.array(lg["err"]))
+
+
+def fused_gw():
+    # 12. entropic fused GW (ot/gromov/_bregman.py:997-1241, :1244-1403)
+    rng = np.random.default_rng(41)
+    xs = rng.standard_normal((30, 2))
+    xt = rng.standard_normal((24, 3))
+    C1, C2 = ot.dist(xs, xs), ot.dist(xt, xt)
+    C1 /= C1.max()
+    C2 /= C2.max()
+    Fs = rng.standard_normal((30, 4))
+    Ft = rng.standard_normal((24, 4)) + 0.5
+    M = ot.dist(Fs, Ft)
+    M /= M.max()
+    p = ot.unif(30)
+    q = rng.random(24) + 0.5
+    q /= q.sum()
+    out = dict(C1=C1, C2=C2, M=M, p=p, q=q)
+    for tag, kw in (("pgd", dict(alpha=0.5)), ("pgd_a02_warm", dict(alpha=0.2, warmstart=True)),
+                    ("ppa", dict(alpha=0.7, solver="PPA"))):
+        (T, lg), w = call_warn(ot.gromov.entropic_fused_gromov_wasserstein, M, C1, C2, p, q, epsilon=0.05,
+                               max_iter=200, tol=1e-9, log=True, **kw)
+        out[tag + "_T"] = T
+        out[tag + "_err"] = np.array(lg["err"], dtype=np.float64)
+        out[tag + "_fgw"] = lg["fgw_dist"]
+    val, lg2 = ot.gromov.entropic_fused_gromov_wasserstein2(M, C1, C2, p, q, epsilon=0.05, alpha=0.5, max_iter=200,
+                                                           tol=1e-9, log=True)
+    out["fgw2"] = val
+    out["fgw2_quad"] = lg2["quad_loss"]
+    out["fgw2_lin"] = lg2["lin_loss"]
+    save("fgw_30x24", **out)
+    C1a = C1 + 0.3 * rng.random((30, 30))
+    (T, lg), w = call_warn(ot.gromov.entropic_fused_gromov_wasserstein, M, C1a, C2, p, q, epsilon=0.05, alpha=0.6,
+                           max_iter=200, tol=1e-9, log=True)
+    save("fgw_asym_30x24", C1=C1a, C2=C2, M=M, p=p, q=q, T=T, err=np.array(lg["err"]), fgw=lg["fgw_dist"])
+
+
+def barycenters():
+    # 13. entropic barycenters (ot/bregman/_barycenter.py:141-259, :403-473)
+    x = np.arange(60, dtype=np.float64)
+    M = ot.dist(x.reshape(-1, 1), x.reshape(-1, 1))
+    M /= M.max()
+    A = np.stack([np.exp(-(x - c) ** 2 / (2 * s ** 2)) for c, s in ((15, 4), (40, 6), (30, 10))], 1)
+    A /= A.sum(0, keepdims=True)
+    w = np.array([0.2, 0.5, 0.3])
+    out = dict(A=A, M=M, w=w)
+    for tag, method, reg in (("sk", "sinkhorn", 0.01), ("log", "sinkhorn_log", 0.01), ("log_small", "sinkhorn_log",
+                                                                                        1e-3)):
+        (bar, lg), wn = call_warn(ot.bregman.barycenter, A, M, reg, weights=w, method=method, numItermax=2000,
+                                  stopThr=1e-8, log=True)
+        out[tag + "_bar"] = bar
+        out[tag + "_err"] = np.array(lg["err"], dtype=np.float64)
+        out[tag + "_niter"] = lg["niter"]
+        out[tag + "_nonconv"] = int(any("did not converge" in m for m in wn))
+    bar = ot.bregman.barycenter(A, M, 0.05)
+    out["default_bar"] = bar
+    save("bary_60x3", **out)
+    rng = np.random.default_rng(51)
+    X = rng.standard_normal((300, 2))
+    M = ot.dist(X, X)
+    M /= M.max()
+    A = rng.random((300, 5)) ** 3
+    A /= A.sum(0, keepdims=True)
+    (bar, lg), wn = call_warn(ot.bregman.barycenter_sinkhorn, A, M, 0.02, numItermax=300, stopThr=1e-9, log=True)
+    (bar2, lg2), wn2 = call_warn(ot.bregman.barycenter, A, M, 0.02, method="sinkhorn_log", numItermax=300,
+                                 stopThr=1e-9, log=True)
+    save("bary_300x5", A=A, x=X, sk_bar=bar, sk_err=np.array(lg["err"]), sk_niter=lg["niter"], log_bar=bar2,
+         log_err=np.array(lg2["err"]), log_niter=lg2["niter"])
+
+
+SECTIONS = {"core": core, "next": next_rows, "fgw": fused_gw, "bary": barycenters}
+
+
+def main(names):
+    for k in names or list(SECTIONS):
+        SECTIONS[k]()
+
+
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -116,3 +116,45 @@ def test_egw_log_inner_vs_oracle(cuda):
         T = T.double().cpu().numpy()
         assert np.abs(T - Tref).sum() / Tref.sum() <= tol_t, dt
         assert abs(lg["gw_dist"] - lref["gw_dist"]) <= tol_g * abs(lref["gw_dist"]), dt
+
+
+@pytest.mark.parametrize("tag,kw", [("pgd", dict(alpha=0.5)), ("pgd_a02_warm", dict(alpha=0.2, warmstart=True)),
+                                    ("ppa", dict(alpha=0.7, solver="PPA"))])
+def test_fused_egw_f64_golden(cuda, tag, kw):
+    g = golden("fgw_30x24")
+    T, lg = pgw.entropic_fused_gromov_wasserstein(g["M"], g["C1"], g["C2"], g["p"], g["q"], epsilon=0.05,
+                                                  max_iter=200, tol=1e-9, log=True, **kw)
+    np.testing.assert_allclose(T, g[tag + "_T"], rtol=1e-7, atol=1e-13)
+    np.testing.assert_allclose(np.array(lg["err"], dtype=float), g[tag + "_err"], rtol=1e-6, atol=1e-13)
+    assert abs(float(lg["fgw_dist"]) - float(g[tag + "_fgw"])) <= 1e-9 * abs(float(g[tag + "_fgw"]))
+
+
+def test_fused_egw2_and_asymmetric_f64_golden(cuda):
+    g = golden("fgw_30x24")
+    val, lg = pgw.entropic_fused_gromov_wasserstein2(g["M"], g["C1"], g["C2"], g["p"], g["q"], epsilon=0.05,
+                                                     alpha=0.5, max_iter=200, tol=1e-9, log=True)
+    assert abs(float(val) - float(g["fgw2"])) <= 1e-9 * abs(float(g["fgw2"]))
+    assert abs(float(lg["quad_loss"]) - float(g["fgw2_quad"])) <= 1e-9 * abs(float(g["fgw2_quad"]))
+    assert abs(float(lg["lin_loss"]) - float(g["fgw2_lin"])) <= 1e-9 * abs(float(g["fgw2_lin"]))
+    g = golden("fgw_asym_30x24")
+    T, lg = pgw.entropic_fused_gromov_wasserstein(g["M"], g["C1"], g["C2"], g["p"], g["q"], epsilon=0.05,
+                                                  alpha=0.6, max_iter=200, tol=1e-9, log=True)
+    np.testing.assert_allclose(T, g["T"], rtol=1e-7, atol=1e-13)
+    assert abs(float(lg["fgw_dist"]) - float(g["fgw"])) <= 1e-9 * abs(float(g["fgw"]))
+
+
+@pytest.mark.parametrize("name", ["fgw_30x24", "fgw_asym_30x24"])
+def test_fused_egw_f32_tensor_cores_vs_oracle(cuda, name):
+    g = golden(name)
+    alpha = 0.5 if name == "fgw_30x24" else 0.6
+    Tref, lref = oracle.entropic_fused_gromov_wasserstein(g["M"], g["C1"], g["C2"], g["p"], g["q"], epsilon=0.05,
+                                                          alpha=alpha, max_iter=200, tol=1e-9)
+    f = lambda x: torch.tensor(x, dtype=torch.float32, device=cuda)  # noqa: E731
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        T, lg = pgw.entropic_fused_gromov_wasserstein(f(g["M"]), f(g["C1"]), f(g["C2"]), f(g["p"]), f(g["q"]),
+                                                      epsilon=0.05, alpha=alpha, max_iter=200, tol=1e-9, log=True)
+    T = T.double().cpu().numpy()
+    assert np.abs(T - Tref).sum() / Tref.sum() <= 1e-3
+    assert abs(float(lg["fgw_dist"]) - lref["fgw_dist"]) <= 1e-4 * abs(lref["fgw_dist"])

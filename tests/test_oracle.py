@@ -160,3 +160,111 @@ def test_gromov_batch(name):
     np.testing.assert_allclose(r["plan"], g["plan"], rtol=1e-8, atol=1e-14)
     np.testing.assert_allclose(r["value"], g["value"], rtol=1e-8)
     np.testing.assert_allclose(r["value_quad"], g["value_quad"], rtol=1e-8)
+
+
+STAB = golden_names("stab_")
+
+
+def _stab_kw(g):
+    kw = {k[3:]: (int(v) if k in ("kw_numItermax", "kw_print_period") else float(v))
+          for k, v in g.items() if k.startswith("kw_")}
+    if "ws_alpha" in g:
+        kw["warmstart"] = (g["ws_alpha"], g["ws_beta"])
+    return kw
+
+
+@pytest.mark.parametrize("name", STAB)
+def test_stabilized(name):
+    g = golden(name)
+    M = _M(g)
+    P, lg = oracle.sinkhorn_stabilized(g["a"], g["b"], M, float(g["reg"]), **_stab_kw(g))
+    assert lg["n_iter"] == int(g["n_iter"])
+    np.testing.assert_allclose(lg["err"], g["err"], rtol=1e-7, atol=1e-15)
+    np.testing.assert_allclose(lg["logu"], g["logu"], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(lg["logv"], g["logv"], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(lg["alpha"], g["alpha"], rtol=1e-9, atol=1e-12)
+    assert abs(float(np.sum(M * P)) - float(g["loss"])) <= 1e-9 * abs(float(g["loss"]))
+    if "plan" in g:
+        np.testing.assert_allclose(P, g["plan"], rtol=1e-8, atol=1e-300)
+    assert (oracle.NONCONV in lg["_warnings"]) == bool(g["warn_nonconv"])
+
+
+@pytest.mark.parametrize("name", golden_names("epsscale_"))
+def test_epsilon_scaling(name):
+    g = golden(name)
+    kw = {k[3:]: (float(v) if k == "kw_epsilon0" else int(v)) for k, v in g.items() if k.startswith("kw_")}
+    G, lg = oracle.sinkhorn_epsilon_scaling(g["a"], g["b"], g["M"], float(g["reg"]), **kw)
+    assert lg["niter"] == int(g["niter"])
+    np.testing.assert_allclose(lg["err"], g["err"], rtol=1e-6, atol=1e-20)
+    np.testing.assert_allclose(G, g["plan"], rtol=1e-7, atol=1e-300)
+    np.testing.assert_allclose(lg["alpha"], g["alpha"], rtol=1e-8, atol=1e-12)
+    assert sum(w == oracle.NONCONV for w in lg["_warnings"]) == int(g["warn_nonconv"])
+
+
+@pytest.mark.parametrize("name", ["solve_40x30_KL", "solve_40x30_entropy", "solve_40x30_iter7"])
+def test_solve_entropic(name):
+    g = golden(name)
+    kw = dict(max_iter=7, tol=0.0) if name.endswith("iter7") else {}
+    r = oracle.solve_entropic(g["M"], g["a"], g["b"], float(g["reg"]),
+                              reg_type="entropy" if name.endswith("entropy") else "KL", **kw)
+    np.testing.assert_allclose(r["plan"], g["plan"], rtol=1e-10)
+    assert abs(r["value"] - float(g["value"])) <= 1e-10 * abs(float(g["value"]))
+    assert abs(r["value_linear"] - float(g["value_linear"])) <= 1e-10 * abs(float(g["value_linear"]))
+    np.testing.assert_allclose(r["potentials"][0], g["pa"], rtol=1e-10)
+
+
+def test_empirical_sinkhorn2_lazy():
+    g = golden("emp2_lazy_40x30")
+    loss, lg = oracle.empirical_sinkhorn2_lazy(g["x"], g["y"], float(g["reg"]), g["a"], g["b"], numIterMax=300,
+                                               stopThr=1e-9, batchSize=11)
+    assert lg["niter"] == int(g["niter"])
+    assert abs(loss - float(g["loss"])) <= 1e-10 * abs(float(g["loss"]))
+    np.testing.assert_allclose(lg["u"], g["f"], rtol=1e-10)
+    g = golden("solve_sample_lazy_40x30")
+    loss, lg = oracle.empirical_sinkhorn2_lazy(g["x"], g["y"], float(g["reg"]), g["a"], g["b"], numIterMax=1000,
+                                               stopThr=1e-10, batchSize=7)
+    assert lg["niter"] == int(g["niter"])
+    assert abs(loss - float(g["value_linear"])) <= 1e-10 * abs(loss)
+    np.testing.assert_allclose(lg["u"], g["pa"], rtol=1e-10)
+
+
+@pytest.mark.parametrize("tag,kw", [("pgd", dict(alpha=0.5)), ("pgd_a02_warm", dict(alpha=0.2, warmstart=True)),
+                                    ("ppa", dict(alpha=0.7, solver="PPA"))])
+def test_fused_gw(tag, kw):
+    g = golden("fgw_30x24")
+    T, lg = oracle.entropic_fused_gromov_wasserstein(g["M"], g["C1"], g["C2"], g["p"], g["q"], epsilon=0.05,
+                                                     max_iter=200, tol=1e-9, **kw)
+    np.testing.assert_allclose(T, g[tag + "_T"], rtol=1e-9, atol=1e-15)
+    np.testing.assert_allclose(lg["err"], g[tag + "_err"], rtol=1e-7, atol=1e-15)
+    assert abs(lg["fgw_dist"] - float(g[tag + "_fgw"])) <= 1e-10 * abs(float(g[tag + "_fgw"]))
+
+
+def test_fused_gw_asymmetric():
+    g = golden("fgw_asym_30x24")
+    T, lg = oracle.entropic_fused_gromov_wasserstein(g["M"], g["C1"], g["C2"], g["p"], g["q"], epsilon=0.05,
+                                                     alpha=0.6, max_iter=200, tol=1e-9)
+    np.testing.assert_allclose(T, g["T"], rtol=1e-9, atol=1e-15)
+    assert abs(lg["fgw_dist"] - float(g["fgw"])) <= 1e-10 * abs(float(g["fgw"]))
+
+
+@pytest.mark.parametrize("tag,reg", [("sk", 0.01), ("log", 0.01), ("log_small", 1e-3)])
+def test_barycenter(tag, reg):
+    g = golden("bary_60x3")
+    fn = oracle.barycenter_sinkhorn if tag == "sk" else oracle.barycenter_sinkhorn_log
+    bar, lg = fn(g["A"], g["M"], reg, g["w"], numItermax=2000, stopThr=1e-8)
+    assert lg["niter"] == int(g[tag + "_niter"])
+    np.testing.assert_allclose(lg["err"], g[tag + "_err"], rtol=1e-6, atol=1e-16)
+    np.testing.assert_allclose(bar, g[tag + "_bar"], rtol=1e-9, atol=1e-300)
+    assert (oracle.NONCONV in lg["_warnings"]) == bool(g[tag + "_nonconv"])
+    bar, _ = oracle.barycenter_sinkhorn(g["A"], g["M"], 0.05)
+    np.testing.assert_allclose(bar, g["default_bar"], rtol=1e-9)
+
+
+def test_barycenter_300():
+    g = golden("bary_300x5")
+    M = oracle.sqeuclidean(g["x"])
+    M /= M.max()
+    for tag, fn in (("sk", oracle.barycenter_sinkhorn), ("log", oracle.barycenter_sinkhorn_log)):
+        bar, lg = fn(g["A"], M, 0.02, numItermax=300, stopThr=1e-9)
+        assert lg["niter"] == int(g[tag + "_niter"])
+        np.testing.assert_allclose(bar, g[tag + "_bar"], rtol=1e-8, atol=1e-300)
