@@ -31,6 +31,8 @@ extern "C" {
 #define OTG_METHOD_LOG 1   /* log form,      ot/bregman/_sinkhorn.py:690 sinkhorn_log   */
 #define OTG_METHOD_STAB 2  /* log-stabilised scaling form with absorption,
                               ot/bregman/_sinkhorn.py:1105 sinkhorn_stabilized       */
+#define OTG_METHOD_UNB 3   /* unbalanced scaling form with KL marginal penalties,
+                              ot/unbalanced/_sinkhorn.py:565 sinkhorn_knopp_unbalanced */
 
 /* return codes */
 #define OTG_OK 0
@@ -51,7 +53,7 @@ extern "C" {
  * Dense-cost Sinkhorn, one problem, the whole iteration loop in one
  * persistent cooperative launch.
  * Replaces the loops of ot/bregman/_sinkhorn.py:626-663 (sinkhorn_knopp),
- * :880-899 (sinkhorn_log) and :1272-1327 (sinkhorn_stabilized) behind
+ * :880-899 (sinkhorn_log) and :1273-1327 (sinkhorn_stabilized) behind
  * ot.sinkhorn / ot.sinkhorn2 (ot/bregman/_sinkhorn.py:21, :237).
  *
  * OTG_METHOD_STAB runs the log iteration on F = alpha/reg + log u,
@@ -64,6 +66,13 @@ extern "C" {
  *   logu = F - k log n,  logv = G + k log n                (info[6] == 0)
  *   logu = F - k log n,  logv = G + (k-1) log n - log m    (info[6] == 1)
  * with k = info[5]; alpha = reg logu, beta = reg logv.
+ *
+ * OTG_METHOD_UNB iterates u first, u = (a / K v)^fi1, v = (b / K^T u)^fi2
+ * with fi = reg_m / (reg_m + reg) and K = exp(-M/reg) c, and logs the
+ * relative sup-norm change of (u, v) at EVERY iteration (hist_cap >=
+ * max_iter; the history holds the errors themselves, not their squares);
+ * out_u, out_v receive the scalings u, v; a zero K^T u or a non-finite
+ * scaling keeps the previous pair (status OTG_STATUS_NUMERICAL).
  * ---------------------------------------------------------------------- */
 typedef struct OtgDenseProblem {
   int32_t dtype;      /* OTG_F32 or OTG_F64: type of M, a, b, warm_*, out_* */
@@ -86,6 +95,9 @@ typedef struct OtgDenseProblem {
   double tau;         /* STAB: absorption threshold on the scalings (> 0)    */
   int32_t check_period; /* STAB: iterations between marginal checks (>= 1) */
   int32_t reserved;
+  double reg_m1, reg_m2; /* UNB: marginal penalties (INFINITY = hard constraint) */
+  int32_t c_ones;     /* UNB: 0 -> c = a b^T (reg_type 'kl'), 1 -> c = ones    */
+  int32_t reserved2;
 } OtgDenseProblem;
 
 /* Workspace size for otg_sinkhorn_dense (device bytes, 256-byte aligned). */

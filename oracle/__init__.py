@@ -23,6 +23,7 @@ from .entropic import (  # noqa: F401
     sinkhorn_epsilon_scaling,
     barycenter_sinkhorn,
     barycenter_sinkhorn_log,
+    sinkhorn_knopp_unbalanced,
     solve_entropic,
     empirical_sinkhorn2_lazy,
     log_projection_batch,

@@ -407,6 +407,66 @@ def barycenter_sinkhorn_log(A, M, reg, weights=None, numItermax=1000, stopThr=1e
     return np.exp(log_bar), {"err": errs, "niter": ii, "_warnings": warns}
 
 
+def sinkhorn_knopp_unbalanced(a, b, M, reg, reg_m, reg_type="kl", c=None, warmstart=None, numItermax=1000,
+                              stopThr=1e-6):
+    """Unbalanced scaling Sinkhorn with KL marginal penalties,
+    ``ot/unbalanced/_sinkhorn.py:565-818`` (1-D ``b``):
+    ``K = exp(-M/reg) * c`` with ``c = a b^T`` (or ones for
+    ``reg_type='entropy'``); per iteration ``u = (a / K v)^fi1`` then
+    ``v = (b / K^T u)^fi2`` with ``fi = reg_m / (reg_m + reg)`` (1 for an
+    infinite ``reg_m``); a zero ``K^T u`` or a non-finite scaling reverts to
+    the previous pair; the error ``0.5 (|du|_inf / max(|u|_inf, |uprev|_inf, 1)
+    + same for v)`` is logged every iteration and stops the loop when
+    ``< stopThr``.  The log holds ``err, logu, logv, cost, total_cost``."""
+    M = _f64(M)
+    a, b = _uniform_if_empty(a, b, M)
+    n, m = M.shape
+    rm1, rm2 = (float(reg_m), float(reg_m)) if np.isscalar(reg_m) else (float(reg_m[0]), float(reg_m[1]))
+    if warmstart is None:
+        u, v = np.ones(n), np.ones(m)
+    else:
+        u, v = np.exp(_f64(warmstart[0])), np.exp(_f64(warmstart[1]))
+    warns = []
+    if reg_type.lower() == "entropy":
+        warns.append("If reg_type = entropy, then the matrix c is overwritten by the one matrix.")
+        c = np.ones((n, m))
+    c = np.outer(a, b) if c is None else _f64(c)
+    K = np.exp(-M / reg) * c
+    fi1 = rm1 / (rm1 + reg) if rm1 != float("inf") else 1
+    fi2 = rm2 / (rm2 + reg) if rm2 != float("inf") else 1
+    errs = []
+    i = 0
+    with np.errstate(all="ignore"):
+        for i in range(numItermax):
+            uprev, vprev = u, v
+            u = (a / (K @ v)) ** fi1
+            Ktu = K.T @ u
+            v = (b / Ktu) ** fi2
+            if (np.any(Ktu == 0.0) or np.any(np.isnan(u)) or np.any(np.isnan(v)) or np.any(np.isinf(u))
+                    or np.any(np.isinf(v))):
+                warns.append("Numerical errors at iteration %s" % i)
+                u, v = uprev, vprev
+                break
+            err_u = np.max(np.abs(u - uprev)) / max(np.max(np.abs(u)), np.max(np.abs(uprev)), 1.0)
+            err_v = np.max(np.abs(v - vprev)) / max(np.max(np.abs(v)), np.max(np.abs(vprev)), 1.0)
+            err = 0.5 * (err_u + err_v)
+            errs.append(float(err))
+            if err < stopThr:
+                break
+        plan = u[:, None] * K * v[None, :]
+        cost = float(np.sum(plan * M))
+
+        def kl(p, q):
+            return float(np.sum(p * np.log(p / q + 1e-16)))
+        total = cost + reg * kl(plan, c)
+        if rm1 != float("inf"):
+            total += rm1 * kl(plan.sum(1), a)
+        if rm2 != float("inf"):
+            total += rm2 * kl(plan.sum(0), b)
+    return plan, {"err": errs, "logu": np.log(u + 1e-300), "logv": np.log(v + 1e-300), "cost": cost,
+                  "total_cost": total, "niter": i, "_warnings": warns}
+
+
 def log_projection_batch(K, a=None, b=None, max_iter=10000, tol=1e-5):
     """Batched log-domain Bregman projection, ``ot/batch/_utils.py:165-290``.
 

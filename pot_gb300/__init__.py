@@ -16,6 +16,7 @@ from . import gromov  # noqa: F401
 from .empirical import empirical_sinkhorn  # noqa: F401
 from .solvers import solve, solve_sample, empirical_sinkhorn2  # noqa: F401
 from .barycenters import barycenter, barycenter_sinkhorn  # noqa: F401
+from .unbalanced import sinkhorn_unbalanced, sinkhorn_unbalanced2, sinkhorn_knopp_unbalanced  # noqa: F401
 from .utils import dist, OTResult  # noqa: F401
 from .patch import patch_pot, unpatch_pot  # noqa: F401
 

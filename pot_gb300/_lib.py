@@ -11,7 +11,7 @@ import torch
 from . import _build
 
 OTG_F32, OTG_F64 = 0, 1
-OTG_METHOD_KNOPP, OTG_METHOD_LOG, OTG_METHOD_STAB = 0, 1, 2
+OTG_METHOD_KNOPP, OTG_METHOD_LOG, OTG_METHOD_STAB, OTG_METHOD_UNB = 0, 1, 2, 3
 STATUS_CONVERGED, STATUS_MAXITER, STATUS_NUMERICAL, STATUS_ABORTED = 0, 1, 2, 3
 _ERRORS = {-1: "invalid argument", -2: "unsupported dtype", -3: "workspace too small",
            -4: "CUDA launch error", -5: "unsupported configuration",
@@ -25,7 +25,8 @@ class OtgDenseProblem(ctypes.Structure):
                 ("ldm", c_i64), ("a", c_vp), ("b", c_vp), ("warm_u", c_vp), ("warm_v", c_vp),
                 ("reg", c_dbl), ("max_iter", c_i32), ("hist_cap", c_i32), ("stop_thr", c_dbl),
                 ("out_u", c_vp), ("out_v", c_vp), ("workspace_bytes", c_sz), ("grid", c_i32),
-                ("timeout_ms", c_i32), ("tau", c_dbl), ("check_period", c_i32), ("reserved", c_i32)]
+                ("timeout_ms", c_i32), ("tau", c_dbl), ("check_period", c_i32), ("reserved", c_i32),
+                ("reg_m1", c_dbl), ("reg_m2", c_dbl), ("c_ones", c_i32), ("reserved2", c_i32)]
 
 
 class OtgBatchProblem(ctypes.Structure):

@@ -167,6 +167,7 @@ def batched_plan(layout, M_packed, u, v, a_packed, b_packed, reg_t, method, kl=F
     dev = layout.device
     P = torch.empty_like(M_packed) if want_plan else None
     vals = torch.empty(3 * layout.B, dtype=torch.float64, device=dev)
+    reg_t = reg_t.to(torch.float64).contiguous()  # the plan table reads float64 regularisations
     t = _lib.OtgPlanTable(dtype=_lib.dtype_code(layout.dtype), method=method, nprob=layout.B, kl=int(kl),
                           M=M_packed.data_ptr(), m_off=layout.m_off.data_ptr(), rows=layout.rows.data_ptr(),
                           cols=layout.cols.data_ptr(), ldm=layout.ldm.data_ptr(), r_off=layout.r_off.data_ptr(),

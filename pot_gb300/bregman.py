@@ -30,7 +30,7 @@ def _hist_cap(max_iter):
 
 
 class DenseResult:
-    __slots__ = ("u", "v", "status", "niter", "errs", "workspace", "layout", "nabs", "absorbed_last")
+    __slots__ = ("u", "v", "status", "niter", "errs", "workspace", "layout", "nabs", "absorbed_last", "method")
 
 
 def default_grid(n, m):
@@ -43,7 +43,7 @@ def default_grid(n, m):
 
 
 def solve_dense(M, a, b, reg, method, max_iter, stop_thr, warm_u=None, warm_v=None, grid=None,
-                timeout_ms=0, read_back=True, tau=0.0, check_period=10):
+                timeout_ms=0, read_back=True, tau=0.0, check_period=10, unbalanced=None):
     """Run one dense solve on device tensors (contiguous rows, same dtype).
 
     Returns a DenseResult whose ``u, v`` are scalings (knopp) or natural-log
@@ -67,12 +67,15 @@ def solve_dense(M, a, b, reg, method, max_iter, stop_thr, warm_u=None, warm_v=No
         reg=float(reg), max_iter=int(max_iter), hist_cap=cap, stop_thr=float(stop_thr),
         out_u=out_u.data_ptr(), out_v=out_v.data_ptr(), workspace_bytes=wsb, grid=grid,
         timeout_ms=timeout_ms, tau=float(tau), check_period=int(check_period))
+    if unbalanced is not None:
+        p.reg_m1, p.reg_m2, p.c_ones = float(unbalanced[0]), float(unbalanced[1]), int(unbalanced[2])
     _lib.check(lib.otg_sinkhorn_dense(ctypes.byref(p), ctypes.c_void_p(ws.data_ptr()),
                                       _lib.stream_handle(M.device)), "otg_sinkhorn_dense")
     r = DenseResult()
     r.u, r.v, r.workspace = out_u, out_v, ws
     r.status, r.niter, r.errs = None, None, None
     r.layout = (dt, n, m, cap, grid)
+    r.method = method
     if read_back:
         read_result(r)
     return r
@@ -91,7 +94,8 @@ def read_result(r):
     r.nabs, r.absorbed_last = int(info[5]), bool(info[6])
     if int(info[3]) != 0:
         r.status = _lib.STATUS_ABORTED
-    r.errs = np.sqrt(hist[:nchk])
+    # the unbalanced form logs the errors themselves, the others squared norms
+    r.errs = hist[:nchk].copy() if r.method == _lib.OTG_METHOD_UNB else np.sqrt(hist[:nchk])
     if r.status == _lib.STATUS_ABORTED:
         raise RuntimeError("pot_gb300: a device-side wait timed out; the solve was abandoned")
     return r

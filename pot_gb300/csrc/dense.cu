@@ -9,6 +9,12 @@
 //                              same check :884-899)
 //   sinkhorn_stabilized :1105-1368 (scalings over absorbed potentials; see
 //                              "Stabilised form" below)
+// and ot/unbalanced/_sinkhorn.py
+//   sinkhorn_knopp_unbalanced :565-818 (u first: u = (a / K v)^fi1,
+//                              v = (b / K^T u)^fi2 with K = exp(-M/reg) c and
+//                              c = alpha beta^T; revert on a zero K^T u or a
+//                              non-finite scaling; the relative sup-norm change
+//                              of (u, v) checked EVERY iteration)
 //
 // One iteration is one COLUMN pass and one ROW pass over M:
 //   column pass  : partial column reductions over row chunks      -> barrier
@@ -79,10 +85,21 @@ struct DenseArgs {
   T *sa, *sb;                           // absorption reference points (base 2)
   T log2n, log2m, log2tau;
   int period;                           // iterations between marginal checks
-  unsigned long long* mslot;            // [2] max(F - SA), [2] max(G - SB), ordered keys
+  unsigned long long* mslot;            // STAB: [2] max(F - SA), [2] max(G - SB); UNB: [2][6] maxima
+  // unbalanced form only (sa, sb then hold alpha*u and beta*v)
+  T fi1, fi2;
+  const T* alw; const T* bew;           // c = alw bew^T (null: ones)
 };
 
-template <int METHOD> struct LogDomain { static constexpr bool value = METHOD != OTG_METHOD_KNOPP; };
+// Per-thread maxima carried out of a pass (stabilised: d0; unbalanced:
+// |u_new - u_old|, |u_new|, |u_old|).
+struct Track {
+  double d0 = -INFINITY, d1 = -INFINITY, d2 = -INFINITY;
+};
+
+template <int METHOD> struct LogDomain {
+  static constexpr bool value = METHOD == OTG_METHOD_LOG || METHOD == OTG_METHOD_STAB;
+};
 
 // Order-preserving map of doubles to unsigned keys (atomicMax on keys = max
 // on values; key 0 is below every value).
@@ -216,6 +233,11 @@ __device__ __forceinline__ T row_finalize(const DenseArgs<T>& A, int64_t i, T mx
     const T unew = __ldcg(A.loga2 + i) - lse_value(mx, s);
     if (METHOD == OTG_METHOD_STAB && isnan(unew)) atomicExch(numflag, 1);
     return unew;
+  } else if (METHOD == OTG_METHOD_UNB) {
+    const T al = A.alw ? A.alw[i] : T(1);
+    const T unew = pow(A.a[i] / (al * s), A.fi1);
+    if (!isfinite(unew)) atomicExch(numflag, 1);
+    return unew;
   } else {
     T unew = T(1) / ((T(1) / A.a[i]) * s);
     if (!isfinite(unew)) atomicExch(numflag, 1);
@@ -223,9 +245,24 @@ __device__ __forceinline__ T row_finalize(const DenseArgs<T>& A, int64_t i, T mx
   }
 }
 
+// Bookkeeping after a row update: the stabilised form's absorption test, the
+// unbalanced form's alpha*u and change maxima.
+template <typename T, int METHOD>
+__device__ __forceinline__ void row_after(const DenseArgs<T>& A, int64_t i, T un, const T* __restrict__ uold,
+                                          Track& tr) {
+  if (METHOD == OTG_METHOD_STAB) tr.d0 = fmax(tr.d0, (double)(un - __ldcg(A.sa + i)));
+  if (METHOD == OTG_METHOD_UNB) {
+    A.sa[i] = (A.alw ? A.alw[i] : T(1)) * un;
+    const T uo = __ldcg(uold + i);
+    tr.d0 = fmax(tr.d0, (double)fabs(un - uo));
+    tr.d1 = fmax(tr.d1, (double)fabs(un));
+    tr.d2 = fmax(tr.d2, (double)fabs(uo));
+  }
+}
+
 template <typename T, int METHOD, bool VEC>
 __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __restrict__ unew, int lane,
-                         double& umax) {
+                         const T* __restrict__ uold, Track& tr) {
   constexpr int VW = Vec<T>::N;
   using V = typename Vec<T>::type;
   __shared__ T r_mx[8][RW], r_s[8][RW];
@@ -304,7 +341,7 @@ __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __re
         if (A.Sc == 1) {
           const T un = row_finalize<T, METHOD>(A, row, M0, S0, A.info + 4);
           unew[row] = un;
-          if (METHOD == OTG_METHOD_STAB) umax = fmax(umax, (double)(un - __ldcg(A.sa + row)));
+          row_after<T, METHOD>(A, row, un, uold, tr);
         } else {
           A.prow[cc * n + row] = Pair<T>{M0, S0};
         }
@@ -315,7 +352,8 @@ __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __re
 }
 
 template <typename T, int METHOD>
-__device__ void row_merge(const DenseArgs<T>& A, T* __restrict__ unew, long gtid, long nthreads, double& umax) {
+__device__ void row_merge(const DenseArgs<T>& A, T* __restrict__ unew, long gtid, long nthreads,
+                          const T* __restrict__ uold, Track& tr) {
   for (int64_t i = gtid; i < A.n; i += nthreads) {
     T mx = -INFINITY, s = 0;
     const T* base = reinterpret_cast<const T*>(A.prow + i);
@@ -323,7 +361,7 @@ __device__ void row_merge(const DenseArgs<T>& A, T* __restrict__ unew, long gtid
     else s = sum_strided(base, 2 * A.n, A.Sc);
     const T un = row_finalize<T, METHOD>(A, i, mx, s, A.info + 4);
     unew[i] = un;
-    if (METHOD == OTG_METHOD_STAB) umax = fmax(umax, (double)(un - __ldcg(A.sa + i)));
+    row_after<T, METHOD>(A, i, un, uold, tr);
   }
 }
 
@@ -334,7 +372,7 @@ __device__ void row_merge(const DenseArgs<T>& A, T* __restrict__ unew, long gtid
 template <typename T, int METHOD>
 __device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* __restrict__ vnxt,
                           bool check, bool update, double* err_slot, long gtid, long nthreads, T err_shift,
-                          double& vmax) {
+                          Track& tr) {
   double e2 = 0.0;
   for (int64_t j = gtid; j < A.m; j += nthreads) {
     T mx = -INFINITY, s = 0;
@@ -353,7 +391,7 @@ __device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* 
         vnxt[j] = vn;
         if (METHOD == OTG_METHOD_STAB) {
           if (isnan(vn)) atomicExch(A.info + 4, 1);
-          vmax = fmax(vmax, (double)(vn - __ldcg(A.sb + j)));
+          tr.d0 = fmax(tr.d0, (double)(vn - __ldcg(A.sb + j)));
         }
       }
     } else {
@@ -361,7 +399,17 @@ __device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* 
         double cs = (double)(__ldcg(vcur + j) * s);
         e2 += (cs - (double)bj) * (cs - (double)bj);
       }
-      if (update) {
+      if (update && METHOD == OTG_METHOD_UNB) {
+        const T be = A.bew ? A.bew[j] : T(1);
+        const T vn = pow(bj / (be * s), A.fi2);
+        if (s == T(0) || !isfinite(vn)) atomicExch(A.info + 4, 1);
+        vnxt[j] = vn;
+        A.sb[j] = be * vn;
+        const T vo = __ldcg(vcur + j);
+        tr.d0 = fmax(tr.d0, (double)fabs(vn - vo));
+        tr.d1 = fmax(tr.d1, (double)fabs(vn));
+        tr.d2 = fmax(tr.d2, (double)fabs(vo));
+      } else if (update) {
         T vn = bj / s;
         if (s == T(0) || !isfinite(vn)) atomicExch(A.info + 4, 1);
         vnxt[j] = vn;
@@ -397,7 +445,9 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
 
   // Phase 0: initial state.
   for (int64_t i = gtid; i < A.n; i += nthreads) {
-    if (METHOD == OTG_METHOD_STAB) {
+    if (METHOD == OTG_METHOD_UNB) {
+      A.u0[i] = A.warm_u ? exp(A.warm_u[i]) : T(1);
+    } else if (METHOD == OTG_METHOD_STAB) {
       const T s0 = A.warm_u ? A.warm_u[i] * L2E : T(0);
       A.sa[i] = s0;
       A.u0[i] = s0 - A.log2n;
@@ -410,7 +460,11 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
     }
   }
   for (int64_t j = gtid; j < A.m; j += nthreads) {
-    if (METHOD == OTG_METHOD_STAB) {
+    if (METHOD == OTG_METHOD_UNB) {
+      const T v0 = A.warm_v ? exp(A.warm_v[j]) : T(1);
+      A.v0[j] = v0;
+      A.sb[j] = (A.bew ? A.bew[j] : T(1)) * v0;
+    } else if (METHOD == OTG_METHOD_STAB) {
       const T s0 = A.warm_v ? A.warm_v[j] * L2E : T(0);
       A.sb[j] = s0;
       A.v0[j] = s0 - A.log2m;
@@ -430,15 +484,52 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
   int nabs = 0;
   int nchk = 0;
   int status = OTG_STATUS_MAXITER, niter = A.max_iter - 1;
-  for (int ii = 0;; ++ii) {
+  if (METHOD == OTG_METHOD_UNB) {
+    // u first; the relative change of (u, v) is the error of every iteration
+    for (int ii = 0; ii < A.max_iter; ++ii) {
+      unsigned long long* sl = A.mslot + 6 * (ii & 1);
+      Track ut;
+      row_pass<T, METHOD, VEC>(A, A.sb, unxt, lane, ucur, ut);
+      if (A.Sc == 1) {
+        block_max_atomic(ut.d0, sl); block_max_atomic(ut.d1, sl + 1); block_max_atomic(ut.d2, sl + 2);
+      }
+      if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+      if (A.Sc > 1) {
+        row_merge<T, METHOD>(A, unxt, gtid, nthreads, ucur, ut);
+        block_max_atomic(ut.d0, sl); block_max_atomic(ut.d1, sl + 1); block_max_atomic(ut.d2, sl + 2);
+        if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+      }
+      col_pass<T, METHOD, VEC>(A, A.sa, lane);
+      if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+      Track vt;
+      col_merge<T, METHOD>(A, vcur, vnxt, false, true, nullptr, gtid, nthreads, T(0), vt);
+      block_max_atomic(vt.d0, sl + 3); block_max_atomic(vt.d1, sl + 4); block_max_atomic(vt.d2, sl + 5);
+      if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+      if (ld_acquire_i(A.info + 4)) { status = OTG_STATUS_NUMERICAL; niter = ii; break; }  // previous pair kept
+      double mk[6];
+      for (int q = 0; q < 6; ++q) mk[q] = key_value(__ldcg(sl + q));
+      const double err = 0.5 * (mk[0] / fmax(fmax(mk[1], mk[2]), 1.0) + mk[3] / fmax(fmax(mk[4], mk[5]), 1.0));
+      if (gtid == 0) {
+        if (ii < A.hist_cap) A.hist[ii] = err;
+        unsigned long long* other = A.mslot + 6 * ((ii + 1) & 1);
+        for (int q = 0; q < 6; ++q) other[q] = 0ull;
+      }
+      nchk = ii + 1;
+      T* t;
+      t = ucur; ucur = unxt; unxt = t;
+      t = vcur; vcur = vnxt; vnxt = t;
+      if (err < A.stop_thr) { status = OTG_STATUS_CONVERGED; niter = ii; break; }
+    }
+  }
+  for (int ii = 0; METHOD != OTG_METHOD_UNB; ++ii) {
     col_pass<T, METHOD, VEC>(A, ucur, lane);
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     const bool update = ii < A.max_iter;
     double* slot = A.hist + (nchk < A.hist_cap ? nchk : A.hist_cap - 1);
-    double vmax = -INFINITY;
+    Track vt;
     const T shift = (METHOD == OTG_METHOD_STAB && absorbed) ? -(A.log2n + A.log2m) : T(0);
-    col_merge<T, METHOD>(A, vcur, vnxt, prev_check, update, slot, gtid, nthreads, shift, vmax);
-    if (METHOD == OTG_METHOD_STAB && update) block_max_atomic(vmax, A.mslot + 2 + (ii & 1));
+    col_merge<T, METHOD>(A, vcur, vnxt, prev_check, update, slot, gtid, nthreads, shift, vt);
+    if (METHOD == OTG_METHOD_STAB && update) block_max_atomic(vt.d0, A.mslot + 2 + (ii & 1));
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     if (prev_check) {
       double e2 = *(volatile double*)slot;
@@ -451,13 +542,13 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
       // zero column sum or non-finite v: revert to the previous pair
       status = OTG_STATUS_NUMERICAL; niter = ii; break;
     }
-    double umax = -INFINITY;
-    row_pass<T, METHOD, VEC>(A, vnxt, unxt, lane, umax);
-    if (METHOD == OTG_METHOD_STAB && A.Sc == 1) block_max_atomic(umax, A.mslot + (ii & 1));
+    Track ut;
+    row_pass<T, METHOD, VEC>(A, vnxt, unxt, lane, ucur, ut);
+    if (METHOD == OTG_METHOD_STAB && A.Sc == 1) block_max_atomic(ut.d0, A.mslot + (ii & 1));
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     if (A.Sc > 1) {
-      row_merge<T, METHOD>(A, unxt, gtid, nthreads, umax);
-      if (METHOD == OTG_METHOD_STAB) block_max_atomic(umax, A.mslot + (ii & 1));
+      row_merge<T, METHOD>(A, unxt, gtid, nthreads, ucur, ut);
+      if (METHOD == OTG_METHOD_STAB) block_max_atomic(ut.d0, A.mslot + (ii & 1));
       if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     }
     if (METHOD != OTG_METHOD_LOG && ld_acquire_i(A.info + 4)) {
@@ -627,7 +718,7 @@ Layout make_layout(int64_t n, int64_t m, int hist_cap, int grid) {
   L.off_pcol = off; off = align_up(off + sizeof(Pair<T>) * (size_t)L.Sr * m, 256);
   L.off_prow = off; off = align_up(off + sizeof(Pair<T>) * (size_t)(L.Sc > 1 ? L.Sc : 0) * n, 256);
   L.off_hist = off; off = align_up(off + sizeof(double) * (size_t)hist_cap, 256);
-  L.off_ctrl = off; off = align_up(off + 128, 256);
+  L.off_ctrl = off; off = align_up(off + 256, 256);
   L.total = off;
   return L;
 }
@@ -672,6 +763,12 @@ int launch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
   A.log2tau = (T)(METHOD == OTG_METHOD_STAB ? std::log2(p->tau) : 0.0);
   A.period = METHOD == OTG_METHOD_STAB ? p->check_period : 10;
   A.mslot = reinterpret_cast<unsigned long long*>(base + L.off_ctrl + 64);
+  if (METHOD == OTG_METHOD_UNB) {
+    A.fi1 = (T)(std::isinf(p->reg_m1) ? 1.0 : p->reg_m1 / (p->reg_m1 + p->reg));
+    A.fi2 = (T)(std::isinf(p->reg_m2) ? 1.0 : p->reg_m2 / (p->reg_m2 + p->reg));
+    A.alw = p->c_ones ? nullptr : static_cast<const T*>(p->a);
+    A.bew = p->c_ones ? nullptr : static_cast<const T*>(p->b);
+  }
   cudaError_t e = cudaMemsetAsync(base + L.off_hist, 0, L.total - L.off_hist, st);
   if (e != cudaSuccess) return OTG_ERR_CUDA;
   void* args[] = {&A};
@@ -688,6 +785,8 @@ int dispatch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
     return vec ? launch_dense<T, OTG_METHOD_LOG, true>(p, ws, st) : launch_dense<T, OTG_METHOD_LOG, false>(p, ws, st);
   if (p->method == OTG_METHOD_STAB)
     return vec ? launch_dense<T, OTG_METHOD_STAB, true>(p, ws, st) : launch_dense<T, OTG_METHOD_STAB, false>(p, ws, st);
+  if (p->method == OTG_METHOD_UNB)
+    return vec ? launch_dense<T, OTG_METHOD_UNB, true>(p, ws, st) : launch_dense<T, OTG_METHOD_UNB, false>(p, ws, st);
   return vec ? launch_dense<T, OTG_METHOD_KNOPP, true>(p, ws, st) : launch_dense<T, OTG_METHOD_KNOPP, false>(p, ws, st);
 }
 
@@ -695,7 +794,10 @@ int check_problem(const OtgDenseProblem* p) {
   if (!p || !p->M || !p->a || !p->b || !p->out_u || !p->out_v) return OTG_ERR_ARG;
   if (p->n < 1 || p->m < 1 || p->ldm < p->m || p->hist_cap < 1) return OTG_ERR_ARG;
   if (p->dtype != OTG_F32 && p->dtype != OTG_F64) return OTG_ERR_DTYPE;
-  if (p->method != OTG_METHOD_LOG && p->method != OTG_METHOD_KNOPP && p->method != OTG_METHOD_STAB)
+  if (p->method != OTG_METHOD_LOG && p->method != OTG_METHOD_KNOPP && p->method != OTG_METHOD_STAB &&
+      p->method != OTG_METHOD_UNB)
+    return OTG_ERR_ARG;
+  if (p->method == OTG_METHOD_UNB && (!(p->reg_m1 > 0) || !(p->reg_m2 > 0) || p->hist_cap < p->max_iter))
     return OTG_ERR_ARG;
   if (p->method == OTG_METHOD_STAB && (p->check_period < 1 || !(p->tau > 0))) return OTG_ERR_ARG;
   if (p->max_iter < 0) return OTG_ERR_ARG;
@@ -735,6 +837,7 @@ int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, i
   if (loss) cudaMemsetAsync(loss, 0, sizeof(double), stream);
   const double c = -OTG_LOG2E / reg;
   if (method == OTG_METHOD_STAB) method = OTG_METHOD_LOG;  // plan of natural-log potentials
+  if (method == OTG_METHOD_UNB) method = OTG_METHOD_KNOPP; // plan of scalings (alpha u, beta v)
   if (dtype == OTG_F64) {
     if (method == OTG_METHOD_LOG)
       dense_plan_kernel<double, OTG_METHOD_LOG><<<blocks, 256, 0, stream>>>((const double*)M, n, m, ldm, (const double*)u, (const double*)v, c, (double*)P, ldp, loss);

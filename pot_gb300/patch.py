@@ -19,6 +19,8 @@ replaces the hot-path names in every module that imported them:
     ot/batch/_quadratic.py:14    bregman_log_projection_batch
     ot/solvers.py:14             sinkhorn_log, empirical_sinkhorn2 (the entropic branches of
                                  ot.solve / ot.solve_sample)
+    ot/unbalanced/__init__.py    sinkhorn_unbalanced(2), sinkhorn_knopp_unbalanced
+    ot/unbalanced/_sinkhorn.py   sinkhorn_knopp_unbalanced (the dispatcher's callee)
 
 Calls the GPU path does not cover (other methods, metrics or losses) raise
 NotImplementedError from the GPU function; ``unpatch_pot`` restores the
@@ -26,7 +28,7 @@ original bindings.
 """
 import importlib
 
-from . import bregman, batch, gromov, empirical, solvers, barycenters
+from . import bregman, batch, gromov, empirical, solvers, barycenters, unbalanced
 
 GPU = {
     "sinkhorn": bregman.sinkhorn,
@@ -38,6 +40,9 @@ GPU = {
     "empirical_sinkhorn2": solvers.empirical_sinkhorn2,
     "barycenter": barycenters.barycenter,
     "barycenter_sinkhorn": barycenters.barycenter_sinkhorn,
+    "sinkhorn_unbalanced": unbalanced.sinkhorn_unbalanced,
+    "sinkhorn_unbalanced2": unbalanced.sinkhorn_unbalanced2,
+    "sinkhorn_knopp_unbalanced": unbalanced.sinkhorn_knopp_unbalanced,
     "empirical_sinkhorn": empirical.empirical_sinkhorn,
     "entropic_gromov_wasserstein": gromov.entropic_gromov_wasserstein,
     "entropic_gromov_wasserstein2": gromov.entropic_gromov_wasserstein2,
@@ -65,6 +70,8 @@ MODULES = {
     ".batch._linear": ["solve_batch", "dist_batch", "bregman_log_projection_batch", "bregman_projection_batch"],
     ".batch._quadratic": ["bregman_log_projection_batch"],
     ".solvers": ["sinkhorn_log", "empirical_sinkhorn2"],
+    ".unbalanced": ["sinkhorn_unbalanced", "sinkhorn_unbalanced2", "sinkhorn_knopp_unbalanced"],
+    ".unbalanced._sinkhorn": ["sinkhorn_knopp_unbalanced"],
 }
 
 _saved = {}

@@ -67,7 +67,7 @@ def solve(M, a=None, b=None, reg=None, c=None, reg_type="KL", unbalanced=None, u
     if grad == "last_step":
         return _last_step(bd, M, a, b, Md, ad, bv, lu, lv, float(reg), kl, max_iter, r)
     layout, Mp = pb._uniform_batch(Md[None])
-    reg_t = torch.full((1,), float(reg), dtype=Md.dtype, device=Md.device)
+    reg_t = torch.full((1,), float(reg), dtype=torch.float64, device=Md.device)
     P, vals = pb.batched_plan(layout, Mp, lu, lv, ad, bv, reg_t, bregman._lib.OTG_METHOD_LOG, kl=kl)
     n, m = Md.shape
     P = P.view(n, int(layout.ldm_np[0]))[:, :m]

@@ -372,7 +372,40 @@ def barycenters():
          log_err=np.array(lg2["err"]), log_niter=lg2["niter"])
 
 
-SECTIONS = {"core": core, "next": next_rows, "fgw": fused_gw, "bary": barycenters}
+def unbalanced():
+    # 14. unbalanced scaling Sinkhorn (ot/unbalanced/_sinkhorn.py:565-818)
+    rng = np.random.default_rng(61)
+    x = rng.standard_normal((50, 2))
+    y = rng.standard_normal((40, 2)) + 0.7
+    M = ot.dist(x, y)
+    M /= M.max()
+    a = rng.random(50) + 0.1
+    a /= a.sum()
+    b = 1.5 * (rng.random(40) + 0.1) / 40
+    out = dict(x=x, y=y, a=a, b=b, M=M)
+    cases = (("kl", dict(reg=0.05, reg_m=1.0)), ("kl_pair", dict(reg=0.05, reg_m=(0.5, float("inf")))),
+             ("ent", dict(reg=0.1, reg_m=2.0, reg_type="entropy")), ("kl_small", dict(reg=0.005, reg_m=0.3)),
+             ("warm", dict(reg=0.05, reg_m=1.0, warmstart=(rng.standard_normal(50) * 0.1,
+                                                           rng.standard_normal(40) * 0.1))),
+             ("iter5", dict(reg=0.05, reg_m=1.0, numItermax=5)))
+    for tag, kw in cases:
+        kw = dict(kw)
+        reg, reg_m = kw.pop("reg"), kw.pop("reg_m")
+        (P, lg), w = call_warn(ot.unbalanced.sinkhorn_unbalanced, a, b, M, reg, reg_m, log=True, **kw)
+        out[tag + "_plan"] = P
+        out[tag + "_err"] = np.array(lg["err"], dtype=np.float64)
+        out[tag + "_logu"] = lg["logu"]
+        out[tag + "_logv"] = lg["logv"]
+        out[tag + "_cost"] = lg["cost"]
+        out[tag + "_total"] = lg["total_cost"]
+        if "warmstart" in kw:
+            out["warm_wu"], out["warm_wv"] = kw["warmstart"]
+    out["u2_linear"] = ot.unbalanced.sinkhorn_unbalanced2(a, b, M, 0.05, 1.0)
+    out["u2_total"] = ot.unbalanced.sinkhorn_unbalanced2(a, b, M, 0.05, 1.0, returnCost="total")
+    save("unbal_50x40", **out)
+
+
+SECTIONS = {"core": core, "next": next_rows, "fgw": fused_gw, "bary": barycenters, "unbal": unbalanced}
 
 
 def main(names):

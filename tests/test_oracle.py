@@ -268,3 +268,23 @@ def test_barycenter_300():
         bar, lg = fn(g["A"], M, 0.02, numItermax=300, stopThr=1e-9)
         assert lg["niter"] == int(g[tag + "_niter"])
         np.testing.assert_allclose(bar, g[tag + "_bar"], rtol=1e-8, atol=1e-300)
+
+
+UNBAL = [("kl", dict(reg=0.05, reg_m=1.0)), ("kl_pair", dict(reg=0.05, reg_m=(0.5, float("inf")))),
+         ("ent", dict(reg=0.1, reg_m=2.0, reg_type="entropy")), ("kl_small", dict(reg=0.005, reg_m=0.3)),
+         ("warm", dict(reg=0.05, reg_m=1.0)), ("iter5", dict(reg=0.05, reg_m=1.0, numItermax=5))]
+
+
+@pytest.mark.parametrize("tag,kw", UNBAL)
+def test_unbalanced(tag, kw):
+    g = golden("unbal_50x40")
+    kw = dict(kw)
+    reg, reg_m = kw.pop("reg"), kw.pop("reg_m")
+    if tag == "warm":
+        kw["warmstart"] = (g["warm_wu"], g["warm_wv"])
+    P, lg = oracle.sinkhorn_knopp_unbalanced(g["a"], g["b"], g["M"], reg, reg_m, **kw)
+    assert len(lg["err"]) == len(g[tag + "_err"])
+    np.testing.assert_allclose(lg["err"], g[tag + "_err"], rtol=1e-7, atol=1e-15)
+    np.testing.assert_allclose(P, g[tag + "_plan"], rtol=1e-9, atol=1e-300)
+    np.testing.assert_allclose(lg["logu"], g[tag + "_logu"], rtol=1e-9, atol=1e-12)
+    assert abs(lg["total_cost"] - float(g[tag + "_total"])) <= 1e-9 * abs(float(g[tag + "_total"]))

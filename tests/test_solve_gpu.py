@@ -121,3 +121,12 @@ def test_solve_not_on_gpu_path(cuda):
     for kw in (dict(reg=None), dict(reg=1.0, unbalanced=1.0), dict(reg=1.0, reg_type="L2")):
         with pytest.raises(NotImplementedError):
             pg.solve(M, **kw)
+
+
+def test_solve_f32(cuda):
+    g = golden("solve_40x30_KL")
+    f = lambda x: torch.tensor(x, dtype=torch.float32, device=cuda)  # noqa: E731
+    res = pg.solve(f(g["M"]), f(g["a"]), f(g["b"]), reg=float(g["reg"]), tol=1e-6)
+    assert res.plan.dtype == torch.float32
+    assert rel_l1(res.plan.double().cpu().numpy(), g["plan"]) <= 1e-5
+    assert abs(float(res.value) - float(g["value"])) <= 1e-5 * abs(float(g["value"]))
