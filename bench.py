@@ -36,7 +36,7 @@ WS_N, WS_D, WS_REG, WS_TOL = 2048, 16, 0.02, 1e-6
 # DRAM traffic / algorithmic bytes of multi_sinkhorn_kernel, from one ncu capture of the
 # same workload on 128 pairs (profiles/multi_sinkhorn_warmstart_gmm2048.md); the launch's
 # traffic scales with the problem-iterations it processes
-MULTI_TRAFFIC_RATIO = 132.42 / 133.61
+MULTI_TRAFFIC_RATIO = 132.02 / 133.61  # ncu dram bytes / algorithmic bytes, one plain-arm launch on 128 pairs
 EVAL_SEED = 10_000_000
 
 

@@ -14,7 +14,7 @@ from . import batch  # noqa: F401
 from .batch import solve_batch, solve_sample_batch, dist_batch  # noqa: F401
 from . import gromov  # noqa: F401
 from .empirical import empirical_sinkhorn  # noqa: F401
-from .solvers import solve, solve_sample, empirical_sinkhorn2  # noqa: F401
+from .solvers import solve, solve_sample, empirical_sinkhorn2, empirical_sinkhorn_divergence  # noqa: F401
 from .barycenters import barycenter, barycenter_sinkhorn  # noqa: F401
 from .unbalanced import sinkhorn_unbalanced, sinkhorn_unbalanced2, sinkhorn_knopp_unbalanced  # noqa: F401
 from .utils import dist, OTResult  # noqa: F401

@@ -38,6 +38,7 @@ GPU = {
     "sinkhorn_stabilized": bregman.sinkhorn_stabilized,
     "sinkhorn_epsilon_scaling": bregman.sinkhorn_epsilon_scaling,
     "empirical_sinkhorn2": solvers.empirical_sinkhorn2,
+    "empirical_sinkhorn_divergence": solvers.empirical_sinkhorn_divergence,
     "barycenter": barycenters.barycenter,
     "barycenter_sinkhorn": barycenters.barycenter_sinkhorn,
     "sinkhorn_unbalanced": unbalanced.sinkhorn_unbalanced,
@@ -59,7 +60,7 @@ MODULES = {
     "": ["sinkhorn", "sinkhorn2"],
     ".bregman": ["sinkhorn", "sinkhorn2", "sinkhorn_knopp", "sinkhorn_log", "sinkhorn_stabilized",
                  "sinkhorn_epsilon_scaling", "empirical_sinkhorn", "empirical_sinkhorn2", "barycenter",
-                 "barycenter_sinkhorn"],
+                 "barycenter_sinkhorn", "empirical_sinkhorn_divergence"],
     ".bregman._sinkhorn": ["sinkhorn_knopp", "sinkhorn_log", "sinkhorn_stabilized", "sinkhorn_epsilon_scaling"],
     ".bregman._empirical": ["sinkhorn", "sinkhorn2"],
     ".gromov": ["entropic_gromov_wasserstein", "entropic_gromov_wasserstein2", "entropic_fused_gromov_wasserstein",

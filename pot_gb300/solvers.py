@@ -46,7 +46,9 @@ def solve(M, a=None, b=None, reg=None, c=None, reg_type="KL", unbalanced=None, u
     if reg is None or reg == 0:
         raise _not_gpu("exact OT (reg=None or 0)")
     if unbalanced is not None:
-        raise _not_gpu("unbalanced OT")
+        if isinstance(reg_type, tuple) or reg_type.lower() != "kl" or unbalanced_type.lower() != "kl":
+            raise _not_gpu("unbalanced OT with reg_type=%r, unbalanced_type=%r" % (reg_type, unbalanced_type))
+        return _solve_unbalanced(M, a, b, reg, c, unbalanced, potentials_init, max_iter, tol, verbose)
     if isinstance(reg_type, tuple) or reg_type.lower() not in ("kl", "entropy"):
         raise _not_gpu("reg_type=%r" % (reg_type,))
     if grad not in ("autodiff", "envelope", "last_step", "detach"):
@@ -78,6 +80,18 @@ def solve(M, a=None, b=None, reg=None, c=None, reg_type="KL", unbalanced=None, u
         value = envelope_loss(value, P.contiguous(), r, bregman._lib.OTG_METHOD_LOG, float(reg), a, b, M)
     return OTResult(potentials=(bd.out(lu), bd.out(lv)), value=bd.scalar(value),
                     value_linear=bd.scalar(value_linear), plan=bd.out(P.contiguous()), backend=bd.kind)
+
+
+def _solve_unbalanced(M, a, b, reg, c, reg_m, potentials_init, max_iter, tol, verbose):
+    """``ot.solve`` with ``reg > 0`` and a KL marginal penalty
+    (``ot/solvers.py:525-550``): ``sinkhorn_knopp_unbalanced`` with
+    ``c = a b^T`` unless given, ``max_iter = 1000``, ``tol = 1e-9``; value =
+    total cost, value_linear = linear cost, potentials = (logu, logv)."""
+    from .unbalanced import sinkhorn_knopp_unbalanced
+    P, lg = sinkhorn_knopp_unbalanced(a if a is not None else [], b if b is not None else [], M, reg, reg_m,
+                                      "kl", c, potentials_init, numItermax=1000 if max_iter is None else max_iter,
+                                      stopThr=1e-9 if tol is None else tol, verbose=verbose, log=True)
+    return OTResult(potentials=(lg["logu"], lg["logv"]), value=lg["total_cost"], value_linear=lg["cost"], plan=P)
 
 
 def _needs_grad(*xs):
@@ -157,3 +171,30 @@ def empirical_sinkhorn2(X_s, X_t, reg, a=None, b=None, metric="sqeuclidean", num
     f, g = res[0], res[1]
     loss = empirical.lazy_loss(X_s, X_t, f, g, reg)
     return (loss, res[2]) if log else loss
+
+
+def empirical_sinkhorn_divergence(X_s, X_t, reg, a=None, b=None, metric="sqeuclidean", numIterMax=10000,
+                                  stopThr=1e-9, verbose=False, log=False, warn=True, warmstart=None, **kwargs):
+    """GPU ``ot.bregman.empirical_sinkhorn_divergence``
+    (``ot/bregman/_empirical.py:520-763``): ``W(a, b) - (W(a, a) + W(b, b)) / 2``
+    from three ``empirical_sinkhorn2`` solves, clipped at zero; the warm
+    start ``(u, v)`` seeds the cross solve and ``(u, u)``, ``(v, v)`` the
+    two self solves."""
+    ws_a = ws_b = None
+    if warmstart is not None:
+        u, v = warmstart
+        ws_a, ws_b = (u, u), (v, v)
+    kw = dict(metric=metric, numIterMax=numIterMax, stopThr=stopThr, verbose=verbose, log=log, warn=warn)
+    ab = empirical_sinkhorn2(X_s, X_t, reg, a, b, warmstart=warmstart, **kw, **kwargs)
+    aa = empirical_sinkhorn2(X_s, X_s, reg, a, a, warmstart=ws_a, **kw, **kwargs)
+    bb = empirical_sinkhorn2(X_t, X_t, reg, b, b, warmstart=ws_b, **kw, **kwargs)
+    if log:
+        (lab, log_ab), (la, log_a), (lb, log_b) = ab, aa, bb
+    else:
+        lab, la, lb = ab, aa, bb
+    div = lab - 0.5 * (la + lb)
+    div = np.maximum(0, div) if not isinstance(div, torch.Tensor) else torch.clamp(div, min=0)
+    if log:
+        return div, {"sinkhorn_loss_ab": lab, "sinkhorn_loss_a": la, "sinkhorn_loss_b": lb,
+                     "log_sinkhorn_ab": log_ab, "log_sinkhorn_a": log_a, "log_sinkhorn_b": log_b}
+    return div

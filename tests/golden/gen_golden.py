@@ -302,6 +302,9 @@ def next_rows():
                                               stopThr=1e-9, log=True)
     save("emp2_lazy_40x30", x=x, y=y, a=a, b=b, reg=0.5, loss=float(loss), f=lg["u"], g=lg["v"],
          niter=lg["niter"], err=np.array(lg["err"]))
+    div = ot.bregman.empirical_sinkhorn_divergence(x, y, 0.5, a, b)
+    div_lazy = ot.bregman.empirical_sinkhorn_divergence(x, y, 0.5, a, b, isLazy=True, batchSize=9, stopThr=1e-9)
+    save("emp_div_40x30", x=x, y=y, a=a, b=b, reg=0.5, div=float(div), div_lazy=float(div_lazy))
 
 
 def fused_gw():
@@ -400,6 +403,9 @@ def unbalanced():
         out[tag + "_total"] = lg["total_cost"]
         if "warmstart" in kw:
             out["warm_wu"], out["warm_wv"] = kw["warmstart"]
+    res = ot.solve(M, a, b, reg=0.05, unbalanced=1.0)
+    out["solve_plan"], out["solve_value"], out["solve_value_linear"] = res.plan, res.value, res.value_linear
+    out["solve_pa"], out["solve_pb"] = res.potentials
     out["u2_linear"] = ot.unbalanced.sinkhorn_unbalanced2(a, b, M, 0.05, 1.0)
     out["u2_total"] = ot.unbalanced.sinkhorn_unbalanced2(a, b, M, 0.05, 1.0, returnCost="total")
     save("unbal_50x40", **out)

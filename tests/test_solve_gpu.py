@@ -118,7 +118,7 @@ def test_solve_grad_modes(cuda, grad):
 
 def test_solve_not_on_gpu_path(cuda):
     M = np.random.default_rng(0).random((4, 5))
-    for kw in (dict(reg=None), dict(reg=1.0, unbalanced=1.0), dict(reg=1.0, reg_type="L2")):
+    for kw in (dict(reg=None), dict(reg=1.0, unbalanced=1.0, unbalanced_type="L2"), dict(reg=1.0, reg_type="L2")):
         with pytest.raises(NotImplementedError):
             pg.solve(M, **kw)
 
@@ -130,3 +130,12 @@ def test_solve_f32(cuda):
     assert res.plan.dtype == torch.float32
     assert rel_l1(res.plan.double().cpu().numpy(), g["plan"]) <= 1e-5
     assert abs(float(res.value) - float(g["value"])) <= 1e-5 * abs(float(g["value"]))
+
+
+def test_empirical_sinkhorn_divergence(cuda):
+    g = golden("emp_div_40x30")
+    d = pg.empirical_sinkhorn_divergence(g["x"], g["y"], float(g["reg"]), g["a"], g["b"])
+    assert abs(float(d) - float(g["div"])) <= 1e-8 * abs(float(g["div"]))
+    dl = pg.empirical_sinkhorn_divergence(g["x"], g["y"], float(g["reg"]), g["a"], g["b"], isLazy=True, batchSize=9,
+                                          stopThr=1e-6)
+    assert abs(float(dl) - float(g["div_lazy"])) <= 1e-4 * abs(float(g["div_lazy"]))

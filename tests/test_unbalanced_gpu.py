@@ -63,3 +63,13 @@ def test_unbalanced_f32(cuda):
     P = pg.sinkhorn_unbalanced(f(g["a"]), f(g["b"]), f(g["M"]), 0.05, 1.0, stopThr=1e-6)
     assert P.dtype == torch.float32 and P.device.type == "cuda"
     assert rel_l1(P.double().cpu().numpy(), Pref) <= 1e-4
+
+
+def test_solve_unbalanced_golden(cuda):
+    g = golden("unbal_50x40")
+    res = pg.solve(g["M"], g["a"], g["b"], reg=0.05, unbalanced=1.0)
+    assert rel_l1(res.plan, g["solve_plan"]) < 1e-9
+    # the total cost nearly cancels here (about 1e-9): compare with an absolute floor
+    assert abs(float(res.value) - float(g["solve_value"])) <= 1e-9 * abs(float(g["solve_value"])) + 1e-14
+    assert abs(float(res.value_linear) - float(g["solve_value_linear"])) <= 1e-9 * abs(float(g["solve_value_linear"]))
+    np.testing.assert_allclose(res.potentials[0], g["solve_pa"], rtol=1e-8, atol=1e-10)
