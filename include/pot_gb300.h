@@ -299,6 +299,8 @@ typedef struct OtgCostTable {
   const int64_t* m_off;
   const int32_t* ldm;
   void* max_out;
+  int32_t fixed_dim;  /* 0, or the dimension every problem shares when it is 2, 3, 8 or 16
+                         (float32: register-tiled kernel; must equal max_dim) */
 } OtgCostTable;
 int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t stream);
 

@@ -50,7 +50,7 @@ class OtgMultiProblem(ctypes.Structure):
 class OtgCostTable(ctypes.Structure):
     _fields_ = [("dtype", c_i32), ("nprob", c_i32), ("X", c_vp), ("Y", c_vp), ("x_off", c_vp), ("y_off", c_vp),
                 ("rows", c_vp), ("cols", c_vp), ("dim", c_vp), ("max_dim", c_i32), ("M", c_vp), ("m_off", c_vp),
-                ("ldm", c_vp), ("max_out", c_vp)]
+                ("ldm", c_vp), ("max_out", c_vp), ("fixed_dim", c_i32)]
 
 
 class OtgPlanTable(ctypes.Structure):

@@ -99,6 +99,95 @@ __global__ void __launch_bounds__(256) batched_sqdist_kernel(OtgCostTable t) {
   }
 }
 
+// Register-tiled float32 cost blocks for the common point dimensions: a CTA
+// computes 64 rows x 256 columns of one problem, both point tiles staged in
+// shared memory dimension-major; each thread owns 8 rows x 8 adjacent columns
+// (64 accumulators) and writes them as 16-byte stores.  Same arithmetic as
+// the kernel above: sum_k (x_k - y_k)^2 in order of k, +inf padding.
+// grid = (column-tile stride, row tiles, problems).
+constexpr int SQ_R = 64, SQ_C = 256;
+
+template <int D>
+__device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, const float* __restrict__ Y, int n, int m,
+                                               int ldm, float* __restrict__ M, int r0, float* xt, float* yt,
+                                               float& local_max) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int e = threadIdx.x; e < SQ_R * D; e += blockDim.x) {
+    const int r = e / D, k = e % D;
+    xt[k * SQ_R + r] = (r0 + r < n) ? X[(int64_t)(r0 + r) * D + k] : 0.f;
+  }
+  for (int c0 = blockIdx.x * SQ_C; c0 < ldm; c0 += gridDim.x * SQ_C) {
+    __syncthreads();  // previous tile's reads of yt are done (and xt is staged)
+    for (int e = threadIdx.x; e < SQ_C * D; e += blockDim.x) {
+      const int c = e / D, k = e % D;
+      yt[k * SQ_C + c] = (c0 + c < m) ? Y[(int64_t)(c0 + c) * D + k] : 0.f;
+    }
+    __syncthreads();
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const float4 xa = *reinterpret_cast<const float4*>(xt + k * SQ_R + warp * 8);
+      const float4 xb = *reinterpret_cast<const float4*>(xt + k * SQ_R + warp * 8 + 4);
+      const float4 ya = *reinterpret_cast<const float4*>(yt + k * SQ_C + lane * 8);
+      const float4 yb = *reinterpret_cast<const float4*>(yt + k * SQ_C + lane * 8 + 4);
+      const float xv[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
+      const float yv[8] = {ya.x, ya.y, ya.z, ya.w, yb.x, yb.y, yb.z, yb.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { const float df = xv[i] - yv[j]; acc[i][j] = fmaf(df, df, acc[i][j]); }
+    }
+    const int cb = c0 + lane * 8;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int row = r0 + warp * 8 + i;
+      if (row >= n) break;
+      float v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (cb + j < m) { v[j] = acc[i][j]; local_max = fmaxf(local_max, acc[i][j]); }
+        else v[j] = INFINITY;
+      }
+      float* dst = M + (int64_t)row * ldm + cb;
+      if (cb + 8 <= ldm) {
+        reinterpret_cast<float4*>(dst)[0] = make_float4(v[0], v[1], v[2], v[3]);
+        reinterpret_cast<float4*>(dst)[1] = make_float4(v[4], v[5], v[6], v[7]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) if (cb + j < ldm) dst[j] = v[j];
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) sqdist_regtile_kernel(OtgCostTable t) {
+  extern __shared__ __align__(16) float sq_smem[];
+  const int p = blockIdx.z;
+  if (p >= t.nprob) return;
+  const int n = t.rows[p], m = t.cols[p], d = t.dim[p], ldm = t.ldm[p];
+  const int r0 = blockIdx.y * SQ_R;
+  if (r0 >= n) return;
+  const float* X = static_cast<const float*>(t.X) + t.x_off[p];
+  const float* Y = static_cast<const float*>(t.Y) + t.y_off[p];
+  float* M = static_cast<float*>(t.M) + t.m_off[p];
+  float* xt = sq_smem;
+  float* yt = sq_smem + SQ_R * t.max_dim;
+  float local_max = 0.f;
+  if (d == 16) sqdist_regtile<16>(X, Y, n, m, ldm, M, r0, xt, yt, local_max);
+  else if (d == 8) sqdist_regtile<8>(X, Y, n, m, ldm, M, r0, xt, yt, local_max);
+  else if (d == 3) sqdist_regtile<3>(X, Y, n, m, ldm, M, r0, xt, yt, local_max);
+  else if (d == 2) sqdist_regtile<2>(X, Y, n, m, ldm, M, r0, xt, yt, local_max);
+  if (t.max_out) {
+    local_max = warp_max(local_max);
+    if ((threadIdx.x & 31) == 0)
+      atomicMax(reinterpret_cast<unsigned int*>(static_cast<float*>(t.max_out) + p), __float_as_uint(local_max));
+  }
+}
+
 // Plan and values per problem.  grid = (row tiles, problems).
 // out_vals[3p+0] = value_linear, [3p+1] = sum T log(T+1e-16) (entropy form)
 // or sum T log(T/(a b) + 1e-16) (KL form), [3p+2] = sum T.
@@ -276,6 +365,9 @@ int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t str
       !t->m_off || t->nprob < 1 || max_rows < 1 || t->max_dim < 1)
     return OTG_ERR_ARG;
   if (t->nprob > 65535) return OTG_ERR_UNSUPPORTED;
+  if (t->fixed_dim && t->fixed_dim != 2 && t->fixed_dim != 3 && t->fixed_dim != 8 && t->fixed_dim != 16)
+    return OTG_ERR_ARG;
+  if (t->fixed_dim && t->fixed_dim != t->max_dim) return OTG_ERR_ARG;
   dim3 grid((max_rows + 31) / 32, t->nprob);
   if (t->max_out) {
     size_t es = t->dtype == OTG_F64 ? 8 : 4;
@@ -283,6 +375,10 @@ int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t str
   }
   if (t->dtype == OTG_F64) {
     batched_sqdist_kernel<double><<<grid, 256, 32 * t->max_dim * sizeof(double), stream>>>(*t);
+  } else if (t->dtype == OTG_F32 && t->fixed_dim) {
+    // every problem has the same dimension, one of 2, 3, 8, 16: register tiles
+    const dim3 g2(8, (unsigned)((max_rows + SQ_R - 1) / SQ_R), (unsigned)t->nprob);
+    sqdist_regtile_kernel<<<g2, 256, (SQ_R + SQ_C) * t->max_dim * sizeof(float), stream>>>(*t);
   } else if (t->dtype == OTG_F32) {
     batched_sqdist_kernel<float><<<grid, 256, 32 * t->max_dim * sizeof(float), stream>>>(*t);
   } else {

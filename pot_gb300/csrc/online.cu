@@ -10,10 +10,10 @@
 // memory as high/low half planes; it streams the other cloud in tiles of 128
 // points through a TMA ring.  For every tile, one thread issues 3 tcgen05 MMAs
 // per 16-wide k-step (Ah Bh + Ah Bl + Al Bh: the dot products x.y with about
-// 22 significant bits) into one of two TMEM buffers; eight epilogue warps
-// (two per TMEM lane quarter, each taking 64 of the 128 columns) read the tile
-// and fold  t_ij = alpha * acc_ij + h_j  into a running base-2 (max, sum) per
-// row, where
+// 22 significant bits) into one of four TMEM buffers (the MMAs run up to three
+// tiles ahead of the epilogue); sixteen epilogue warps (four per TMEM lane
+// quarter, each taking 32 of the 128 columns) read the tile and fold
+// t_ij = alpha * acc_ij + h_j  into a running base-2 (max, sum) per row, where
 //   alpha = 2 log2(e) / (reg sx sy)     (acc carries the operand prescales)
 //   h_j   = g2_j - log2(e) |y_j|^2 / reg  (-inf for padding)
 //   and the row term -log2(e) |x_i|^2 / reg is added after the reduction.
@@ -36,7 +36,9 @@ constexpr uint32_t OL_TILE = OL_M * OL_K * 2;          // one half plane tile (1
 constexpr uint32_t OL_HVEC = OL_N * 4;                 // h slice of a tile (512 B)
 constexpr uint32_t OL_STAGE = 2 * OL_TILE;             // streamed hi, lo (1024-aligned tiles)
 constexpr int OL_MAXKT = 2;                            // d <= 128
-constexpr int OL_THREADS = 320;                        // 8 epilogue warps + producer + MMA
+constexpr int OL_EPI = 16;                             // epilogue warps (4 per TMEM lane quarter)
+constexpr int OL_NBUF = 4;                             // TMEM accumulator buffers of 128 columns
+constexpr int OL_THREADS = OL_EPI * 32 + 64;           // + producer + MMA
 
 struct OnlinePass {
   int n_rows;          // valid rows of the resident side
@@ -68,11 +70,11 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
   uint64_t* res_full = bars;            // resident operand landed
   uint64_t* full = bars + 1;            // [OL_STAGES]
   uint64_t* empty = full + OL_STAGES;   // [OL_STAGES]
-  uint64_t* accf = empty + OL_STAGES;   // [2]
-  uint64_t* acce = accf + 2;            // [2]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(acce + 2);
-  float* red = reinterpret_cast<float*>(tslot + 4);                 // [2][128] (mx, s) of warpgroup 1
-  unsigned* relcnt = reinterpret_cast<unsigned*>(red + 2 * OL_M);   // [OL_STAGES] epilogue warps done
+  uint64_t* accf = empty + OL_STAGES;   // [OL_NBUF]
+  uint64_t* acce = accf + OL_NBUF;      // [OL_NBUF]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(acce + OL_NBUF);
+  float* red = reinterpret_cast<float*>(tslot + 4);                 // [3][2][128] (mx, s) of column groups 1-3
+  unsigned* relcnt = reinterpret_cast<unsigned*>(red + 6 * OL_M);   // [OL_STAGES] epilogue warps done
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r0 = blockIdx.x * OL_M;
   const int nsteps = P.col_tiles * P.k_tiles;  // streamed (tile, k-tile) steps
@@ -80,18 +82,18 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
   if (threadIdx.x == 0) {
     mbar_init(res_full, 1);
     for (int s = 0; s < OL_STAGES; ++s) { mbar_init(full + s, 1); mbar_init(empty + s, 1); }
-    for (int b = 0; b < 2; ++b) { mbar_init(accf + b, 1); mbar_init(acce + b, 8); }
+    for (int b = 0; b < OL_NBUF; ++b) { mbar_init(accf + b, 1); mbar_init(acce + b, OL_EPI); }
     for (int s2 = 0; s2 < OL_STAGES; ++s2) relcnt[s2] = 0u;
     fence_mbar_init();
     prefetch_tmap(&tAh); prefetch_tmap(&tAl); prefetch_tmap(&tBh); prefetch_tmap(&tBl);
   }
-  if (warp == 9) tmem_alloc(tslot, 2 * OL_N);
+  if (warp == OL_EPI + 1) tmem_alloc(tslot, OL_NBUF * OL_N);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
 
-  if (warp == 8) {
+  if (warp == OL_EPI) {
     // producer
     if (lane == 0) {
       mbar_arrive_expect_tx(res_full, 2 * OL_TILE * P.k_tiles);
@@ -120,15 +122,15 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
       const uint64_t t0 = globaltimer();
       while (!mbar_try_wait(res_full, 0)) if (globaltimer() - t0 > P.timeout_ns) break;
     }
-  } else if (warp == 9) {
-    // MMA issuer: one accumulator tile per streamed tile, alternating TMEM buffers
+  } else if (warp == OL_EPI + 1) {
+    // MMA issuer: one accumulator tile per streamed tile, TMEM buffers in turn
     if (lane == 0) {
       const uint32_t idesc = umma_idesc_f16(OL_M, OL_N, false);
       bool ok = mbar_wait(res_full, 0, P.abort_flag, P.timeout_ns);
       int q = 0, committed = 0;
       for (int tile = 0; tile < P.col_tiles && ok; ++tile) {
-        const int b = tile & 1;
-        if (!mbar_wait(acce + b, ((tile >> 1) & 1) ^ 1, P.abort_flag, P.timeout_ns)) break;
+        const int b = tile % OL_NBUF;
+        if (!mbar_wait(acce + b, ((tile / OL_NBUF) & 1) ^ 1, P.abort_flag, P.timeout_ns)) break;
         tc_fence_after();
         const uint32_t dst = tmem + (uint32_t)(b * OL_N);
         uint32_t acc = 0;
@@ -160,13 +162,13 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
       if (committed > 0) {
         const int c = committed - 1;
         const uint64_t t0 = globaltimer();
-        while (!mbar_try_wait(accf + (c & 1), (c >> 1) & 1)) if (globaltimer() - t0 > P.timeout_ns) break;
+        while (!mbar_try_wait(accf + (c % OL_NBUF), (c / OL_NBUF) & 1)) if (globaltimer() - t0 > P.timeout_ns) break;
       }
     }
   } else {
-    // epilogue: warps 0-3 (columns 0-63) and 4-7 (columns 64-127); lane
-    // quarter = warp % 4, row = r0 + 32 * (warp % 4) + lane
-    const int quarter = warp & 3, half = warp >> 2;
+    // epilogue: warp w reads TMEM lane quarter w % 4 (rows 32 (w % 4) + lane)
+    // and columns 32 (w / 4) .. +31 of each tile
+    const int quarter = warp & 3, cgrp = warp >> 2;
     const int row_local = quarter * 32 + lane;
     // running (max, sum) per row; the sum is Kahan-compensated (sc) and each
     // tile adds one partial sum of 32 terms, so rounding does not grow with
@@ -174,8 +176,8 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
     float mx = -INFINITY, sm = 0.f, sc = 0.f;
     int ok = 1;
     for (int tile = 0; tile < P.col_tiles && ok; ++tile) {
-      const int b = tile & 1;
-      if (lane == 0) ok = (mbar_wait(accf + b, (tile >> 1) & 1, P.abort_flag, P.timeout_ns) &&
+      const int b = tile % OL_NBUF;
+      if (lane == 0) ok = (mbar_wait(accf + b, (tile / OL_NBUF) & 1, P.abort_flag, P.timeout_ns) &&
                            !*(volatile int*)P.abort_flag) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       __syncwarp();
@@ -184,10 +186,9 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
       // the last k-step's stage holds this tile's h slice
       const int qlast = tile * P.k_tiles + P.k_tiles - 1;
       const float* h = hbuf + (qlast % OL_STAGES) * OL_N;
-#pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 32) {
+      {
         float v[32];
-        const int col = half * 64 + c0;
+        const int col = cgrp * 32;
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * OL_N + col), v);
         float t[32];
         float gm = -INFINITY;
@@ -212,17 +213,17 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
       __syncwarp();
       if (lane == 0) {
         mbar_arrive(acce + b);
-        // the tile's last stage (its h slice) is released once all 8
+        // the tile's last stage (its h slice) is released once all
         // epilogue warps have read it
         const int s = qlast % OL_STAGES;
-        if (atomicAdd(relcnt + s, 1u) == 7u) { atomicExch(relcnt + s, 0u); mbar_arrive(empty + s); }
+        if (atomicAdd(relcnt + s, 1u) == (unsigned)(OL_EPI - 1)) { atomicExch(relcnt + s, 0u); mbar_arrive(empty + s); }
       }
     }
-    // merge the two column halves of each row
-    if (half == 1) { red[row_local] = mx; red[OL_M + row_local] = sm; }
-    named_bar(1, 256);
-    if (half == 0 && ok) {
-      lse_merge(mx, sm, red[row_local], red[OL_M + row_local]);
+    // merge the four column groups of each row
+    if (cgrp > 0) { red[(cgrp - 1) * 2 * OL_M + row_local] = mx; red[(cgrp - 1) * 2 * OL_M + OL_M + row_local] = sm; }
+    named_bar(1, OL_EPI * 32);
+    if (cgrp == 0 && ok) {
+      for (int g = 0; g < 3; ++g) lse_merge(mx, sm, red[g * 2 * OL_M + row_local], red[g * 2 * OL_M + OL_M + row_local]);
       const int row = r0 + row_local;
       if (row < P.n_rows) {
         const float L = lse_value(mx, sm) + P.rterm[row];  // base-2 LSE_j(g2_j - C_ij log2e/reg)
@@ -240,9 +241,9 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 9) {
+  if (warp == OL_EPI + 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, 2 * OL_N);
+    tmem_dealloc(tmem, OL_NBUF * OL_N);
   }
 }
 
@@ -321,7 +322,7 @@ bool ol_plane_map(CUtensorMap* m, const void* base, int64_t rows, int64_t ld) {
 }
 
 constexpr size_t OL_SMEM = (size_t)OL_MAXKT * 2 * OL_TILE + (size_t)OL_STAGES * OL_STAGE + OL_STAGES * OL_HVEC +
-                           1024 /*align*/ + 256 /*barriers*/ + 2 * OL_M * 4 /*red*/ + 64 /*counters*/;
+                           1024 /*align*/ + 256 /*barriers*/ + 6 * OL_M * 4 /*red*/ + 64 /*counters*/;
 
 size_t a16(size_t x) { return (x + 255) / 256 * 256; }
 

@@ -115,7 +115,10 @@ def cell_masses(X, centres):
     return w
 
 
-def coarse_potential(X, Y, maxc, reg_rel=0.02, k=128, tol=1e-5, taus=None):
+COARSE_TOL = 1e-3  # coarse-problem stop: tighter costs time and saves no fine iterations (measured)
+
+
+def coarse_potential(X, Y, maxc, reg_rel=0.02, k=128, tol=COARSE_TOL, taus=None):
     """Multiscale prior: the first k points of each cloud (the points are
     i.i.d., so a random sample) become atoms weighted by the exact mass of
     their Voronoi cells in the full cloud; that coarse problem is solved and
@@ -170,7 +173,7 @@ def _head_inputs(Xn, F):
     return torch.cat([Xn, F], 2).contiguous()
 
 
-def predict(net, X, Y, maxc, F, chunk=64):
+def predict(net, X, Y, maxc, F, chunk=1024):
     """Network output: the centred residual over the coarse prior
     (max-normalised cost units)."""
     out = []

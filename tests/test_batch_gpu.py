@@ -185,3 +185,59 @@ def test_solve_gromov_batch(cuda, name):
     np.testing.assert_allclose(res.value_quad, ref["value_quad"], rtol=1e-7, atol=1e-13)
     np.testing.assert_allclose(res.plan, g["plan"], atol=1e-5)
     np.testing.assert_allclose(res.value, g["value"], atol=1e-4)
+
+
+@pytest.mark.parametrize("d", [2, 3, 8, 16, 5])
+def test_cost_blocks_register_tiled(cuda, d):
+    """float32 cost blocks of a ragged batch with a shared dimension (the
+    register-tiled kernel for d in {2, 3, 8, 16}, the generic one for 5):
+    sum_k (x_k - y_k)^2 against float64, +inf padding, per-problem maxima."""
+    rng = np.random.default_rng(d)
+    rows, cols = [1, 63, 64, 65, 300, 2048], [1, 255, 257, 64, 1000, 2048]
+    X = [rng.standard_normal((n, d)) for n in rows]
+    Y = [rng.standard_normal((m, d)) + 0.5 for m in cols]
+    layout = pb.RaggedLayout(rows, cols, torch.float32, cuda)
+    xo = np.concatenate([[0], np.cumsum([n * d for n in rows])[:-1]])
+    yo = np.concatenate([[0], np.cumsum([m * d for m in cols])[:-1]])
+    Xp = torch.tensor(np.concatenate([x.ravel() for x in X]), dtype=torch.float32, device=cuda)
+    Yp = torch.tensor(np.concatenate([y.ravel() for y in Y]), dtype=torch.float32, device=cuda)
+    M, mx = pb.batched_sqdist(layout, Xp, Yp, xo, yo, [d] * len(rows), want_max=True)
+    M = M.cpu().numpy()
+    mx = mx.cpu().numpy()
+    for p, (n, m) in enumerate(zip(rows, cols)):
+        ld = int(layout.ldm_np[p])
+        blk = M[int(layout.m_off_np[p]):int(layout.m_off_np[p]) + n * ld].reshape(n, ld)
+        x32 = X[p].astype(np.float32).astype(np.float64)
+        y32 = Y[p].astype(np.float32).astype(np.float64)
+        ref = ((x32[:, None, :] - y32[None, :, :]) ** 2).sum(-1)
+        np.testing.assert_allclose(blk[:, :m], ref, rtol=2e-6, atol=1e-6)
+        assert np.all(np.isinf(blk[:, m:]))
+        assert abs(mx[p] - ref.max()) <= 2e-6 * ref.max()
+
+
+def test_multi_tail_launch_matches_single_launch(cuda):
+    """Problems still running after `tail_after` iterations continue in a
+    second, smaller launch; the result equals one launch (float64)."""
+    rng = np.random.default_rng(77)
+    B = 12
+    rows = rng.integers(20, 90, B)
+    cols = rng.integers(20, 90, B)
+    layout = pb.RaggedLayout(rows, cols, torch.float64, cuda)
+    Ms = []
+    for n, m in zip(rows, cols):
+        x = rng.random((n, 2))
+        y = rng.random((m, 2))
+        M = oracle.sqeuclidean(x, y)
+        Ms.append(torch.tensor(M / M.max(), device=cuda))
+    Mp = pb.pack_dense(layout, Ms)
+    a = torch.cat([torch.full((int(n),), 1.0 / n, dtype=torch.float64, device=cuda) for n in rows])
+    b = torch.cat([torch.full((int(m),), 1.0 / m, dtype=torch.float64, device=cuda) for m in cols])
+    reg = torch.tensor(10.0 ** rng.uniform(-2.5, -1, B), dtype=torch.float64)
+    one = pb.run_multi(layout, Mp, a, b, reg, 5000, 1e-9, tail_after=0)
+    two = pb.run_multi(layout, Mp, a, b, reg, 5000, 1e-9, tail_after=100)
+    n1, n2 = one[3].cpu().numpy(), two[3].cpu().numpy()
+    assert (n1 > 100).any() and (n1 < 100).any()
+    np.testing.assert_array_equal(n1, n2)
+    np.testing.assert_array_equal(one[2].cpu().numpy(), two[2].cpu().numpy())
+    np.testing.assert_allclose(two[0].cpu().numpy(), one[0].cpu().numpy(), rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(two[1].cpu().numpy(), one[1].cpu().numpy(), rtol=1e-9, atol=1e-9)
