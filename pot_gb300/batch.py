@@ -119,89 +119,23 @@ def run_batched(layout, M_packed, a_packed, b_packed, reg, method, max_iter, tol
     return out_u, out_v, status, niter, err, reg_t
 
 
-TAIL_AFTER = 200          # iterations of the full-grid launch before the slow problems move on
-TAIL_GROWTH = 10          # each later launch runs up to this factor more iterations
-TAIL_BYTES_PER_CTA = 256 << 10
-TAIL_MIN_GRID = 16
-
-
 def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-              events=None, tail_after=TAIL_AFTER):
+              events=None):
     """Work-balanced persistent launch (csrc/multi.cu), log form, per-problem
-    sinkhorn_log order and stop test.  Returns (u, v, status, niter, err, reg).
-
-    Problems still running after `tail_after` iterations (a multiple of 10,
-    so the every-10th-iteration checks stay aligned) continue in further
-    launches over only those problems (after 10x, 100x, ... as many
-    iterations), warm-started from their potentials, each on a grid sized to
-    the bytes still being iterated: a long tail of a few slow problems is
-    then paced by cheap grid barriers over few CTAs instead of all of them."""
-    if tail_after and max_iter > tail_after and layout.B > 1:
-        return _run_multi_staged(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u, grid, timeout_ms,
-                                 events, tail_after)
+    sinkhorn_log order and stop test.  Returns (u, v, status, niter, err, reg)."""
     return _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u, grid, timeout_ms,
                            events)
 
 
-class _SubLayout:
-    """A subset of a layout's problems over the same packed buffers."""
-
-    def __init__(self, layout, idx):
-        it = torch.as_tensor(idx, dtype=torch.int64, device=layout.device)
-        self.device, self.dtype, self.B = layout.device, layout.dtype, len(idx)
-        for name in ("m_off", "rows", "cols", "ldm", "r_off", "c_off", "nsr_max", "pc_off"):
-            setattr(self, name, getattr(layout, name).index_select(0, it).contiguous())
-        self.total_r, self.total_c, self.total_partials = layout.total_r, layout.total_c, layout.total_partials
-
-
-def _run_multi_staged(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u, grid, timeout_ms, events,
-                      tail_after):
-    K = tail_after - tail_after % 10
-    u, v, status, niter, err, reg_t = _run_multi_once(layout, M_packed, a_packed, b_packed, reg, K, tol, warm_u,
-                                                      grid, timeout_ms, events)
-    done = K
-    es = 4 if layout.dtype == torch.float32 else 8
-    while done < max_iter:
-        idx = np.nonzero(status.cpu().numpy() == _lib.STATUS_MAXITER)[0]
-        if len(idx) == 0:
-            break
-        span = min(max_iter - done, done * (TAIL_GROWTH - 1))  # a multiple of 10 unless it is the last
-        sub = _SubLayout(layout, idx)
-        work = int((layout.rows_np[idx].astype(np.int64) * layout.ldm_np[idx]).sum()) * es
-        g = max(TAIL_MIN_GRID, -(-work // TAIL_BYTES_PER_CTA))
-        if grid:
-            g = min(g, grid)
-        it = torch.as_tensor(idx, dtype=torch.int64, device=layout.device)
-        u2, v2, s2, n2, e2, _ = _run_multi_once(sub, M_packed, a_packed, b_packed, reg_t.index_select(0, it), span,
-                                                tol, u.clone(), g, timeout_ms, None, ws_layout=layout)
-        # the launch wrote its problems' potentials into its own buffers at the same offsets
-        rmask = np.zeros(layout.total_r, dtype=bool)
-        cmask = np.zeros(layout.total_c, dtype=bool)
-        for p in idx:
-            r0, c0 = int(layout.r_off_np[p]), int(layout.c_off_np[p])
-            rmask[r0:r0 + int(layout.rows_np[p])] = True
-            cmask[c0:c0 + int(layout.cols_np[p])] = True
-        u = torch.where(torch.from_numpy(rmask).to(layout.device), u2, u)
-        v = torch.where(torch.from_numpy(cmask).to(layout.device), v2, v)
-        # a problem that hits this launch's limit keeps MAXITER; the last launch's limit is max_iter
-        status.index_copy_(0, it, s2)
-        niter.index_copy_(0, it, n2 + done)
-        err.index_copy_(0, it, e2)
-        done += span
-    if events is not None:
-        events[1].record()
-    return u, v, status, niter, err, reg_t
-
-
 def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-                    events=None, ws_layout=None):
+                    events=None):
     lib = _lib.load()
     dev, dt = layout.device, layout.dtype
     B = layout.B
     reg_t = torch.as_tensor(reg, dtype=torch.float64, device=dev).reshape(-1)
     if reg_t.numel() == 1:
         reg_t = reg_t.expand(B).contiguous()
-    if ws_layout is None and not hasattr(layout, "pc_off"):
+    if not hasattr(layout, "pc_off"):
         nsr_max = np.maximum(1, np.minimum(64, (layout.rows_np + 15) // 16)).astype(np.int32)
         sizes = nsr_max.astype(np.int64) * layout.cols_np
         layout.nsr_max_np = nsr_max

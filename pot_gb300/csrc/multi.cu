@@ -324,9 +324,12 @@ __device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leavi
     atomicAdd(reinterpret_cast<unsigned long long*>(&s_slabs), (unsigned long long)part);
   }
   __syncthreads();
-  // capped at 16 chunks: more splits only lengthen the merge
+  // capped at 16 chunks while the batch fills the GPU (more splits only
+  // lengthen the merge); a few remaining problems split up to 64 ways, since
+  // then the time per pass is that of one unit
   int64_t S = s_slabs > 0 ? (8 * nwarps + s_slabs - 1) / s_slabs : 1;
-  S = S > 16 ? 16 : S;
+  const int64_t cap = s_slabs * 16 >= nwarps ? 16 : 64;
+  S = S > cap ? cap : S;
   for (int k = threadIdx.x; k < s_base; k += blockDim.x) {
     const int p = A.active[k];
     const int n = A.rows[p];

@@ -214,30 +214,3 @@ def test_cost_blocks_register_tiled(cuda, d):
         assert np.all(np.isinf(blk[:, m:]))
         assert abs(mx[p] - ref.max()) <= 2e-6 * ref.max()
 
-
-def test_multi_tail_launch_matches_single_launch(cuda):
-    """Problems still running after `tail_after` iterations continue in a
-    second, smaller launch; the result equals one launch (float64)."""
-    rng = np.random.default_rng(77)
-    B = 12
-    rows = rng.integers(20, 90, B)
-    cols = rng.integers(20, 90, B)
-    layout = pb.RaggedLayout(rows, cols, torch.float64, cuda)
-    Ms = []
-    for n, m in zip(rows, cols):
-        x = rng.random((n, 2))
-        y = rng.random((m, 2))
-        M = oracle.sqeuclidean(x, y)
-        Ms.append(torch.tensor(M / M.max(), device=cuda))
-    Mp = pb.pack_dense(layout, Ms)
-    a = torch.cat([torch.full((int(n),), 1.0 / n, dtype=torch.float64, device=cuda) for n in rows])
-    b = torch.cat([torch.full((int(m),), 1.0 / m, dtype=torch.float64, device=cuda) for m in cols])
-    reg = torch.tensor(10.0 ** rng.uniform(-2.5, -1, B), dtype=torch.float64)
-    one = pb.run_multi(layout, Mp, a, b, reg, 5000, 1e-9, tail_after=0)
-    two = pb.run_multi(layout, Mp, a, b, reg, 5000, 1e-9, tail_after=100)
-    n1, n2 = one[3].cpu().numpy(), two[3].cpu().numpy()
-    assert (n1 > 100).any() and (n1 < 100).any()
-    np.testing.assert_array_equal(n1, n2)
-    np.testing.assert_array_equal(one[2].cpu().numpy(), two[2].cpu().numpy())
-    np.testing.assert_allclose(two[0].cpu().numpy(), one[0].cpu().numpy(), rtol=1e-9, atol=1e-9)
-    np.testing.assert_allclose(two[1].cpu().numpy(), one[1].cpu().numpy(), rtol=1e-9, atol=1e-9)
