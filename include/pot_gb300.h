@@ -242,6 +242,11 @@ typedef struct OtgMultiProblem {
   void* workspace;
   size_t workspace_bytes;
   int32_t timeout_ms;
+  /* over-relaxation of the potential updates, f <- (1 - omega) f + omega f_new
+   * (1 or 0: plain Sinkhorn, the reference's iteration).  No reference
+   * counterpart: used by the warm-start refinement; the stop test is still the
+   * exact column-marginal error of the iterate. */
+  double omega;
 } OtgMultiProblem;
 size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, int64_t total_cols,
                                  int64_t total_partials);

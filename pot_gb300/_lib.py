@@ -44,7 +44,7 @@ class OtgMultiProblem(ctypes.Structure):
                 ("reg", c_vp), ("max_iter", c_i32), ("grid", c_i32), ("stop_thr", c_dbl), ("nsr_max", c_vp),
                 ("pc_off", c_vp), ("total_rows", c_i64), ("total_cols", c_i64), ("total_partials", c_i64),
                 ("out_u", c_vp), ("out_v", c_vp), ("status", c_vp), ("niter", c_vp), ("err", c_vp),
-                ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32)]
+                ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32), ("omega", c_dbl)]
 
 
 class OtgCostTable(ctypes.Structure):

@@ -120,15 +120,17 @@ def run_batched(layout, M_packed, a_packed, b_packed, reg, method, max_iter, tol
 
 
 def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-              events=None):
+              events=None, omega=1.0):
     """Work-balanced persistent launch (csrc/multi.cu), log form, per-problem
-    sinkhorn_log order and stop test.  Returns (u, v, status, niter, err, reg)."""
+    sinkhorn_log order and stop test.  Returns (u, v, status, niter, err, reg).
+    ``omega != 1`` over-relaxes the potential updates (no reference
+    counterpart; the stop test is unchanged)."""
     return _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u, grid, timeout_ms,
-                           events)
+                           events, omega)
 
 
 def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-                    events=None):
+                    events=None, omega=1.0):
     lib = _lib.load()
     dev, dt = layout.device, layout.dtype
     B = layout.B
@@ -158,7 +160,8 @@ def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, wa
         grid=int(grid), stop_thr=float(tol), nsr_max=layout.nsr_max.data_ptr(), pc_off=layout.pc_off.data_ptr(),
         total_rows=layout.total_r, total_cols=layout.total_c, total_partials=layout.total_partials,
         out_u=out_u.data_ptr(), out_v=out_v.data_ptr(), status=status.data_ptr(), niter=niter.data_ptr(),
-        err=err.data_ptr(), workspace=ws.data_ptr(), workspace_bytes=wsb, timeout_ms=int(timeout_ms))
+        err=err.data_ptr(), workspace=ws.data_ptr(), workspace_bytes=wsb, timeout_ms=int(timeout_ms),
+        omega=float(omega))
     if events is not None:
         events[0].record()
     _lib.check(lib.otg_sinkhorn_multi(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_multi")

@@ -65,6 +65,8 @@ struct MultiArgs {
   T* out_u; T* out_v;
   int32_t* status; int32_t* niter; double* err;
   uint64_t timeout_ns;
+  T omega;                  // over-relaxation (1: plain)
+  bool relax;
 };
 
 // Index of the active slot whose prefix range holds `unit` (pre[k] <= unit < pre[k+1]).
@@ -174,7 +176,7 @@ __device__ void mt_col_pass(const MultiArgs<T>& A, int nact, long gwarp, long nw
 // squared marginal error of (u_cur, v_cur) is accumulated when `check`.
 template <typename T>
 __device__ void mt_col_merge(const MultiArgs<T>& A, int nact, const T* vcur, T* vnxt, bool check, bool update,
-                             long gtid, long nthreads) {
+                             long gtid, long nthreads, bool relax_v) {
   const int64_t total = __ldcg(A.colpre + nact);
   // each warp takes a contiguous range of columns, its lanes adjacent ones
   const long w = gtid >> 5, nw = nthreads >> 5;
@@ -212,7 +214,10 @@ __device__ void mt_col_merge(const MultiArgs<T>& A, int nact, const T* vcur, T* 
       }
       if ((threadIdx.x & 31) == leader) atomicAdd(A.err2 + p, e2);
     }
-    if (update) vnxt[cj] = lg2(bj) - L;
+    if (update) {
+      const T vn = lg2(bj) - L;
+      vnxt[cj] = relax_v ? fma(A.omega, vn - __ldcg(vcur + cj), __ldcg(vcur + cj)) : vn;
+    }
   }
 }
 
@@ -277,7 +282,8 @@ __device__ void mt_row_pass(const MultiArgs<T>& A, int nact, const T* v, long gw
     for (int r = 0; r < MT_RW; ++r) {
       if (lane == r && r0 + r < n) {
         const int64_t ri = A.r_off[p] + r0 + r;
-        A.u[ri] = lg2(A.a[ri]) - lse_value(mx[r], s[r]);
+        const T un = lg2(A.a[ri]) - lse_value(mx[r], s[r]);
+        A.u[ri] = A.relax ? fma(A.omega, un - __ldcg(A.u + ri), __ldcg(A.u + ri)) : un;
       }
     }
   }
@@ -405,7 +411,8 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
     }
     mt_col_pass<T>(A, nact, gwarp, nwarps, lane);
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
-    mt_col_merge<T>(A, nact, vcur, vnxt, prev_check, ii < A.max_iter, gtid, nthreads);
+    // the first v comes from u alone (v0 is not an iterate): relaxed from the second on
+    mt_col_merge<T>(A, nact, vcur, vnxt, prev_check, ii < A.max_iter, gtid, nthreads, A.relax && ii > 0);
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     if (decide) {
       // decide per problem, write out the leaving ones (state of iteration ii-1)
@@ -458,6 +465,8 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   A.out_u = static_cast<T*>(q->out_u); A.out_v = static_cast<T*>(q->out_v);
   A.status = q->status; A.niter = q->niter; A.err = q->err;
   A.timeout_ns = q->timeout_ms > 0 ? (uint64_t)q->timeout_ms * 1000000ull : 4000000000ull;
+  A.relax = q->omega != 0.0 && q->omega != 1.0;
+  A.omega = (T)q->omega;
   // carve the workspace
   char* w = static_cast<char*>(q->workspace);
   size_t off = 0;

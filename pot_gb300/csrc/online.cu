@@ -23,6 +23,7 @@
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 #include "common.cuh"
 #include "tma.cuh"
@@ -56,6 +57,12 @@ struct OnlinePass {
   double* err;         // L1 accumulation (check passes) or null
   int* abort_flag;
   uint64_t timeout_ns;
+  // column split: CTA (b, s) streams tiles [s T / S, (s + 1) T / S) and, with
+  // S > 1, leaves its per-row (max, sum) in part[s][2][rows_pad] for
+  // online_finalize_kernel
+  int split;
+  int rows_pad;
+  float* part;
 };
 
 __global__ void __launch_bounds__(OL_THREADS, 1)
@@ -77,7 +84,10 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
   unsigned* relcnt = reinterpret_cast<unsigned*>(red + 6 * OL_M);   // [OL_STAGES] epilogue warps done
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r0 = blockIdx.x * OL_M;
-  const int nsteps = P.col_tiles * P.k_tiles;  // streamed (tile, k-tile) steps
+  const int cs = blockIdx.y;
+  const int t0 = (int)((int64_t)cs * P.col_tiles / P.split), t1 = (int)((int64_t)(cs + 1) * P.col_tiles / P.split);
+  const int ntl = t1 - t0;                     // this CTA's streamed tiles
+  const int nsteps = ntl * P.k_tiles;          // streamed (tile, k-tile) steps
 
   if (threadIdx.x == 0) {
     mbar_init(res_full, 1);
@@ -105,7 +115,7 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
       for (int q = 0; q < nsteps; ++q) {
         const int s = q % OL_STAGES;
         if (!mbar_wait(empty + s, ((q / OL_STAGES) & 1u) ^ 1u, P.abort_flag, P.timeout_ns)) break;
-        const int tile = q / P.k_tiles, kt = q % P.k_tiles;
+        const int tile = t0 + q / P.k_tiles, kt = q % P.k_tiles;
         unsigned char* st = ring + s * OL_STAGE;
         mbar_arrive_expect_tx(full + s, 2 * OL_TILE + OL_HVEC);
         tma_load_2d(st, &tBh, kt * OL_K, tile * OL_N, full + s);
@@ -128,7 +138,7 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
       const uint32_t idesc = umma_idesc_f16(OL_M, OL_N, false);
       bool ok = mbar_wait(res_full, 0, P.abort_flag, P.timeout_ns);
       int q = 0, committed = 0;
-      for (int tile = 0; tile < P.col_tiles && ok; ++tile) {
+      for (int tile = 0; tile < ntl && ok; ++tile) {
         const int b = tile % OL_NBUF;
         if (!mbar_wait(acce + b, ((tile / OL_NBUF) & 1) ^ 1, P.abort_flag, P.timeout_ns)) break;
         tc_fence_after();
@@ -175,7 +185,7 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
     // the number of streamed points
     float mx = -INFINITY, sm = 0.f, sc = 0.f;
     int ok = 1;
-    for (int tile = 0; tile < P.col_tiles && ok; ++tile) {
+    for (int tile = 0; tile < ntl && ok; ++tile) {
       const int b = tile % OL_NBUF;
       if (lane == 0) ok = (mbar_wait(accf + b, (tile / OL_NBUF) & 1, P.abort_flag, P.timeout_ns) &&
                            !*(volatile int*)P.abort_flag) ? 1 : 0;
@@ -225,7 +235,10 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
     if (cgrp == 0 && ok) {
       for (int g = 0; g < 3; ++g) lse_merge(mx, sm, red[g * 2 * OL_M + row_local], red[g * 2 * OL_M + OL_M + row_local]);
       const int row = r0 + row_local;
-      if (row < P.n_rows) {
+      if (P.split > 1) {
+        P.part[((size_t)cs * 2) * P.rows_pad + row] = mx;
+        P.part[((size_t)cs * 2 + 1) * P.rows_pad + row] = sm;
+      } else if (row < P.n_rows) {
         const float L = lse_value(mx, sm) + P.rterm[row];  // base-2 LSE_j(g2_j - C_ij log2e/reg)
         const float pnew = P.logw2[row] - L;
         P.pot_out2[row] = pnew;
@@ -244,6 +257,39 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
   if (warp == OL_EPI + 1) {
     tc_fence_after();
     tmem_dealloc(tmem, OL_NBUF * OL_N);
+  }
+}
+
+// Column-split passes: merge the S partial (max, sum) pairs of each row and
+// apply the potential update of the pass's epilogue; the check error is
+// reduced per block (one atomic per block).
+__global__ void __launch_bounds__(256) online_finalize_kernel(OnlinePass P) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  double e = 0.0;
+  if (row < P.rows_pad) {
+    if (row < P.n_rows) {
+      float mx = -INFINITY, sm = 0.f;
+      for (int c = 0; c < P.split; ++c)
+        lse_merge(mx, sm, P.part[((size_t)c * 2) * P.rows_pad + row], P.part[((size_t)c * 2 + 1) * P.rows_pad + row]);
+      const float L = lse_value(mx, sm) + P.rterm[row];
+      const float pnew = P.logw2[row] - L;
+      if (P.err) e = fabs((double)ex2(P.pot2[row] + L) - (double)P.w[row]);
+      P.pot_out2[row] = pnew;
+      P.h_out[row] = pnew - P.other_norm2[row];
+    } else {
+      P.h_out[row] = -INFINITY;
+    }
+  }
+  if (P.err) {
+    __shared__ double red[8];
+    e = warp_sum(e);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+      atomicAdd(P.err, t);
+    }
   }
 }
 
@@ -326,6 +372,24 @@ constexpr size_t OL_SMEM = (size_t)OL_MAXKT * 2 * OL_TILE + (size_t)OL_STAGES * 
 
 size_t a16(size_t x) { return (x + 255) / 256 * 256; }
 
+constexpr int OL_MAX_SPLIT = 8;
+
+// Column split for a pass of `nb` row blocks over `tiles` streamed tiles:
+// the S in 1..8 whose grid (nb x S CTAs, one per SM at a time) loses the
+// least to its last partial wave, keeping at least 32 tiles per CTA (fewer
+// lose more to the pipeline's fill and drain than the wave gains; measured).
+int choose_split(int nb, int tiles, int sms) {
+  int best = 1;
+  double best_eff = 0.0;
+  for (int S = 1; S <= OL_MAX_SPLIT; ++S) {
+    if (S > 1 && tiles / S < 32) break;
+    const double waves = (double)nb * S / sms;
+    const double eff = waves / std::ceil(waves);
+    if (eff > best_eff + 0.02) { best_eff = eff; best = S; }
+  }
+  return best;
+}
+
 }  // namespace
 
 extern "C" {
@@ -338,6 +402,7 @@ size_t otg_online_workspace_bytes(int64_t n, int64_t m, int32_t d) {
   b += 5 * a16(4 * np) + 4 * a16(4 * mp);                    // norms, log2 w, potentials, h
   b += a16(8 * 64);                                          // err slots, flag
   b += a16(4 * np) + a16(4 * mp);                            // negated norms
+  b += a16(4 * 2 * (size_t)OL_MAX_SPLIT * (size_t)std::max(np, mp));  // column-split partials
   return b;
 }
 
@@ -392,7 +457,22 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
   // row terms as separate buffers: -xn2, -yn2
   float* nx = reinterpret_cast<float*>(take(4 * np));
   float* ny = reinterpret_cast<float*>(take(4 * mp));
+  float* part = reinterpret_cast<float*>(take(4 * 2 * (size_t)OL_MAX_SPLIT * (size_t)std::max(np, mp)));
   if (off > p->workspace_bytes) return OTG_ERR_WORKSPACE;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int split_f = choose_split((int)(np / OL_M), (int)(mp / OL_N), sms);
+  const int split_g = choose_split((int)(mp / OL_M), (int)(np / OL_N), sms);
+  // one pass: the pass kernel over (row blocks x column split), then, when
+  // split, the merge of the partials
+  auto pass = [&](OnlinePass& P, const CUtensorMap& ah, const CUtensorMap& al, const CUtensorMap& bh,
+                  const CUtensorMap& bl, int64_t rows_pad, int split) {
+    P.split = split; P.rows_pad = (int)rows_pad; P.part = part;
+    online_pass_kernel<<<dim3((unsigned)(rows_pad / OL_M), (unsigned)split), OL_THREADS, OL_SMEM, st>>>(ah, al, bh,
+                                                                                                       bl, P);
+    if (split > 1) online_finalize_kernel<<<(unsigned)((rows_pad + 255) / 256), 256, 0, st>>>(P);
+  };
   neg_kernel<<<256, 256, 0, st>>>(xn2, n, nx);
   neg_kernel<<<256, 256, 0, st>>>(yn2, m, ny);
   const float alpha = (float)(2.0 * OTG_LOG2E / (p->reg * (double)sx * (double)sy));
@@ -407,7 +487,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     A.n_rows = (int)n; A.col_tiles = (int)(mp / OL_N); A.k_tiles = dp / OL_K; A.alpha = alpha;
     A.h = hy; A.rterm = nx; A.logw2 = la2; A.pot2 = f2[cur]; A.w = p->a; A.pot_out2 = f2[cur ^ 1];
     A.other_norm2 = xn2; A.h_out = hx; A.err = check ? eslot : nullptr; A.abort_flag = flag; A.timeout_ns = tmo;
-    online_pass_kernel<<<(unsigned)(np / OL_M), OL_THREADS, OL_SMEM, st>>>(mxh, mxl, myh, myl, A);
+    pass(A, mxh, mxl, myh, myl, np, split_f);
     if (check) {
       double e = 0;
       if (cudaMemcpyAsync(&e, eslot, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return OTG_ERR_CUDA;
@@ -422,7 +502,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     B.n_rows = (int)m; B.col_tiles = (int)(np / OL_N); B.k_tiles = dp / OL_K; B.alpha = alpha;
     B.h = hx; B.rterm = ny; B.logw2 = lb2; B.pot2 = g2; B.w = p->b; B.pot_out2 = g2;
     B.other_norm2 = yn2; B.h_out = hy; B.err = nullptr; B.abort_flag = flag; B.timeout_ns = tmo;
-    online_pass_kernel<<<(unsigned)(mp / OL_M), OL_THREADS, OL_SMEM, st>>>(myh, myl, mxh, mxl, B);
+    pass(B, myh, myl, mxh, mxl, mp, split_g);
     if (cudaGetLastError() != cudaSuccess) return OTG_ERR_CUDA;
   }
   // a last check at max_iter when (max_iter) % 10 == 0 is done by the next f pass
@@ -433,7 +513,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     A.n_rows = (int)n; A.col_tiles = (int)(mp / OL_N); A.k_tiles = dp / OL_K; A.alpha = alpha;
     A.h = hy; A.rterm = nx; A.logw2 = la2; A.pot2 = f2[cur]; A.w = p->a; A.pot_out2 = f2[cur ^ 1];
     A.other_norm2 = xn2; A.h_out = hx; A.err = eslot; A.abort_flag = flag; A.timeout_ns = tmo;
-    online_pass_kernel<<<(unsigned)(np / OL_M), OL_THREADS, OL_SMEM, st>>>(mxh, mxl, myh, myl, A);
+    pass(A, mxh, mxl, myh, myl, np, split_f);
     double e = 0;
     cudaMemcpyAsync(&e, eslot, 8, cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);

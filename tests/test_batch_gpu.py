@@ -214,3 +214,31 @@ def test_cost_blocks_register_tiled(cuda, d):
         assert np.all(np.isinf(blk[:, m:]))
         assert abs(mx[p] - ref.max()) <= 2e-6 * ref.max()
 
+
+
+def test_multi_over_relaxed_reaches_the_same_solution(cuda):
+    """omega != 1 over-relaxes the updates (warm-start refinement): the stop
+    test is the same exact marginal error, so the result is the plain solve's
+    solution to within the tolerance, reached in fewer iterations."""
+    rng = np.random.default_rng(9)
+    B = 6
+    rows = rng.integers(40, 120, B)
+    cols = rng.integers(40, 120, B)
+    layout = pb.RaggedLayout(rows, cols, torch.float64, cuda)
+    Ms = []
+    for n, m in zip(rows, cols):
+        M = oracle.sqeuclidean(rng.random((n, 3)), rng.random((m, 3)))
+        Ms.append(torch.tensor(M / M.max(), device=cuda))
+    Mp = pb.pack_dense(layout, Ms)
+    a = torch.cat([torch.full((int(n),), 1.0 / n, dtype=torch.float64, device=cuda) for n in rows])
+    b = torch.cat([torch.full((int(m),), 1.0 / m, dtype=torch.float64, device=cuda) for m in cols])
+    reg = 0.02
+    plain = pb.run_multi(layout, Mp, a, b, reg, 20000, 1e-12)
+    relax = pb.run_multi(layout, Mp, a, b, reg, 20000, 1e-12, omega=1.5)
+    assert (relax[2] == 0).all() and (plain[2] == 0).all()
+    assert relax[3].sum() < plain[3].sum()
+    for p in range(B):
+        r0, n = int(layout.r_off_np[p]), int(rows[p])
+        up, ur = plain[0][r0:r0 + n], relax[0][r0:r0 + n]
+        # potentials are defined up to a constant shared by u and -v
+        np.testing.assert_allclose((ur - ur.mean()).cpu().numpy(), (up - up.mean()).cpu().numpy(), atol=1e-6)
