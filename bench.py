@@ -28,6 +28,50 @@ import time
 
 import numpy as np
 
+# ---------------------------------------------------------------------------
+# replicas: under torchrun every rank solves its own batch on its own GPU (the
+# pairs are independent, so nothing is exchanged on the data path); ranks only
+# meet at barriers around the timed regions and to take the slowest time.
+# ---------------------------------------------------------------------------
+_WS = {"rank": 0, "world": 1, "local": 0}
+
+
+def replica_setup(backend=None):
+    """Join the process group when launched with WORLD_SIZE > 1 (nccl with
+    GPUs, gloo without, unless `backend` says); returns (rank, world,
+    local_rank)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = backend or ("nccl" if torch.cuda.is_available() else "gloo")
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+    _WS.update(rank=rank, world=world, local=local)
+    return rank, world, local
+
+
+def replica_barrier():
+    if _WS["world"] > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def replica_max(x):
+    """Largest value of `x` over the ranks (the slowest replica's time)."""
+    if _WS["world"] == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", _WS["local"]) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
@@ -104,9 +148,10 @@ def run_warmstart(args, pk):
     from pot_gb300 import _lib
     from pot_gb300.warmstart import pipeline as wp
 
-    dev = torch.device("cuda:0")
+    dev = torch.device("cuda", _WS["local"])
     B = args.batch
-    X, Y = wp.gen_pairs(EVAL_SEED, B, WS_N, WS_D, dev)
+    # each replica solves its own held-out pairs
+    X, Y = wp.gen_pairs(EVAL_SEED + _WS["rank"] * B, B, WS_N, WS_D, dev)
     net = wp.default_net(dev)
     st = torch.cuda.current_stream()
 
@@ -132,8 +177,10 @@ def run_warmstart(args, pk):
             step(arm)
     torch.cuda.synchronize()
     res = {}
-    with ClockSampler() as cs:
+    with ClockSampler(_WS["local"]) as cs:
         for arm in ARMS:
+            replica_barrier()
+            torch.cuda.synchronize()
             t0 = torch.cuda.Event(enable_timing=True)
             t1 = torch.cuda.Event(enable_timing=True)
             kev = []
@@ -145,7 +192,8 @@ def run_warmstart(args, pk):
                 kev.append(e)
             t1.record(st)
             torch.cuda.synchronize()
-            ms = t0.elapsed_time(t1) / args.steps
+            replica_barrier()
+            ms = replica_max(t0.elapsed_time(t1) / args.steps)
             kms = statistics.mean(a.elapsed_time(b) for a, b in kev)
             nit = out[3].cpu().numpy().astype(np.int64)
             stt = out[2].cpu().numpy()
@@ -162,13 +210,15 @@ def run_warmstart(args, pk):
     Xh, Yh = X.cpu().numpy(), Y.cpu().numpy()
     e2e_steps = max(1, min(args.steps, 3))
     torch.cuda.synchronize()
+    replica_barrier()
     t = time.perf_counter()
     for _ in range(e2e_steps):
         lu, lv, ni = wp.solve_cloud_pairs(Xh, Yh, WS_REG, WS_TOL, warm=True, net=net)
-    e2e_s = (time.perf_counter() - t) / e2e_steps
+    e2e_s = replica_max((time.perf_counter() - t) / e2e_steps)
+    W = _WS["world"]
     return {
-        "value": B / (w["ms"] * 1e-3), "unit": "solves/s", "ms_per_step": w["ms"], "dtype": "f32",
-        "plain": {"value": B / (p["ms"] * 1e-3), "ms_per_step": p["ms"], "niter_mean": p["niter_mean"],
+        "value": W * B / (w["ms"] * 1e-3), "unit": "solves/s", "ms_per_step": w["ms"], "dtype": "f32",
+        "plain": {"value": W * B / (p["ms"] * 1e-3), "ms_per_step": p["ms"], "niter_mean": p["niter_mean"],
                   "niter_max": p["niter_max"], "converged": p["converged"], "max_marginal_err": p["max_err"]},
         "warm": {"niter_mean": w["niter_mean"], "niter_max": w["niter_max"], "converged": w["converged"],
                  "max_marginal_err": w["max_err"]},
@@ -176,12 +226,12 @@ def run_warmstart(args, pk):
         "warm_pipeline": "coarse multiscale prior (Voronoi-weighted 256-point problem + c-transform) + learned "
                          "residual network, then the solve over-relaxed with omega=%.2f; every pair stops on the "
                          "same column-marginal test (err < %g, checked every 10 iterations)" % (OM, WS_TOL),
-        "ablation": {k: {"value": B / (res[k]["ms"] * 1e-3), "niter_mean": res[k]["niter_mean"],
+        "ablation": {k: {"value": W * B / (res[k]["ms"] * 1e-3), "niter_mean": res[k]["niter_mean"],
                          "speedup_vs_plain": p["ms"] / res[k]["ms"]}
                      for k in ("prior_relaxed", "net_plain", "prior_plain", "zero_relaxed")},
         "config": {"workload": "learned warm start vs plain log-Sinkhorn, %d GMM cloud pairs n=m=%d d=%d, "
                                "reg=%.2f x max cost, stopThr=%g, float32" % (B, WS_N, WS_D, WS_REG, WS_TOL),
-                   "pairs_per_step": B, "l2": "inputs larger than L2 (%.1f GiB of cost blocks)" % (
+                   "pairs_per_step": W * B, "replicas": W, "l2": "inputs larger than L2 (%.1f GiB of cost blocks)" % (
                        B * WS_N * WS_N * 4 / 2**30),
                    "held_out_seeds": [EVAL_SEED, EVAL_SEED + B - 1]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
@@ -190,7 +240,7 @@ def run_warmstart(args, pk):
                      "kernel": "multi_sinkhorn_kernel (plain arm)",
                      "alg_bytes_per_launch": p["alg_bytes"], "launch_ms": p["kernel_ms"],
                      "peak_src": pk["src"] + " (of measured)" if pk["src"] == "measured" else pk["src"]},
-        "e2e": {"value": B / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(Xh.nbytes + Yh.nbytes),
+        "e2e": {"value": W * B / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(Xh.nbytes + Yh.nbytes),
                 "d2h_bytes_per_step": int(lu.nbytes + lv.nbytes + ni.nbytes)},
         "gpu_launches": int(w["launches"] * args.steps),
         "clocks": cs.summary(),
@@ -439,7 +489,7 @@ def main():
     ap.add_argument("--full", type=int, default=0)
     ap.add_argument("--outer", type=int, default=50)
     args = ap.parse_args()
-    rank = int(os.environ.get("RANK", "0"))
+    rank, _, _ = replica_setup()
     if args.impl == "reference":
         if rank != 0:
             return
