@@ -123,24 +123,41 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
       yt[k * SQ_C + c] = (c0 + c < m) ? Y[(int64_t)(c0 + c) * D + k] : 0.f;
     }
     __syncthreads();
-    float acc[8][8];
+    // column pairs (j, j+1) in packed fp32x2 registers: one sub.f32x2 and one
+    // fma.f32x2 per pair and dimension, each lane rounding as the scalar ops
+    unsigned long long acc2[8][4];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
-      for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+      for (int j = 0; j < 4; ++j) acc2[i][j] = 0ull;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
       const float4 xa = *reinterpret_cast<const float4*>(xt + k * SQ_R + warp * 8);
       const float4 xb = *reinterpret_cast<const float4*>(xt + k * SQ_R + warp * 8 + 4);
-      const float4 ya = *reinterpret_cast<const float4*>(yt + k * SQ_C + lane * 8);
-      const float4 yb = *reinterpret_cast<const float4*>(yt + k * SQ_C + lane * 8 + 4);
+      const ulonglong2 ya = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_C + lane * 8);
+      const ulonglong2 yb = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_C + lane * 8 + 4);
       const float xv[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
-      const float yv[8] = {ya.x, ya.y, ya.z, ya.w, yb.x, yb.y, yb.z, yb.w};
+      const unsigned long long yp[4] = {ya.x, ya.y, yb.x, yb.y};
 #pragma unroll
-      for (int i = 0; i < 8; ++i)
+      for (int i = 0; i < 8; ++i) {
+        const unsigned long long xx =
+            (unsigned long long)__float_as_uint(xv[i]) | ((unsigned long long)__float_as_uint(xv[i]) << 32);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) { const float df = xv[i] - yv[j]; acc[i][j] = fmaf(df, df, acc[i][j]); }
+        for (int j = 0; j < 4; ++j) {
+          unsigned long long df;
+          asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(df) : "l"(xx), "l"(yp[j]));
+          asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i][j]) : "l"(df));
+        }
+      }
     }
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        acc[i][2 * j] = __uint_as_float((unsigned)(acc2[i][j] & 0xffffffffull));
+        acc[i][2 * j + 1] = __uint_as_float((unsigned)(acc2[i][j] >> 32));
+      }
     const int cb = c0 + lane * 8;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
