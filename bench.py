@@ -417,6 +417,47 @@ def run_dense(args, pk):
                          "kernel": "dense_sinkhorn_kernel", "alg_bytes_per_launch": alg}}
 
 
+def _lib_log():
+    from pot_gb300 import _lib
+    return _lib.OTG_METHOD_LOG
+
+
+def run_batch(args, pk):
+    """ot.batch.solve_batch on a uniform batch: args.batch problems of
+    n = m = args.n (default 1024) points in R^16 (the warm-start clouds),
+    cost / max, reg = 0.05, tol 1e-6, solver 'log_sinkhorn' (the batch
+    order: u first, row-marginal check), float32."""
+    import torch
+    from pot_gb300 import batch as pb
+    from pot_gb300.warmstart import pipeline as wp
+    dev = torch.device("cuda:0")
+    B, n = args.batch, min(args.n, 4096)
+    X, Y = wp.gen_pairs(EVAL_SEED, B, n, WS_D, dev)
+    ps = wp.PairSolver(X, Y)
+    M = ps.M.view(B, n, n) / ps.maxc.view(B, 1, 1)
+    st = torch.cuda.current_stream()
+    ones = torch.full((B, n), 1.0 / n, device=dev)
+    # the solver call of solve_batch, which reports per-problem stop indices
+    solve = lambda: pb._solve_uniform(M, ones, ones, 0.05, _lib_log(), 10000, 1e-6, False)  # noqa: E731
+    for _ in range(args.warmup):
+        solve()
+    kms = []
+    for _ in range(args.steps):
+        (res, ms) = _timed(solve, st)
+        kms.append(ms)
+    ms = statistics.median(kms)
+    nit = res[4].cpu().numpy().astype(np.int64)
+    # passes per problem: u then v per iteration, plus the check pass; the plan pass
+    alg = float((((2 * nit + 3) + 1) * n * n * 4.0).sum())
+    return {"metric": "batched Sinkhorn solves/s (ot.batch.solve_batch)", "value": B / (ms * 1e-3),
+            "unit": "solves/s", "ms_per_step": ms, "dtype": "f32",
+            "config": {"workload": "%d problems %dx%d (GMM clouds d=16, cost / max), reg=0.05, tol=1e-6, "
+                                   "log_sinkhorn" % (B, n, n), "niter_mean": float(nit.mean())},
+            "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": alg / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], "traffic": None,
+                         "kernel": "batched_sinkhorn_kernel (+ plan)", "alg_bytes": alg}}
+
+
 def _oracle_pair_solve(args):
     """One float64 oracle solve of a workload pair (run in a worker process)."""
     x, y = args
@@ -506,7 +547,8 @@ def main():
         return
     pk = peaks()
     if args.workload != "warmstart":
-        fn = {"online": run_online, "gw": run_gw, "ragged": run_ragged, "dense": run_dense}[args.workload]
+        fn = {"online": run_online, "gw": run_gw, "ragged": run_ragged, "dense": run_dense,
+              "batch": run_batch}[args.workload]
         line = {"n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                 "data": "synthetic"}
         line.update(fn(args, pk))

@@ -201,17 +201,26 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
         const int col = cgrp * 32;
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * OL_N + col), v);
         float t[32];
-        float gm = -INFINITY;
 #pragma unroll
-        for (int i = 0; i < 32; ++i) { t[i] = fmaf(v[i], P.alpha, h[col + i]); gm = fmaxf(gm, t[i]); }
-        const float nm = fmaxf(mx, gm);
+        for (int i = 0; i < 32; ++i) t[i] = fmaf(v[i], P.alpha, h[col + i]);
+        // max and sum as trees / independent accumulators: serial 32-long
+        // chains would expose the FP latency on every element
+        float mm[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) mm[i] = fmaxf(t[i], t[i + 16]);
+#pragma unroll
+        for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+          for (int i = 0; i < w; ++i) mm[i] = fmaxf(mm[i], mm[i + w]);
+        const float nm = fmaxf(mx, mm[0]);
         if (nm != -INFINITY) {
           const float r = ex2(mx - nm);
           sm *= r;
           sc *= r;
-          float part = 0.f;
+          float ps[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-          for (int i = 0; i < 32; ++i) part += ex2(t[i] - nm);
+          for (int i = 0; i < 32; ++i) ps[i & 3] += ex2(t[i] - nm);
+          const float part = (ps[0] + ps[1]) + (ps[2] + ps[3]);
           const float y = part - sc;
           const float tt = sm + y;
           sc = (tt - sm) - y;
