@@ -159,6 +159,15 @@ typedef struct OtgBaryProblem {
 size_t otg_barycenter_workspace_bytes(int dtype, int method, int64_t dim, int32_t n_hists);
 int otg_barycenter(const OtgBaryProblem* p, cudaStream_t stream);
 
+/* Batched transpose: dst[b] (m x ld_dst, batch stride bs_dst) = src[b]^T
+ * (src[b]: n x m, leading dimension ld_src, batch stride bs_src), with +inf
+ * in the padding columns [n, ld_dst).  The batch order of ot.batch
+ * (u first, row-marginal check; ot/batch/_utils.py:268-278) is the
+ * sinkhorn_log order of the transposed problem, which the work-balanced
+ * kernel (otg_sinkhorn_multi) then solves. */
+int otg_transpose_batched(int dtype, const void* src, int64_t batch, int64_t n, int64_t m, int64_t ld_src,
+                          int64_t bs_src, void* dst, int64_t ld_dst, int64_t bs_dst, cudaStream_t stream);
+
 /* ------------------------------------------------------------------------
  * Batched dense Sinkhorn: many independent problems of uneven size in ONE
  * persistent launch, one CTA per problem at a time, each problem stopping on

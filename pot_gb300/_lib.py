@@ -92,6 +92,8 @@ SIGNATURES = {
                                       c_dbl, c_vp, c_i64, c_vp, c_vp]),
     "otg_barycenter_workspace_bytes": (c_sz, [ctypes.c_int, ctypes.c_int, c_i64, c_i32]),
     "otg_barycenter": (ctypes.c_int, [ctypes.POINTER(OtgBaryProblem), c_vp]),
+    "otg_transpose_batched": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp, c_i64,
+                                             c_i64, c_vp]),
     "otg_lazy_loss": (ctypes.c_int, [ctypes.c_int, c_vp, c_vp, c_i64, c_i64, c_i32, c_vp, c_vp, c_dbl, c_vp, c_vp]),
     "otg_dense_marginals": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_dbl, c_vp, c_vp,
                                            c_vp]),

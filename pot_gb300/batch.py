@@ -232,10 +232,34 @@ def _unpack_rows(layout, packed, width_np, off_np):
     return packed.view(B, w)
 
 
+def _transposed(layout, Mp):
+    """The layout and packed cost blocks of the transposed problems (one
+    transpose pass, otg_transpose_batched)."""
+    lib = _lib.load()
+    B, n, m = layout.B, int(layout.rows_np[0]), int(layout.cols_np[0])
+    lt = RaggedLayout([m] * B, [n] * B, layout.dtype, layout.device)
+    ld, ldt = int(layout.ldm_np[0]), int(lt.ldm_np[0])
+    Mt = torch.empty(lt.total_m, dtype=layout.dtype, device=layout.device)
+    _lib.check(lib.otg_transpose_batched(_lib.dtype_code(layout.dtype), _lib.ptr(Mp), B, n, m, ld, n * ld,
+                                         _lib.ptr(Mt), ldt, m * ldt, _lib.stream_handle(layout.device)),
+               "otg_transpose_batched")
+    return lt, Mt
+
+
 def _solve_uniform(Md, a, b, reg, method, max_iter, tol, kl):
+    """Uniform batch in the ot.batch order (u first, row-marginal check every
+    10th iteration, each problem stopping on its own error).  The log form is
+    the sinkhorn_log order of the transposed problems (a and b swapped) on the
+    work-balanced kernel; the scaling form runs the CTA-per-problem kernel."""
     layout, Mp = _uniform_batch(Md)
     ap, bp = a.reshape(-1).contiguous(), b.reshape(-1).contiguous()
-    u, v, status, niter, err, reg_t = run_batched(layout, Mp, ap, bp, reg, method, max_iter, tol, u_first=1)
+    if method == _lib.OTG_METHOD_LOG and layout.B <= 65535:
+        lt, Mt = _transposed(layout, Mp)
+        vt, ut, status, niter, err, reg_t = run_multi(lt, Mt, bp, ap, reg, max_iter, tol)
+        u, v = ut, vt
+        del Mt
+    else:
+        u, v, status, niter, err, reg_t = run_batched(layout, Mp, ap, bp, reg, method, max_iter, tol, u_first=1)
     P, vals = batched_plan(layout, Mp, u, v, ap, bp, reg_t, method, kl=kl)
     B, n, m = Md.shape
     ld = int(layout.ldm_np[0])

@@ -205,6 +205,31 @@ __global__ void __launch_bounds__(256) sqdist_regtile_kernel(OtgCostTable t) {
   }
 }
 
+// Batched transpose through 32 x 32 shared-memory tiles: dst[b][j][i] =
+// src[b][i][j] for i < n, j < m, and +inf in the padding columns i in
+// [n, ld_dst) of every destination row (they add nothing to any LSE).
+// grid = (column tiles of the source, tiles over ld_dst, batch).
+template <typename T>
+__global__ void __launch_bounds__(256) transpose_batched_kernel(const T* __restrict__ src, int64_t n, int64_t m,
+                                                                int64_t ld_src, int64_t bs_src, T* __restrict__ dst,
+                                                                int64_t ld_dst, int64_t bs_dst) {
+  __shared__ T tile[32][33];
+  const int64_t b = blockIdx.z;
+  const int64_t j0 = (int64_t)blockIdx.x * 32, i0 = (int64_t)blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  const T* S = src + b * bs_src;
+  T* D = dst + b * bs_dst;
+  for (int r = ty; r < 32; r += 8) {
+    const int64_t i = i0 + r, j = j0 + tx;
+    tile[r][tx] = (i < n && j < m) ? S[i * ld_src + j] : T(INFINITY);
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int64_t j = j0 + r, i = i0 + tx;
+    if (j < m && i < ld_dst) D[j * ld_dst + i] = tile[tx][r];
+  }
+}
+
 // Plan and values per problem.  grid = (row tiles, problems).
 // out_vals[3p+0] = value_linear, [3p+1] = sum T log(T+1e-16) (entropy form)
 // or sum T log(T/(a b) + 1e-16) (KL form), [3p+2] = sum T.
@@ -221,21 +246,29 @@ __global__ void __launch_bounds__(256) batched_plan_kernel(OtgPlanTable t) {
   T* P = t.P ? static_cast<T*>(t.P) + t.m_off[p] : nullptr;
   const T c = (T)(-OTG_LOG2E / t.reg[p]);
   const T L2E = T(OTG_LOG2E);
+  // sums in the working type within a row, in fp64 across rows: float
+  // inputs keep their logarithms in fp32 (GB300's fp64 rate is a small
+  // fraction of fp32; a per-element fp64 log made this kernel the batch
+  // path's bottleneck), double inputs stay in fp64 throughout
   double lin = 0, reg_term = 0, mass = 0;
   for (int i = blockIdx.x; i < n; i += gridDim.x) {
     const T ui = u[i];
+    const T ai = a[i];
+    T lr = 0, rr = 0, mr = 0;
     for (int j = threadIdx.x; j < m; j += blockDim.x) {
       const T x = M[(int64_t)i * ldm + j];
       T pij;
       if (METHOD == OTG_METHOD_LOG) pij = ex2(fma(x, c, (ui + v[j]) * L2E));
       else pij = ui * ex2(x * c) * v[j];
       if (P) P[(int64_t)i * ldm + j] = pij;
-      const double pd = (double)pij;
-      lin += (double)x * pd;
-      mass += pd;
-      if (t.kl) reg_term += pd * log(pd / ((double)a[i] * (double)b[j]) + 1e-16);
-      else reg_term += pd * log(pd + 1e-16);
+      lr = fma(x, pij, lr);
+      mr += pij;
+      if (t.kl) rr = fma(pij, log(pij / (ai * b[j]) + T(1e-16)), rr);
+      else rr = fma(pij, log(pij + T(1e-16)), rr);
     }
+    lin += (double)lr;
+    mass += (double)mr;
+    reg_term += (double)rr;
   }
   __shared__ double red[3][8];
   lin = warp_sum(lin); reg_term = warp_sum(reg_term); mass = warp_sum(mass);
@@ -473,6 +506,23 @@ int otg_lazy_loss(int dtype, const void* X, const void* Y, int64_t n, int64_t m,
   } else {
     return OTG_ERR_DTYPE;
   }
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_transpose_batched(int dtype, const void* src, int64_t batch, int64_t n, int64_t m, int64_t ld_src,
+                          int64_t bs_src, void* dst, int64_t ld_dst, int64_t bs_dst, cudaStream_t stream) {
+  if (!src || !dst || batch < 1 || n < 1 || m < 1 || ld_src < m || ld_dst < n || bs_src < n * ld_src ||
+      bs_dst < m * ld_dst || batch > 65535)
+    return OTG_ERR_ARG;
+  const dim3 grid((unsigned)((m + 31) / 32), (unsigned)((ld_dst + 31) / 32), (unsigned)batch);
+  if (dtype == OTG_F64)
+    transpose_batched_kernel<double><<<grid, 256, 0, stream>>>((const double*)src, n, m, ld_src, bs_src, (double*)dst,
+                                                               ld_dst, bs_dst);
+  else if (dtype == OTG_F32)
+    transpose_batched_kernel<float><<<grid, 256, 0, stream>>>((const float*)src, n, m, ld_src, bs_src, (float*)dst,
+                                                              ld_dst, bs_dst);
+  else
+    return OTG_ERR_DTYPE;
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 
