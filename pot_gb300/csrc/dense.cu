@@ -602,14 +602,16 @@ __global__ void __launch_bounds__(256) dense_plan_kernel(const T* __restrict__ M
   for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
     const T ui = u[i];
     const T* Mrow = M + i * ldm;
+    T racc = 0;  // this thread's share of the row in the working type, fp64 across rows
     for (int64_t j = threadIdx.x; j < m; j += blockDim.x) {
       const T x = Mrow[j];
       T p;
       if (LogDomain<METHOD>::value) p = ex2(fma(x, c, (ui + v[j]) * L2E));
       else p = ui * ex2(x * c) * v[j];
       if (P) P[i * ldp + j] = p;
-      if (loss) acc += (double)x * (double)p;
+      racc = fma(x, p, racc);
     }
+    if (loss) acc += (double)racc;
   }
   if (loss) {
     acc = warp_sum(acc);
