@@ -17,8 +17,8 @@ replaces the hot-path names in every module that imported them:
                                  bregman_log_projection_batch, bregman_projection_batch
     ot/batch/_linear.py          the same (module-level callers)
     ot/batch/_quadratic.py:14    bregman_log_projection_batch
-    ot/solvers.py:14             sinkhorn_log, empirical_sinkhorn2 (the entropic branches of
-                                 ot.solve / ot.solve_sample)
+    ot/solvers.py:13-14          sinkhorn_log, empirical_sinkhorn2, sinkhorn_knopp_unbalanced (the
+                                 entropic branches of ot.solve / ot.solve_sample)
     ot/unbalanced/__init__.py    sinkhorn_unbalanced(2), sinkhorn_knopp_unbalanced
     ot/unbalanced/_sinkhorn.py   sinkhorn_knopp_unbalanced (the dispatcher's callee)
 
@@ -70,7 +70,7 @@ MODULES = {
                "bregman_projection_batch"],
     ".batch._linear": ["solve_batch", "dist_batch", "bregman_log_projection_batch", "bregman_projection_batch"],
     ".batch._quadratic": ["bregman_log_projection_batch"],
-    ".solvers": ["sinkhorn_log", "empirical_sinkhorn2"],
+    ".solvers": ["sinkhorn_log", "empirical_sinkhorn2", "sinkhorn_knopp_unbalanced"],
     ".unbalanced": ["sinkhorn_unbalanced", "sinkhorn_unbalanced2", "sinkhorn_knopp_unbalanced"],
     ".unbalanced._sinkhorn": ["sinkhorn_knopp_unbalanced"],
 }
