@@ -157,19 +157,22 @@ def run_warmstart(args, pk):
 
     OM = wp.REFINE_OMEGA
     # arms: the headline warm start (multiscale prior + learned residual,
-    # over-relaxed solve), the plain solve, and the ablations
-    ARMS = {"warm": ("net", OM), "plain": (None, 1.0), "prior_relaxed": ("prior", OM),
-            "net_plain": ("net", 1.0), "prior_plain": ("prior", 1.0), "zero_relaxed": (None, OM)}
+    # over-relaxed solve), the plain solve, and the ablations; (start, omega,
+    # iterations between stop tests: 10 is the reference's schedule, 1 tests
+    # every iteration with the same criterion)
+    ARMS = {"warm": ("net", OM, 10), "plain": (None, 1.0, 10), "prior_relaxed": ("prior", OM, 10),
+            "net_plain": ("net", 1.0, 10), "prior_plain": ("prior", 1.0, 10), "zero_relaxed": (None, OM, 10),
+            "plain_check1": (None, 1.0, 1), "warm_check1": ("net", OM, 1), "prior_relaxed_check1": ("prior", OM, 1)}
 
     def step(arm, ev=None):
-        init, om = ARMS[arm]
+        init, om, per = ARMS[arm]
         ps = wp.PairSolver(X, Y)
         wu = None
         if init == "net":
             wu = wp.warm_potential(net, X, Y, ps, WS_REG)
         elif init == "prior":
             wu = wp.coarse_potential(X, Y, ps.maxc, WS_REG, wp.COARSE_K) / WS_REG
-        out = ps.solve(WS_REG, WS_TOL, warm_u=wu, events=ev, omega=om)
+        out = ps.solve(WS_REG, WS_TOL, warm_u=wu, events=ev, omega=om, check_period=per)
         return ps, out
 
     for _ in range(args.warmup):
@@ -227,8 +230,13 @@ def run_warmstart(args, pk):
                          "residual network, then the solve over-relaxed with omega=%.2f; every pair stops on the "
                          "same column-marginal test (err < %g, checked every 10 iterations)" % (OM, WS_TOL),
         "ablation": {k: {"value": W * B / (res[k]["ms"] * 1e-3), "niter_mean": res[k]["niter_mean"],
-                         "speedup_vs_plain": p["ms"] / res[k]["ms"]}
-                     for k in ("prior_relaxed", "net_plain", "prior_plain", "zero_relaxed")},
+                         "speedup_vs_plain": p["ms"] / res[k]["ms"], "check_period": ARMS[k][2],
+                         "max_marginal_err": res[k]["max_err"], "converged": res[k]["converged"]}
+                     for k in ("prior_relaxed", "net_plain", "prior_plain", "zero_relaxed", "plain_check1",
+                               "warm_check1", "prior_relaxed_check1")},
+        # both arms stop at the first iteration whose column-marginal error is
+        # below the tolerance (stop test every iteration)
+        "speedup_warm_vs_plain_check1": res["plain_check1"]["ms"] / res["warm_check1"]["ms"],
         "config": {"workload": "learned warm start vs plain log-Sinkhorn, %d GMM cloud pairs n=m=%d d=%d, "
                                "reg=%.2f x max cost, stopThr=%g, float32" % (B, WS_N, WS_D, WS_REG, WS_TOL),
                    "pairs_per_step": W * B, "replicas": W, "l2": "inputs larger than L2 (%.1f GiB of cost blocks)" % (

@@ -256,6 +256,11 @@ typedef struct OtgMultiProblem {
    * counterpart: used by the warm-start refinement; the stop test is still the
    * exact column-marginal error of the iterate. */
   double omega;
+  /* iterations between stop tests: 0 or 10 is the reference's schedule
+   * (sinkhorn_log tests at ii % 10 == 0); 1 tests every iteration with the
+   * same criterion (no reference counterpart). */
+  int32_t check_period;
+  int32_t reserved;
 } OtgMultiProblem;
 size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, int64_t total_cols,
                                  int64_t total_partials);
@@ -448,6 +453,15 @@ int otg_gemm_f64(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, 
 #define OTG_NOALLOC_SCRATCH_BYTES (16u << 20)
 int otg_sinkhorn_dense_noalloc(const OtgDenseProblem* p, double* err_hist, int32_t* info,
                                cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
+ * ABI self-description (host only, no GPU needed).  For the struct named
+ * `name` (e.g. "OtgDenseProblem") writes sizeof to out[0] and the offset of
+ * each field, in declaration order, to out[1..]; returns the count written
+ * (1 + fields), or OTG_ERR_ARG for an unknown name or a too small `cap`.
+ * Bindings (ctypes, cgo, JNI) check their struct mirrors with it.
+ * ---------------------------------------------------------------------- */
+int otg_abi_layout(const char* name, int64_t* out, int32_t cap);
 
 #ifdef __cplusplus
 }

@@ -44,7 +44,8 @@ class OtgMultiProblem(ctypes.Structure):
                 ("reg", c_vp), ("max_iter", c_i32), ("grid", c_i32), ("stop_thr", c_dbl), ("nsr_max", c_vp),
                 ("pc_off", c_vp), ("total_rows", c_i64), ("total_cols", c_i64), ("total_partials", c_i64),
                 ("out_u", c_vp), ("out_v", c_vp), ("status", c_vp), ("niter", c_vp), ("err", c_vp),
-                ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32), ("omega", c_dbl)]
+                ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32), ("omega", c_dbl),
+                ("check_period", c_i32), ("reserved", c_i32)]
 
 
 class OtgCostTable(ctypes.Structure):
@@ -85,6 +86,7 @@ class OtgOnlineProblem(ctypes.Structure):
 
 # name -> (restype, argtypes)
 SIGNATURES = {
+    "otg_abi_layout": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(c_i64), c_i32]),
     "otg_dense_workspace_bytes": (c_sz, [ctypes.c_int, c_i64, c_i64, ctypes.c_int, ctypes.c_int]),
     "otg_dense_info_offset": (c_sz, [ctypes.c_int, c_i64, c_i64, ctypes.c_int, ctypes.c_int]),
     "otg_sinkhorn_dense": (ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp]),

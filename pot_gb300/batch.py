@@ -120,17 +120,18 @@ def run_batched(layout, M_packed, a_packed, b_packed, reg, method, max_iter, tol
 
 
 def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-              events=None, omega=1.0):
+              events=None, omega=1.0, check_period=10):
     """Work-balanced persistent launch (csrc/multi.cu), log form, per-problem
     sinkhorn_log order and stop test.  Returns (u, v, status, niter, err, reg).
-    ``omega != 1`` over-relaxes the potential updates (no reference
-    counterpart; the stop test is unchanged)."""
+    ``omega != 1`` over-relaxes the potential updates and ``check_period``
+    other than 10 moves the stop tests (no reference counterpart for either;
+    the stop criterion is unchanged)."""
     return _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u, grid, timeout_ms,
-                           events, omega)
+                           events, omega, check_period)
 
 
 def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-                    events=None, omega=1.0):
+                    events=None, omega=1.0, check_period=10):
     lib = _lib.load()
     dev, dt = layout.device, layout.dtype
     B = layout.B
@@ -161,7 +162,7 @@ def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, wa
         total_rows=layout.total_r, total_cols=layout.total_c, total_partials=layout.total_partials,
         out_u=out_u.data_ptr(), out_v=out_v.data_ptr(), status=status.data_ptr(), niter=niter.data_ptr(),
         err=err.data_ptr(), workspace=ws.data_ptr(), workspace_bytes=wsb, timeout_ms=int(timeout_ms),
-        omega=float(omega))
+        omega=float(omega), check_period=int(check_period))
     if events is not None:
         events[0].record()
     _lib.check(lib.otg_sinkhorn_multi(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_multi")

@@ -67,6 +67,7 @@ struct MultiArgs {
   uint64_t timeout_ns;
   T omega;                  // over-relaxation (1: plain)
   bool relax;
+  int period;               // iterations between stop tests
 };
 
 // Index of the active slot whose prefix range holds `unit` (pre[k] <= unit < pre[k+1]).
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
     const int nact2 = ld_acquire_i(A.ctl);
     mt_row_pass<T>(A, nact2, vcur, gwarp, nwarps, lane);
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
-    prev_check = (ii % 10 == 0);
+    prev_check = (ii % A.period == 0);
   }
 }
 
@@ -467,6 +468,7 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   A.timeout_ns = q->timeout_ms > 0 ? (uint64_t)q->timeout_ms * 1000000ull : 4000000000ull;
   A.relax = q->omega != 0.0 && q->omega != 1.0;
   A.omega = (T)q->omega;
+  A.period = q->check_period > 0 ? q->check_period : 10;
   // carve the workspace
   char* w = static_cast<char*>(q->workspace);
   size_t off = 0;

@@ -58,7 +58,8 @@ class PairSolver:
         self.b = (torch.full((self.P * self.m,), 1.0 / self.m, dtype=torch.float32, device=X.device) if b is None
                   else b.reshape(-1).float().contiguous())
 
-    def solve(self, reg_rel, tol, max_iter=100000, warm_u=None, engine="multi", events=None, omega=1.0):
+    def solve(self, reg_rel, tol, max_iter=100000, warm_u=None, engine="multi", events=None, omega=1.0,
+              check_period=10):
         """Log-domain solve of every pair (sinkhorn_log order and stop test);
         with `warm_u` the first half-step (the c-transform) derives v from it."""
         reg = self.maxc.double() * reg_rel
@@ -66,7 +67,8 @@ class PairSolver:
             warm_u = warm_u.reshape(-1).contiguous()
         if engine == "multi":
             u, v, status, niter, err, _ = pb.run_multi(self.layout, self.M, self.a, self.b, reg, max_iter, tol,
-                                                       warm_u=warm_u, events=events, omega=omega)
+                                                       warm_u=warm_u, events=events, omega=omega,
+                                                       check_period=check_period)
         else:
             wv = None if warm_u is None else torch.zeros(self.P * self.m, dtype=torch.float32, device=self.M.device)
             u, v, status, niter, err, _ = pb.run_batched(self.layout, self.M, self.a, self.b, reg,

@@ -242,3 +242,41 @@ def test_multi_over_relaxed_reaches_the_same_solution(cuda):
         up, ur = plain[0][r0:r0 + n], relax[0][r0:r0 + n]
         # potentials are defined up to a constant shared by u and -v
         np.testing.assert_allclose((ur - ur.mean()).cpu().numpy(), (up - up.mean()).cpu().numpy(), atol=1e-6)
+
+
+def test_multi_stop_test_every_iteration(cuda):
+    """check_period=1 applies the reference's stop criterion (column-marginal
+    L2 error of the iterate below stopThr) at every iteration: each problem
+    stops at the first iteration that meets it, with the potentials of the
+    oracle's sinkhorn_log run for exactly that many iterations."""
+    rng = np.random.default_rng(21)
+    B = 5
+    rows = rng.integers(30, 90, B)
+    cols = rng.integers(30, 90, B)
+    layout = pb.RaggedLayout(rows, cols, torch.float64, cuda)
+    Ms = []
+    for n, m in zip(rows, cols):
+        M = oracle.sqeuclidean(rng.random((n, 3)), rng.random((m, 3)))
+        Ms.append(M / M.max())
+    Mp = pb.pack_dense(layout, [torch.tensor(M, device=cuda) for M in Ms])
+    a = torch.cat([torch.full((int(n),), 1.0 / n, dtype=torch.float64, device=cuda) for n in rows])
+    b = torch.cat([torch.full((int(m),), 1.0 / m, dtype=torch.float64, device=cuda) for m in cols])
+    reg, tol = 0.03, 1e-9
+    every = pb.run_multi(layout, Mp, a, b, reg, 20000, tol, check_period=1)
+    tenth = pb.run_multi(layout, Mp, a, b, reg, 20000, tol)
+    assert (every[2] == 0).all() and (tenth[2] == 0).all()
+    n1, n10 = every[3].cpu().numpy(), tenth[3].cpu().numpy()
+    assert (n10 % 10 == 0).all() and (n1 <= n10).all() and (n1 % 10 != 0).any()
+
+    def col_err(M, n, m, it):
+        _, lg = oracle.sinkhorn_log(np.full(n, 1.0 / n), np.full(m, 1.0 / m), M, reg, numItermax=it, stopThr=0.0)
+        P = np.exp(lg["log_u"][:, None] - M / reg + lg["log_v"][None, :])
+        return np.linalg.norm(P.sum(0) - 1.0 / m), lg
+
+    for p in range(B):
+        n, m, k = int(rows[p]), int(cols[p]), int(n1[p])
+        e, lg = col_err(Ms[p], n, m, k + 1)
+        assert e < tol and col_err(Ms[p], n, m, k)[0] >= tol, (p, k)
+        assert abs(float(every[4][p]) - e) <= 1e-6 * tol + 1e-3 * e
+        r0 = int(layout.r_off_np[p])
+        np.testing.assert_allclose(every[0][r0:r0 + n].cpu().numpy(), lg["log_u"], rtol=1e-9, atol=1e-9)
