@@ -98,6 +98,14 @@ typedef struct OtgDenseProblem {
   double reg_m1, reg_m2; /* UNB: marginal penalties (INFINITY = hard constraint) */
   int32_t c_ones;     /* UNB: 0 -> c = a b^T (reg_type 'kl'), 1 -> c = ones    */
   int32_t reserved2;
+  /* KNOPP: optional Gibbs kernel K = exp(-M/reg) from otg_gibbs_kernel (same
+   * dtype, n x m, row stride ldk, 16-byte aligned rows for the vector path),
+   * or NULL.  The passes then read K instead of taking an exponential of
+   * every cost entry each iteration, as the reference does (K of
+   * ot/bregman/_sinkhorn.py:621); the iterates are bit-identical either way.
+   * Pays where exponentials bound the solve (float64). */
+  const void* K;
+  int64_t ldk;
 } OtgDenseProblem;
 
 /* Workspace size for otg_sinkhorn_dense (device bytes, 256-byte aligned). */
@@ -118,6 +126,12 @@ int otg_sinkhorn_dense(const OtgDenseProblem* p, void* workspace, cudaStream_t s
 int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, int64_t ldm,
                    const void* u, const void* v, double reg, void* P, int64_t ldp, double* loss,
                    cudaStream_t stream);
+
+/* K = exp(-M/reg) (n x m, row stride ldk), computed exactly as the scaling
+ * form of otg_sinkhorn_dense computes it on the fly: the Gibbs kernel of
+ * ot/bregman/_sinkhorn.py:621. */
+int otg_gibbs_kernel(int dtype, const void* M, int64_t n, int64_t m, int64_t ldm, double reg, void* K,
+                     int64_t ldk, cudaStream_t stream);
 
 /* Row and column sums of P = exp(-M/reg + u + v) (natural-log potentials),
  * accumulated in fp64 (rowsum: n, colsum: m).  The marginal error of the
@@ -260,7 +274,14 @@ typedef struct OtgMultiProblem {
    * (sinkhorn_log tests at ii % 10 == 0); 1 tests every iteration with the
    * same criterion (no reference counterpart). */
   int32_t check_period;
-  int32_t reserved;
+  /* schedule (0: default): column-pass units aimed at per warp (8), the
+   * row-split cap while the batch fills the GPU (16) and once few problems
+   * remain (64; at most 64).  CTAs per SM are set through `grid`.  Changes
+   * how work is divided, not the iteration; chosen per workload by the
+   * autotuner of pot_gb300/tune.py. */
+  int32_t units_per_warp;
+  int32_t split_cap_fill;
+  int32_t split_cap_tail;
 } OtgMultiProblem;
 size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, int64_t total_cols,
                                  int64_t total_partials);

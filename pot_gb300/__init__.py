@@ -13,6 +13,7 @@ from .bregman import sinkhorn_stabilized, sinkhorn_epsilon_scaling  # noqa: F401
 from . import batch  # noqa: F401
 from .batch import solve_batch, solve_sample_batch, dist_batch  # noqa: F401
 from . import gromov  # noqa: F401
+from . import graphs, tune  # noqa: F401
 from .empirical import empirical_sinkhorn  # noqa: F401
 from .solvers import solve, solve_sample, empirical_sinkhorn2, empirical_sinkhorn_divergence  # noqa: F401
 from .barycenters import barycenter, barycenter_sinkhorn  # noqa: F401

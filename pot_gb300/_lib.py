@@ -26,7 +26,8 @@ class OtgDenseProblem(ctypes.Structure):
                 ("reg", c_dbl), ("max_iter", c_i32), ("hist_cap", c_i32), ("stop_thr", c_dbl),
                 ("out_u", c_vp), ("out_v", c_vp), ("workspace_bytes", c_sz), ("grid", c_i32),
                 ("timeout_ms", c_i32), ("tau", c_dbl), ("check_period", c_i32), ("reserved", c_i32),
-                ("reg_m1", c_dbl), ("reg_m2", c_dbl), ("c_ones", c_i32), ("reserved2", c_i32)]
+                ("reg_m1", c_dbl), ("reg_m2", c_dbl), ("c_ones", c_i32), ("reserved2", c_i32), ("K", c_vp),
+                ("ldk", c_i64)]
 
 
 class OtgBatchProblem(ctypes.Structure):
@@ -45,7 +46,8 @@ class OtgMultiProblem(ctypes.Structure):
                 ("pc_off", c_vp), ("total_rows", c_i64), ("total_cols", c_i64), ("total_partials", c_i64),
                 ("out_u", c_vp), ("out_v", c_vp), ("status", c_vp), ("niter", c_vp), ("err", c_vp),
                 ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32), ("omega", c_dbl),
-                ("check_period", c_i32), ("reserved", c_i32)]
+                ("check_period", c_i32), ("units_per_warp", c_i32), ("split_cap_fill", c_i32),
+                ("split_cap_tail", c_i32)]
 
 
 class OtgCostTable(ctypes.Structure):
@@ -97,6 +99,7 @@ SIGNATURES = {
     "otg_transpose_batched": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp, c_i64,
                                              c_i64, c_vp]),
     "otg_lazy_loss": (ctypes.c_int, [ctypes.c_int, c_vp, c_vp, c_i64, c_i64, c_i32, c_vp, c_vp, c_dbl, c_vp, c_vp]),
+    "otg_gibbs_kernel": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_dbl, c_vp, c_i64, c_vp]),
     "otg_dense_marginals": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_dbl, c_vp, c_vp,
                                            c_vp]),
     "otg_sinkhorn_dense_noalloc": (ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp, c_vp]),

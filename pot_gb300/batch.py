@@ -17,7 +17,7 @@ import ctypes
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, tune
 from ._arrays import Boundary
 from .utils import OTResult
 
@@ -120,19 +120,25 @@ def run_batched(layout, M_packed, a_packed, b_packed, reg, method, max_iter, tol
 
 
 def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-              events=None, omega=1.0, check_period=10):
+              events=None, omega=1.0, check_period=10, schedule=None):
     """Work-balanced persistent launch (csrc/multi.cu), log form, per-problem
     sinkhorn_log order and stop test.  Returns (u, v, status, niter, err, reg).
     ``omega != 1`` over-relaxes the potential updates and ``check_period``
     other than 10 moves the stop tests (no reference counterpart for either;
-    the stop criterion is unchanged)."""
+    the stop criterion is unchanged).  ``schedule`` (a ``tune.Schedule``)
+    divides the work; by default the autotuner's cached choice for this
+    workload class, else the built-in one."""
     return _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u, grid, timeout_ms,
-                           events, omega, check_period)
+                           events, omega, check_period, schedule)
 
 
 def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-                    events=None, omega=1.0, check_period=10):
+                    events=None, omega=1.0, check_period=10, schedule=None):
     lib = _lib.load()
+    if schedule is None:
+        schedule = tune.lookup(layout) or tune.DEFAULT
+    if grid == 0 and schedule.ctas_per_sm > 0:
+        grid = schedule.ctas_per_sm * torch.cuda.get_device_properties(layout.device).multi_processor_count
     dev, dt = layout.device, layout.dtype
     B = layout.B
     reg_t = torch.as_tensor(reg, dtype=torch.float64, device=dev).reshape(-1)
@@ -162,7 +168,8 @@ def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, wa
         total_rows=layout.total_r, total_cols=layout.total_c, total_partials=layout.total_partials,
         out_u=out_u.data_ptr(), out_v=out_v.data_ptr(), status=status.data_ptr(), niter=niter.data_ptr(),
         err=err.data_ptr(), workspace=ws.data_ptr(), workspace_bytes=wsb, timeout_ms=int(timeout_ms),
-        omega=float(omega), check_period=int(check_period))
+        omega=float(omega), check_period=int(check_period), units_per_warp=int(schedule.units_per_warp),
+        split_cap_fill=int(schedule.cap_fill), split_cap_tail=int(schedule.cap_tail))
     if events is not None:
         events[0].record()
     _lib.check(lib.otg_sinkhorn_multi(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_multi")
@@ -369,12 +376,15 @@ class RaggedResult:
 
 
 def solve_sample_ragged(Xs, Ys, reg, as_=None, bs=None, reg_relative=False, max_iter=100000, tol=1e-6,
-                        method="sinkhorn_log", warmstart=None, dtype=torch.float32, device=None, engine="multi"):
+                        method="sinkhorn_log", warmstart=None, dtype=torch.float32, device=None, engine="multi",
+                        autotune=False):
     """Entropic OT between B point-cloud pairs of uneven sizes and dims, in
     one persistent launch.  ``reg`` is a scalar or one value per problem; with
     ``reg_relative`` it multiplies each problem's largest cost.  Per problem
     the iteration order and stopping test are those of ``ot.sinkhorn(...,
-    method='sinkhorn_log')`` (v first, column-marginal L2 error)."""
+    method='sinkhorn_log')`` (v first, column-marginal L2 error).  With
+    ``autotune`` the launch schedule of this workload class is searched
+    first if the tuner has none cached (``pot_gb300.tune``)."""
     device = device or torch.device("cuda", torch.cuda.current_device())
     B = len(Xs)
     rows = [x.shape[0] for x in Xs]
@@ -400,6 +410,8 @@ def solve_sample_ragged(Xs, Ys, reg, as_=None, bs=None, reg_relative=False, max_
     if warmstart is not None:
         wu, wv = warmstart
     if engine == "multi" and code == _lib.OTG_METHOD_LOG:
+        if autotune:
+            tune.tune_multi(layout, M, ap, bp, reg_t)
         u, v, status, niter, err, reg_t = run_multi(layout, M, ap, bp, reg_t, max_iter, tol, warm_u=wu)
     else:
         u, v, status, niter, err, reg_t = run_batched(layout, M, ap, bp, reg_t, code, max_iter, tol, u_first=0,

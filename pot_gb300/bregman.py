@@ -30,7 +30,7 @@ def _hist_cap(max_iter):
 
 
 class DenseResult:
-    __slots__ = ("u", "v", "status", "niter", "errs", "workspace", "layout", "nabs", "absorbed_last", "method")
+    __slots__ = ("u", "v", "status", "niter", "errs", "workspace", "layout", "nabs", "absorbed_last", "method", "K")
 
 
 def default_grid(n, m):
@@ -42,13 +42,21 @@ def default_grid(n, m):
     return max(4, elems // 16384)
 
 
+# largest Gibbs kernel (bytes) precomputed for a float64 scaling-form solve
+GIBBS_MAX_BYTES = 16 << 30
+
+
 def solve_dense(M, a, b, reg, method, max_iter, stop_thr, warm_u=None, warm_v=None, grid=None,
-                timeout_ms=0, read_back=True, tau=0.0, check_period=10, unbalanced=None):
+                timeout_ms=0, read_back=True, tau=0.0, check_period=10, unbalanced=None, gibbs=None):
     """Run one dense solve on device tensors (contiguous rows, same dtype).
 
     Returns a DenseResult whose ``u, v`` are scalings (knopp) or natural-log
     potentials (log).  With ``read_back`` the status, last loop index and
-    error history are copied to the host (one synchronisation)."""
+    error history are copied to the host (one synchronisation).  ``gibbs``
+    (default: float64 scaling form) first stores K = exp(-M/reg) so the
+    passes read it instead of exponentiating every cost entry each
+    iteration (float64 exponentials bound the solve on this GPU); the
+    iterates are bit-identical."""
     lib = _lib.load()
     n, m = M.shape
     if grid is None:
@@ -69,10 +77,19 @@ def solve_dense(M, a, b, reg, method, max_iter, stop_thr, warm_u=None, warm_v=No
         timeout_ms=timeout_ms, tau=float(tau), check_period=int(check_period))
     if unbalanced is not None:
         p.reg_m1, p.reg_m2, p.c_ones = float(unbalanced[0]), float(unbalanced[1]), int(unbalanced[2])
+    if gibbs is None:
+        gibbs = (method == _lib.OTG_METHOD_KNOPP and unbalanced is None and M.dtype == torch.float64
+                 and n * m * 8 <= GIBBS_MAX_BYTES)
+    K = None
+    if gibbs:
+        K = torch.empty((n, m), dtype=M.dtype, device=M.device)
+        _lib.check(lib.otg_gibbs_kernel(dt, ctypes.c_void_p(M.data_ptr()), n, m, M.stride(0), float(reg),
+                                        _lib.ptr(K), m, _lib.stream_handle(M.device)), "otg_gibbs_kernel")
+        p.K, p.ldk = K.data_ptr(), m
     _lib.check(lib.otg_sinkhorn_dense(ctypes.byref(p), ctypes.c_void_p(ws.data_ptr()),
                                       _lib.stream_handle(M.device)), "otg_sinkhorn_dense")
     r = DenseResult()
-    r.u, r.v, r.workspace = out_u, out_v, ws
+    r.u, r.v, r.workspace, r.K = out_u, out_v, ws, K
     r.status, r.niter, r.errs = None, None, None
     r.layout = (dt, n, m, cap, grid)
     r.method = method

@@ -33,7 +33,9 @@ namespace {
   X(reg_m1) \
   X(reg_m2) \
   X(c_ones) \
-  X(reserved2)
+  X(reserved2) \
+  X(K) \
+  X(ldk)
 #define OTG_FIELDS_OtgBaryProblem(X) \
   X(dtype) \
   X(method) \
@@ -112,7 +114,9 @@ namespace {
   X(timeout_ms) \
   X(omega) \
   X(check_period) \
-  X(reserved)
+  X(units_per_warp) \
+  X(split_cap_fill) \
+  X(split_cap_tail)
 #define OTG_FIELDS_OtgOnlineProblem(X) \
   X(X) \
   X(Y) \

@@ -101,6 +101,27 @@ template <int METHOD> struct LogDomain {
   static constexpr bool value = METHOD == OTG_METHOD_LOG || METHOD == OTG_METHOD_STAB;
 };
 
+// Internal variant of the scaling form whose matrix operand is the Gibbs
+// kernel K = ex2(M * c) itself (OtgDenseProblem::K), not the cost.
+constexpr int OTG_METHOD_KNOPP_K = 16;
+
+// Gibbs factor of one loaded entry: the entry itself when it is K, else the
+// exponential of the cost entry (the same ex2(M * c) either way).
+template <typename T, int METHOD>
+__device__ __forceinline__ T gibbs(T x, T c) {
+  if (METHOD == OTG_METHOD_KNOPP_K) return x;
+  return ex2(x * c);
+}
+
+// K = ex2(M * c) entry by entry (c = -log2(e)/reg, the factor of the
+// solver's passes), one row per CTA iteration.
+template <typename T>
+__global__ void gibbs_kernel(const T* __restrict__ M, int64_t n, int64_t m, int64_t ldm, T c, T* __restrict__ K,
+                             int64_t ldk) {
+  for (int64_t i = blockIdx.x; i < n; i += gridDim.x)
+    for (int64_t j = threadIdx.x; j < m; j += blockDim.x) K[i * ldk + j] = gibbs<T, OTG_METHOD_KNOPP>(M[i * ldm + j], c);
+}
+
 // Order-preserving map of doubles to unsigned keys (atomicMax on keys = max
 // on values; key 0 is below every value).
 __device__ __forceinline__ unsigned long long order_key(double x) {
@@ -197,7 +218,7 @@ __device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, int lan
 #pragma unroll
           for (int k = 0; k < VW; ++k) {
 #pragma unroll
-            for (int g = 0; g < GCOL; ++g) s[k] = fma(ex2(x[g][k] * A.c), ur[g], s[k]);
+            for (int g = 0; g < GCOL; ++g) s[k] = fma(gibbs<T, METHOD>(x[g][k], A.c), ur[g], s[k]);
           }
         }
       }
@@ -315,7 +336,7 @@ __device__ void row_pass(const DenseArgs<T>& A, const T* __restrict__ v, T* __re
           }
         } else {
 #pragma unroll
-          for (int k = 0; k < VW; ++k) s[r] = fma(ex2(x[r][k] * A.c), vv[k], s[r]);
+          for (int k = 0; k < VW; ++k) s[r] = fma(gibbs<T, METHOD>(x[r][k], A.c), vv[k], s[r]);
         }
       }
     }
@@ -782,6 +803,15 @@ int launch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
 template <typename T>
 int dispatch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
   constexpr int VW = Vec<T>::N;
+  if (p->method == OTG_METHOD_KNOPP && p->K) {
+    // the passes read K in place of M
+    OtgDenseProblem q = *p;
+    q.M = p->K;
+    q.ldm = p->ldk;
+    const bool vk = (q.m % VW == 0) && (q.ldm % VW == 0) && ((uintptr_t)q.M % 16 == 0);
+    return vk ? launch_dense<T, OTG_METHOD_KNOPP_K, true>(&q, ws, st)
+              : launch_dense<T, OTG_METHOD_KNOPP_K, false>(&q, ws, st);
+  }
   const bool vec = (p->m % VW == 0) && (p->ldm % VW == 0) && ((uintptr_t)p->M % 16 == 0);
   if (p->method == OTG_METHOD_LOG)
     return vec ? launch_dense<T, OTG_METHOD_LOG, true>(p, ws, st) : launch_dense<T, OTG_METHOD_LOG, false>(p, ws, st);
@@ -795,6 +825,7 @@ int dispatch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
 int check_problem(const OtgDenseProblem* p) {
   if (!p || !p->M || !p->a || !p->b || !p->out_u || !p->out_v) return OTG_ERR_ARG;
   if (p->n < 1 || p->m < 1 || p->ldm < p->m || p->hist_cap < 1) return OTG_ERR_ARG;
+  if (p->K && p->ldk < p->m) return OTG_ERR_ARG;
   if (p->dtype != OTG_F32 && p->dtype != OTG_F64) return OTG_ERR_DTYPE;
   if (p->method != OTG_METHOD_LOG && p->method != OTG_METHOD_KNOPP && p->method != OTG_METHOD_STAB &&
       p->method != OTG_METHOD_UNB)
@@ -853,6 +884,25 @@ int otg_dense_plan(int dtype, int method, const void* M, int64_t n, int64_t m, i
   } else {
     return OTG_ERR_DTYPE;
   }
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_gibbs_kernel(int dtype, const void* M, int64_t n, int64_t m, int64_t ldm, double reg, void* K,
+                     int64_t ldk, cudaStream_t stream) {
+  // any reg: the factor c = -log2(e)/reg is the solver's (reg = 0 gives its non-finite K)
+  if (!M || !K || n < 1 || m < 1 || ldm < m || ldk < m) return OTG_ERR_ARG;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t blocks = std::min<int64_t>(n, (int64_t)sms * 16);
+  if (dtype == OTG_F64)
+    gibbs_kernel<double><<<blocks, 256, 0, stream>>>((const double*)M, n, m, ldm, (double)(-OTG_LOG2E / reg),
+                                                     (double*)K, ldk);
+  else if (dtype == OTG_F32)
+    gibbs_kernel<float><<<blocks, 256, 0, stream>>>((const float*)M, n, m, ldm, (float)(-OTG_LOG2E / reg),
+                                                    (float*)K, ldk);
+  else
+    return OTG_ERR_DTYPE;
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 

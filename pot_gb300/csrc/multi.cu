@@ -68,6 +68,7 @@ struct MultiArgs {
   T omega;                  // over-relaxation (1: plain)
   bool relax;
   int period;               // iterations between stop tests
+  int upw, cap_fill, cap_tail;  // schedule: units per warp, row-split caps
 };
 
 // Index of the active slot whose prefix range holds `unit` (pre[k] <= unit < pre[k+1]).
@@ -318,7 +319,8 @@ __device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leavi
     if (threadIdx.x == blockDim.x - 1) s_base += s_scan[threadIdx.x];
     __syncthreads();
   }
-  // split factor: about 8 column-pass units per warp over the remaining work
+  // split factor: about upw (default 8) column-pass units per warp over the
+  // remaining work
   __shared__ int64_t s_slabs;
   if (threadIdx.x == 0) s_slabs = 0;
   __syncthreads();
@@ -331,11 +333,11 @@ __device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leavi
     atomicAdd(reinterpret_cast<unsigned long long*>(&s_slabs), (unsigned long long)part);
   }
   __syncthreads();
-  // capped at 16 chunks while the batch fills the GPU (more splits only
-  // lengthen the merge); a few remaining problems split up to 64 ways, since
-  // then the time per pass is that of one unit
-  int64_t S = s_slabs > 0 ? (8 * nwarps + s_slabs - 1) / s_slabs : 1;
-  const int64_t cap = s_slabs * 16 >= nwarps ? 16 : 64;
+  // capped at cap_fill (16) chunks while the batch fills the GPU (more
+  // splits only lengthen the merge); a few remaining problems split up to
+  // cap_tail (64) ways, since then the time per pass is that of one unit
+  int64_t S = s_slabs > 0 ? ((int64_t)A.upw * nwarps + s_slabs - 1) / s_slabs : 1;
+  const int64_t cap = s_slabs * A.cap_fill >= nwarps ? A.cap_fill : A.cap_tail;
   S = S > cap ? cap : S;
   for (int k = threadIdx.x; k < s_base; k += blockDim.x) {
     const int p = A.active[k];
@@ -469,6 +471,9 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   A.relax = q->omega != 0.0 && q->omega != 1.0;
   A.omega = (T)q->omega;
   A.period = q->check_period > 0 ? q->check_period : 10;
+  A.upw = q->units_per_warp > 0 ? std::min(q->units_per_warp, 1024) : 8;
+  A.cap_fill = q->split_cap_fill > 0 ? std::min(q->split_cap_fill, 64) : 16;
+  A.cap_tail = q->split_cap_tail > 0 ? std::min(q->split_cap_tail, 64) : 64;
   // carve the workspace
   char* w = static_cast<char*>(q->workspace);
   size_t off = 0;

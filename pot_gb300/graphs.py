@@ -1,0 +1,101 @@
+"""Repeated dense solves of one shape, replayed from a CUDA graph.
+
+A small ``ot.sinkhorn`` call (n = m = 1024 in float64: the cost matrix sits
+in L2 and the solve stops after a few tens of iterations) is bound by launch
+and host latency, not by HBM.  The iteration loop of a solve is already one
+launch (the persistent kernel of ``csrc/dense.cu`` decides convergence on the
+device); ``SinkhornGraph`` captures that launch together with the plan and
+the loss kernels into one CUDA graph, so a solve costs one graph launch and
+one read of the result block.  Results equal ``sinkhorn`` /
+``sinkhorn_log`` (``ot/bregman/_sinkhorn.py:487-687``, ``:690-918``) and
+``sinkhorn2``'s loss (``:435-438``) on the same inputs: the captured calls
+are the same C entry points.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from .bregman import NONCONV_MSG, default_grid, read_result, solve_dense
+
+_METHODS = {"sinkhorn": _lib.OTG_METHOD_KNOPP, "sinkhorn_knopp": _lib.OTG_METHOD_KNOPP,
+            "sinkhorn_log": _lib.OTG_METHOD_LOG}
+
+
+class SinkhornGraph:
+    """Solver for many dense problems of one shape (``n x m``, one dtype,
+    one ``reg``), each solve a replay of a captured CUDA graph.
+
+    ``__call__(a, b, M)`` takes device tensors, copies them into the graph's
+    input buffers, replays, and returns the plan (and the log of
+    ``sinkhorn`` / ``sinkhorn_log`` with ``log=True``, plus ``"loss"`` =
+    ``sum(M * P)`` in fp64).  The returned plan is the graph's output buffer:
+    the next call overwrites it (clone it to keep it)."""
+
+    def __init__(self, n, m, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, dtype=torch.float64,
+                 device=None, want_plan=True):
+        if method.lower() not in _METHODS:
+            raise ValueError("Unknown method '%s'." % method)
+        self.method = _METHODS[method.lower()]
+        dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        if dev.type != "cuda":
+            raise ValueError("pot_gb300.SinkhornGraph needs a CUDA device")
+        self.n, self.m, self.reg = int(n), int(m), float(reg)
+        self.numItermax, self.stopThr = int(numItermax), float(stopThr)
+        self.M = torch.zeros(self.n, self.m, dtype=dtype, device=dev)
+        self.a = torch.full((self.n,), 1.0 / self.n, dtype=dtype, device=dev)
+        self.b = torch.full((self.m,), 1.0 / self.m, dtype=dtype, device=dev)
+        self.P = torch.empty(self.n, self.m, dtype=dtype, device=dev) if want_plan else None
+        self.loss = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.grid = default_grid(self.n, self.m)
+        self.M.copy_(torch.rand(self.n, self.m, dtype=dtype, device=dev))
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            self._record()  # once outside the capture: module load, occupancy queries
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._record()
+        self.launches = 1 + (2 if want_plan else 1)  # solve, plan, loss kernels per replay
+
+    def _record(self):
+        lib = _lib.load()
+        self.r = solve_dense(self.M, self.a, self.b, self.reg, self.method, self.numItermax, self.stopThr,
+                             grid=self.grid, read_back=False)
+        st = _lib.stream_handle(self.M.device)
+        dt = _lib.dtype_code(self.M.dtype)
+        if self.P is not None:
+            _lib.check(lib.otg_dense_plan(dt, self.method, ctypes.c_void_p(self.M.data_ptr()), self.n, self.m,
+                                          self.m, _lib.ptr(self.r.u), _lib.ptr(self.r.v), self.reg,
+                                          _lib.ptr(self.P), self.m, None, st), "otg_dense_plan")
+        self.loss.zero_()
+        _lib.check(lib.otg_dense_plan(dt, self.method, ctypes.c_void_p(self.M.data_ptr()), self.n, self.m, self.m,
+                                      _lib.ptr(self.r.u), _lib.ptr(self.r.v), self.reg, None, 0,
+                                      _lib.ptr(self.loss), st), "otg_dense_plan")
+
+    def replay(self, a, b, M):
+        """Copy the inputs and launch the graph (no synchronisation)."""
+        if tuple(M.shape) != (self.n, self.m):
+            raise ValueError("SinkhornGraph: M has shape %s, the graph was captured for %s"
+                             % (tuple(M.shape), (self.n, self.m)))
+        self.M.copy_(M)
+        self.a.copy_(a)
+        self.b.copy_(b)
+        self.graph.replay()
+
+    def __call__(self, a, b, M, log=False, warn=True):
+        self.replay(a, b, M)
+        r = read_result(self.r)
+        if r.status == _lib.STATUS_MAXITER and warn:
+            import warnings
+            warnings.warn(NONCONV_MSG)
+        if not log:
+            return self.P
+        lg = {"err": list(r.errs), "niter": r.niter, "loss": float(self.loss[0])}
+        if self.method == _lib.OTG_METHOD_LOG:
+            lg.update(log_u=r.u, log_v=r.v, u=torch.exp(r.u), v=torch.exp(r.v))
+        else:
+            lg.update(u=r.u, v=r.v)
+        return self.P, lg

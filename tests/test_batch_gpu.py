@@ -280,3 +280,30 @@ def test_multi_stop_test_every_iteration(cuda):
         assert abs(float(every[4][p]) - e) <= 1e-6 * tol + 1e-3 * e
         r0 = int(layout.r_off_np[p])
         np.testing.assert_allclose(every[0][r0:r0 + n].cpu().numpy(), lg["log_u"], rtol=1e-9, atol=1e-9)
+
+
+def test_schedules_divide_work_without_changing_results(cuda, tmp_path, monkeypatch):
+    """Every schedule the autotuner may pick (CTAs per SM, units per warp,
+    row-split caps) runs the same per-problem iteration: float64 stop indices
+    identical, potentials to 1e-9; tune_multi picks one of them and caches it."""
+    from pot_gb300 import tune
+    monkeypatch.setenv("POT_GB300_TUNE_CACHE", str(tmp_path / "sched.json"))
+    monkeypatch.setattr(tune, "_TUNER", None)
+    Xs, Ys, As, Bs, regs = _ragged_case(17, 30, 2, 700)
+    base = pb.solve_sample_ragged(Xs, Ys, regs, As, Bs, reg_relative=True, max_iter=20000, tol=1e-9,
+                                  dtype=torch.float64)
+    L = base.layout
+    ap = torch.cat([torch.as_tensor(a, dtype=torch.float64) for a in As]).to(cuda)
+    bp = torch.cat([torch.as_tensor(b, dtype=torch.float64) for b in Bs]).to(cuda)
+    for s in [tune.Schedule(1, 4, 8, 16), tune.Schedule(2, 16, 32, 32), tune.Schedule(1, 8, 16, 64)]:
+        u, v, st, nit, err, _ = pb.run_multi(L, base.M, ap, bp, base.reg, 20000, 1e-9, schedule=s)
+        np.testing.assert_array_equal(nit.cpu().numpy(), base.niter.cpu().numpy())
+        np.testing.assert_allclose(u.cpu().numpy(), base.u.cpu().numpy(), rtol=1e-9, atol=1e-9)
+        np.testing.assert_allclose(v.cpu().numpy(), base.v.cpu().numpy(), rtol=1e-9, atol=1e-9)
+    best = tune.tune_multi(L, base.M, ap, bp, base.reg, iters=10, reps=1)
+    assert best.ctas_per_sm in tune.SPACE["ctas_per_sm"]["f64"]
+    assert tune.lookup(L) == best
+    assert len(tune.tuner().trials) == 1
+    r = pb.solve_sample_ragged(Xs, Ys, regs, As, Bs, reg_relative=True, max_iter=20000, tol=1e-9,
+                               dtype=torch.float64, autotune=True)
+    np.testing.assert_array_equal(r.niter.cpu().numpy(), base.niter.cpu().numpy())

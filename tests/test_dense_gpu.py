@@ -169,3 +169,25 @@ def test_knopp_multi_histogram(cuda):
     lref, lgr = oracle.sinkhorn_knopp(g["a"], g["b"], g["M"], 1.0, stopThr=1e-10)
     assert lg["niter"] == lgr["niter"]
     np.testing.assert_allclose(np.array(lg["err"], dtype=float), lgr["err"], rtol=1e-6)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("shape", [(300, 256), (127, 129)])
+def test_precomputed_gibbs_kernel_is_bit_identical(cuda, dtype, shape):
+    """The scaling form over a stored K = exp(-M/reg) (otg_gibbs_kernel, the
+    float64 default) runs the same iterates as exponentiating every entry
+    in the passes: identical potentials, stop index and error history."""
+    from pot_gb300 import bregman, _lib
+    n, m = shape
+    rng = np.random.default_rng(3)
+    M = oracle.sqeuclidean(rng.normal(size=(n, 2)), rng.normal(size=(m, 2)) + 1.0)
+    M = torch.tensor(M / M.max(), dtype=dtype, device=cuda)
+    a = torch.tensor(rng.dirichlet(np.ones(n)), dtype=dtype, device=cuda)
+    b = torch.tensor(rng.dirichlet(np.ones(m)), dtype=dtype, device=cuda)
+    r0 = bregman.solve_dense(M, a, b, 0.05, _lib.OTG_METHOD_KNOPP, 1000, 1e-9, gibbs=False)
+    r1 = bregman.solve_dense(M, a, b, 0.05, _lib.OTG_METHOD_KNOPP, 1000, 1e-9, gibbs=True)
+    assert r1.K is not None and r0.K is None
+    assert r0.niter == r1.niter and r0.status == r1.status
+    np.testing.assert_array_equal(r0.errs, r1.errs)
+    np.testing.assert_array_equal(r0.u.cpu().numpy(), r1.u.cpu().numpy())
+    np.testing.assert_array_equal(r0.v.cpu().numpy(), r1.v.cpu().numpy())
