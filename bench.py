@@ -393,6 +393,8 @@ def run_ragged(args, pk):
             "dtype": "f32", "config": {"workload": "%d uneven problems n,m~U[32,1024], d in {3,16}, reg=10^U[-3,-1] x "
                                                    "max cost, stopThr=1e-6" % B,
                                        "niter_median": float(np.median(nit)), "niter_max": int(nit.max()),
+                                       "niter_p99": float(np.percentile(nit, 99)),
+                                       "niter_top10": sorted(nit.tolist())[-10:],
                                        "status_counts": np.bincount(res.status.cpu().numpy(), minlength=4).tolist(),
                                        "schedule": dict(sched._asdict()) if sched else None,
                                        "tuning_trials_ms": [[list(c), "fill" if f else "tail", round(t, 3)]

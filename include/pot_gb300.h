@@ -282,10 +282,23 @@ typedef struct OtgMultiProblem {
   int32_t units_per_warp;
   int32_t split_cap_fill;
   int32_t split_cap_tail;
+  /* tail handoff: once at most this many problems remain and each fits the
+   * shared memory of one thread-block cluster, a cluster per problem
+   * finishes them (same iteration and stop test, cluster barriers instead of
+   * grid barriers; clusters take the problems from a queue).  0: default
+   * (three times the clusters the device holds at once); negative: never. */
+  int32_t tail_problems;
+  int32_t reserved;
 } OtgMultiProblem;
 size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, int64_t total_cols,
                                  int64_t total_partials);
 int otg_sinkhorn_multi(const OtgMultiProblem* q, cudaStream_t stream);
+/* The tail handoff's cluster shape on the current device: CTAs per cluster
+ * (0: no tail handoff), clusters resident at once, shared-memory bytes of
+ * cost block per CTA, and the CUDA error code of the last configuration
+ * query (0 when it succeeded). */
+int otg_multi_tail_config(int dtype, int32_t* cluster_ctas, int32_t* max_clusters, int64_t* tile_bytes,
+                          int32_t* cuda_error);
 
 /* ------------------------------------------------------------------------
  * Online ("lazy") log-domain Sinkhorn on point clouds with squared-Euclidean

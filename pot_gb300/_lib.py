@@ -47,7 +47,7 @@ class OtgMultiProblem(ctypes.Structure):
                 ("out_u", c_vp), ("out_v", c_vp), ("status", c_vp), ("niter", c_vp), ("err", c_vp),
                 ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32), ("omega", c_dbl),
                 ("check_period", c_i32), ("units_per_warp", c_i32), ("split_cap_fill", c_i32),
-                ("split_cap_tail", c_i32)]
+                ("split_cap_tail", c_i32), ("tail_problems", c_i32), ("reserved", c_i32)]
 
 
 class OtgCostTable(ctypes.Structure):
@@ -99,6 +99,8 @@ SIGNATURES = {
     "otg_transpose_batched": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp, c_i64,
                                              c_i64, c_vp]),
     "otg_lazy_loss": (ctypes.c_int, [ctypes.c_int, c_vp, c_vp, c_i64, c_i64, c_i32, c_vp, c_vp, c_dbl, c_vp, c_vp]),
+    "otg_multi_tail_config": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
+                                              ctypes.POINTER(c_i64), ctypes.POINTER(c_i32)]),
     "otg_gibbs_kernel": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_dbl, c_vp, c_i64, c_vp]),
     "otg_dense_marginals": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_dbl, c_vp, c_vp,
                                            c_vp]),

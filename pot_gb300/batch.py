@@ -119,21 +119,35 @@ def run_batched(layout, M_packed, a_packed, b_packed, reg, method, max_iter, tol
     return out_u, out_v, status, niter, err, reg_t
 
 
+def multi_tail_config(dtype=torch.float32):
+    """(CTAs per cluster, clusters resident at once, tile bytes per CTA, CUDA
+    error of the configuration query) of the batch kernel's tail handoff on
+    the current device; 0 CTAs means no handoff."""
+    lib = _lib.load()
+    cl, mx, err = _lib.c_i32(), _lib.c_i32(), _lib.c_i32()
+    tile = _lib.c_i64()
+    _lib.check(lib.otg_multi_tail_config(_lib.dtype_code(dtype), ctypes.byref(cl), ctypes.byref(mx),
+                                         ctypes.byref(tile), ctypes.byref(err)), "otg_multi_tail_config")
+    return cl.value, mx.value, tile.value, err.value
+
+
 def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-              events=None, omega=1.0, check_period=10, schedule=None):
+              events=None, omega=1.0, check_period=10, schedule=None, tail_problems=0, info=None):
     """Work-balanced persistent launch (csrc/multi.cu), log form, per-problem
     sinkhorn_log order and stop test.  Returns (u, v, status, niter, err, reg).
     ``omega != 1`` over-relaxes the potential updates and ``check_period``
     other than 10 moves the stop tests (no reference counterpart for either;
     the stop criterion is unchanged).  ``schedule`` (a ``tune.Schedule``)
     divides the work; by default the autotuner's cached choice for this
-    workload class, else the built-in one."""
+    workload class, else the built-in one.  ``tail_problems`` bounds the
+    cluster tail handoff (0: default, negative: off); with a dict ``info``
+    the call synchronises and reports the handoff iteration (-1: none)."""
     return _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u, grid, timeout_ms,
-                           events, omega, check_period, schedule)
+                           events, omega, check_period, schedule, tail_problems, info)
 
 
 def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-                    events=None, omega=1.0, check_period=10, schedule=None):
+                    events=None, omega=1.0, check_period=10, schedule=None, tail_problems=0, info=None):
     lib = _lib.load()
     if schedule is None:
         schedule = tune.lookup(layout) or tune.DEFAULT
@@ -169,12 +183,18 @@ def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, wa
         out_u=out_u.data_ptr(), out_v=out_v.data_ptr(), status=status.data_ptr(), niter=niter.data_ptr(),
         err=err.data_ptr(), workspace=ws.data_ptr(), workspace_bytes=wsb, timeout_ms=int(timeout_ms),
         omega=float(omega), check_period=int(check_period), units_per_warp=int(schedule.units_per_warp),
-        split_cap_fill=int(schedule.cap_fill), split_cap_tail=int(schedule.cap_tail))
+        split_cap_fill=int(schedule.cap_fill), split_cap_tail=int(schedule.cap_tail),
+        tail_problems=int(tail_problems))
     if events is not None:
         events[0].record()
     _lib.check(lib.otg_sinkhorn_multi(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_multi")
     if events is not None:
         events[1].record()
+    if info is not None:
+        # control block: the last 256 bytes of the workspace; [3] handoff iteration, [5] handed off
+        ctl = ws[wsb - 256:wsb - 256 + 32].cpu().numpy().view(np.int32)
+        info["handoff_ii"] = int(ctl[3]) if ctl[5] else -1
+        info["handoff_problems"] = int(ctl[0]) if ctl[5] else 0
     return out_u, out_v, status, niter, err, reg_t
 
 

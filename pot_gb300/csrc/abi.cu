@@ -116,7 +116,9 @@ namespace {
   X(check_period) \
   X(units_per_warp) \
   X(split_cap_fill) \
-  X(split_cap_tail)
+  X(split_cap_tail) \
+  X(tail_problems) \
+  X(reserved)
 #define OTG_FIELDS_OtgOnlineProblem(X) \
   X(X) \
   X(Y) \

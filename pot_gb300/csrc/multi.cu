@@ -18,9 +18,25 @@
 // All active problems share the iteration index, so the v buffers swap
 // globally.  Work units map to problems through prefix sums over the active
 // list (binary search).
+//
+// Tail.  Once few problems are left, an iteration costs the latency of its
+// grid barriers and dependent loads (~19 us, whatever the grid size), so a
+// batch whose last problems are slow to converge spends most of its time
+// there.  When at most tail_max problems remain and each fits (about) the
+// shared memory of one thread-block cluster, the batch kernel stops at the
+// decision point and multi_tail_kernel (launched behind it on the same
+// stream) finishes them: one cluster per problem, its cost block resident in
+// the CTAs' shared memory (rows beyond a CTA's tile, up to as many again,
+// read from the block each pass), column partials merged through
+// distributed shared memory and two hardware cluster barriers per
+// iteration.  The iteration, the stop test and the outputs are those of the
+// batch kernel.
 #include <algorithm>
+#include <cooperative_groups.h>
 #include "common.cuh"
 #include "../../include/pot_gb300.h"
+
+namespace cg = cooperative_groups;
 
 namespace otg {
 
@@ -69,7 +85,16 @@ struct MultiArgs {
   bool relax;
   int period;               // iterations between stop tests
   int upw, cap_fill, cap_tail;  // schedule: units per warp, row-split caps
+  // tail handoff: most problems handed over (0: never), CTAs per cluster,
+  // shared-memory bytes for one CTA's rows of a cost block
+  int tail_max, tail_cl;
+  int64_t tail_tile;
 };
+
+// Tail kernel limits: columns, rows per CTA
+constexpr int TL_MAXM = 2048;
+constexpr int TL_MAXR = 1024;
+constexpr int TL_THREADS = 256;
 
 // Index of the active slot whose prefix range holds `unit` (pre[k] <= unit < pre[k+1]).
 __device__ __forceinline__ int mt_find(const int64_t* pre, int n, int64_t unit) {
@@ -361,6 +386,15 @@ __device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leavi
       cc += m;
     }
     A.ucol_pre[na] = uc; A.urow_pre[na] = ur; A.colpre[na] = cc;
+    // hand the rest to the tail kernel when every remaining block fits a cluster
+    int tail = A.tail_max > 0 && na > 0 && na <= A.tail_max;
+    for (int k = 0; tail && k < na; ++k) {
+      const int p = A.active[k];
+      const int64_t rcap = (A.rows[p] + A.tail_cl - 1) / A.tail_cl;
+      // rows beyond the shared tile are streamed: up to twice the tile per CTA
+      if (A.cols[p] > TL_MAXM || rcap > TL_MAXR || rcap * A.ldm[p] * (int64_t)sizeof(T) > 2 * A.tail_tile) tail = 0;
+    }
+    A.ctl[2] = tail;
     A.ctl[0] = na;
     __threadfence();
   }
@@ -443,6 +477,17 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
       if (blockIdx.x == 0) mt_rebuild<T>(A, nact, leaving, s_scan, nwarps);
       if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
       if (ld_acquire_i(A.ctl) == 0) break;
+      if (ld_acquire_i(A.ctl + 2)) {
+        // handoff: v of iteration ii is in vnxt, u of ii-1 in A.u; the tail
+        // kernel continues with this iteration's row pass
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+          A.ctl[3] = ii;
+          A.ctl[4] = vnxt == A.v1 ? 1 : 0;
+          __threadfence();
+          A.ctl[5] = 1;
+        }
+        break;
+      }
     }
     { T* t = vcur; vcur = vnxt; vnxt = t; }
     const int nact2 = ld_acquire_i(A.ctl);
@@ -452,11 +497,323 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
   }
 }
 
+// Shared-memory layout of one tail CTA: its rows of the cost block (tile),
+// then column partials, row-group scratch, the full v, its share of the new
+// v, its rows' u and log2(a), and its squared-error partial.
+template <typename T>
+struct TailSmem {
+  static constexpr int VW = Vec<T>::N;
+  static constexpr size_t part = sizeof(MPair<T>) * TL_MAXM;
+  static constexpr size_t scratch = sizeof(MPair<T>) * 16 * 32 * VW;
+  static constexpr size_t vec = sizeof(T) * TL_MAXM;
+  static constexpr size_t rows = sizeof(T) * TL_MAXR;
+  static constexpr size_t aux = part + scratch + 2 * vec + 2 * rows + 16;
+};
+
+// One handed-over problem (slot q of the active list), solved by the calling
+// cluster to its end; every CTA of the cluster calls it.
+template <typename T>
+__device__ void tail_solve(const MultiArgs<T>& A, int q, cg::cluster_group& cl) {
+  constexpr int VW = Vec<T>::N;
+  using V = typename Vec<T>::type;
+  using SM = TailSmem<T>;
+  extern __shared__ __align__(16) unsigned char tl_smem[];
+  const int CL = (int)cl.num_blocks();
+  const int rank = (int)cl.block_rank();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
+  const int p = __ldcg(A.active + q);
+  const int n = A.rows[p], m = A.cols[p], ldm = A.ldm[p];
+  const int rcap = (n + CL - 1) / CL;
+  const int i0 = min(n, rank * rcap), i1 = min(n, i0 + rcap), nr = i1 - i0;
+  const int jb = (int)((int64_t)m * rank / CL), je = (int)((int64_t)m * (rank + 1) / CL);
+  const T c = (T)(-OTG_LOG2E / A.reg[p]);
+  const T L2E = T(OTG_LOG2E), LN2 = T(OTG_LN2);
+  const int64_t ro = A.r_off[p], co = A.c_off[p];
+  const size_t tile_bytes = (size_t)A.tail_tile;
+  T* tile = reinterpret_cast<T*>(tl_smem);
+  MPair<T>* part = reinterpret_cast<MPair<T>*>(tl_smem + tile_bytes);
+  MPair<T>* scr = reinterpret_cast<MPair<T>*>(tl_smem + tile_bytes + SM::part);
+  T* vfull = reinterpret_cast<T*>(tl_smem + tile_bytes + SM::part + SM::scratch);
+  T* vshare = vfull + TL_MAXM;
+  T* us = vshare + TL_MAXM;
+  T* las = us + TL_MAXR;
+  double* errp = reinterpret_cast<double*>(las + TL_MAXR);
+  __shared__ double s_red[TL_THREADS / 32];
+  // the first nres rows live in the tile, the rest are read from the cost block
+  const T* gM = A.M + A.m_off[p] + (int64_t)i0 * ldm;
+  const int nres = min(nr, (int)(tile_bytes / ((size_t)ldm * sizeof(T))));
+  auto ldrow = [&](int i, int j) -> V {
+    if (i < nres) return *reinterpret_cast<const V*>(tile + (int64_t)i * ldm + j);
+    return ld_stream(reinterpret_cast<const V*>(gM + (int64_t)i * ldm + j));
+  };
+  (void)L2E;
+
+  // load this CTA's rows of the cost block, its u, log2(a), and v of the handoff
+  {
+    const V* src = reinterpret_cast<const V*>(gM);
+    V* dst = reinterpret_cast<V*>(tile);
+    const int64_t nv = (int64_t)nres * ldm / VW;
+    for (int64_t k = tid; k < nv; k += TL_THREADS) dst[k] = ld_stream(src + k);
+    for (int i = tid; i < nr; i += TL_THREADS) {
+      us[i] = __ldcg(A.u + ro + i0 + i);
+      las[i] = lg2(A.a[ro + i0 + i]);
+    }
+    const T* vh = (__ldcg(A.ctl + 4) ? A.v1 : A.v0) + co;
+    for (int j = tid; j < m; j += TL_THREADS) vfull[j] = __ldcg(vh + j);
+  }
+  cl.sync();
+
+  // row pass over this CTA's rows with vfull; u relaxed like the batch kernel
+  auto row_pass = [&]() {
+    const int groups = (nr + MT_RW - 1) / MT_RW;
+    for (int grp = warp; grp < groups; grp += TL_THREADS / 32) {
+      const int r0 = grp * MT_RW;
+      T mx[MT_RW], s[MT_RW];
+#pragma unroll
+      for (int r = 0; r < MT_RW; ++r) { mx[r] = -INFINITY; s[r] = 0; }
+      for (int j = lane * VW; j < m; j += 32 * VW) {
+        T vv[VW];
+#pragma unroll
+        for (int k = 0; k < VW; ++k) vv[k] = (j + k < m) ? vfull[j + k] : T(-INFINITY);
+#pragma unroll
+        for (int r = 0; r < MT_RW; ++r) {
+          const int row = min(r0 + r, nr - 1);
+          T x[VW];
+          unpack(ldrow(row, j), x);
+          T t[VW];
+          T gm = -INFINITY;
+#pragma unroll
+          for (int k = 0; k < VW; ++k) { t[k] = fma(x[k], c, vv[k]); gm = fmax(gm, t[k]); }
+          const T nm = fmax(mx[r], gm);
+          if (nm != -INFINITY) {
+            T acc = s[r] * ex2(mx[r] - nm);
+#pragma unroll
+            for (int k = 0; k < VW; ++k) acc += ex2(t[k] - nm);
+            s[r] = acc;
+            mx[r] = nm;
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < MT_RW; ++r) warp_lse(mx[r], s[r]);
+#pragma unroll
+      for (int r = 0; r < MT_RW; ++r) {
+        if (lane == r && r0 + r < nr) {
+          const T un = las[r0 + r] - lse_value(mx[r], s[r]);
+          us[r0 + r] = A.relax ? fma(A.omega, un - us[r0 + r], us[r0 + r]) : un;
+        }
+      }
+    }
+    __syncthreads();
+  };
+
+  // column pass: partial (max, sum) per column over this CTA's rows -> part
+  auto col_pass = [&]() {
+    const int nslabs = (m + 32 * VW - 1) / (32 * VW);
+    const int RG = nslabs >= 8 ? 1 : (8 + nslabs - 1) / nslabs;
+    for (int unit = warp; unit < nslabs * RG; unit += TL_THREADS / 32) {
+      const int slab = unit % nslabs, g = unit / nslabs;
+      const int ra = nr * g / RG, rb = nr * (g + 1) / RG;
+      const int j0 = slab * 32 * VW + lane * VW;
+      T mx[VW], s[VW];
+#pragma unroll
+      for (int k = 0; k < VW; ++k) { mx[k] = -INFINITY; s[k] = 0; }
+      if (j0 < m) {
+        for (int i = ra; i < rb; i += MT_GCOL) {
+          T x[MT_GCOL][VW], ur[MT_GCOL];
+#pragma unroll
+          for (int gg = 0; gg < MT_GCOL; ++gg) {
+            if (i + gg < rb) {
+              unpack(ldrow(i + gg, j0), x[gg]);
+              ur[gg] = us[i + gg];
+            } else {
+#pragma unroll
+              for (int k = 0; k < VW; ++k) x[gg][k] = 0;
+              ur[gg] = -INFINITY;
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < VW; ++k) {
+            T t[MT_GCOL];
+            T gm = -INFINITY;
+#pragma unroll
+            for (int gg = 0; gg < MT_GCOL; ++gg) { t[gg] = fma(x[gg][k], c, ur[gg]); gm = fmax(gm, t[gg]); }
+            const T nm = fmax(mx[k], gm);
+            if (nm != -INFINITY) {
+              T acc = s[k] * ex2(mx[k] - nm);
+#pragma unroll
+              for (int gg = 0; gg < MT_GCOL; ++gg) acc += ex2(t[gg] - nm);
+              s[k] = acc;
+              mx[k] = nm;
+            }
+          }
+        }
+        MPair<T>* dst = RG == 1 ? part : scr + (int64_t)g * m;
+#pragma unroll
+        for (int k = 0; k < VW; ++k)
+          if (j0 + k < m) dst[j0 + k] = MPair<T>{mx[k], s[k]};
+      }
+    }
+    __syncthreads();
+    if (RG > 1) {
+      for (int j = tid; j < m; j += TL_THREADS) {
+        T mx = -INFINITY, s = 0;
+        for (int g = 0; g < RG; ++g) lse_merge(mx, s, scr[(int64_t)g * m + j].mx, scr[(int64_t)g * m + j].s);
+        part[j] = MPair<T>{mx, s};
+      }
+      __syncthreads();
+    }
+  };
+
+  auto write_out = [&](int status, int niter, double e) {
+    for (int i = tid; i < nr; i += TL_THREADS) A.out_u[ro + i0 + i] = us[i] * LN2;
+    if (rank == 0) {
+      for (int j = tid; j < m; j += TL_THREADS) A.out_v[co + j] = vfull[j] * LN2;
+      if (tid == 0) { A.status[p] = status; A.niter[p] = niter; A.err[p] = e; }
+    }
+  };
+
+  const int ii0 = __ldcg(A.ctl + 3);
+  row_pass();
+  bool prev_check = (ii0 % A.period == 0);
+  for (int it = ii0 + 1;; ++it) {
+    if (it == A.max_iter && !prev_check) {
+      cl.sync();  // no CTA leaves while another may still read its shared memory
+      write_out(OTG_STATUS_MAXITER, A.max_iter - 1, -1.0);
+      return;
+    }
+    col_pass();
+    cl.sync();
+    // merge this CTA's share of the columns; new v into vshare
+    double e2 = 0.0;
+    const bool update = it < A.max_iter;
+    for (int j = jb + tid; j < je; j += TL_THREADS) {
+      T mx = -INFINITY, s = 0;
+      for (int r2 = 0; r2 < CL; ++r2) {
+        const MPair<T> pr = cl.map_shared_rank(part, r2)[j];
+        lse_merge(mx, s, pr.mx, pr.s);
+      }
+      const T L = lse_value(mx, s);
+      const T bj = A.b[co + j];
+      if (prev_check) {
+        const double cs = (double)ex2(vfull[j] + L) - (double)bj;
+        e2 += cs * cs;
+      }
+      if (update) {
+        const T vn = lg2(bj) - L;
+        vshare[j] = A.relax ? fma(A.omega, vn - vfull[j], vfull[j]) : vn;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+    if (lane == 0) s_red[warp] = e2;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < TL_THREADS / 32; ++w) t += s_red[w];
+      *errp = t;
+    }
+    cl.sync();
+    if (prev_check || it == A.max_iter) {
+      double t = 0.0;
+      for (int r2 = 0; r2 < CL; ++r2) t += *cl.map_shared_rank(errp, r2);
+      const double e = prev_check ? sqrt(t) : -1.0;
+      const bool conv = prev_check && e < A.stop_thr;
+      if (conv || it == A.max_iter) {
+        cl.sync();
+        write_out(conv ? OTG_STATUS_CONVERGED : OTG_STATUS_MAXITER, conv ? it - 1 : A.max_iter - 1, e);
+        return;
+      }
+    }
+    // gather the new v from the owners of its shares
+    for (int j = tid; j < m; j += TL_THREADS) {
+      const int owner = (int)(((int64_t)(j + 1) * CL + m - 1) / m) - 1;
+      vfull[j] = cl.map_shared_rank(vshare, owner)[j];
+    }
+    __syncthreads();
+    row_pass();
+    prev_check = (it % A.period == 0);
+  }
+}
+
+// Tail workers: each cluster takes handed-over problems from a queue (slot
+// counter in the control block) until none is left, so more problems than
+// resident clusters can be handed over.
+template <typename T>
+__global__ void __launch_bounds__(TL_THREADS) multi_tail_kernel(MultiArgs<T> A) {
+  cg::cluster_group cl = cg::this_cluster();
+  // uniform over the grid: written by the batch kernel before it ended
+  if (__ldcg(A.ctl + 5) == 0 || __ldcg(A.ctl + 1) != 0) return;
+  const int nact = __ldcg(A.ctl);
+  __shared__ int s_q;
+  for (;;) {
+    if (cl.block_rank() == 0 && threadIdx.x == 0) s_q = atomicAdd(A.ctl + 6, 1);
+    cl.sync();
+    const int q = *cl.map_shared_rank(&s_q, 0);
+    cl.sync();  // every CTA has read rank 0's slot before rank 0 moves on or leaves
+    if (q >= nact) return;
+    tail_solve<T>(A, q, cl);
+  }
+}
+
 }  // namespace otg
 
 using namespace otg;
 
 namespace {
+// Cluster shape of the tail kernel on this device: 16 CTAs per cluster when
+// the device schedules such clusters at full shared memory, else 8 (the
+// portable size); max = clusters resident at once (the tail workers).
+// Queried once per device and type.
+struct TailCfg { int cl = 0, max = 0; size_t smem = 0; int64_t tile = 0; int err = 0; };
+
+template <typename T>
+TailCfg tail_config() {
+  static TailCfg cache[16];
+  static bool known[16] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 16) return TailCfg{};
+  if (known[dev]) return cache[dev];
+  TailCfg tc;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t smem = optin > 1024 ? (size_t)optin - 1024 : 0;  // room for the static shared arrays
+  cudaError_t e0 = smem > TailSmem<T>::aux + 16 * 1024
+                       ? cudaFuncSetAttribute(multi_tail_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                       : cudaErrorInvalidValue;
+  tc.err = (int)e0;
+  if (e0 == cudaSuccess) {
+    cudaFuncSetAttribute(multi_tail_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (int cl : {16, 8}) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)cl);
+      cfg.blockDim = dim3(TL_THREADS);
+      cfg.dynamicSmemBytes = smem;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)cl;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int ncl = 0;
+      const cudaError_t eq = cudaOccupancyMaxActiveClusters(&ncl, multi_tail_kernel<T>, &cfg);
+      tc.err = (int)eq;
+      if (eq == cudaSuccess && ncl >= 1) {
+        tc.cl = cl;
+        tc.max = ncl;
+        tc.smem = smem;
+        tc.tile = (int64_t)((smem - TailSmem<T>::aux) / 16 * 16);
+        break;
+      }
+    }
+  }
+  cudaGetLastError();  // a refused attribute or query leaves no error behind
+  cache[dev] = tc;
+  known[dev] = true;
+  return tc;
+}
+
 template <typename T>
 int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   MultiArgs<T> A{};
@@ -474,6 +831,10 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   A.upw = q->units_per_warp > 0 ? std::min(q->units_per_warp, 1024) : 8;
   A.cap_fill = q->split_cap_fill > 0 ? std::min(q->split_cap_fill, 64) : 16;
   A.cap_tail = q->split_cap_tail > 0 ? std::min(q->split_cap_tail, 64) : 64;
+  const TailCfg tc = tail_config<T>();
+  A.tail_cl = tc.cl;
+  A.tail_tile = tc.tile;
+  A.tail_max = q->tail_problems < 0 || tc.cl == 0 ? 0 : (q->tail_problems > 0 ? q->tail_problems : 3 * tc.max);
   // carve the workspace
   char* w = static_cast<char*>(q->workspace);
   size_t off = 0;
@@ -505,7 +866,25 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   void* args[] = {&A, &leaving};
   cudaError_t e = cudaLaunchCooperativeKernel((const void*)multi_sinkhorn_kernel<T>, dim3(grid), dim3(MT_THREADS),
                                               args, 0, st);
-  return e == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+  if (e != cudaSuccess) return OTG_ERR_CUDA;
+  if (A.tail_max > 0) {
+    // behind the batch kernel on the stream; returns at once unless it was handed problems
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(std::min(A.tail_max, tc.max) * A.tail_cl));  // resident workers
+    cfg.blockDim = dim3(TL_THREADS);
+    cfg.dynamicSmemBytes = tc.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)A.tail_cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, multi_tail_kernel<T>, A);
+    if (e != cudaSuccess) return OTG_ERR_CUDA;
+  }
+  return OTG_OK;
 }
 
 size_t multi_ws(int dtype, int64_t nprob, int64_t rows, int64_t cols, int64_t partials) {
@@ -521,6 +900,20 @@ extern "C" {
 size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, int64_t total_cols,
                                  int64_t total_partials) {
   return multi_ws(dtype, nprob, total_rows, total_cols, total_partials);
+}
+
+int otg_multi_tail_config(int dtype, int32_t* cluster_ctas, int32_t* max_clusters, int64_t* tile_bytes,
+                          int32_t* cuda_error) {
+  if (!cluster_ctas || !max_clusters || !tile_bytes || !cuda_error) return OTG_ERR_ARG;
+  TailCfg tc;
+  if (dtype == OTG_F64) tc = tail_config<double>();
+  else if (dtype == OTG_F32) tc = tail_config<float>();
+  else return OTG_ERR_DTYPE;
+  *cluster_ctas = tc.cl;
+  *max_clusters = tc.max;
+  *tile_bytes = tc.tile;
+  *cuda_error = tc.err;
+  return OTG_OK;
 }
 
 int otg_sinkhorn_multi(const OtgMultiProblem* q, cudaStream_t stream) {

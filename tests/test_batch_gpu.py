@@ -307,3 +307,52 @@ def test_schedules_divide_work_without_changing_results(cuda, tmp_path, monkeypa
     r = pb.solve_sample_ragged(Xs, Ys, regs, As, Bs, reg_relative=True, max_iter=20000, tol=1e-9,
                                dtype=torch.float64, autotune=True)
     np.testing.assert_array_equal(r.niter.cpu().numpy(), base.niter.cpu().numpy())
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_tail_clusters_continue_the_batch_iteration(cuda, dtype):
+    """When few problems remain and each fits a cluster's shared memory, one
+    thread-block cluster per problem finishes them: same stop indices
+    (float64) and potentials as the batch kernel run to the end alone."""
+    rng = np.random.default_rng(31)
+    B = 12
+    rows = np.concatenate([rng.integers(20, 60, B - 3), [301, 177, 5]])
+    cols = np.concatenate([rng.integers(20, 60, B - 3), [190, 333, 700]])
+    Ms = []
+    for n, m in zip(rows, cols):
+        M = oracle.sqeuclidean(rng.random((n, 3)), rng.random((m, 3)))
+        Ms.append(torch.tensor(M / M.max(), dtype=dtype, device=cuda))
+    # small reg on the three large problems: they run long after the others stop
+    reg = torch.tensor([0.05] * (B - 3) + [0.004, 0.004, 0.01], dtype=torch.float64, device=cuda)
+    tol = 1e-9 if dtype == torch.float64 else 1e-6
+    cl, ncl, tile, err = pb.multi_tail_config(dtype)
+    assert cl in (8, 16) and ncl >= 1 and tile >= 64 * 1024, (cl, ncl, tile, err)
+    # (iterations, problems, handoff threshold): the whole batch from the start
+    # (more problems than resident clusters: a queue), a late handoff of the
+    # last four problems, and a handoff of problems that end at max_iter
+    for max_iter, sub, tp in ((20000, slice(0, B), 0), (20000, slice(0, B), 4), (37, slice(B - 4, B), 0)):
+        lay = pb.RaggedLayout(rows[sub], cols[sub], dtype, cuda)
+        Mq = pb.pack_dense(lay, Ms[sub])
+        aq = torch.cat([torch.full((int(n),), 1.0 / n, dtype=dtype, device=cuda) for n in rows[sub]])
+        bq = torch.cat([torch.full((int(m),), 1.0 / m, dtype=dtype, device=cuda) for m in cols[sub]])
+        info = {}
+        off = pb.run_multi(lay, Mq, aq, bq, reg[sub], max_iter, tol, tail_problems=-1, info=info)
+        assert info["handoff_ii"] == -1
+        on = pb.run_multi(lay, Mq, aq, bq, reg[sub], max_iter, tol, tail_problems=tp, info=info)
+        nb = lay.B
+        limit = tp if tp > 0 else 3 * ncl
+        assert info["handoff_ii"] >= 1 and 1 <= info["handoff_problems"] <= min(nb, limit)
+        assert (info["handoff_ii"] == 1) == (nb <= limit)
+        np.testing.assert_array_equal(on[2].cpu().numpy(), off[2].cpu().numpy())
+        if dtype == torch.float64:
+            np.testing.assert_array_equal(on[3].cpu().numpy(), off[3].cpu().numpy())
+            np.testing.assert_allclose(on[0].cpu().numpy(), off[0].cpu().numpy(), rtol=1e-9, atol=1e-9)
+            np.testing.assert_allclose(on[1].cpu().numpy(), off[1].cpu().numpy(), rtol=1e-9, atol=1e-9)
+            np.testing.assert_allclose(on[4].cpu().numpy(), off[4].cpu().numpy(), rtol=1e-6, atol=1e-15)
+        else:
+            assert np.abs(on[3].cpu().numpy() - off[3].cpu().numpy()).max() <= 10
+            for p in range(nb):
+                r0, n = int(lay.r_off_np[p]), int(lay.rows_np[p])
+                uo, uf = on[0][r0:r0 + n].double(), off[0][r0:r0 + n].double()
+                np.testing.assert_allclose((uo - uo.mean()).cpu().numpy(), (uf - uf.mean()).cpu().numpy(),
+                                           atol=2e-3 * max(1.0, float(uf.abs().max())))
