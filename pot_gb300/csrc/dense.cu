@@ -89,6 +89,7 @@ struct DenseArgs {
   // unbalanced form only (sa, sb then hold alpha*u and beta*v)
   T fi1, fi2;
   const T* alw; const T* bew;           // c = alw bew^T (null: ones)
+  unsigned* slab_cnt;                   // [nslabs] column-pass units done per slab
 };
 
 // Per-thread maxima carried out of a pass (stabilised: d0; unbalanced:
@@ -156,8 +157,24 @@ constexpr int GCOL = 4;   // rows folded per max update in the column pass
 // warp results are merged in shared memory, so each column has one partial
 // pair per row chunk (few chunks: a short merge).
 // ---------------------------------------------------------------------------
+template <typename T, int METHOD>
+__device__ __forceinline__ void merge_col(const DenseArgs<T>& A, int64_t j, const T* __restrict__ vcur,
+                                          T* __restrict__ vnxt, bool check, bool update, T err_shift, double& e2,
+                                          Track& tr);
+
+// Column merge folded into the column pass: the CTA that completes the last
+// row chunk of a slab merges that slab's columns (per-thread error and
+// tracking accumulators), so the pass needs no grid barrier before the merge.
+template <typename T> struct ColFuse {
+  const T* vcur; T* vnxt;
+  bool check, update;
+  T shift;
+  double e2;
+  Track tr;
+};
+
 template <typename T, int METHOD, bool VEC>
-__device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, int lane) {
+__device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, int lane, ColFuse<T>* fuse = nullptr) {
   constexpr int VW = Vec<T>::N;
   using V = typename Vec<T>::type;
   __shared__ T s_mx[8][32 * Vec<T>::N], s_s[8][32 * Vec<T>::N];
@@ -236,6 +253,26 @@ __device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, int lan
           else S0 += s_s[w][c];
         }
         A.pcol[r * m + j] = Pair<T>{M0, S0};
+      }
+    }
+    if (fuse) {
+      __shared__ int s_last;
+      __threadfence();  // this unit's partials, before its arrival is counted
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const unsigned prev = atomicAdd(A.slab_cnt + slab, 1u);
+        s_last = prev == (unsigned)(A.Sr - 1);
+        if (s_last) atomicExch(A.slab_cnt + slab, 0u);  // every chunk has arrived: ready for the next pass
+      }
+      __syncthreads();
+      if (s_last) {
+        __threadfence();
+        for (int c = threadIdx.x; c < slab_w; c += blockDim.x) {
+          const int64_t j = slab * slab_w + c;
+          if (j < m)
+            merge_col<T, METHOD>(A, j, fuse->vcur, fuse->vnxt, fuse->check, fuse->update, fuse->shift, fuse->e2,
+                                 fuse->tr);
+        }
       }
     }
     __syncthreads();
@@ -391,11 +428,10 @@ __device__ void row_merge(const DenseArgs<T>& A, T* __restrict__ unew, long gtid
 // plan scaled by 2^err_shift).  The stabilised form also returns the
 // thread's max of v_new - SB.
 template <typename T, int METHOD>
-__device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* __restrict__ vnxt,
-                          bool check, bool update, double* err_slot, long gtid, long nthreads, T err_shift,
-                          Track& tr) {
-  double e2 = 0.0;
-  for (int64_t j = gtid; j < A.m; j += nthreads) {
+__device__ __forceinline__ void merge_col(const DenseArgs<T>& A, int64_t j, const T* __restrict__ vcur,
+                                          T* __restrict__ vnxt, bool check, bool update, T err_shift, double& e2,
+                                          Track& tr) {
+  {
     T mx = -INFINITY, s = 0;
     const T* base = reinterpret_cast<const T*>(A.pcol + j);
     if (LogDomain<METHOD>::value) lse_merge_strided(mx, s, base, 2 * A.m, A.Sr);
@@ -437,6 +473,28 @@ __device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* 
       }
     }
   }
+}
+
+// Block sum of the per-thread squared errors, one fp64 atomic per CTA.
+__device__ __forceinline__ void block_err_atomic(double e2, double* err_slot) {
+  __shared__ double red[32];
+  e2 = warp_sum(e2);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    atomicAdd(err_slot, t);
+  }
+  __syncthreads();
+}
+
+template <typename T, int METHOD>
+__device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* __restrict__ vnxt,
+                          bool check, bool update, double* err_slot, long gtid, long nthreads, T err_shift,
+                          Track& tr) {
+  double e2 = 0.0;
+  for (int64_t j = gtid; j < A.m; j += nthreads) merge_col<T, METHOD>(A, j, vcur, vnxt, check, update, err_shift, e2, tr);
   if (check) {
     // block reduction, then one fp64 atomic per CTA
     __shared__ double red[32];
@@ -543,14 +601,13 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
     }
   }
   for (int ii = 0; METHOD != OTG_METHOD_UNB; ++ii) {
-    col_pass<T, METHOD, VEC>(A, ucur, lane);
-    if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     const bool update = ii < A.max_iter;
     double* slot = A.hist + (nchk < A.hist_cap ? nchk : A.hist_cap - 1);
-    Track vt;
     const T shift = (METHOD == OTG_METHOD_STAB && absorbed) ? -(A.log2n + A.log2m) : T(0);
-    col_merge<T, METHOD>(A, vcur, vnxt, prev_check, update, slot, gtid, nthreads, shift, vt);
-    if (METHOD == OTG_METHOD_STAB && update) block_max_atomic(vt.d0, A.mslot + 2 + (ii & 1));
+    ColFuse<T> cf{vcur, vnxt, prev_check, update, shift, 0.0, Track{}};
+    col_pass<T, METHOD, VEC>(A, ucur, lane, &cf);
+    if (prev_check) block_err_atomic(cf.e2, slot);
+    if (METHOD == OTG_METHOD_STAB && update) block_max_atomic(cf.tr.d0, A.mslot + 2 + (ii & 1));
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     if (prev_check) {
       double e2 = *(volatile double*)slot;
@@ -694,7 +751,7 @@ namespace {
 struct Layout {
   int grid, Sr, Sc;
   int64_t rchunk, cchunk;
-  size_t off_state, off_pcol, off_prow, off_hist, off_ctrl, total;
+  size_t off_state, off_pcol, off_prow, off_hist, off_ctrl, off_cnt, total;
 };
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -742,6 +799,7 @@ Layout make_layout(int64_t n, int64_t m, int hist_cap, int grid) {
   L.off_prow = off; off = align_up(off + sizeof(Pair<T>) * (size_t)(L.Sc > 1 ? L.Sc : 0) * n, 256);
   L.off_hist = off; off = align_up(off + sizeof(double) * (size_t)hist_cap, 256);
   L.off_ctrl = off; off = align_up(off + 256, 256);
+  L.off_cnt = off; off = align_up(off + sizeof(unsigned) * (size_t)nslabs, 256);
   L.total = off;
   return L;
 }
@@ -786,6 +844,7 @@ int launch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
   A.log2tau = (T)(METHOD == OTG_METHOD_STAB ? std::log2(p->tau) : 0.0);
   A.period = METHOD == OTG_METHOD_STAB ? p->check_period : 10;
   A.mslot = reinterpret_cast<unsigned long long*>(base + L.off_ctrl + 64);
+  A.slab_cnt = reinterpret_cast<unsigned*>(base + L.off_cnt);
   if (METHOD == OTG_METHOD_UNB) {
     A.fi1 = (T)(std::isinf(p->reg_m1) ? 1.0 : p->reg_m1 / (p->reg_m1 + p->reg));
     A.fi2 = (T)(std::isinf(p->reg_m2) ? 1.0 : p->reg_m2 / (p->reg_m2 + p->reg));
