@@ -496,6 +496,43 @@ def run_small(args, pk):
                          "alg_bytes_per_launch": alg}}
 
 
+def run_tail(args, pk):
+    """Cost of one iteration once few problems remain: the batch kernel alone
+    against the cluster tail (fixed iteration counts, stop threshold 0, so
+    every problem runs them all), float32, reg = 0.001 x raw squared distance,
+    points ~ U[0,1]^3."""
+    import torch
+    from pot_gb300 import batch as pb
+    dev = torch.device("cuda:0")
+    g = torch.Generator(device=dev); g.manual_seed(5)
+    out = {}
+    for shape in ([(375, 190), (191, 179)], [(64, 64)], [(800, 800)]):
+        rows = np.array([r for r, _ in shape]); cols = np.array([c for _, c in shape])
+        layout = pb.RaggedLayout(rows, cols, torch.float32, dev)
+        Ms = [torch.cdist(torch.rand(n, 3, generator=g, device=dev), torch.rand(m, 3, generator=g, device=dev)).pow(2)
+              for n, m in shape]
+        Mp = pb.pack_dense(layout, Ms)
+        a = torch.cat([torch.full((int(n),), 1.0 / n, device=dev) for n in rows])
+        b = torch.cat([torch.full((int(m),), 1.0 / m, device=dev) for m in cols])
+        key = " + ".join("%dx%d" % sh for sh in shape)
+        out[key] = {}
+        for name, tp in (("batch_kernel", -1), ("cluster_tail", 0)):
+            for _ in range(args.warmup):
+                pb.run_multi(layout, Mp, a, b, 0.001, 200, 0.0, tail_problems=tp)
+            its = 6000
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            pb.run_multi(layout, Mp, a, b, 0.001, its, 0.0, tail_problems=tp)
+            e1.record()
+            torch.cuda.synchronize()
+            out[key][name] = e0.elapsed_time(e1) / its * 1e3
+    first = out["375x190 + 191x179"]
+    return {"metric": "us per iteration, last problems of a batch", "value": first["cluster_tail"], "unit": "us",
+            "higher_is_better": False, "dtype": "f32", "per_shape_us": out,
+            "config": {"workload": "problems left at the end of a batch, fixed 6000 iterations, float32"}}
+
+
 def _lib_log():
     from pot_gb300 import _lib
     return _lib.OTG_METHOD_LOG
@@ -630,7 +667,7 @@ def main():
     pk = peaks()
     if args.workload != "warmstart":
         fn = {"online": run_online, "gw": run_gw, "ragged": run_ragged, "dense": run_dense,
-              "batch": run_batch, "small": run_small}[args.workload]
+              "batch": run_batch, "small": run_small, "tail": run_tail}[args.workload]
         line = {"n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                 "data": "synthetic"}
         line.update(fn(args, pk))
