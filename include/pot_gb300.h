@@ -353,7 +353,8 @@ typedef struct OtgCostTable {
   const int32_t* ldm;
   void* max_out;
   int32_t fixed_dim;  /* 0, or the dimension every problem shares when it is 2, 3, 8 or 16
-                         (float32: register-tiled kernel; must equal max_dim) */
+                         (float32: register-tiled kernel with 16-byte stores; must equal
+                         max_dim, and every m_off[p] and ldm[p] must be a multiple of 4) */
 } OtgCostTable;
 int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t stream);
 
@@ -390,6 +391,16 @@ int otg_nearest_mass(const float* X, const float* C, int32_t nprob, int32_t n, i
  * out[(r_off[p]+i)*ntau + k] = -tau_k ln sum_j b_j exp(g_j - M_ij / (scale[p] tau_k)).
  * g (natural-log target potentials packed like b) may be NULL (zero
  * potential).  f32 problem table as for otg_sinkhorn_batched. */
+/* Soft-mins of the n points of each cloud of X (P x n x d, pair stride sx)
+ * over the k weighted atoms C of the pair (P x k x d, stride sc; weights b,
+ * P x k), squared distances computed on the fly: out_f (P x n, optional) =
+ * the c-transform -g_tau log sum_k b_k exp(g_k - |x - y_k|^2 / (scale g_tau)),
+ * out_F (P x n x ntau) = the same with g = 0 at each taus[t]; units of
+ * scale[p].  d in {2, 3, 8, 16}; OTG_ERR_UNSUPPORTED otherwise.  (Learned
+ * warm start: the multiscale prior and the network's distance features.) */
+int otg_softmin_points(const float* X, const float* C, int32_t nprob, int32_t n, int32_t k, int32_t d, int64_t sx,
+                       int64_t sc, const float* b, const float* g, float g_tau, const float* scale,
+                       const float* taus, int32_t ntau, float* out_f, float* out_F, cudaStream_t stream);
 int otg_softmin_features(const float* M, const int64_t* m_off, const int32_t* rows, const int32_t* cols,
                          const int32_t* ldm, const int64_t* r_off, const int64_t* c_off, const float* b,
                          const float* scale, const float* taus, int32_t ntau, int32_t nprob, int32_t max_rows,
@@ -401,6 +412,16 @@ int otg_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, c
                  cudaStream_t stream);
 int otg_mlp_relu_bwd(float* dY, const float* Y, int64_t n, cudaStream_t stream);
 int otg_mlp_colsum(const float* X, int64_t R, int64_t C, float* out, cudaStream_t stream);
+/* Fused inference of the warm-start network (shipped sizes d = 16, widths
+ * 32/32, head input 22 + 2 x 32, head width 64; OTG_ERR_UNSUPPORTED for
+ * others): encoder + mean pooling of P clouds of n points into s (P x h2),
+ * and the head over the per-point inputs Z (P x n x dz) with the pooled
+ * summaries sX, sY -> f (P x n). */
+int otg_mlp_encode_pool(const float* X, int64_t P, int64_t n, int32_t d, int32_t h1, int32_t h2, const float* W1,
+                        const float* b1, const float* W2, const float* b2, float* s, cudaStream_t stream);
+int otg_mlp_head(const float* Z, int64_t P, int64_t n, int32_t dz, int32_t h2, int32_t h3, const float* sX,
+                 const float* sY, const float* W3, const float* b3, const float* W4, const float* b4, const float* W5,
+                 const float* b5, float* f, cudaStream_t stream);
 int otg_mlp_segment_mean(const float* X, int64_t P, int64_t n, int64_t C, float* out, cudaStream_t stream);
 int otg_mlp_segment_mean_bwd(const float* dS, int64_t P, int64_t n, int64_t C, float* dX, int accumulate,
                              cudaStream_t stream);

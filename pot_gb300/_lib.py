@@ -115,6 +115,12 @@ SIGNATURES = {
     "otg_batched_sqdist": (ctypes.c_int, [ctypes.POINTER(OtgCostTable), c_i32, c_vp]),
     "otg_batched_plan": (ctypes.c_int, [ctypes.POINTER(OtgPlanTable), c_i32, c_vp]),
     "otg_nearest_mass": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i64, c_i64, c_vp, c_vp]),
+    "otg_mlp_encode_pool": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                            c_vp]),
+    "otg_mlp_head": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                     c_vp, c_vp, c_vp]),
+    "otg_softmin_points": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i64, c_i64, c_vp, c_vp,
+                                           ctypes.c_float, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
     "otg_softmin_features": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32,
                                             c_i32, c_vp, c_vp, c_vp]),
     "otg_gemm_f32": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, c_i64, c_i64, c_i64, ctypes.c_float, c_vp, c_i64,

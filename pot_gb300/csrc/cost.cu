@@ -101,8 +101,9 @@ __global__ void __launch_bounds__(256) batched_sqdist_kernel(OtgCostTable t) {
 
 // Register-tiled float32 cost blocks for the common point dimensions: a CTA
 // computes 64 rows x 256 columns of one problem, both point tiles staged in
-// shared memory dimension-major; each thread owns 8 rows x 8 adjacent columns
-// (64 accumulators) and writes them as 16-byte stores.  Same arithmetic as
+// shared memory dimension-major; each thread owns 8 rows x (4 + 4) columns --
+// columns 4l..4l+3 and 128+4l..128+4l+3 for lane l -- so each 16-byte store
+// of a warp covers 512 contiguous bytes (64 accumulators per thread).  Same arithmetic as
 // the kernel above: sum_k (x_k - y_k)^2 in order of k, +inf padding.
 // grid = (column-tile stride, row tiles, problems).
 constexpr int SQ_R = 64, SQ_C = 256;
@@ -134,8 +135,8 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
     for (int k = 0; k < D; ++k) {
       const float4 xa = *reinterpret_cast<const float4*>(xt + k * SQ_R + warp * 8);
       const float4 xb = *reinterpret_cast<const float4*>(xt + k * SQ_R + warp * 8 + 4);
-      const ulonglong2 ya = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_C + lane * 8);
-      const ulonglong2 yb = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_C + lane * 8 + 4);
+      const ulonglong2 ya = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_C + lane * 4);
+      const ulonglong2 yb = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_C + SQ_C / 2 + lane * 4);
       const float xv[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
       const unsigned long long yp[4] = {ya.x, ya.y, yb.x, yb.y};
 #pragma unroll
@@ -158,7 +159,9 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
         acc[i][2 * j] = __uint_as_float((unsigned)(acc2[i][j] & 0xffffffffull));
         acc[i][2 * j + 1] = __uint_as_float((unsigned)(acc2[i][j] >> 32));
       }
-    const int cb = c0 + lane * 8;
+    // columns of acc[i][0..3]: ca + 0..3; of acc[i][4..7]: cz + 0..3 (ldm is a
+    // multiple of 4, so a group starting below ldm ends within it)
+    const int ca = c0 + lane * 4, cz = c0 + SQ_C / 2 + lane * 4;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int row = r0 + warp * 8 + i;
@@ -166,17 +169,13 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
       float v[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        if (cb + j < m) { v[j] = acc[i][j]; local_max = fmaxf(local_max, acc[i][j]); }
+        const int col = (j < 4 ? ca : cz) + (j & 3);
+        if (col < m) { v[j] = acc[i][j]; local_max = fmaxf(local_max, acc[i][j]); }
         else v[j] = INFINITY;
       }
-      float* dst = M + (int64_t)row * ldm + cb;
-      if (cb + 8 <= ldm) {
-        reinterpret_cast<float4*>(dst)[0] = make_float4(v[0], v[1], v[2], v[3]);
-        reinterpret_cast<float4*>(dst)[1] = make_float4(v[4], v[5], v[6], v[7]);
-      } else {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) if (cb + j < ldm) dst[j] = v[j];
-      }
+      float* dst = M + (int64_t)row * ldm;
+      if (ca < ldm) *reinterpret_cast<float4*>(dst + ca) = make_float4(v[0], v[1], v[2], v[3]);
+      if (cz < ldm) *reinterpret_cast<float4*>(dst + cz) = make_float4(v[4], v[5], v[6], v[7]);
     }
   }
 }
@@ -335,6 +334,78 @@ __global__ void __launch_bounds__(256) softmin_features_kernel(const float* __re
   }
 }
 
+// Soft-min of every source point over the k weighted atoms of its pair, the
+// squared distances computed on the fly (no cost block): one thread per
+// point, the pair's atoms in shared memory (stride D + 1: conflict-free).
+// Two sweeps over the atoms -- the maxima, then the sums -- so every term
+// costs one exponential; the squared distances are recomputed in the second
+// sweep (FMAs are cheaper than storing them).  Column 0 of the result is the
+// c-transform of the atoms' potential g at temperature g_tau (if g is given),
+// columns 1.. the soft-mins of the zero potential at taus[]; all in units of
+// scale[p], as softmin_features_kernel computes them from a cost block.
+template <int D>
+__global__ void __launch_bounds__(256) softmin_points_kernel(const float* __restrict__ X, const float* __restrict__ C,
+                                                             int n, int k, int64_t sx, int64_t sc,
+                                                             const float* __restrict__ bw,
+                                                             const float* __restrict__ gw, float g_tau,
+                                                             const float* __restrict__ scale,
+                                                             const float* __restrict__ taus, int ntau,
+                                                             float* __restrict__ out_f, float* __restrict__ out_F) {
+  extern __shared__ float sp_smem[];
+  const int p = blockIdx.y;
+  float* cs = sp_smem;                         // [k][D + 1]
+  float* lb = cs + (size_t)k * (D + 1);        // log2 b
+  float* lg = lb + k;                          // log2 b + g log2 e
+  const float* Cp = C + p * sc;
+  for (int e = threadIdx.x; e < k * D; e += blockDim.x) cs[(e / D) * (D + 1) + e % D] = Cp[e];
+  for (int c = threadIdx.x; c < k; c += blockDim.x) {
+    const float l = lg2(bw[(int64_t)p * k + c]);
+    lb[c] = l;
+    lg[c] = gw ? l + gw[(int64_t)p * k + c] * (float)OTG_LOG2E : l;
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float x[D];
+#pragma unroll
+  for (int q = 0; q < D; ++q) x[q] = X[p * sx + (int64_t)i * D + q];
+  const int nt = ntau + 1;                     // slot 0: the c-transform of g
+  float ck[SM_MAXTAU + 1], mx[SM_MAXTAU + 1], s[SM_MAXTAU + 1];
+#pragma unroll
+  for (int t = 0; t <= SM_MAXTAU; ++t) {
+    const float tau = t == 0 ? g_tau : (t <= ntau ? taus[t - 1] : 1.f);
+    ck[t] = -(float)OTG_LOG2E / (scale[p] * tau);
+    mx[t] = -INFINITY;
+    s[t] = 0.f;
+  }
+  auto dist = [&](int c) {
+    const float* y = cs + c * (D + 1);
+    float d2 = 0.f;
+#pragma unroll
+    for (int q = 0; q < D; ++q) { const float df = x[q] - y[q]; d2 = fmaf(df, df, d2); }
+    return d2;
+  };
+  for (int c = 0; c < k; ++c) {
+    const float d2 = dist(c);
+    mx[0] = fmaxf(mx[0], fmaf(d2, ck[0], lg[c]));
+#pragma unroll
+    for (int t = 1; t <= SM_MAXTAU; ++t)
+      if (t < nt) mx[t] = fmaxf(mx[t], fmaf(d2, ck[t], lb[c]));
+  }
+  for (int c = 0; c < k; ++c) {
+    const float d2 = dist(c);
+    s[0] += ex2(fmaf(d2, ck[0], lg[c]) - mx[0]);
+#pragma unroll
+    for (int t = 1; t <= SM_MAXTAU; ++t)
+      if (t < nt) s[t] += ex2(fmaf(d2, ck[t], lb[c]) - mx[t]);
+  }
+  const int64_t row = (int64_t)p * n + i;
+  if (out_f) out_f[row] = -g_tau * (float)OTG_LN2 * lse_value(mx[0], s[0]);
+#pragma unroll
+  for (int t = 1; t <= SM_MAXTAU; ++t)
+    if (t < nt) out_F[row * ntau + (t - 1)] = -taus[t - 1] * (float)OTG_LN2 * lse_value(mx[t], s[t]);
+}
+
 // Voronoi cell masses: for every point of cloud p (n points, rows of X), the
 // nearest of its k centres (the first k points of the paired centre cloud)
 // gains weight 1/n.  Centres are staged in shared memory; one thread per point.
@@ -467,6 +538,27 @@ int otg_nearest_mass(const float* X, const float* C, int32_t nprob, int32_t n, i
   else if (d == 3) nearest_mass_kernel<3><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, w);
   else if (d == 2) nearest_mass_kernel<2><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, w);
   else return OTG_ERR_UNSUPPORTED;
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_softmin_points(const float* X, const float* C, int32_t nprob, int32_t n, int32_t k, int32_t d, int64_t sx,
+                       int64_t sc, const float* b, const float* g, float g_tau, const float* scale,
+                       const float* taus, int32_t ntau, float* out_f, float* out_F, cudaStream_t stream) {
+  if (!X || !C || !b || !scale || nprob < 1 || nprob > 65535 || n < 1 || k < 1) return OTG_ERR_ARG;
+  if (ntau < 0 || ntau > SM_MAXTAU || (ntau > 0 && (!taus || !out_F)) || (!out_f && ntau == 0)) return OTG_ERR_ARG;
+  if (out_f && !(g_tau > 0)) return OTG_ERR_ARG;
+  const size_t sm = sizeof(float) * ((size_t)k * (d + 1) + 2 * (size_t)k);
+  if (sm > 48 * 1024) return OTG_ERR_UNSUPPORTED;
+  dim3 grid((unsigned)((n + 255) / 256), (unsigned)nprob);
+  const float gt = out_f ? g_tau : 1.f;
+#define OTG_SOFTMIN_POINTS(DD) \
+  softmin_points_kernel<DD><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, b, g, gt, scale, taus, ntau, out_f, out_F)
+  if (d == 16) OTG_SOFTMIN_POINTS(16);
+  else if (d == 8) OTG_SOFTMIN_POINTS(8);
+  else if (d == 3) OTG_SOFTMIN_POINTS(3);
+  else if (d == 2) OTG_SOFTMIN_POINTS(2);
+  else return OTG_ERR_UNSUPPORTED;
+#undef OTG_SOFTMIN_POINTS
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 

@@ -236,6 +236,121 @@ static int gemm_batched(int ta, int tb, int64_t M, int64_t N, int64_t K, T alpha
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------------------
+// Fused inference of the warm-start network (no activations in memory).
+//
+// Encoder + pooling: s[p] = mean_i relu(relu(x_i W1 + b1) W2 + b2) over the
+// n points of cloud p; one thread per point, weights in shared memory, the
+// block's sum added to s[p] (pre-scaled by 1/n) with one atomic per output.
+template <int D, int H1, int H2>
+__global__ void __launch_bounds__(256) mlp_encode_pool_kernel(const float* __restrict__ X, int n,
+                                                              const float* __restrict__ W1, const float* __restrict__ b1,
+                                                              const float* __restrict__ W2, const float* __restrict__ b2,
+                                                              float* __restrict__ s) {
+  __shared__ float w1[D * H1], sb1[H1], w2[H1 * H2], sb2[H2], acc[H2];
+  const int p = blockIdx.y;
+  for (int e = threadIdx.x; e < D * H1; e += blockDim.x) w1[e] = W1[e];
+  for (int e = threadIdx.x; e < H1 * H2; e += blockDim.x) w2[e] = W2[e];
+  for (int e = threadIdx.x; e < H1; e += blockDim.x) sb1[e] = b1[e];
+  for (int e = threadIdx.x; e < H2; e += blockDim.x) { sb2[e] = b2[e]; acc[e] = 0.f; }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float h2v[H2];
+#pragma unroll
+  for (int o = 0; o < H2; ++o) h2v[o] = 0.f;
+  if (i < n) {
+    float x[D];
+#pragma unroll
+    for (int q = 0; q < D; ++q) x[q] = X[((int64_t)p * n + i) * D + q];
+    float h1v[H1];
+#pragma unroll
+    for (int o = 0; o < H1; ++o) {
+      float a = sb1[o];
+#pragma unroll
+      for (int q = 0; q < D; ++q) a = fmaf(x[q], w1[q * H1 + o], a);
+      h1v[o] = fmaxf(a, 0.f);
+    }
+    const float inv = 1.f / (float)n;
+#pragma unroll
+    for (int o = 0; o < H2; ++o) {
+      float a = sb2[o];
+#pragma unroll
+      for (int q = 0; q < H1; ++q) a = fmaf(h1v[q], w2[q * H2 + o], a);
+      h2v[o] = fmaxf(a, 0.f) * inv;
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < H2; ++o) {
+    float v = h2v[o];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(acc + o, v);
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < H2; o += blockDim.x) atomicAdd(s + (int64_t)p * H2 + o, acc[o]);
+}
+
+// Head: f_i = relu(relu([z_i, sX_p, sY_p] W3 + b3) W4 + b4) W5 + b5.  The
+// summaries' part of the first layer is the same for every point of a pair:
+// it is folded into a per-pair bias once per block.  One thread per point.
+template <int DZ, int H2, int H3>
+__global__ void __launch_bounds__(128) mlp_head_kernel(const float* __restrict__ Z, int n,
+                                                       const float* __restrict__ sX, const float* __restrict__ sY,
+                                                       const float* __restrict__ W3, const float* __restrict__ b3,
+                                                       const float* __restrict__ W4, const float* __restrict__ b4,
+                                                       const float* __restrict__ W5, const float* __restrict__ b5,
+                                                       float* __restrict__ f) {
+  __shared__ __align__(16) float w3[DZ * H3];
+  __shared__ __align__(16) float w4t[H3 * H3];  // transposed: [out][in]
+  __shared__ float cb[H3], sb4[H3], w5[H3];
+  const int p = blockIdx.y;
+  for (int e = threadIdx.x; e < DZ * H3; e += blockDim.x) w3[e] = W3[e];
+  for (int e = threadIdx.x; e < H3 * H3; e += blockDim.x) { const int a = e / H3, b = e % H3; w4t[b * H3 + a] = W4[e]; }
+  for (int o = threadIdx.x; o < H3; o += blockDim.x) {
+    float a = b3[o];
+    for (int q = 0; q < H2; ++q) a = fmaf(sX[(int64_t)p * H2 + q], W3[(DZ + q) * H3 + o], a);
+    for (int q = 0; q < H2; ++q) a = fmaf(sY[(int64_t)p * H2 + q], W3[(DZ + H2 + q) * H3 + o], a);
+    cb[o] = a;
+    sb4[o] = b4[o];
+    w5[o] = W5[o];
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float z[DZ];
+#pragma unroll
+  for (int q = 0; q < DZ; ++q) z[q] = Z[((int64_t)p * n + i) * DZ + q];
+  float h3v[H3];
+#pragma unroll
+  for (int o = 0; o < H3; ++o) h3v[o] = cb[o];
+#pragma unroll
+  for (int q = 0; q < DZ; ++q) {
+#pragma unroll
+    for (int o = 0; o < H3; o += 4) {
+      const float4 w = *reinterpret_cast<const float4*>(w3 + q * H3 + o);
+      h3v[o] = fmaf(z[q], w.x, h3v[o]);
+      h3v[o + 1] = fmaf(z[q], w.y, h3v[o + 1]);
+      h3v[o + 2] = fmaf(z[q], w.z, h3v[o + 2]);
+      h3v[o + 3] = fmaf(z[q], w.w, h3v[o + 3]);
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < H3; ++o) h3v[o] = fmaxf(h3v[o], 0.f);
+  float out = b5[0];
+  for (int o = 0; o < H3; ++o) {
+    float a = sb4[o];
+#pragma unroll
+    for (int q = 0; q < H3; q += 4) {
+      const float4 w = *reinterpret_cast<const float4*>(w4t + o * H3 + q);
+      a = fmaf(h3v[q], w.x, a);
+      a = fmaf(h3v[q + 1], w.y, a);
+      a = fmaf(h3v[q + 2], w.z, a);
+      a = fmaf(h3v[q + 3], w.w, a);
+    }
+    out = fmaf(fmaxf(a, 0.f), w5[o], out);
+  }
+  f[(int64_t)p * n + i] = out;
+}
+
 extern "C" {
 
 int otg_gemm_f32(int ta, int tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda,
@@ -270,6 +385,27 @@ int otg_mlp_colsum(const float* X, int64_t R, int64_t C, float* out, cudaStream_
   if (cudaMemsetAsync(out, 0, sizeof(float) * C, stream) != cudaSuccess) return OTG_ERR_CUDA;
   dim3 grid((unsigned)((C + 127) / 128), (unsigned)std::min<int64_t>(R, 256));
   colsum_kernel<<<grid, 128, 0, stream>>>(X, R, C, out, 1);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_encode_pool(const float* X, int64_t P, int64_t n, int32_t d, int32_t h1, int32_t h2, const float* W1,
+                        const float* b1, const float* W2, const float* b2, float* s, cudaStream_t stream) {
+  if (!X || !W1 || !b1 || !W2 || !b2 || !s || P < 1 || P > 65535 || n < 1) return OTG_ERR_ARG;
+  if (!(d == 16 && h1 == 32 && h2 == 32)) return OTG_ERR_UNSUPPORTED;
+  if (cudaMemsetAsync(s, 0, sizeof(float) * (size_t)P * h2, stream) != cudaSuccess) return OTG_ERR_CUDA;
+  dim3 grid((unsigned)((n + 255) / 256), (unsigned)P);
+  mlp_encode_pool_kernel<16, 32, 32><<<grid, 256, 0, stream>>>(X, (int)n, W1, b1, W2, b2, s);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_mlp_head(const float* Z, int64_t P, int64_t n, int32_t dz, int32_t h2, int32_t h3, const float* sX,
+                 const float* sY, const float* W3, const float* b3, const float* W4, const float* b4, const float* W5,
+                 const float* b5, float* f, cudaStream_t stream) {
+  if (!Z || !sX || !sY || !W3 || !b3 || !W4 || !b4 || !W5 || !b5 || !f || P < 1 || P > 65535 || n < 1)
+    return OTG_ERR_ARG;
+  if (!(dz == 22 && h2 == 32 && h3 == 64)) return OTG_ERR_UNSUPPORTED;
+  dim3 grid((unsigned)((n + 127) / 128), (unsigned)P);
+  mlp_head_kernel<22, 32, 64><<<grid, 128, 0, stream>>>(Z, (int)n, sX, sY, W3, b3, W4, b4, W5, b5, f);
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 

@@ -139,6 +139,30 @@ class WarmStartNet:
             self._cache = (X, Y, P, n, m, hx1, hx2, hy1, hy2, z, h3, h4)
         return f.view(-1)
 
+    def infer(self, X, Y, P, n, m, Z):
+        """The forward pass for prediction: fused kernels (encoder + pooling,
+        head with the summaries folded into a per-pair bias) for the shipped
+        sizes, no activations stored; the layer-by-layer forward otherwise."""
+        sX = torch.empty(P, self.h2, dtype=torch.float32, device=self.device)
+        sY = torch.empty(P, self.h2, dtype=torch.float32, device=self.device)
+        f = torch.empty(P * n, dtype=torch.float32, device=self.device)
+        lib, st = self.lib, self._st()
+        rc = lib.otg_mlp_encode_pool(_p(X), P, n, self.d, self.h1, self.h2, _p(self.P("W1x")), _p(self.P("b1x")),
+                                     _p(self.P("W2x")), _p(self.P("b2x")), _p(sX), st)
+        if rc == -5:  # OTG_ERR_UNSUPPORTED: not the shipped sizes
+            return self.forward(X, Y, P, n, m, Z=Z)
+        _lib.check(rc, "otg_mlp_encode_pool")
+        _lib.check(lib.otg_mlp_encode_pool(_p(Y), P, m, self.d, self.h1, self.h2, _p(self.P("W1y")),
+                                           _p(self.P("b1y")), _p(self.P("W2y")), _p(self.P("b2y")), _p(sY), st),
+                   "otg_mlp_encode_pool")
+        rc = lib.otg_mlp_head(_p(Z), P, n, self.dz, self.h2, self.h3, _p(sX), _p(sY), _p(self.P("W3")),
+                              _p(self.P("b3")), _p(self.P("W4")), _p(self.P("b4")), _p(self.P("W5")),
+                              _p(self.P("b5")), _p(f), st)
+        if rc == -5:
+            return self.forward(X, Y, P, n, m, Z=Z)
+        _lib.check(rc, "otg_mlp_head")
+        return f
+
     def backward(self, df):
         X, Y, P, n, m, hx1, hx2, hy1, hy2, z, h3, h4 = self._cache
         d = self.dz

@@ -98,6 +98,29 @@ def softmin(ps, taus, g=None):
     return out.view(ps.P, ps.n, K)
 
 
+def softmin_points(X, C, b, scale, taus=(), g=None, g_tau=None):
+    """Soft-mins of the points of X (P, n, d) over the weighted atoms C
+    (P, k, d) with weights b (P, k), squared distances computed on the fly
+    (csrc/cost.cu softmin_points_kernel): (c-transform of g at g_tau, (P, n)
+    or None; zero-potential soft-mins at taus, (P, n, len(taus)) or None), in
+    units of scale (P,).  None for both when d has no kernel instance."""
+    lib = _lib.load()
+    P, n, d = X.shape
+    k = C.shape[1]
+    out_f = torch.empty(P, n, dtype=torch.float32, device=X.device) if g is not None else None
+    out_F = torch.empty(P, n, len(taus), dtype=torch.float32, device=X.device) if len(taus) else None
+    tt = torch.tensor(list(taus) or [1.0], dtype=torch.float32, device=X.device)
+    gp = None if g is None else g.reshape(P, k).float().contiguous()
+    rc = lib.otg_softmin_points(_lib.ptr(X), _lib.ptr(C), P, n, k, d, X.stride(0), C.stride(0),
+                                _lib.ptr(b.float().contiguous()), _lib.ptr(gp), float(g_tau or 0.0),
+                                _lib.ptr(scale.float().contiguous()), _lib.ptr(tt), len(taus), _lib.ptr(out_f),
+                                _lib.ptr(out_F), _lib.stream_handle(X.device))
+    if rc == -5:  # OTG_ERR_UNSUPPORTED: no instance for this dimension
+        return None, None
+    _lib.check(rc, "otg_softmin_points")
+    return out_f, out_F
+
+
 def features(ps, taus=TAUS):
     """Per-point inputs of the head: soft-min distances at several
     temperatures, centred per pair and scaled to O(1)."""
@@ -136,12 +159,16 @@ def coarse_potential(X, Y, maxc, reg_rel=0.02, k=128, tol=COARSE_TOL, taus=None,
     wa, wb = cell_masses(X, Xs), cell_masses(Y, Ys)
     sub = PairSolver(Xs, Ys, maxc=maxc, a=wa, b=wb)
     _, v, _, _, _ = sub.solve(reg_rel, tol, omega=coarse_omega)
-    cross = PairSolver(X, Ys, maxc=maxc, b=wb)
-    f = softmin(cross, (reg_rel,), g=v)[..., 0]
+    # one pass over the atoms per source point, distances on the fly
+    f, F = softmin_points(X.contiguous(), Ys, wb, maxc, taus or (), g=v, g_tau=reg_rel)
+    if f is None:  # no kernel instance for this dimension: through a cross cost block
+        cross = PairSolver(X, Ys, maxc=maxc, b=wb)
+        f = softmin(cross, (reg_rel,), g=v)[..., 0]
+        F = softmin(cross, taus) if taus is not None else None
     f = (f - f.mean(1, keepdim=True)).contiguous()
     if taus is None:
         return f
-    return f, softmin(cross, taus)
+    return f, F
 
 
 COARSE_K = 256
@@ -186,8 +213,8 @@ def predict(net, X, Y, maxc, F, chunk=1024):
         Xn, Yn = normalise_pairs(X[s:s + chunk], Y[s:s + chunk], maxc[s:s + chunk])
         P, n, d = Xn.shape
         Z = _head_inputs(Xn, F[s:s + chunk])
-        f = net.forward(Xn.view(P * n, d), Yn.view(P * Yn.shape[1], d), P, n, Yn.shape[1],
-                        Z=Z.view(P * n, -1)).view(P, n)
+        f = net.infer(Xn.reshape(P * n, d).contiguous(), Yn.reshape(P * Yn.shape[1], d).contiguous(), P, n,
+                      Yn.shape[1], Z.reshape(P * n, -1).contiguous()).view(P, n)
         out.append(f - f.mean(1, keepdim=True))
     return torch.cat(out)
 

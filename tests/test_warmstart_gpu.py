@@ -73,3 +73,56 @@ def test_trained_network_reduces_iterations(cuda):
     assert (st0 == 0).all() and (st1 == 0).all()
     assert (err1 < 1e-6).all() and (err0 < 1e-6).all()
     assert nit1.float().mean() < nit0.float().mean()
+
+
+@pytest.mark.parametrize("d", [16, 3])
+def test_softmin_points_matches_the_cost_block_path(cuda, d):
+    """The fused point-to-atom soft-min (distances on the fly) gives the
+    c-transform and the distance features of the cost-block path, and both
+    follow the float64 definition -tau log sum_k b_k exp(g_k - c_ik / (s tau))."""
+    g = torch.Generator(device=cuda)
+    g.manual_seed(3)
+    P, n, k = 3, 300, 40
+    X = torch.randn(P, n, d, generator=g, device=cuda)
+    C = X[:, :k].contiguous() + 0.3 * torch.randn(P, k, d, generator=g, device=cuda)
+    b = torch.rand(P, k, generator=g, device=cuda) + 0.1
+    b = b / b.sum(1, keepdim=True)
+    gp = 0.5 * torch.randn(P, k, generator=g, device=cuda)
+    scale = torch.tensor([2.0, 5.0, 9.0], device=cuda)
+    taus = (0.02, 0.1, 0.6)
+    f, F = wp.softmin_points(X, C, b, scale, taus, g=gp, g_tau=0.05)
+    cross = wp.PairSolver(X, C, maxc=scale, b=b)
+    f2 = wp.softmin(cross, (0.05,), g=gp)[..., 0]
+    F2 = wp.softmin(cross, taus)
+    np.testing.assert_allclose(f.cpu().numpy(), f2.cpu().numpy(), rtol=2e-5, atol=2e-5)
+    np.testing.assert_allclose(F.cpu().numpy(), F2.cpu().numpy(), rtol=2e-5, atol=2e-5)
+    Xd, Cd = X.double().cpu().numpy(), C.double().cpu().numpy()
+    cost = ((Xd[:, :, None, :] - Cd[:, None, :, :]) ** 2).sum(-1)
+    bd, gd, sd = b.double().cpu().numpy(), gp.double().cpu().numpy(), scale.double().cpu().numpy()
+
+    def smin(tau, pot):
+        z = np.log(bd)[:, None, :] + pot[:, None, :] - cost / (sd[:, None, None] * tau)
+        mz = z.max(-1, keepdims=True)
+        return -tau * (mz[..., 0] + np.log(np.exp(z - mz).sum(-1)))
+
+    np.testing.assert_allclose(f.cpu().numpy(), smin(0.05, gd), rtol=1e-4, atol=1e-4)
+    for t, tau in enumerate(taus):
+        np.testing.assert_allclose(F[..., t].cpu().numpy(), smin(tau, 0 * gd), rtol=1e-4, atol=1e-4)
+
+
+def test_fused_inference_matches_layerwise_forward(cuda):
+    """The fused prediction kernels (encoder + pooling, head with the pooled
+    summaries folded into a per-pair bias) give the layer-by-layer forward's
+    output for the shipped sizes (d 16, widths 32/32/64, 22 head inputs)."""
+    net = wp.new_net(16, device=cuda, seed=4)
+    rng = np.random.default_rng(1)
+    for k in [n for n, _ in net.shapes if n.startswith("b")]:
+        net.P(k).copy_(torch.tensor(rng.standard_normal(tuple(net.P(k).shape)) * 0.1, dtype=torch.float32))
+    P, n, m = 5, 300, 257
+    X = torch.tensor(rng.standard_normal((P * n, 16)), dtype=torch.float32, device=cuda)
+    Y = torch.tensor(rng.standard_normal((P * m, 16)), dtype=torch.float32, device=cuda)
+    Z = torch.tensor(rng.standard_normal((P * n, net.dz)), dtype=torch.float32, device=cuda)
+    f0 = net.forward(X, Y, P, n, m, Z=Z).cpu().numpy()
+    f1 = net.infer(X, Y, P, n, m, Z).cpu().numpy()
+    assert net.dz == 22
+    np.testing.assert_allclose(f1, f0, rtol=1e-4, atol=1e-5 * float(np.abs(f0).max()))
