@@ -107,6 +107,9 @@ __global__ void __launch_bounds__(256) batched_sqdist_kernel(OtgCostTable t) {
 // the kernel above: sum_k (x_k - y_k)^2 in order of k, +inf padding.
 // grid = (column-tile stride, row tiles, problems).
 constexpr int SQ_R = 64, SQ_C = 256;
+// shared-memory row strides of the staged tiles: +4 floats keeps 16-byte
+// alignment and spreads the transposing stores over the banks
+constexpr int SQ_RP = SQ_R + 4, SQ_CP = SQ_C + 4;
 
 template <int D>
 __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, const float* __restrict__ Y, int n, int m,
@@ -115,13 +118,13 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int e = threadIdx.x; e < SQ_R * D; e += blockDim.x) {
     const int r = e / D, k = e % D;
-    xt[k * SQ_R + r] = (r0 + r < n) ? X[(int64_t)(r0 + r) * D + k] : 0.f;
+    xt[k * SQ_RP + r] = (r0 + r < n) ? X[(int64_t)(r0 + r) * D + k] : 0.f;
   }
   for (int c0 = blockIdx.x * SQ_C; c0 < ldm; c0 += gridDim.x * SQ_C) {
     __syncthreads();  // previous tile's reads of yt are done (and xt is staged)
     for (int e = threadIdx.x; e < SQ_C * D; e += blockDim.x) {
       const int c = e / D, k = e % D;
-      yt[k * SQ_C + c] = (c0 + c < m) ? Y[(int64_t)(c0 + c) * D + k] : 0.f;
+      yt[k * SQ_CP + c] = (c0 + c < m) ? Y[(int64_t)(c0 + c) * D + k] : 0.f;
     }
     __syncthreads();
     // column pairs (j, j+1) in packed fp32x2 registers: one sub.f32x2 and one
@@ -133,10 +136,10 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
       for (int j = 0; j < 4; ++j) acc2[i][j] = 0ull;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-      const float4 xa = *reinterpret_cast<const float4*>(xt + k * SQ_R + warp * 8);
-      const float4 xb = *reinterpret_cast<const float4*>(xt + k * SQ_R + warp * 8 + 4);
-      const ulonglong2 ya = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_C + lane * 4);
-      const ulonglong2 yb = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_C + SQ_C / 2 + lane * 4);
+      const float4 xa = *reinterpret_cast<const float4*>(xt + k * SQ_RP + warp * 8);
+      const float4 xb = *reinterpret_cast<const float4*>(xt + k * SQ_RP + warp * 8 + 4);
+      const ulonglong2 ya = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_CP + lane * 4);
+      const ulonglong2 yb = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_CP + SQ_C / 2 + lane * 4);
       const float xv[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
       const unsigned long long yp[4] = {ya.x, ya.y, yb.x, yb.y};
 #pragma unroll
@@ -191,7 +194,7 @@ __global__ void __launch_bounds__(256) sqdist_regtile_kernel(OtgCostTable t) {
   const float* Y = static_cast<const float*>(t.Y) + t.y_off[p];
   float* M = static_cast<float*>(t.M) + t.m_off[p];
   float* xt = sq_smem;
-  float* yt = sq_smem + SQ_R * t.max_dim;
+  float* yt = sq_smem + SQ_RP * t.max_dim;
   float local_max = 0.f;
   if (d == 16) sqdist_regtile<16>(X, Y, n, m, ldm, M, r0, xt, yt, local_max);
   else if (d == 8) sqdist_regtile<8>(X, Y, n, m, ldm, M, r0, xt, yt, local_max);
@@ -499,7 +502,7 @@ int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t str
   } else if (t->dtype == OTG_F32 && t->fixed_dim) {
     // every problem has the same dimension, one of 2, 3, 8, 16: register tiles
     const dim3 g2(8, (unsigned)((max_rows + SQ_R - 1) / SQ_R), (unsigned)t->nprob);
-    sqdist_regtile_kernel<<<g2, 256, (SQ_R + SQ_C) * t->max_dim * sizeof(float), stream>>>(*t);
+    sqdist_regtile_kernel<<<g2, 256, (SQ_RP + SQ_CP) * t->max_dim * sizeof(float), stream>>>(*t);
   } else if (t->dtype == OTG_F32) {
     batched_sqdist_kernel<float><<<grid, 256, 32 * t->max_dim * sizeof(float), stream>>>(*t);
   } else {
