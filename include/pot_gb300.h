@@ -354,7 +354,10 @@ typedef struct OtgCostTable {
   void* max_out;
   int32_t fixed_dim;  /* 0, or the dimension every problem shares when it is 2, 3, 8 or 16
                          (float32: register-tiled kernel with 16-byte stores; must equal
-                         max_dim, and every m_off[p] and ldm[p] must be a multiple of 4) */
+                         max_dim, and every m_off[p] and ldm[p] must be a multiple of 4;
+                         for 8 and 16 also 16-byte loads of the points: X and Y 16-byte
+                         aligned, every x_off[p], y_off[p] a multiple of 4, else the
+                         generic kernel runs) */
 } OtgCostTable;
 int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t stream);
 

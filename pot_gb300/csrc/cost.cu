@@ -116,15 +116,38 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
                                                int ldm, float* __restrict__ M, int r0, float* xt, float* yt,
                                                float& local_max) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int e = threadIdx.x; e < SQ_R * D; e += blockDim.x) {
-    const int r = e / D, k = e % D;
-    xt[k * SQ_RP + r] = (r0 + r < n) ? X[(int64_t)(r0 + r) * D + k] : 0.f;
+  // D a multiple of 4: rows of X and Y are 16-byte aligned (the packed clouds
+  // start at multiples of D elements), so points are staged as float4 loads
+  constexpr bool V4 = D % 4 == 0;
+  if (V4) {
+    for (int e = threadIdx.x; e < SQ_R * D / 4; e += blockDim.x) {
+      const int r = e / (D / 4), k = (e % (D / 4)) * 4;
+      const float4 v = (r0 + r < n) ? *reinterpret_cast<const float4*>(X + (int64_t)(r0 + r) * D + k)
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+      xt[k * SQ_RP + r] = v.x; xt[(k + 1) * SQ_RP + r] = v.y;
+      xt[(k + 2) * SQ_RP + r] = v.z; xt[(k + 3) * SQ_RP + r] = v.w;
+    }
+  } else {
+    for (int e = threadIdx.x; e < SQ_R * D; e += blockDim.x) {
+      const int r = e / D, k = e % D;
+      xt[k * SQ_RP + r] = (r0 + r < n) ? X[(int64_t)(r0 + r) * D + k] : 0.f;
+    }
   }
   for (int c0 = blockIdx.x * SQ_C; c0 < ldm; c0 += gridDim.x * SQ_C) {
     __syncthreads();  // previous tile's reads of yt are done (and xt is staged)
-    for (int e = threadIdx.x; e < SQ_C * D; e += blockDim.x) {
-      const int c = e / D, k = e % D;
-      yt[k * SQ_CP + c] = (c0 + c < m) ? Y[(int64_t)(c0 + c) * D + k] : 0.f;
+    if (V4) {
+      for (int e = threadIdx.x; e < SQ_C * D / 4; e += blockDim.x) {
+        const int c = e / (D / 4), k = (e % (D / 4)) * 4;
+        const float4 v = (c0 + c < m) ? *reinterpret_cast<const float4*>(Y + (int64_t)(c0 + c) * D + k)
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+        yt[k * SQ_CP + c] = v.x; yt[(k + 1) * SQ_CP + c] = v.y;
+        yt[(k + 2) * SQ_CP + c] = v.z; yt[(k + 3) * SQ_CP + c] = v.w;
+      }
+    } else {
+      for (int e = threadIdx.x; e < SQ_C * D; e += blockDim.x) {
+        const int c = e / D, k = e % D;
+        yt[k * SQ_CP + c] = (c0 + c < m) ? Y[(int64_t)(c0 + c) * D + k] : 0.f;
+      }
     }
     __syncthreads();
     // column pairs (j, j+1) in packed fp32x2 registers: one sub.f32x2 and one
@@ -499,7 +522,8 @@ int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t str
   }
   if (t->dtype == OTG_F64) {
     batched_sqdist_kernel<double><<<grid, 256, 32 * t->max_dim * sizeof(double), stream>>>(*t);
-  } else if (t->dtype == OTG_F32 && t->fixed_dim) {
+  } else if (t->dtype == OTG_F32 && t->fixed_dim &&
+             (t->fixed_dim % 4 != 0 || ((uintptr_t)t->X % 16 == 0 && (uintptr_t)t->Y % 16 == 0))) {
     // every problem has the same dimension, one of 2, 3, 8, 16: register tiles
     const dim3 g2(8, (unsigned)((max_rows + SQ_R - 1) / SQ_R), (unsigned)t->nprob);
     sqdist_regtile_kernel<<<g2, 256, (SQ_RP + SQ_CP) * t->max_dim * sizeof(float), stream>>>(*t);
