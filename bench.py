@@ -496,6 +496,54 @@ def run_small(args, pk):
                          "alg_bytes_per_launch": alg}}
 
 
+def run_warm_eval(args, pk):
+    """Held-out evaluation of the learned warm start: 10 batches of 1024 pairs
+    (seeds EVAL_SEED .. EVAL_SEED + 10239, never used in training), warm
+    start (prior + network, over-relaxed) against the plain zero-started solve,
+    both stopping on the same column-marginal test (1e-6, every 10
+    iterations); mean stop index, relative error of the predicted potential,
+    and wall time per batch."""
+    import torch
+    from pot_gb300.warmstart import pipeline as wp
+    dev = torch.device("cuda:0")
+    net = wp.default_net(dev)
+    B, nb = 1024, 10
+    res = {"warm": [], "plain": [], "err": [], "prior_err": []}
+    t_warm = t_plain = 0.0
+    for k in range(nb):
+        X, Y = wp.gen_pairs(EVAL_SEED + k * B, B, WS_N, WS_D, dev)
+        for arm in ("warm", "plain"):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            ps = wp.PairSolver(X, Y)
+            wu = wp.warm_potential(net, X, Y, ps, WS_REG) if arm == "warm" else None
+            out = ps.solve(WS_REG, WS_TOL, warm_u=wu, omega=wp.REFINE_OMEGA if arm == "warm" else 1.0)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t
+            if arm == "warm":
+                t_warm += dt
+                # error of the prediction against this batch's converged potential
+                f = WS_REG * (out[0] - out[0].mean(1, keepdim=True))
+                F, prior = wp.inputs(ps, X, Y, WS_REG)
+                pred = prior + wp.predict(net, X, Y, ps.maxc, F)
+                res["err"].append(float(wp.relative_error(pred, f).median()))
+                res["prior_err"].append(float(wp.relative_error(prior, f).median()))
+            else:
+                t_plain += dt
+            assert bool((out[2] == 0).all()), "a pair did not converge"
+            res[arm].append(float(out[3].double().mean()))
+            del ps
+    n = B * nb
+    return {"metric": "held-out warm-start evaluation (10240 pairs)", "value": n / t_warm, "unit": "solves/s",
+            "dtype": "f32", "plain_value": n / t_plain, "speedup_warm_vs_plain": t_plain / t_warm,
+            "mean_stop_index": {"warm": float(np.mean(res["warm"])), "plain": float(np.mean(res["plain"]))},
+            "median_rel_error_potential": {"prior_plus_network": float(np.mean(res["err"])),
+                                           "prior_only": float(np.mean(res["prior_err"]))},
+            "config": {"workload": "%d held-out GMM cloud pairs n=m=%d d=%d, reg=%.2f x max cost, stopThr=%g, "
+                                   "seeds %d..%d, wall time per batch incl. cost blocks and warm start"
+                                   % (n, WS_N, WS_D, WS_REG, WS_TOL, EVAL_SEED, EVAL_SEED + n - 1)}}
+
+
 def run_tail(args, pk):
     """Cost of one iteration once few problems remain: the batch kernel alone
     against the cluster tail (fixed iteration counts, stop threshold 0, so
@@ -667,7 +715,8 @@ def main():
     pk = peaks()
     if args.workload != "warmstart":
         fn = {"online": run_online, "gw": run_gw, "ragged": run_ragged, "dense": run_dense,
-              "batch": run_batch, "small": run_small, "tail": run_tail}[args.workload]
+              "batch": run_batch, "small": run_small, "tail": run_tail,
+              "warm_eval": run_warm_eval}[args.workload]
         line = {"n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                 "data": "synthetic"}
         line.update(fn(args, pk))
