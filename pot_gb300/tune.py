@@ -18,7 +18,8 @@ schedule: each candidate runs a fixed number of iterations (stop threshold
 0, so every problem runs them all) timed with CUDA events on the launching
 stream, the fill-phase parameters on the caller's whole batch and the tail
 cap on its largest few problems.  Results are cached in memory and in a JSON
-file (``POT_GB300_TUNE_CACHE``, default ``~/.cache/pot_gb300/schedules.json``).
+file (``POT_GB300_TUNE_CACHE``, default ``schedules.json`` next to the built
+library in ``pot_gb300/_lib``, an untracked build directory).
 """
 import json
 import math
@@ -57,7 +58,7 @@ def schedule_key(dtype_tag, rows, cols):
 
 def cache_path():
     return os.environ.get("POT_GB300_TUNE_CACHE",
-                          os.path.join(os.path.expanduser("~"), ".cache", "pot_gb300", "schedules.json"))
+                          os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "schedules.json"))
 
 
 class Tuner:
