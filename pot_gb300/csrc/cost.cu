@@ -369,6 +369,8 @@ __global__ void __launch_bounds__(256) softmin_features_kernel(const float* __re
 // c-transform of the atoms' potential g at temperature g_tau (if g is given),
 // columns 1.. the soft-mins of the zero potential at taus[]; all in units of
 // scale[p], as softmin_features_kernel computes them from a cost block.
+// Every thread reads the same atom at the same time (broadcast), so the atoms
+// are stored densely and read as float4 when D is a multiple of 4.
 template <int D>
 __global__ void __launch_bounds__(256) softmin_points_kernel(const float* __restrict__ X, const float* __restrict__ C,
                                                              int n, int k, int64_t sx, int64_t sc,
@@ -377,13 +379,13 @@ __global__ void __launch_bounds__(256) softmin_points_kernel(const float* __rest
                                                              const float* __restrict__ scale,
                                                              const float* __restrict__ taus, int ntau,
                                                              float* __restrict__ out_f, float* __restrict__ out_F) {
-  extern __shared__ float sp_smem[];
+  extern __shared__ __align__(16) float sp_smem[];
   const int p = blockIdx.y;
-  float* cs = sp_smem;                         // [k][D + 1]
-  float* lb = cs + (size_t)k * (D + 1);        // log2 b
+  float* cs = sp_smem;                         // [k][D]
+  float* lb = cs + (size_t)k * D;              // log2 b
   float* lg = lb + k;                          // log2 b + g log2 e
   const float* Cp = C + p * sc;
-  for (int e = threadIdx.x; e < k * D; e += blockDim.x) cs[(e / D) * (D + 1) + e % D] = Cp[e];
+  for (int e = threadIdx.x; e < k * D; e += blockDim.x) cs[e] = Cp[e];
   for (int c = threadIdx.x; c < k; c += blockDim.x) {
     const float l = lg2(bw[(int64_t)p * k + c]);
     lb[c] = l;
@@ -405,10 +407,21 @@ __global__ void __launch_bounds__(256) softmin_points_kernel(const float* __rest
     s[t] = 0.f;
   }
   auto dist = [&](int c) {
-    const float* y = cs + c * (D + 1);
+    const float* y = cs + c * D;
     float d2 = 0.f;
+    if (D % 4 == 0) {
 #pragma unroll
-    for (int q = 0; q < D; ++q) { const float df = x[q] - y[q]; d2 = fmaf(df, df, d2); }
+      for (int q = 0; q < D; q += 4) {
+        const float4 w = *reinterpret_cast<const float4*>(y + q);
+        float df = x[q] - w.x; d2 = fmaf(df, df, d2);
+        df = x[q + 1] - w.y; d2 = fmaf(df, df, d2);
+        df = x[q + 2] - w.z; d2 = fmaf(df, df, d2);
+        df = x[q + 3] - w.w; d2 = fmaf(df, df, d2);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < D; ++q) { const float df = x[q] - y[q]; d2 = fmaf(df, df, d2); }
+    }
     return d2;
   };
   for (int c = 0; c < k; ++c) {
@@ -438,7 +451,7 @@ __global__ void __launch_bounds__(256) softmin_points_kernel(const float* __rest
 template <int D>
 __global__ void __launch_bounds__(256) nearest_mass_kernel(const float* __restrict__ X, const float* __restrict__ Cc,
                                                            int n, int k, int64_t sx, int64_t sc, float* w) {
-  extern __shared__ float cs[];
+  extern __shared__ __align__(16) float cs[];
   const int p = blockIdx.y;
   const float* C = Cc + p * sc;
   for (int e = threadIdx.x; e < k * D; e += blockDim.x) cs[e] = C[e];
@@ -452,8 +465,19 @@ __global__ void __launch_bounds__(256) nearest_mass_kernel(const float* __restri
   int arg = 0;
   for (int c = 0; c < k; ++c) {
     float d2 = 0.f;
+    if (D % 4 == 0) {  // every thread reads centre c: broadcast float4 loads
 #pragma unroll
-    for (int q = 0; q < D; ++q) { const float df = x[q] - cs[c * D + q]; d2 = fmaf(df, df, d2); }
+      for (int q = 0; q < D; q += 4) {
+        const float4 w = *reinterpret_cast<const float4*>(cs + c * D + q);
+        float df = x[q] - w.x; d2 = fmaf(df, df, d2);
+        df = x[q + 1] - w.y; d2 = fmaf(df, df, d2);
+        df = x[q + 2] - w.z; d2 = fmaf(df, df, d2);
+        df = x[q + 3] - w.w; d2 = fmaf(df, df, d2);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < D; ++q) { const float df = x[q] - cs[c * D + q]; d2 = fmaf(df, df, d2); }
+    }
     if (d2 < best) { best = d2; arg = c; }
   }
   atomicAdd(w + (int64_t)p * k + arg, 1.0f / (float)n);
@@ -574,7 +598,7 @@ int otg_softmin_points(const float* X, const float* C, int32_t nprob, int32_t n,
   if (!X || !C || !b || !scale || nprob < 1 || nprob > 65535 || n < 1 || k < 1) return OTG_ERR_ARG;
   if (ntau < 0 || ntau > SM_MAXTAU || (ntau > 0 && (!taus || !out_F)) || (!out_f && ntau == 0)) return OTG_ERR_ARG;
   if (out_f && !(g_tau > 0)) return OTG_ERR_ARG;
-  const size_t sm = sizeof(float) * ((size_t)k * (d + 1) + 2 * (size_t)k);
+  const size_t sm = sizeof(float) * ((size_t)k * d + 2 * (size_t)k);
   if (sm > 48 * 1024) return OTG_ERR_UNSUPPORTED;
   dim3 grid((unsigned)((n + 255) / 256), (unsigned)nprob);
   const float gt = out_f ? g_tau : 1.f;
