@@ -169,7 +169,7 @@ def load(build_if_missing=True):
     return lib
 
 
-LAUNCHES = [0]  # C-ABI calls that launched kernels (each call launches its own kernels)
+LAUNCHES = [0]  # kernel-launching C-ABI calls (plus the tail kernel queued behind each batch solve)
 
 
 def check(rc, what):

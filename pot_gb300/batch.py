@@ -131,6 +131,15 @@ def multi_tail_config(dtype=torch.float32):
     return cl.value, mx.value, tile.value, err.value
 
 
+_TAIL_ON = {}
+
+
+def _tail_enabled(dtype):
+    if dtype not in _TAIL_ON:
+        _TAIL_ON[dtype] = multi_tail_config(dtype)[0] > 0
+    return _TAIL_ON[dtype]
+
+
 def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
               events=None, omega=1.0, check_period=10, schedule=None, tail_problems=0, info=None):
     """Work-balanced persistent launch (csrc/multi.cu), log form, per-problem
@@ -188,6 +197,8 @@ def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, wa
     if events is not None:
         events[0].record()
     _lib.check(lib.otg_sinkhorn_multi(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_multi")
+    if tail_problems >= 0 and _tail_enabled(dt):
+        _lib.LAUNCHES[0] += 1  # the tail kernel launched behind the batch kernel
     if events is not None:
         events[1].record()
     if info is not None:
