@@ -286,7 +286,8 @@ typedef struct OtgMultiProblem {
    * shared memory of one thread-block cluster, a cluster per problem
    * finishes them (same iteration and stop test, cluster barriers instead of
    * grid barriers; clusters take the problems from a queue).  0: default
-   * (three times the clusters the device holds at once); negative: never. */
+   * (three times the clusters the device holds at once in float32; never in
+   * float64, whose passes are bound by FP64 throughput); negative: never. */
   int32_t tail_problems;
   int32_t reserved;
 } OtgMultiProblem;

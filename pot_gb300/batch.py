@@ -197,7 +197,7 @@ def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, wa
     if events is not None:
         events[0].record()
     _lib.check(lib.otg_sinkhorn_multi(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_multi")
-    if tail_problems >= 0 and _tail_enabled(dt):
+    if (tail_problems > 0 or (tail_problems == 0 and dt == torch.float32)) and _tail_enabled(dt):
         _lib.LAUNCHES[0] += 1  # the tail kernel launched behind the batch kernel
     if events is not None:
         events[1].record()

@@ -834,7 +834,10 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   const TailCfg tc = tail_config<T>();
   A.tail_cl = tc.cl;
   A.tail_tile = tc.tile;
-  A.tail_max = q->tail_problems < 0 || tc.cl == 0 ? 0 : (q->tail_problems > 0 ? q->tail_problems : 3 * tc.max);
+  // float64 passes are bound by FP64 throughput, which every SM of the batch
+  // kernel supplies and one cluster per problem does not: no default handoff
+  const int def_tail = sizeof(T) == 8 ? 0 : 3 * tc.max;
+  A.tail_max = q->tail_problems < 0 || tc.cl == 0 ? 0 : (q->tail_problems > 0 ? q->tail_problems : def_tail);
   // carve the workspace
   char* w = static_cast<char*>(q->workspace);
   size_t off = 0;

@@ -338,9 +338,11 @@ def test_tail_clusters_continue_the_batch_iteration(cuda, dtype):
         info = {}
         off = pb.run_multi(lay, Mq, aq, bq, reg[sub], max_iter, tol, tail_problems=-1, info=info)
         assert info["handoff_ii"] == -1
-        on = pb.run_multi(lay, Mq, aq, bq, reg[sub], max_iter, tol, tail_problems=tp, info=info)
+        # float64 hands over only on request (its passes are FP64-bound)
+        tp_on = tp if (tp > 0 or dtype == torch.float32) else 3 * ncl
+        on = pb.run_multi(lay, Mq, aq, bq, reg[sub], max_iter, tol, tail_problems=tp_on, info=info)
         nb = lay.B
-        limit = tp if tp > 0 else 3 * ncl
+        limit = tp_on if tp_on > 0 else 3 * ncl
         assert info["handoff_ii"] >= 1 and 1 <= info["handoff_problems"] <= min(nb, limit)
         assert (info["handoff_ii"] == 1) == (nb <= limit)
         np.testing.assert_array_equal(on[2].cpu().numpy(), off[2].cpu().numpy())
@@ -356,3 +358,21 @@ def test_tail_clusters_continue_the_batch_iteration(cuda, dtype):
                 uo, uf = on[0][r0:r0 + n].double(), off[0][r0:r0 + n].double()
                 np.testing.assert_allclose((uo - uo.mean()).cpu().numpy(), (uf - uf.mean()).cpu().numpy(),
                                            atol=2e-3 * max(1.0, float(uf.abs().max())))
+
+
+def test_float64_batches_keep_every_sm_by_default(cuda):
+    """float64 passes are bound by FP64 throughput: the batch kernel keeps its
+    last problems on every SM unless a handoff is requested."""
+    rng = np.random.default_rng(2)
+    rows, cols = np.array([40, 50]), np.array([45, 30])
+    layout = pb.RaggedLayout(rows, cols, torch.float64, cuda)
+    Ms = [torch.tensor(oracle.sqeuclidean(rng.random((n, 3)), rng.random((m, 3))), device=cuda)
+          for n, m in zip(rows, cols)]
+    Mp = pb.pack_dense(layout, Ms)
+    a = torch.cat([torch.full((int(n),), 1.0 / n, dtype=torch.float64, device=cuda) for n in rows])
+    b = torch.cat([torch.full((int(m),), 1.0 / m, dtype=torch.float64, device=cuda) for m in cols])
+    info = {}
+    pb.run_multi(layout, Mp, a, b, 0.05, 1000, 1e-9, info=info)
+    assert info["handoff_ii"] == -1
+    pb.run_multi(layout, Mp, a, b, 0.05, 1000, 1e-9, tail_problems=4, info=info)
+    assert info["handoff_ii"] == 1
