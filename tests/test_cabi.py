@@ -54,3 +54,32 @@ def test_struct_mirrors_match_compiled_layout():
             assert buf[k + 1] == getattr(mirror, field).offset, (name, field)
     assert fn(b"NoSuchStruct", (ctypes.c_int64 * 4)(), 4) == -1  # OTG_ERR_ARG
     assert fn(b"OtgDenseProblem", (ctypes.c_int64 * 4)(), 4) == -1  # cap too small
+
+
+def test_invalid_arguments_are_rejected_before_any_device_work():
+    """The C ABI reports bad arguments with its error codes before touching a
+    device (these calls run without a GPU): null problem structs and buffers,
+    unknown dtypes, sizes the fused kernels do not cover."""
+    from pot_gb300 import _build, _lib
+    lib = ctypes.CDLL(_build.build())
+    for name, (res, args) in _lib.SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype, fn.argtypes = res, args
+    ERR_ARG, ERR_DTYPE, ERR_UNSUPPORTED = -1, -2, -5
+    assert lib.otg_sinkhorn_dense(None, None, None) == ERR_ARG
+    assert lib.otg_sinkhorn_dense_noalloc(None, None, None, None) == ERR_ARG
+    assert lib.otg_sinkhorn_multi(None, None) == ERR_ARG
+    assert lib.otg_batched_sqdist(None, 1, None) == ERR_ARG
+    assert lib.otg_dense_plan(0, 1, None, 4, 4, 4, None, None, 1.0, None, 0, None, None) == ERR_ARG
+    assert lib.otg_gibbs_kernel(0, None, 4, 4, 4, 1.0, None, 4, None) == ERR_ARG
+    assert lib.otg_softmin_points(None, None, 1, 8, 4, 16, 128, 64, None, None, 0.0, None, None, 0, None, None,
+                                  None) == ERR_ARG
+    cl, mx, err = _lib.c_i32(), _lib.c_i32(), _lib.c_i32()
+    tile = _lib.c_i64()
+    assert lib.otg_multi_tail_config(7, ctypes.byref(cl), ctypes.byref(mx), ctypes.byref(tile),
+                                     ctypes.byref(err)) == ERR_DTYPE
+    # the fused network kernels cover the shipped sizes only (pointers are not read)
+    fake = ctypes.c_void_p(16)
+    assert lib.otg_mlp_encode_pool(fake, 1, 1, 5, 32, 32, fake, fake, fake, fake, fake, None) == ERR_UNSUPPORTED
+    assert lib.otg_mlp_head(fake, 1, 1, 7, 32, 64, fake, fake, fake, fake, fake, fake, fake, fake, fake,
+                            None) == ERR_UNSUPPORTED
