@@ -121,13 +121,6 @@ def softmin_points(X, C, b, scale, taus=(), g=None, g_tau=None):
     return out_f, out_F
 
 
-def features(ps, taus=TAUS):
-    """Per-point inputs of the head: soft-min distances at several
-    temperatures, centred per pair and scaled to O(1)."""
-    F = softmin(ps, taus)
-    return ((F - F.mean(1, keepdim=True)) * FEATURE_SCALE).contiguous()
-
-
 def cell_masses(X, centres):
     """Voronoi cell masses of each cloud of X over its centres (csrc/cost.cu
     nearest_mass_kernel): (P, k), rows summing to one."""
