@@ -47,7 +47,7 @@ class SinkhornGraph:
         self.b = torch.full((self.m,), 1.0 / self.m, dtype=dtype, device=dev)
         self.P = torch.empty(self.n, self.m, dtype=dtype, device=dev) if want_plan else None
         self.loss = torch.zeros(1, dtype=torch.float64, device=dev)
-        self.grid = default_grid(self.n, self.m)
+        self.grid = default_grid(self.n, self.m, dtype)
         self.M.copy_(torch.rand(self.n, self.m, dtype=dtype, device=dev))
         side = torch.cuda.Stream(dev)
         side.wait_stream(torch.cuda.current_stream(dev))
