@@ -44,3 +44,27 @@ def test_schedule_search_returns_a_candidate_no_slower_than_the_start(weights, t
     start = tune.DEFAULT._replace(ctas_per_sm=max(tune.SPACE["ctas_per_sm"]["f32"]))
     assert cost(best) <= cost(start)
     assert t.get("k") == best
+
+
+@hypothesis.given(st.integers(2, 30), st.integers(2, 30), st.floats(0.05, 1.0), st.integers(0, 10_000))
+@hypothesis.settings(max_examples=30, deadline=None)
+def test_oracle_forms_agree(n, m, reg, seed):
+    """The oracle's scaling and log forms run the same iteration: the same
+    stop index and plans equal to rounding (the reference's own
+    test_sinkhorn_variants compares them within 1e-5); the stabilised form
+    without absorptions equals them too."""
+    import oracle
+    rng = np.random.default_rng(seed)
+    M = oracle.sqeuclidean(rng.random((n, 2)), rng.random((m, 2)))
+    M /= max(M.max(), 1e-12)
+    a, b = rng.dirichlet(np.ones(n)), rng.dirichlet(np.ones(m))
+    P1, l1 = oracle.sinkhorn_knopp(a, b, M, reg, stopThr=1e-10)
+    P2, l2 = oracle.sinkhorn_log(a, b, M, reg, stopThr=1e-10)
+    P3, l3 = oracle.sinkhorn_stabilized(a, b, M, reg, stopThr=1e-10, tau=1e300)
+    assert l1["niter"] == l2["niter"]
+    np.testing.assert_allclose(P1, P2, rtol=1e-8, atol=1e-14)
+    np.testing.assert_allclose(P3, P2, rtol=1e-8, atol=1e-14)
+    # the returned plan meets the stop test (column-marginal L2 error below stopThr)
+    # unless the iteration cap ended the solve
+    if l2["niter"] < 999:
+        assert np.linalg.norm(P2.sum(0) - b) < 1e-10
