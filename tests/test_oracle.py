@@ -288,3 +288,30 @@ def test_unbalanced(tag, kw):
     np.testing.assert_allclose(P, g[tag + "_plan"], rtol=1e-9, atol=1e-300)
     np.testing.assert_allclose(lg["logu"], g[tag + "_logu"], rtol=1e-9, atol=1e-12)
     assert abs(lg["total_cost"] - float(g[tag + "_total"])) <= 1e-9 * abs(float(g[tag + "_total"]))
+
+
+def test_accelerated_oracles_reach_the_solution_faster():
+    """The over-relaxed and Anderson-accelerated restatements (the checkers of
+    the warm-start refinement) are sinkhorn_log with the acceleration off, and
+    reach the same solution in fewer iterations with it on."""
+    from oracle import accelerated as acc
+    rng = np.random.default_rng(5)
+    n, m = 120, 100
+    X = rng.standard_normal((n, 4))
+    Y = rng.standard_normal((m, 4)) * 0.7 + 0.5
+    M = oracle.sqeuclidean(X, Y)
+    M /= M.max()
+    a, b = rng.dirichlet(np.ones(n) * 3), rng.dirichlet(np.ones(m) * 3)
+    reg = 0.02
+    _, lg = oracle.sinkhorn_log(a, b, M, reg, numItermax=20000, stopThr=1e-9)
+    u1, v1, it1, _ = acc.sinkhorn_log_relaxed(a, b, M, reg, omega=1.0, numItermax=20000, stopThr=1e-9)
+    assert it1 == lg["niter"]
+    np.testing.assert_allclose(u1, lg["log_u"], rtol=1e-12, atol=1e-12)
+    ur, vr, itr, _ = acc.sinkhorn_log_relaxed(a, b, M, reg, omega=1.5, numItermax=20000, stopThr=1e-9,
+                                              check_period=1)
+    ua, va, ita, errs = acc.sinkhorn_log_anderson(a, b, M, reg, depth=5, numItermax=20000, stopThr=1e-9)
+    assert errs[-1] < 1e-9 and itr < it1 and ita < itr
+    for u, v in ((ur, vr), (ua, va)):
+        P = np.exp(-M / reg + u[:, None] + v[None, :])
+        P0 = np.exp(-M / reg + lg["log_u"][:, None] + lg["log_v"][None, :])
+        assert np.abs(P - P0).sum() / P0.sum() < 1e-6
