@@ -59,3 +59,20 @@ def test_patch_rebinds_every_importing_module(tmp_path, monkeypatch):
         for k in list(sys.modules):
             if k == "fakeot" or k.startswith("fakeot."):
                 del sys.modules[k]
+
+
+def test_otresult_fields_and_marginals():
+    """OTResult (the container of ot.solve / ot.batch results, ot/utils.py:1127)
+    exposes the reference's field names; marginals sum the plan over its last
+    two axes (batched plans keep their batch axis)."""
+    import numpy as np
+    from pot_gb300.utils import OTResult
+    P = np.arange(24, dtype=float).reshape(2, 3, 4)
+    r = OTResult(potentials=("u", "v"), value=1.5, value_linear=1.0, plan=P, log={"n_iter": 3}, status=0)
+    assert r.potential_a == "u" and r.potential_b == "v" and r.value == 1.5 and r.value_linear == 1.0
+    np.testing.assert_array_equal(r.marginal_a, P.sum(-1))
+    np.testing.assert_array_equal(r.marginal_b, P.sum(-2))
+    assert r.log["n_iter"] == 3 and r.status == 0
+    assert "value=1.5" in repr(r) and "shape=(2, 3, 4)" in repr(r)
+    empty = OTResult()
+    assert empty.marginals == (None, None) and empty.potential_a is None and repr(empty) == "OTResult()"
