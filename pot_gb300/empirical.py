@@ -11,7 +11,6 @@ builds the dense cost on the GPU and calls the dense scaling-form solver,
 as the reference calls ``sinkhorn``.
 """
 import ctypes
-import math
 import warnings
 
 import numpy as np

@@ -14,7 +14,6 @@ folded into the cost as ``M - reg log c``.  The plan and the costs of the
 log (``cost``, ``total_cost``) come from the plan and marginal kernels.
 """
 import ctypes
-import math
 import warnings
 
 import numpy as np
