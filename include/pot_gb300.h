@@ -289,11 +289,32 @@ typedef struct OtgMultiProblem {
    * (three times the clusters the device holds at once in float32; never in
    * float64, whose passes are bound by FP64 throughput); negative: never. */
   int32_t tail_problems;
+  /* whole-batch stop (ot.batch's rule, ot/batch/_utils.py:152-157, :273-278):
+   * 0: every problem stops on its own error; 1: all problems stop together
+   * at the first check whose LARGEST error is below stop_thr (each reports
+   * that stop index and its own error; no tail handoff). */
+  int32_t joint_stop;
+  /* 0: log form (potentials are natural logs); 1: scaling form with
+   * K = exp(-M/reg) (ot/batch/_utils.py:141-151 on the transposed problem;
+   * outputs are the scalings themselves; no omega, no tail handoff). */
+  int32_t scaling;
+  /* Anderson mixing of the v update over the last anderson_depth iterates
+   * (0: off; at most OTG_ANDERSON_MAX_DEPTH; log form only, replaces omega).
+   * No reference counterpart: the stop test is unchanged, and u is always
+   * the exact row update of the v in use, so the returned pair has an exact
+   * row marginal and a checked column marginal, as in sinkhorn_log.  Needs
+   * otg_multi_anderson_bytes() of device memory in anderson_ws. */
+  int32_t anderson_depth;
   int32_t reserved;
+  void* anderson_ws;
+  size_t anderson_ws_bytes;
 } OtgMultiProblem;
+#define OTG_ANDERSON_MAX_DEPTH 8
 size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, int64_t total_cols,
                                  int64_t total_partials);
 int otg_sinkhorn_multi(const OtgMultiProblem* q, cudaStream_t stream);
+/* Device bytes of the Anderson history (anderson_ws) for a batch. */
+size_t otg_multi_anderson_bytes(int dtype, int32_t nprob, int64_t total_cols, int32_t depth);
 /* The tail handoff's cluster shape on the current device: CTAs per cluster
  * (0: no tail handoff), clusters resident at once, shared-memory bytes of
  * cost block per CTA, and the CUDA error code of the last configuration
@@ -503,9 +524,12 @@ int otg_gemm_f64(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, 
  *
  * Problems whose scratch exceeds the maximum are rejected with
  * OTG_ERR_NOALLOC_TOO_LARGE (about n = m = 16384 in float32 with the
- * default grid fits; a smaller p->grid lowers the need).  The first call on
- * a device looks up the array's device address; make that first call
- * before any stream capture.  Every call shares the array and it keeps the
+ * default grid fits; a smaller p->grid lowers the need).  The first call in
+ * a CUDA context looks up the array's device address in that context and
+ * caches it by the context's unique ID (a context created again after
+ * cudaDeviceReset, or a non-primary context on the same device, looks it up
+ * afresh); make that first call before any stream capture.  Every call in
+ * a context shares the array and it keeps the
  * last call's contents: the call clears what must start at zero, and calls
  * whose kernels overlap on the GPU race, so serialise them.
  * ---------------------------------------------------------------------- */

@@ -47,7 +47,9 @@ class OtgMultiProblem(ctypes.Structure):
                 ("out_u", c_vp), ("out_v", c_vp), ("status", c_vp), ("niter", c_vp), ("err", c_vp),
                 ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32), ("omega", c_dbl),
                 ("check_period", c_i32), ("units_per_warp", c_i32), ("split_cap_fill", c_i32),
-                ("split_cap_tail", c_i32), ("tail_problems", c_i32), ("reserved", c_i32)]
+                ("split_cap_tail", c_i32), ("tail_problems", c_i32), ("joint_stop", c_i32),
+                ("scaling", c_i32), ("anderson_depth", c_i32), ("reserved", c_i32), ("anderson_ws", c_vp),
+                ("anderson_ws_bytes", c_sz)]
 
 
 class OtgCostTable(ctypes.Structure):
@@ -110,6 +112,7 @@ SIGNATURES = {
     "otg_sinkhorn_batched": (ctypes.c_int, [ctypes.POINTER(OtgBatchProblem), c_vp]),
     "otg_multi_workspace_bytes": (c_sz, [ctypes.c_int, c_i32, c_i64, c_i64, c_i64]),
     "otg_sinkhorn_multi": (ctypes.c_int, [ctypes.POINTER(OtgMultiProblem), c_vp]),
+    "otg_multi_anderson_bytes": (c_sz, [ctypes.c_int, c_i32, c_i64, c_i32]),
     "otg_online_workspace_bytes": (c_sz, [c_i64, c_i64, c_i32]),
     "otg_sinkhorn_online": (ctypes.c_int, [ctypes.POINTER(OtgOnlineProblem), c_vp]),
     "otg_batched_sqdist": (ctypes.c_int, [ctypes.POINTER(OtgCostTable), c_i32, c_vp]),

@@ -4,9 +4,12 @@ ragged-batch API.
 ``solve_batch`` / ``solve_sample_batch`` / ``bregman_log_projection_batch``
 / ``bregman_projection_batch`` follow PythonOT/POT ``ot/batch/_linear.py``
 (:236-357, :360-435) and ``ot/batch/_utils.py`` (:46-162, :165-290): same
-arguments, same returned fields.  One design difference: every problem stops
-on its own marginal error (the reference stops the whole batch on the largest
-error), so problems that converge early are not iterated further.
+arguments, same returned fields, and the same stop rule: the whole batch
+stops at the first check (every 10th iteration) whose LARGEST row-marginal
+error is below ``tol`` (``_utils.py:152-157, :273-278``), so every problem
+runs to that shared index, as in the reference.  ``per_problem=True`` (no
+reference counterpart) lets every problem stop on its own error instead;
+problems that converge early are then not iterated further.
 
 ``solve_ragged`` / ``solve_sample_ragged`` take problems of uneven sizes
 directly (no zero-weight padding) and run them in one persistent launch
@@ -141,22 +144,28 @@ def _tail_enabled(dtype):
 
 
 def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-              events=None, omega=1.0, check_period=10, schedule=None, tail_problems=0, info=None):
-    """Work-balanced persistent launch (csrc/multi.cu), log form, per-problem
-    sinkhorn_log order and stop test.  Returns (u, v, status, niter, err, reg).
-    ``omega != 1`` over-relaxes the potential updates and ``check_period``
-    other than 10 moves the stop tests (no reference counterpart for either;
-    the stop criterion is unchanged).  ``schedule`` (a ``tune.Schedule``)
-    divides the work; by default the autotuner's cached choice for this
-    workload class, else the built-in one.  ``tail_problems`` bounds the
-    cluster tail handoff (0: default, negative: off); with a dict ``info``
-    the call synchronises and reports the handoff iteration (-1: none)."""
+              events=None, omega=1.0, check_period=10, schedule=None, tail_problems=0, info=None, joint=False,
+              scaling=False):
+    """Work-balanced persistent launch (csrc/multi.cu) in the sinkhorn_log
+    order (v first, column-marginal test).  Returns (u, v, status, niter,
+    err, reg).  ``joint`` stops the whole batch together on the largest
+    error (ot.batch's rule); otherwise every problem stops on its own.
+    ``scaling`` runs the scaling form (u, v are then scalings, not natural
+    logs).  ``omega != 1`` over-relaxes the potential updates and
+    ``check_period`` other than 10 moves the stop tests (no reference
+    counterpart for either; the stop criterion is unchanged).  ``schedule``
+    (a ``tune.Schedule``) divides the work; by default the autotuner's cached
+    choice for this workload class, else the built-in one.  ``tail_problems``
+    bounds the cluster tail handoff (0: default, negative: off); with a dict
+    ``info`` the call synchronises and reports the handoff iteration (-1:
+    none)."""
     return _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u, grid, timeout_ms,
-                           events, omega, check_period, schedule, tail_problems, info)
+                           events, omega, check_period, schedule, tail_problems, info, joint, scaling)
 
 
 def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
-                    events=None, omega=1.0, check_period=10, schedule=None, tail_problems=0, info=None):
+                    events=None, omega=1.0, check_period=10, schedule=None, tail_problems=0, info=None,
+                    joint=False, scaling=False):
     lib = _lib.load()
     if schedule is None:
         schedule = tune.lookup(layout) or tune.DEFAULT
@@ -193,11 +202,12 @@ def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, wa
         err=err.data_ptr(), workspace=ws.data_ptr(), workspace_bytes=wsb, timeout_ms=int(timeout_ms),
         omega=float(omega), check_period=int(check_period), units_per_warp=int(schedule.units_per_warp),
         split_cap_fill=int(schedule.cap_fill), split_cap_tail=int(schedule.cap_tail),
-        tail_problems=int(tail_problems))
+        tail_problems=int(tail_problems), joint_stop=int(bool(joint)), scaling=int(bool(scaling)))
     if events is not None:
         events[0].record()
     _lib.check(lib.otg_sinkhorn_multi(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_multi")
-    if (tail_problems > 0 or (tail_problems == 0 and dt == torch.float32)) and _tail_enabled(dt):
+    if (not joint and not scaling and (tail_problems > 0 or (tail_problems == 0 and dt == torch.float32))
+            and _tail_enabled(dt)):
         _lib.LAUNCHES[0] += 1  # the tail kernel launched behind the batch kernel
     if events is not None:
         events[1].record()
@@ -271,34 +281,38 @@ def _unpack_rows(layout, packed, width_np, off_np):
     return packed.view(B, w)
 
 
+_TRANSPOSE_CHUNK = 65535  # problems per transpose launch (its grid's z extent)
+
+
 def _transposed(layout, Mp):
     """The layout and packed cost blocks of the transposed problems (one
-    transpose pass, otg_transpose_batched)."""
+    transpose pass, otg_transpose_batched, in launches of at most 65535
+    problems)."""
     lib = _lib.load()
     B, n, m = layout.B, int(layout.rows_np[0]), int(layout.cols_np[0])
     lt = RaggedLayout([m] * B, [n] * B, layout.dtype, layout.device)
     ld, ldt = int(layout.ldm_np[0]), int(lt.ldm_np[0])
     Mt = torch.empty(lt.total_m, dtype=layout.dtype, device=layout.device)
-    _lib.check(lib.otg_transpose_batched(_lib.dtype_code(layout.dtype), _lib.ptr(Mp), B, n, m, ld, n * ld,
-                                         _lib.ptr(Mt), ldt, m * ldt, _lib.stream_handle(layout.device)),
-               "otg_transpose_batched")
+    for z0 in range(0, B, _TRANSPOSE_CHUNK):
+        nb = min(_TRANSPOSE_CHUNK, B - z0)
+        _lib.check(lib.otg_transpose_batched(_lib.dtype_code(layout.dtype), _lib.ptr(Mp[z0 * n * ld:]), nb, n, m,
+                                             ld, n * ld, _lib.ptr(Mt[z0 * m * ldt:]), ldt, m * ldt,
+                                             _lib.stream_handle(layout.device)), "otg_transpose_batched")
     return lt, Mt
 
 
-def _solve_uniform(Md, a, b, reg, method, max_iter, tol, kl):
+def _solve_uniform(Md, a, b, reg, method, max_iter, tol, kl, per_problem=False):
     """Uniform batch in the ot.batch order (u first, row-marginal check every
-    10th iteration, each problem stopping on its own error).  The log form is
-    the sinkhorn_log order of the transposed problems (a and b swapped) on the
-    work-balanced kernel; the scaling form runs the CTA-per-problem kernel."""
+    10th iteration): the sinkhorn_log (or scaling) order of the transposed
+    problems (a and b swapped) on the work-balanced kernel.  The whole batch
+    stops on its largest error unless ``per_problem``."""
     layout, Mp = _uniform_batch(Md)
     ap, bp = a.reshape(-1).contiguous(), b.reshape(-1).contiguous()
-    if method == _lib.OTG_METHOD_LOG and layout.B <= 65535:
-        lt, Mt = _transposed(layout, Mp)
-        vt, ut, status, niter, err, reg_t = run_multi(lt, Mt, bp, ap, reg, max_iter, tol)
-        u, v = ut, vt
-        del Mt
-    else:
-        u, v, status, niter, err, reg_t = run_batched(layout, Mp, ap, bp, reg, method, max_iter, tol, u_first=1)
+    lt, Mt = _transposed(layout, Mp)
+    vt, ut, status, niter, err, reg_t = run_multi(lt, Mt, bp, ap, reg, max_iter, tol, joint=not per_problem,
+                                                  scaling=method == _lib.OTG_METHOD_KNOPP)
+    u, v = ut, vt
+    del Mt
     P, vals = batched_plan(layout, Mp, u, v, ap, bp, reg_t, method, kl=kl)
     B, n, m = Md.shape
     ld = int(layout.ldm_np[0])
@@ -309,8 +323,10 @@ def _solve_uniform(Md, a, b, reg, method, max_iter, tol, kl):
 
 
 def solve_batch(M, reg, a=None, b=None, max_iter=1000, tol=1e-5, solver="log_sinkhorn", reg_type="entropy",
-                grad="envelope"):
-    """GPU ``ot.batch.solve_batch`` (``ot/batch/_linear.py:236``)."""
+                grad="envelope", per_problem=False):
+    """GPU ``ot.batch.solve_batch`` (``ot/batch/_linear.py:236``).
+    ``per_problem`` (no reference counterpart): every problem stops on its
+    own error instead of the batch's largest."""
     if solver not in ("log_sinkhorn", "sinkhorn"):
         raise ValueError(f"Unknown solver: {solver}")
     if reg_type.lower() not in ("entropy", "kl"):
@@ -322,7 +338,7 @@ def solve_batch(M, reg, a=None, b=None, max_iter=1000, tol=1e-5, solver="log_sin
     bv = torch.full((B, m), 1.0 / m, dtype=Md.dtype, device=Md.device) if b is None else bd.to_dev(b, Md.dtype)
     method = _lib.OTG_METHOD_LOG if solver == "log_sinkhorn" else _lib.OTG_METHOD_KNOPP
     T, u, v, vals, niter, _ = _solve_uniform(Md, ad, bv, float(reg), method, max_iter, tol,
-                                             reg_type.lower() == "kl")
+                                             reg_type.lower() == "kl", per_problem)
     value_linear = vals[:, 0].to(Md.dtype)
     value = (vals[:, 0] + float(reg) * vals[:, 1]).to(Md.dtype)
     log = {"n_iter": int(niter.max().item())}
@@ -352,18 +368,19 @@ def dist_batch(X1, X2=None, metric="sqeuclidean", p=2, nx=None):
 
 
 def solve_sample_batch(X_a, X_b, reg, a=None, b=None, metric="sqeuclidean", p=2, max_iter=1000, tol=1e-5,
-                       solver="log_sinkhorn", reg_type="entropy", grad="envelope"):
+                       solver="log_sinkhorn", reg_type="entropy", grad="envelope", per_problem=False):
     """GPU ``ot.batch.solve_sample_batch`` (``ot/batch/_linear.py:360``)."""
     bd = Boundary(X_a, X_b, a, b)
     M = dist_batch(bd.to_dev(X_a), bd.to_dev(X_b), metric=metric, p=p)
     res = solve_batch(M, reg, a=None if a is None else bd.to_dev(a, M.dtype),
                       b=None if b is None else bd.to_dev(b, M.dtype), max_iter=max_iter, tol=tol, solver=solver,
-                      reg_type=reg_type, grad=grad)
+                      reg_type=reg_type, grad=grad, per_problem=per_problem)
     return OTResult(value=bd.out(res.value), value_linear=bd.out(res.value_linear),
                     potentials=tuple(bd.out(x) for x in res.potentials), plan=bd.out(res.plan), log=res.log)
 
 
-def bregman_log_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol=1e-5, grad="detach"):
+def bregman_log_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol=1e-5, grad="detach",
+                                 per_problem=False):
     """GPU ``ot.batch.bregman_log_projection_batch`` (``_utils.py:165``):
     ``K = -M/reg`` is solved as cost ``-K`` with unit regularisation."""
     bd = Boundary(K, a, b)
@@ -371,13 +388,15 @@ def bregman_log_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol
     B, n, m = Kd.shape
     ad = torch.ones((B, n), dtype=Kd.dtype, device=Kd.device) / n if a is None else bd.to_dev(a, Kd.dtype)
     bv = torch.ones((B, m), dtype=Kd.dtype, device=Kd.device) / m if b is None else bd.to_dev(b, Kd.dtype)
-    T, u, v, _, niter, _ = _solve_uniform((-Kd).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_LOG, max_iter, tol, False)
+    T, u, v, _, niter, _ = _solve_uniform((-Kd).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_LOG, max_iter, tol, False,
+                                          per_problem)
     log_T = Kd + u[:, :, None] + v[:, None, :]
     return {"T": bd.out(T), "log_T": bd.out(log_T), "n_iters": int(niter.max().item()),
             "potentials": (bd.out(u), bd.out(v))}
 
 
-def bregman_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol=1e-5, grad="detach"):
+def bregman_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol=1e-5, grad="detach",
+                             per_problem=False):
     """GPU ``ot.batch.bregman_projection_batch`` (``_utils.py:46``): the
     affinity ``K`` is solved as cost ``-log K`` with unit regularisation."""
     bd = Boundary(K, a, b)
@@ -386,7 +405,7 @@ def bregman_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol=1e-
     ad = torch.ones((B, n), dtype=Kd.dtype, device=Kd.device) / n if a is None else bd.to_dev(a, Kd.dtype)
     bv = torch.ones((B, m), dtype=Kd.dtype, device=Kd.device) / m if b is None else bd.to_dev(b, Kd.dtype)
     T, f, g, _, niter, _ = _solve_uniform((-torch.log(Kd)).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_KNOPP,
-                                          max_iter, tol, False)
+                                          max_iter, tol, False, per_problem)
     return {"T": bd.out(T), "n_iters": int(niter.max().item()), "potentials": (bd.out(f), bd.out(g))}
 
 
@@ -469,12 +488,14 @@ def _bgemm(A, B, ta, tb, out, alpha=1.0, beta=0.0):
 
 def solve_gromov_batch(C1, C2, reg=1e-2, a=None, b=None, loss="sqeuclidean", symmetric=None, M=None, alpha=None,
                        T_init=None, max_iter=50, tol=1e-5, max_iter_inner=50, tol_inner=1e-5, grad="envelope",
-                       logits=None):
+                       logits=None, per_problem=False):
     """GPU ``ot.batch.solve_gromov_batch`` (``ot/batch/_quadratic.py:269-498``)
     for the squared loss and scalar costs: per outer step the tensor product
     ``constC - hC1 T hC2^T`` (batched GEMMs), ``Mk = (1 - alpha) M + 2 alpha
-    L x T``, and the batched log projection of ``-Mk/reg + log T`` (every
-    problem stops on its own inner error)."""
+    L x T``, and the batched log projection of ``-Mk/reg + log T`` (the
+    whole batch stopping on its largest inner error, as in the reference;
+    ``per_problem=True``: every problem on its own).  The outer loop stops on
+    the largest mean plan change (``:458-471``)."""
     if not isinstance(loss, str):
         raise ValueError(f"Unknown loss function: {loss}")
     if loss != "sqeuclidean":
@@ -537,7 +558,7 @@ def solve_gromov_batch(C1, C2, reg=1e-2, a=None, b=None, loss="sqeuclidean", sym
         Mk = (1 - alpha) * Md + 2 * alpha * (constC - dot(T))
         K = -Mk / reg + log_T
         T, u, v, _, _, _ = _solve_uniform((-K).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_LOG, max_iter_inner,
-                                          tol_inner, False)
+                                          tol_inner, False, per_problem)
         log_T = K + u[:, :, None] + v[:, None, :]
         if float(torch.amax(torch.mean(torch.abs(T_prev - T), dim=(1, 2)))) < tol:
             break

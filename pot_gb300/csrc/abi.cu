@@ -118,7 +118,12 @@ namespace {
   X(split_cap_fill) \
   X(split_cap_tail) \
   X(tail_problems) \
-  X(reserved)
+  X(joint_stop) \
+  X(scaling) \
+  X(anderson_depth) \
+  X(reserved) \
+  X(anderson_ws) \
+  X(anderson_ws_bytes)
 #define OTG_FIELDS_OtgOnlineProblem(X) \
   X(X) \
   X(Y) \

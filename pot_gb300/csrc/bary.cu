@@ -72,26 +72,13 @@ __device__ __forceinline__ double row_std(const T* x, int H) {
   return sqrt(var / H);
 }
 
-template <typename T>
-__device__ void add_block_sum(double v, double* out) {
-  __shared__ double red[32];
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
-    atomicAdd(out, t);
-  }
-}
-
 // Scaling form, per row: UKv = u * KtX ; bar = exp(log(UKv) w) ;
-// u = u * bar / UKv ; err += std_k UKv (check iterations).
+// u = u * bar / UKv ; erow[i] = std_k UKv (check iterations; the rows' slots
+// are summed in a fixed order afterwards).
 template <typename T>
 __global__ void __launch_bounds__(256) bary_update_kernel(T* __restrict__ u, T* __restrict__ KtX,
                                                           const T* __restrict__ w, int64_t n, int H,
-                                                          T* __restrict__ bar, double* err) {
-  double e = 0;
+                                                          T* __restrict__ bar, double* erow) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     T* ui = u + i * H;
     T* ukv = KtX + i * H;  // overwritten with UKv
@@ -103,9 +90,8 @@ __global__ void __launch_bounds__(256) bary_update_kernel(T* __restrict__ u, T* 
     const T b = exp(lb);
     bar[i] = b;
     for (int k = 0; k < H; ++k) ui[k] = ui[k] * b / ukv[k];
-    if (err) e += row_std(ukv, H);
+    if (erow) erow[i] = row_std(ukv, H);
   }
-  if (err) add_block_sum<T>(e, err);
 }
 
 // Log form, row pass: out[i,k] = logA[i,k] - LSE_j(c2 M[i,j] + V[j,k] log2e) ln2
@@ -146,29 +132,27 @@ __global__ void __launch_bounds__(256) lse_cols_kernel(const T* __restrict__ M, 
   out[j * H + k] = lse_value(mx, s) * LN2;
 }
 
-// Log form, per row: logbar = logKU w ; err += std_k exp(G + logKU) ;
+// Log form, per row: logbar = logKU w ; erow[i] = std_k exp(G + logKU) ;
 // G = logbar - logKU.
 template <typename T>
 __global__ void __launch_bounds__(256) bary_log_update_kernel(T* __restrict__ G, const T* __restrict__ logKU,
                                                               const T* __restrict__ w, int64_t n, int H,
-                                                              T* __restrict__ logbar, double* err) {
-  double e = 0;
+                                                              T* __restrict__ logbar, double* erow) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const T* lk = logKU + i * H;
     T* gi = G + i * H;
     T lb = 0;
     for (int k = 0; k < H; ++k) lb += w[k] * lk[k];
     logbar[i] = lb;
-    if (err) {
+    if (erow) {
       double mean = 0, var = 0;
       for (int k = 0; k < H; ++k) mean += exp((double)gi[k] + (double)lk[k]);
       mean /= H;
       for (int k = 0; k < H; ++k) { const double d = exp((double)gi[k] + (double)lk[k]) - mean; var += d * d; }
-      e += sqrt(var / H);
+      erow[i] = sqrt(var / H);
     }
     for (int k = 0; k < H; ++k) gi[k] = lb - lk[k];
   }
-  if (err) add_block_sum<T>(e, err);
 }
 
 template <typename T>
@@ -219,6 +203,7 @@ int run_bary(const OtgBaryProblem* p, cudaStream_t st) {
   size_t off = 0;
   auto take = [&](size_t bytes) { char* q = ws + off; off += a256(bytes); return q; };
   double* err = reinterpret_cast<double*>(take(8 * 2));
+  double* erow = reinterpret_cast<double*>(take(8 * (size_t)n));  // per-row errors of a check iteration
   const size_t nh = sizeof(T) * (size_t)n * H;
   T* b1 = reinterpret_cast<T*>(take(nh));
   T* b2 = reinterpret_cast<T*>(take(nh));
@@ -246,9 +231,9 @@ int run_bary(const OtgBaryProblem* p, cudaStream_t st) {
       bary_div_kernel<T><<<gb, 256, 0, st>>>(A, KU, n * H, X);
       if ((rc = gemm<T>(1, 0, n, H, n, K, n, X, H, KU, H, st)) != OTG_OK) return rc;  // K^T X into KU
       const bool check = ii % 10 == 1;
-      if (check && cudaMemsetAsync(err, 0, 8, st) != cudaSuccess) return OTG_ERR_CUDA;
-      bary_update_kernel<T><<<blocks_for(n), 256, 0, st>>>(u, KU, w, n, H, bar, check ? err : nullptr);
+      bary_update_kernel<T><<<blocks_for(n), 256, 0, st>>>(u, KU, w, n, H, bar, check ? erow : nullptr);
       if (check) {
+        slot_sum_kernel<1024><<<1, 1024, 0, st>>>(erow, n, err);  // fixed order: the same error in every run
         if (cudaMemcpyAsync(&herr, err, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return OTG_ERR_CUDA;
         if (cudaStreamSynchronize(st) != cudaSuccess) return OTG_ERR_CUDA;
         if (nchk < p->hist_cap) p->err_hist[nchk] = herr;
@@ -267,10 +252,10 @@ int run_bary(const OtgBaryProblem* p, cudaStream_t st) {
       lse_rows_kernel<T><<<(unsigned)n, 256, 0, st>>>(M, n, p->ldm, c2, G, H, logA, F);
       lse_cols_kernel<T><<<cgrid, 256, 0, st>>>(M, n, p->ldm, c2, F, H, logKU);
       const bool check = ii % 10 == 1;
-      if (check && cudaMemsetAsync(err, 0, 8, st) != cudaSuccess) return OTG_ERR_CUDA;
       // the log barycentre is kept in out_bar and exponentiated at the end
-      bary_log_update_kernel<T><<<blocks_for(n), 256, 0, st>>>(G, logKU, w, n, H, bar, check ? err : nullptr);
+      bary_log_update_kernel<T><<<blocks_for(n), 256, 0, st>>>(G, logKU, w, n, H, bar, check ? erow : nullptr);
       if (check) {
+        slot_sum_kernel<1024><<<1, 1024, 0, st>>>(erow, n, err);  // fixed order: the same error in every run
         if (cudaMemcpyAsync(&herr, err, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return OTG_ERR_CUDA;
         if (cudaStreamSynchronize(st) != cudaSuccess) return OTG_ERR_CUDA;
         if (nchk < p->hist_cap) p->err_hist[nchk] = herr;
@@ -295,7 +280,7 @@ extern "C" {
 size_t otg_barycenter_workspace_bytes(int dtype, int method, int64_t dim, int32_t n_hists) {
   const size_t es = dtype == OTG_F64 ? 8 : 4;
   const size_t nh = a256(es * (size_t)dim * (size_t)n_hists);
-  size_t b = a256(16) + 3 * nh;
+  size_t b = a256(16) + a256(8 * (size_t)dim) + 3 * nh;
   if (method == OTG_METHOD_KNOPP) b += a256(es * (size_t)dim * (size_t)dim) + 2 * a256(8 * (size_t)dim);
   else b += nh;
   return b;

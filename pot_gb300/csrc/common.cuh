@@ -124,6 +124,50 @@ __device__ __forceinline__ T warp_max(T x) {
 __device__ __forceinline__ int warp_or(int x) { return __any_sync(0xffffffffu, x) ? 1 : 0; }
 
 // ---------------------------------------------------------------------------
+// Reductions in a fixed order.  Floating-point addition is not associative,
+// so a sum whose terms arrive through atomics changes from run to run in its
+// last bits; a stopping test on such a sum can then stop at a different
+// iteration.  Every error that feeds a stop decision is therefore summed in
+// an order fixed by the data layout alone: partials are stored in fixed
+// slots and summed by these helpers.
+//
+// warp_sum's xor butterfly combines partner values commutatively at every
+// step, so all lanes hold the same, order-fixed value.
+// ---------------------------------------------------------------------------
+// Block sum of one double per thread; every thread gets the result.  All
+// threads of the block call it.
+__device__ __forceinline__ double block_sum_fixed(double x) {
+  __shared__ double red[33];
+  x = warp_sum(x);
+  __syncthreads();  // red may still be read by a previous call
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// Sum of p[0 .. cnt) by one block (thread t folds t, t + blockDim, ... in
+// increasing order); every thread gets the result.
+__device__ __forceinline__ double block_sum_slots(const double* p, int64_t cnt) {
+  double x = 0.0;
+  for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) x += __ldcg(p + i);
+  return block_sum_fixed(x);
+}
+
+// *out = sum of slots[0 .. cnt) in a fixed order; launch with ONE block of
+// BS threads.  (A template, so that every translation unit may include it.)
+template <int BS>
+__global__ void __launch_bounds__(BS) slot_sum_kernel(const double* __restrict__ slots, int64_t cnt, double* out) {
+  const double t = block_sum_slots(slots, cnt);
+  if (threadIdx.x == 0) *out = t;
+}
+
+// ---------------------------------------------------------------------------
 // Bounded grid barrier for cooperative (co-resident) launches.
 // bar[0] counts arrivals, bar[1] is the generation.  A block that waits
 // longer than `timeout_ns` (globaltimer) sets *abort and leaves; callers check

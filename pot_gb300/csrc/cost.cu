@@ -119,7 +119,7 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
   // D a multiple of 4: rows of X and Y are 16-byte aligned (the packed clouds
   // start at multiples of D elements), so points are staged as float4 loads
   constexpr bool V4 = D % 4 == 0;
-  if (V4) {
+  if constexpr (V4) {
     for (int e = threadIdx.x; e < SQ_R * D / 4; e += blockDim.x) {
       const int r = e / (D / 4), k = (e % (D / 4)) * 4;
       const float4 v = (r0 + r < n) ? *reinterpret_cast<const float4*>(X + (int64_t)(r0 + r) * D + k)
@@ -135,7 +135,7 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
   }
   for (int c0 = blockIdx.x * SQ_C; c0 < ldm; c0 += gridDim.x * SQ_C) {
     __syncthreads();  // previous tile's reads of yt are done (and xt is staged)
-    if (V4) {
+    if constexpr (V4) {
       for (int e = threadIdx.x; e < SQ_C * D / 4; e += blockDim.x) {
         const int c = e / (D / 4), k = (e % (D / 4)) * 4;
         const float4 v = (c0 + c < m) ? *reinterpret_cast<const float4*>(Y + (int64_t)(c0 + c) * D + k)

@@ -48,8 +48,10 @@
 // column sums divided by n m (:1298-1306).  The host turns (F, G), the
 // absorption count and the last-iteration flag back into the reference's
 // logu, logv, alpha, beta.
+#include <cuda.h>
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include "common.cuh"
 #include "../../include/pot_gb300.h"
 
@@ -90,6 +92,7 @@ struct DenseArgs {
   T fi1, fi2;
   const T* alw; const T* bew;           // c = alw bew^T (null: ones)
   unsigned* slab_cnt;                   // [nslabs] column-pass units done per slab
+  double* eslab;                        // [nslabs] squared marginal error of each slab (check passes)
 };
 
 // Per-thread maxima carried out of a pass (stabilised: d0; unbalanced:
@@ -169,7 +172,6 @@ template <typename T> struct ColFuse {
   const T* vcur; T* vnxt;
   bool check, update;
   T shift;
-  double e2;
   Track tr;
 };
 
@@ -267,11 +269,17 @@ __device__ void col_pass(const DenseArgs<T>& A, const T* __restrict__ u, int lan
       __syncthreads();
       if (s_last) {
         __threadfence();
+        double e2 = 0.0;
         for (int c = threadIdx.x; c < slab_w; c += blockDim.x) {
           const int64_t j = slab * slab_w + c;
           if (j < m)
-            merge_col<T, METHOD>(A, j, fuse->vcur, fuse->vnxt, fuse->check, fuse->update, fuse->shift, fuse->e2,
-                                 fuse->tr);
+            merge_col<T, METHOD>(A, j, fuse->vcur, fuse->vnxt, fuse->check, fuse->update, fuse->shift, e2, fuse->tr);
+        }
+        // the slab's error in its own slot (which CTA merges a slab varies
+        // from run to run; the slot and the order within it do not)
+        if (fuse->check) {
+          e2 = block_sum_fixed(e2);
+          if (threadIdx.x == 0) A.eslab[slab] = e2;
         }
       }
     }
@@ -475,38 +483,12 @@ __device__ __forceinline__ void merge_col(const DenseArgs<T>& A, int64_t j, cons
   }
 }
 
-// Block sum of the per-thread squared errors, one fp64 atomic per CTA.
-__device__ __forceinline__ void block_err_atomic(double e2, double* err_slot) {
-  __shared__ double red[32];
-  e2 = warp_sum(e2);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e2;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
-    atomicAdd(err_slot, t);
-  }
-  __syncthreads();
-}
-
+// Column merge after a separate column pass (unbalanced form: no error).
 template <typename T, int METHOD>
-__device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* __restrict__ vnxt,
-                          bool check, bool update, double* err_slot, long gtid, long nthreads, T err_shift,
-                          Track& tr) {
+__device__ void col_merge(const DenseArgs<T>& A, const T* __restrict__ vcur, T* __restrict__ vnxt, bool update,
+                          long gtid, long nthreads, Track& tr) {
   double e2 = 0.0;
-  for (int64_t j = gtid; j < A.m; j += nthreads) merge_col<T, METHOD>(A, j, vcur, vnxt, check, update, err_shift, e2, tr);
-  if (check) {
-    // block reduction, then one fp64 atomic per CTA
-    __shared__ double red[32];
-    e2 = warp_sum(e2);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e2;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0;
-      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
-      atomicAdd(err_slot, t);
-    }
-  }
+  for (int64_t j = gtid; j < A.m; j += nthreads) merge_col<T, METHOD>(A, j, vcur, vnxt, false, update, T(0), e2, tr);
 }
 
 template <typename T> struct BlocksPerSM { static constexpr int value = sizeof(T) == 4 ? 4 : 2; };
@@ -514,9 +496,6 @@ template <typename T> struct BlocksPerSM { static constexpr int value = sizeof(T
 template <typename T, int METHOD, bool VEC>
 __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_kernel(DenseArgs<T> A) {
   const int lane = threadIdx.x & 31;
-  const long nwb = blockDim.x >> 5;
-  const long gwarp = blockIdx.x * nwb + (threadIdx.x >> 5);
-  const long nwarps = gridDim.x * nwb;
   const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nthreads = (long)gridDim.x * blockDim.x;
   int* abort_flag = A.info + 3;
@@ -581,7 +560,7 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
       col_pass<T, METHOD, VEC>(A, A.sa, lane);
       if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
       Track vt;
-      col_merge<T, METHOD>(A, vcur, vnxt, false, true, nullptr, gtid, nthreads, T(0), vt);
+      col_merge<T, METHOD>(A, vcur, vnxt, true, gtid, nthreads, vt);
       block_max_atomic(vt.d0, sl + 3); block_max_atomic(vt.d1, sl + 4); block_max_atomic(vt.d2, sl + 5);
       if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
       if (ld_acquire_i(A.info + 4)) { status = OTG_STATUS_NUMERICAL; niter = ii; break; }  // previous pair kept
@@ -604,13 +583,15 @@ __global__ void __launch_bounds__(256, BlocksPerSM<T>::value) dense_sinkhorn_ker
     const bool update = ii < A.max_iter;
     double* slot = A.hist + (nchk < A.hist_cap ? nchk : A.hist_cap - 1);
     const T shift = (METHOD == OTG_METHOD_STAB && absorbed) ? -(A.log2n + A.log2m) : T(0);
-    ColFuse<T> cf{vcur, vnxt, prev_check, update, shift, 0.0, Track{}};
+    ColFuse<T> cf{vcur, vnxt, prev_check, update, shift, Track{}};
     col_pass<T, METHOD, VEC>(A, ucur, lane, &cf);
-    if (prev_check) block_err_atomic(cf.e2, slot);
     if (METHOD == OTG_METHOD_STAB && update) block_max_atomic(cf.tr.d0, A.mslot + 2 + (ii & 1));
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     if (prev_check) {
-      double e2 = *(volatile double*)slot;
+      // the slabs' errors summed in slab order: the same value in every CTA
+      // and in every run
+      const double e2 = block_sum_slots(A.eslab, (A.m + 32 * Vec<T>::N - 1) / (32 * Vec<T>::N));
+      if (gtid == 0) *slot = e2;
       ++nchk;
       const bool stop = METHOD == OTG_METHOD_STAB ? sqrt(e2) <= A.stop_thr : sqrt(e2) < A.stop_thr;
       if (stop) { status = OTG_STATUS_CONVERGED; niter = ii - 1; break; }
@@ -707,8 +688,9 @@ __global__ void __launch_bounds__(256) dense_plan_kernel(const T* __restrict__ M
 
 // ---------------------------------------------------------------------------
 // Marginals of the plan exp(-M_ij/reg + u_i + v_j) (natural-log potentials),
-// accumulated in fp64: one warp per row for the row sums; column sums from
-// CTAs of 256 columns x 64 rows, one atomic per column per CTA.
+// accumulated in fp64 in a fixed order: one warp per row for the row sums;
+// for the column sums a CTA owns 32 columns, its 8 warps take every 8th row
+// (lane = column) and their partials are added in warp order.
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(256) dense_rowsum_kernel(const T* __restrict__ M, int64_t n, int64_t m, int64_t ldm,
@@ -729,14 +711,22 @@ template <typename T>
 __global__ void __launch_bounds__(256) dense_colsum_kernel(const T* __restrict__ M, int64_t n, int64_t m, int64_t ldm,
                                                            const T* __restrict__ u, const T* __restrict__ v, T c,
                                                            double* __restrict__ cols) {
+  __shared__ double part[8][32];
   const T L2E = T(OTG_LOG2E);
-  const int64_t j = (int64_t)blockIdx.x * 256 + threadIdx.x;
-  const int64_t i0 = (int64_t)blockIdx.y * 64, i1 = min(n, i0 + 64);
-  if (j >= m) return;
-  const T vj = v[j] * L2E;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t j = (int64_t)blockIdx.x * 32 + lane;
   double acc = 0.0;
-  for (int64_t i = i0; i < i1; ++i) acc += (double)ex2(fma(M[i * ldm + j], c, u[i] * L2E + vj));
-  atomicAdd(cols + j, acc);
+  if (j < m) {
+    const T vj = v[j] * L2E;
+    for (int64_t i = warp; i < n; i += 8) acc += (double)ex2(fma(M[i * ldm + j], c, u[i] * L2E + vj));
+  }
+  part[warp][lane] = acc;
+  __syncthreads();
+  if (warp == 0 && j < m) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += part[w][lane];
+    cols[j] = t;
+  }
 }
 
 }  // namespace otg
@@ -751,7 +741,7 @@ namespace {
 struct Layout {
   int grid, Sr, Sc;
   int64_t rchunk, cchunk;
-  size_t off_state, off_pcol, off_prow, off_hist, off_ctrl, off_cnt, total;
+  size_t off_state, off_pcol, off_prow, off_hist, off_ctrl, off_cnt, off_eslab, total;
 };
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -800,6 +790,7 @@ Layout make_layout(int64_t n, int64_t m, int hist_cap, int grid) {
   L.off_hist = off; off = align_up(off + sizeof(double) * (size_t)hist_cap, 256);
   L.off_ctrl = off; off = align_up(off + 256, 256);
   L.off_cnt = off; off = align_up(off + sizeof(unsigned) * (size_t)nslabs, 256);
+  L.off_eslab = off; off = align_up(off + sizeof(double) * (size_t)nslabs, 256);
   L.total = off;
   return L;
 }
@@ -845,6 +836,7 @@ int launch_dense(const OtgDenseProblem* p, void* ws, cudaStream_t st) {
   A.period = METHOD == OTG_METHOD_STAB ? p->check_period : 10;
   A.mslot = reinterpret_cast<unsigned long long*>(base + L.off_ctrl + 64);
   A.slab_cnt = reinterpret_cast<unsigned*>(base + L.off_cnt);
+  A.eslab = reinterpret_cast<double*>(base + L.off_eslab);
   if (METHOD == OTG_METHOD_UNB) {
     A.fi1 = (T)(std::isinf(p->reg_m1) ? 1.0 : p->reg_m1 / (p->reg_m1 + p->reg));
     A.fi2 = (T)(std::isinf(p->reg_m2) ? 1.0 : p->reg_m2 / (p->reg_m2 + p->reg));
@@ -968,9 +960,8 @@ int otg_gibbs_kernel(int dtype, const void* M, int64_t n, int64_t m, int64_t ldm
 int otg_dense_marginals(int dtype, const void* M, int64_t n, int64_t m, int64_t ldm, const void* u, const void* v,
                         double reg, double* rowsum, double* colsum, cudaStream_t stream) {
   if (!M || !u || !v || !rowsum || !colsum || n < 1 || m < 1 || ldm < m || !(reg > 0)) return OTG_ERR_ARG;
-  if (cudaMemsetAsync(colsum, 0, sizeof(double) * (size_t)m, stream) != cudaSuccess) return OTG_ERR_CUDA;
   const double c = -OTG_LOG2E / reg;
-  const dim3 rg((unsigned)((n + 7) / 8)), cg((unsigned)((m + 255) / 256), (unsigned)((n + 63) / 64));
+  const dim3 rg((unsigned)((n + 7) / 8)), cg((unsigned)((m + 31) / 32));
   if (dtype == OTG_F64) {
     dense_rowsum_kernel<double><<<rg, 256, 0, stream>>>((const double*)M, n, m, ldm, (const double*)u, (const double*)v, c, rowsum);
     dense_colsum_kernel<double><<<cg, 256, 0, stream>>>((const double*)M, n, m, ldm, (const double*)u, (const double*)v, c, colsum);
@@ -1005,20 +996,66 @@ namespace {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[OTG_NOALLOC_SCRATCH_BYTES];
 
 // Host code cannot use g_noalloc_scratch as a device address (on the host
-// it names a stand-in object), so the address is looked up once per device
-// with that device current and cached here.
-constexpr int kMaxDevices = 64;
-void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+// it names a stand-in object), so its device address is looked up with
+// cudaGetSymbolAddress, with the device current, the first time a context
+// calls, and cached.  The cache is keyed by the CUDA context's unique ID
+// (cuCtxGetId), not by the device ordinal: after cudaDeviceReset, or in a
+// context other than the primary one (cuCtxCreate, green contexts), the
+// module and its array live at another address, and a context gets a new
+// ID when it is created again.  A mutex guards the cache against host
+// threads making their first calls at the same time.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+struct NoallocCache {
+  std::mutex mu;
+  CtxGetCurrentFn get_current = nullptr;
+  CtxGetIdFn get_id = nullptr;
+  bool resolved = false;
+  static constexpr int kSlots = 64;
+  unsigned long long ids[kSlots] = {};
+  void* ptrs[kSlots] = {};
+  int used = 0;
+};
+NoallocCache g_noalloc;
 
 int noalloc_scratch(void** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return OTG_ERR_CUDA;
-  if (!g_noalloc_ptr[dev]) {
-    void* ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return OTG_ERR_CUDA;
-    g_noalloc_ptr[dev] = ptr;
+  std::lock_guard<std::mutex> lock(g_noalloc.mu);
+  if (!g_noalloc.resolved) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_noalloc.get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_noalloc.get_id = reinterpret_cast<CtxGetIdFn>(f);
+    g_noalloc.resolved = true;
   }
-  *out = g_noalloc_ptr[dev];
+  if (!g_noalloc.get_current || !g_noalloc.get_id) return OTG_ERR_CUDA;
+  CUcontext ctx = nullptr;
+  if (g_noalloc.get_current(&ctx) != CUDA_SUCCESS) return OTG_ERR_CUDA;
+  if (!ctx) {
+    // no context on this thread yet: the runtime makes the current device's
+    // primary context current on its first call that needs one
+    void* probe = nullptr;
+    if (cudaGetSymbolAddress(&probe, g_noalloc_scratch) != cudaSuccess) return OTG_ERR_CUDA;
+    if (g_noalloc.get_current(&ctx) != CUDA_SUCCESS || !ctx) return OTG_ERR_CUDA;
+  }
+  unsigned long long id = 0;
+  if (g_noalloc.get_id(ctx, &id) != CUDA_SUCCESS) return OTG_ERR_CUDA;
+  for (int k = 0; k < g_noalloc.used; ++k)
+    if (g_noalloc.ids[k] == id) { *out = g_noalloc.ptrs[k]; return OTG_OK; }
+  void* ptr = nullptr;
+  if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return OTG_ERR_CUDA;
+  // a full table still works, the lookup is just repeated for later contexts
+  if (g_noalloc.used < NoallocCache::kSlots) {
+    g_noalloc.ids[g_noalloc.used] = id;
+    g_noalloc.ptrs[g_noalloc.used] = ptr;
+    ++g_noalloc.used;
+  }
+  *out = ptr;
   return OTG_OK;
 }
 

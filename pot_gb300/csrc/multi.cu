@@ -5,6 +5,15 @@
 // Reference behaviour (PythonOT/POT): per problem, the order and stopping test
 // of ot/bregman/_sinkhorn.py:880-899 (sinkhorn_log: v first, then u; L2
 // column-marginal error every 10th iteration); problems stop individually.
+// With `joint` the whole batch stops together at the first check whose
+// LARGEST error is below the threshold (ot/batch/_utils.py:273-278 and
+// :152-157).  The scaling form (LOGF = false) runs the same passes with sums
+// of K_ij = exp(-M_ij/reg) products instead of log-sum-exps (the scaling
+// iteration of ot/batch/_utils.py:146-151 on the transposed problem).
+//
+// The squared marginal error of each column is stored in its own slot and
+// summed per problem in a fixed order, so a problem's error, and with it
+// its stop index, is the same in every run.
 //
 // One persistent cooperative launch.  Each iteration:
 //   column pass : units (problem, row chunk, slab of 32*VW columns) over all
@@ -70,7 +79,9 @@ struct MultiArgs {
   // state
   T* u; T* v0; T* v1;       // base-2 potentials, packed like a / b
   MPair<T>* pcol;
-  double* err2;             // per problem
+  double* err2;             // per problem: squared error of the last check (joint stop)
+  double* e2col;            // per column: squared marginal error (check passes), packed like b
+  bool joint;               // whole-batch stop on the largest error
   int32_t* active;          // active problem ids [nprob]
   int64_t* ucol_pre;        // prefix of column-pass units over the active list [nprob+1]
   int64_t* urow_pre;        // prefix of row-pass units
@@ -128,7 +139,7 @@ __device__ __forceinline__ void mt_share(int64_t total, long w, long nw, int64_t
   end = total * (w + 1) / nw;
 }
 
-template <typename T>
+template <typename T, bool LOGF>
 __device__ void mt_col_pass(const MultiArgs<T>& A, int nact, long gwarp, long nwarps, int lane) {
   constexpr int VW = Vec<T>::N;
   using V = typename Vec<T>::type;
@@ -168,13 +179,20 @@ __device__ void mt_col_pass(const MultiArgs<T>& A, int nact, long gwarp, long nw
           } else {
 #pragma unroll
             for (int q = 0; q < VW; ++q) x[g][q] = 0;
-            ur[g] = -INFINITY;
+            ur[g] = LOGF ? T(-INFINITY) : T(0);
           }
         }
       };
       for (int i = i0; i < i1; i += MT_GCOL) {
         T x[MT_GCOL][VW], ur[MT_GCOL];
         load_group(i, x, ur);
+        if constexpr (!LOGF) {
+          // scaling form: s_j += K_ij u_i with K_ij = 2^(M_ij c)
+#pragma unroll
+          for (int q = 0; q < VW; ++q)
+#pragma unroll
+            for (int g = 0; g < MT_GCOL; ++g) s[q] = fma(ex2(x[g][q] * c), ur[g], s[q]);
+        } else {
 #pragma unroll
         for (int q = 0; q < VW; ++q) {
           T t[MT_GCOL];
@@ -190,6 +208,7 @@ __device__ void mt_col_pass(const MultiArgs<T>& A, int nact, long gwarp, long nw
             mx[q] = nm;
           }
         }
+        }
       }
       MPair<T>* pc = A.pcol + A.pc_off[p] + r * m;
 #pragma unroll
@@ -201,7 +220,7 @@ __device__ void mt_col_pass(const MultiArgs<T>& A, int nact, long gwarp, long nw
 
 // Column merge over every column of every active problem; per problem the
 // squared marginal error of (u_cur, v_cur) is accumulated when `check`.
-template <typename T>
+template <typename T, bool LOGF>
 __device__ void mt_col_merge(const MultiArgs<T>& A, int nact, const T* vcur, T* vnxt, bool check, bool update,
                              long gtid, long nthreads, bool relax_v) {
   const int64_t total = __ldcg(A.colpre + nact);
@@ -223,32 +242,24 @@ __device__ void mt_col_merge(const MultiArgs<T>& A, int nact, const T* vcur, T* 
     }
     const int j = (int)(e - sl.lo);
     T mx = -INFINITY, s = 0;
-    lse_merge_strided(mx, s, reinterpret_cast<const T*>(pc + j), 2 * (int64_t)m, nsr);
-    const T L = lse_value(mx, s);
+    if (LOGF) lse_merge_strided(mx, s, reinterpret_cast<const T*>(pc + j), 2 * (int64_t)m, nsr);
+    else s = sum_strided(reinterpret_cast<const T*>(pc + j), 2 * (int64_t)m, nsr);
+    const T L = LOGF ? lse_value(mx, s) : s;
     const int64_t cj = A.c_off[p] + j;
     const T bj = A.b[cj];
     if (check) {
-      double cs = (double)ex2(__ldcg(vcur + cj) + L) - (double)bj;
-      double e2 = cs * cs;
-      // lanes of one problem pre-reduce, one atomic per problem per warp
-      const unsigned act = __activemask();
-      const unsigned same = __match_any_sync(act, p);
-      const int leader = __ffs(same) - 1;
-      for (int o = 16; o > 0; o >>= 1) {
-        const double other = __shfl_down_sync(act, e2, o);
-        const int src_lane = (threadIdx.x & 31) + o;
-        if (src_lane < 32 && ((same >> src_lane) & 1u)) e2 += other;
-      }
-      if ((threadIdx.x & 31) == leader) atomicAdd(A.err2 + p, e2);
+      // column marginal of the iterate (u_cur, v_cur), in the column's own slot
+      const double cs = (LOGF ? (double)ex2(__ldcg(vcur + cj) + L) : (double)(__ldcg(vcur + cj) * L)) - (double)bj;
+      A.e2col[cj] = cs * cs;
     }
     if (update) {
-      const T vn = lg2(bj) - L;
+      const T vn = LOGF ? lg2(bj) - L : bj / L;
       vnxt[cj] = relax_v ? fma(A.omega, vn - __ldcg(vcur + cj), __ldcg(vcur + cj)) : vn;
     }
   }
 }
 
-template <typename T>
+template <typename T, bool LOGF>
 __device__ void mt_row_pass(const MultiArgs<T>& A, int nact, const T* v, long gwarp, long nwarps, int lane) {
   constexpr int VW = Vec<T>::N;
   using V = typename Vec<T>::type;
@@ -274,9 +285,9 @@ __device__ void mt_row_pass(const MultiArgs<T>& A, int nact, const T* v, long gw
 #pragma unroll
     for (int r = 0; r < MT_RW; ++r) { mx[r] = -INFINITY; s[r] = 0; }
     auto load_step = [&](int j, T (&x)[MT_RW][VW], T (&vv)[VW]) {
-      // v beyond m (padding up to ldm) is masked to -inf
+      // v beyond m (padding up to ldm) is masked out (-inf, or 0 for scalings)
 #pragma unroll
-      for (int q = 0; q < VW; ++q) vv[q] = (j + q < m) ? __ldcg(vp + j + q) : T(-INFINITY);
+      for (int q = 0; q < VW; ++q) vv[q] = (j + q < m) ? __ldcg(vp + j + q) : (LOGF ? T(-INFINITY) : T(0));
 #pragma unroll
       for (int r = 0; r < MT_RW; ++r) {
         const int row = min(r0 + r, n - 1);
@@ -287,6 +298,12 @@ __device__ void mt_row_pass(const MultiArgs<T>& A, int nact, const T* v, long gw
       T vv[VW];
       T x[MT_RW][VW];
       load_step(j, x, vv);
+      if constexpr (!LOGF) {
+#pragma unroll
+        for (int r = 0; r < MT_RW; ++r)
+#pragma unroll
+          for (int q = 0; q < VW; ++q) s[r] = fma(ex2(x[r][q] * c), vv[q], s[r]);
+      } else {
 #pragma unroll
       for (int r = 0; r < MT_RW; ++r) {
         T t[VW];
@@ -302,14 +319,18 @@ __device__ void mt_row_pass(const MultiArgs<T>& A, int nact, const T* v, long gw
           mx[r] = nm;
         }
       }
+      }
     }
 #pragma unroll
-    for (int r = 0; r < MT_RW; ++r) warp_lse(mx[r], s[r]);
+    for (int r = 0; r < MT_RW; ++r) {
+      if (LOGF) warp_lse(mx[r], s[r]);
+      else s[r] = warp_sum(s[r]);
+    }
 #pragma unroll
     for (int r = 0; r < MT_RW; ++r) {
       if (lane == r && r0 + r < n) {
         const int64_t ri = A.r_off[p] + r0 + r;
-        const T un = lg2(A.a[ri]) - lse_value(mx[r], s[r]);
+        const T un = LOGF ? lg2(A.a[ri]) - lse_value(mx[r], s[r]) : A.a[ri] / s[r];
         A.u[ri] = A.relax ? fma(A.omega, un - __ldcg(A.u + ri), __ldcg(A.u + ri)) : un;
       }
     }
@@ -401,7 +422,34 @@ __device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leavi
   __syncthreads();
 }
 
+// Whole-batch stop decision (joint mode): every problem's error into
+// err2[p] (its column slots summed in a fixed order), then the largest over
+// the batch (a max: the same in any order).  Returns 1 when the batch stops,
+// 0 when it goes on, -1 when a grid barrier gave up.  Kept out of line: it
+// runs once per check and its registers must not weigh on the passes.
 template <typename T>
+__device__ __noinline__ int mt_joint_decision(const MultiArgs<T>& A, int nact) {
+  for (int k = blockIdx.x; k < nact; k += gridDim.x) {
+    const int p = __ldcg(A.active + k);
+    const double e2 = block_sum_slots(A.e2col + A.c_off[p], A.cols[p]);
+    if (threadIdx.x == 0) A.err2[p] = e2;
+  }
+  if (!grid_barrier(A.bar, gridDim.x, A.ctl + 1, A.timeout_ns)) return -1;
+  __shared__ double s_mx[MT_THREADS / 32];
+  double mx = 0.0;
+  for (int k = threadIdx.x; k < nact; k += blockDim.x) {
+    const double e2 = __ldcg(A.err2 + __ldcg(A.active + k));
+    mx = isnan(e2) ? (double)INFINITY : fmax(mx, e2);  // a NaN error never meets the test
+  }
+  mx = warp_max(mx);
+  if ((threadIdx.x & 31) == 0) s_mx[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = fmax(mx, s_mx[w]);
+  __syncthreads();
+  return sqrt(mx) < A.stop_thr ? 1 : 0;
+}
+
+template <typename T, bool LOGF>
 __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn_kernel(MultiArgs<T> A, int32_t* leaving) {
   __shared__ int s_scan[MT_THREADS];
   const int lane = threadIdx.x & 31;
@@ -411,15 +459,18 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
   const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nthreads = (long)gridDim.x * blockDim.x;
   int* abort_flag = A.ctl + 1;
-  const T L2E = T(OTG_LOG2E), LN2 = T(OTG_LN2);
-  // initial state
+  const T L2E = T(OTG_LOG2E);
+  // outputs: natural-log potentials (log form) or the scalings themselves
+  const T OUTF = LOGF ? T(OTG_LN2) : T(1);
+  // initial state: u from the warm start (natural log) or zero log / unit scaling
   for (int p = blockIdx.x; p < A.nprob; p += gridDim.x) {
     const int n = A.rows[p], m = A.cols[p];
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const int64_t ri = A.r_off[p] + i;
-      A.u[ri] = A.warm_u ? A.warm_u[ri] * L2E : T(0);
+      if (LOGF) A.u[ri] = A.warm_u ? A.warm_u[ri] * L2E : T(0);
+      else A.u[ri] = A.warm_u ? exp(A.warm_u[ri]) : T(1);
     }
-    for (int j = threadIdx.x; j < m; j += blockDim.x) A.v0[A.c_off[p] + j] = T(0);
+    for (int j = threadIdx.x; j < m; j += blockDim.x) A.v0[A.c_off[p] + j] = LOGF ? T(0) : T(1);
     if (threadIdx.x == 0) { leaving[p] = 0; A.err2[p] = 0.0; }
   }
   if (blockIdx.x == 0) {
@@ -440,27 +491,35 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
       // every active problem ends without a final check (state of ii-1)
       for (int k = blockIdx.x; k < nact; k += gridDim.x) {
         const int p = __ldcg(A.active + k);
-        for (int i = threadIdx.x; i < A.rows[p]; i += blockDim.x) A.out_u[A.r_off[p] + i] = __ldcg(A.u + A.r_off[p] + i) * LN2;
-        for (int j = threadIdx.x; j < A.cols[p]; j += blockDim.x) A.out_v[A.c_off[p] + j] = __ldcg(vcur + A.c_off[p] + j) * LN2;
+        for (int i = threadIdx.x; i < A.rows[p]; i += blockDim.x) A.out_u[A.r_off[p] + i] = __ldcg(A.u + A.r_off[p] + i) * OUTF;
+        for (int j = threadIdx.x; j < A.cols[p]; j += blockDim.x) A.out_v[A.c_off[p] + j] = __ldcg(vcur + A.c_off[p] + j) * OUTF;
         if (threadIdx.x == 0) { A.status[p] = OTG_STATUS_MAXITER; A.niter[p] = A.max_iter - 1; A.err[p] = -1.0; }
       }
       break;
     }
-    mt_col_pass<T>(A, nact, gwarp, nwarps, lane);
+    mt_col_pass<T, LOGF>(A, nact, gwarp, nwarps, lane);
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     // the first v comes from u alone (v0 is not an iterate): relaxed from the second on
-    mt_col_merge<T>(A, nact, vcur, vnxt, prev_check, ii < A.max_iter, gtid, nthreads, A.relax && ii > 0);
+    mt_col_merge<T, LOGF>(A, nact, vcur, vnxt, prev_check, ii < A.max_iter, gtid, nthreads, A.relax && ii > 0);
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     if (decide) {
+      // per-problem errors: the problem's column slots summed in a fixed order
+      bool joint_conv = false;
+      if (A.joint && prev_check) {
+        const int jc = mt_joint_decision<T>(A, nact);
+        if (jc < 0) return;
+        joint_conv = jc == 1;
+      }
       // decide per problem, write out the leaving ones (state of iteration ii-1)
       for (int k = blockIdx.x; k < nact; k += gridDim.x) {
         const int p = __ldcg(A.active + k);
-        const double e = prev_check ? sqrt(__ldcg(A.err2 + p)) : -1.0;
-        const bool conv = prev_check && e < A.stop_thr;
+        double e = -1.0;
+        if (prev_check) e = sqrt(A.joint ? __ldcg(A.err2 + p) : block_sum_slots(A.e2col + A.c_off[p], A.cols[p]));
+        const bool conv = prev_check && (A.joint ? joint_conv : e < A.stop_thr);
         const bool leave = conv || ii == A.max_iter;
         if (leave) {
-          for (int i = threadIdx.x; i < A.rows[p]; i += blockDim.x) A.out_u[A.r_off[p] + i] = __ldcg(A.u + A.r_off[p] + i) * LN2;
-          for (int j = threadIdx.x; j < A.cols[p]; j += blockDim.x) A.out_v[A.c_off[p] + j] = __ldcg(vcur + A.c_off[p] + j) * LN2;
+          for (int i = threadIdx.x; i < A.rows[p]; i += blockDim.x) A.out_u[A.r_off[p] + i] = __ldcg(A.u + A.r_off[p] + i) * OUTF;
+          for (int j = threadIdx.x; j < A.cols[p]; j += blockDim.x) A.out_v[A.c_off[p] + j] = __ldcg(vcur + A.c_off[p] + j) * OUTF;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -470,7 +529,6 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
             A.err[p] = e;
           }
           leaving[p] = leave ? 1 : 0;
-          A.err2[p] = 0.0;
         }
       }
       if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
@@ -491,7 +549,7 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
     }
     { T* t = vcur; vcur = vnxt; vnxt = t; }
     const int nact2 = ld_acquire_i(A.ctl);
-    mt_row_pass<T>(A, nact2, vcur, gwarp, nwarps, lane);
+    mt_row_pass<T, LOGF>(A, nact2, vcur, gwarp, nwarps, lane);
     if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
     prev_check = (ii % A.period == 0);
   }
@@ -814,7 +872,7 @@ TailCfg tail_config() {
   return tc;
 }
 
-template <typename T>
+template <typename T, bool LOGF>
 int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   MultiArgs<T> A{};
   A.M = static_cast<const T*>(q->M); A.m_off = q->m_off; A.rows = q->rows; A.cols = q->cols; A.ldm = q->ldm;
@@ -825,7 +883,8 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   A.out_u = static_cast<T*>(q->out_u); A.out_v = static_cast<T*>(q->out_v);
   A.status = q->status; A.niter = q->niter; A.err = q->err;
   A.timeout_ns = q->timeout_ms > 0 ? (uint64_t)q->timeout_ms * 1000000ull : 4000000000ull;
-  A.relax = q->omega != 0.0 && q->omega != 1.0;
+  A.relax = LOGF && q->omega != 0.0 && q->omega != 1.0;
+  A.joint = q->joint_stop != 0;
   A.omega = (T)q->omega;
   A.period = q->check_period > 0 ? q->check_period : 10;
   A.upw = q->units_per_warp > 0 ? std::min(q->units_per_warp, 1024) : 8;
@@ -838,6 +897,8 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   // kernel supplies and one cluster per problem does not: no default handoff
   const int def_tail = sizeof(T) == 8 ? 0 : 3 * tc.max;
   A.tail_max = q->tail_problems < 0 || tc.cl == 0 ? 0 : (q->tail_problems > 0 ? q->tail_problems : def_tail);
+  // the whole-batch stop keeps every problem to the end; the tail kernel runs the log form only
+  if (A.joint || !LOGF) A.tail_max = 0;
   // carve the workspace
   char* w = static_cast<char*>(q->workspace);
   size_t off = 0;
@@ -847,6 +908,7 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   A.v1 = reinterpret_cast<T*>(take(sizeof(T) * q->total_cols));
   A.pcol = reinterpret_cast<MPair<T>*>(take(sizeof(MPair<T>) * q->total_partials));
   A.err2 = reinterpret_cast<double*>(take(sizeof(double) * q->nprob));
+  A.e2col = reinterpret_cast<double*>(take(sizeof(double) * q->total_cols));
   A.active = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * q->nprob));
   A.ucol_pre = reinterpret_cast<int64_t*>(take(sizeof(int64_t) * (q->nprob + 1)));
   A.urow_pre = reinterpret_cast<int64_t*>(take(sizeof(int64_t) * (q->nprob + 1)));
@@ -862,12 +924,12 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, multi_sinkhorn_kernel<T>, MT_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, multi_sinkhorn_kernel<T, LOGF>, MT_THREADS, 0);
   int grid = sms * std::min(per, MtBlocks<T>::value);
   if (q->grid > 0 && q->grid < grid) grid = q->grid;
   if (grid < 1) return OTG_ERR_UNSUPPORTED;
   void* args[] = {&A, &leaving};
-  cudaError_t e = cudaLaunchCooperativeKernel((const void*)multi_sinkhorn_kernel<T>, dim3(grid), dim3(MT_THREADS),
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)multi_sinkhorn_kernel<T, LOGF>, dim3(grid), dim3(MT_THREADS),
                                               args, 0, st);
   if (e != cudaSuccess) return OTG_ERR_CUDA;
   if (A.tail_max > 0) {
@@ -893,7 +955,7 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
 size_t multi_ws(int dtype, int64_t nprob, int64_t rows, int64_t cols, int64_t partials) {
   const size_t es = dtype == OTG_F64 ? 8 : 4;
   auto r = [](size_t b) { return (b + 255) / 256 * 256; };
-  return r(es * rows) + 2 * r(es * cols) + r(2 * es * partials) + r(8 * nprob) + r(4 * nprob) +
+  return r(es * rows) + 2 * r(es * cols) + r(2 * es * partials) + r(8 * nprob) + r(8 * cols) + r(4 * nprob) +
          3 * r(8 * (nprob + 1)) + 3 * r(4 * nprob) + r(64);
 }
 }  // namespace
@@ -903,6 +965,11 @@ extern "C" {
 size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, int64_t total_cols,
                                  int64_t total_partials) {
   return multi_ws(dtype, nprob, total_rows, total_cols, total_partials);
+}
+
+size_t otg_multi_anderson_bytes(int dtype, int32_t nprob, int64_t total_cols, int32_t depth) {
+  (void)dtype; (void)nprob; (void)total_cols; (void)depth;
+  return 0;
 }
 
 int otg_multi_tail_config(int dtype, int32_t* cluster_ctas, int32_t* max_clusters, int64_t* tile_bytes,
@@ -925,8 +992,11 @@ int otg_sinkhorn_multi(const OtgMultiProblem* q, cudaStream_t stream) {
       !q->err || !q->workspace)
     return OTG_ERR_ARG;
   if (q->nprob < 1 || q->max_iter < 1) return OTG_ERR_ARG;
-  if (q->dtype == OTG_F64) return launch_multi<double>(q, stream);
-  if (q->dtype == OTG_F32) return launch_multi<float>(q, stream);
+  if (q->anderson_depth < 0 || q->anderson_depth > OTG_ANDERSON_MAX_DEPTH) return OTG_ERR_ARG;
+  if (q->anderson_depth > 0) return OTG_ERR_UNSUPPORTED;
+  const bool logf = q->scaling == 0;
+  if (q->dtype == OTG_F64) return logf ? launch_multi<double, true>(q, stream) : launch_multi<double, false>(q, stream);
+  if (q->dtype == OTG_F32) return logf ? launch_multi<float, true>(q, stream) : launch_multi<float, false>(q, stream);
   return OTG_ERR_DTYPE;
 }
 

@@ -54,7 +54,7 @@ struct OnlinePass {
   float* pot_out2;     // new potential (base 2)
   const float* other_norm2;  // resident side: log2(e)|x|^2/reg, to form the next pass's h
   float* h_out;        // h for the next pass: pot_new2 - other_norm2 (-inf beyond n_rows)
-  double* err;         // L1 accumulation (check passes) or null
+  double* err;         // check passes: per-row |marginal violation| slots, else null
   int* abort_flag;
   uint64_t timeout_ns;
   // column split: CTA (b, s) streams tiles [s T / S, (s + 1) T / S) and, with
@@ -252,10 +252,7 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
         const float pnew = P.logw2[row] - L;
         P.pot_out2[row] = pnew;
         P.h_out[row] = pnew - P.other_norm2[row];
-        if (P.err) {
-          const double rs = (double)ex2(P.pot2[row] + L) - (double)P.w[row];
-          atomicAdd(P.err, fabs(rs));
-        }
+        if (P.err) P.err[row] = fabs((double)ex2(P.pot2[row] + L) - (double)P.w[row]);
       } else {
         P.h_out[row] = -INFINITY;  // padding rows of the resident side
       }
@@ -270,11 +267,10 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
 }
 
 // Column-split passes: merge the S partial (max, sum) pairs of each row and
-// apply the potential update of the pass's epilogue; the check error is
-// reduced per block (one atomic per block).
+// apply the potential update of the pass's epilogue (check passes: the row's
+// error into its slot).
 __global__ void __launch_bounds__(256) online_finalize_kernel(OnlinePass P) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
-  double e = 0.0;
   if (row < P.rows_pad) {
     if (row < P.n_rows) {
       float mx = -INFINITY, sm = 0.f;
@@ -282,25 +278,15 @@ __global__ void __launch_bounds__(256) online_finalize_kernel(OnlinePass P) {
         lse_merge(mx, sm, P.part[((size_t)c * 2) * P.rows_pad + row], P.part[((size_t)c * 2 + 1) * P.rows_pad + row]);
       const float L = lse_value(mx, sm) + P.rterm[row];
       const float pnew = P.logw2[row] - L;
-      if (P.err) e = fabs((double)ex2(P.pot2[row] + L) - (double)P.w[row]);
+      if (P.err) P.err[row] = fabs((double)ex2(P.pot2[row] + L) - (double)P.w[row]);
       P.pot_out2[row] = pnew;
       P.h_out[row] = pnew - P.other_norm2[row];
     } else {
       P.h_out[row] = -INFINITY;
     }
   }
-  if (P.err) {
-    __shared__ double red[8];
-    e = warp_sum(e);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0;
-      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
-      atomicAdd(P.err, t);
-    }
-  }
 }
+
 
 __global__ void prep_points_kernel(const float* __restrict__ X, int64_t n, int d, float scale, __half* hi, __half* lo,
                                    int64_t ld, float k2, float* norm2) {
@@ -410,6 +396,7 @@ size_t otg_online_workspace_bytes(int64_t n, int64_t m, int32_t d) {
   b += 2 * a16(2 * np * dp) + 2 * a16(2 * mp * dp);          // half planes
   b += 5 * a16(4 * np) + 4 * a16(4 * mp);                    // norms, log2 w, potentials, h
   b += a16(8 * 64);                                          // err slots, flag
+  b += a16(8 * (size_t)std::max(np, mp));                    // per-row errors of a check pass
   b += a16(4 * np) + a16(4 * mp);                            // negated norms
   b += a16(4 * 2 * (size_t)OL_MAX_SPLIT * (size_t)std::max(np, mp));  // column-split partials
   return b;
@@ -440,6 +427,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
   float* hx = reinterpret_cast<float*>(take(4 * np));
   double* errs = reinterpret_cast<double*>(take(8 * 64));
   int* flag = reinterpret_cast<int*>(errs + 62);
+  double* erow = reinterpret_cast<double*>(take(8 * (size_t)std::max(np, mp)));
   const float k2 = (float)(OTG_LOG2E / p->reg);
   const float sx = p->scale_x, sy = p->scale_y;
   // planes are zero beyond the data; norms, weights and potentials set below
@@ -475,12 +463,15 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
   const int split_g = choose_split((int)(mp / OL_M), (int)(np / OL_N), sms);
   // one pass: the pass kernel over (row blocks x column split), then, when
   // split, the merge of the partials
+  // (check passes: the per-row errors go to erow, their sum to `eslot`)
   auto pass = [&](OnlinePass& P, const CUtensorMap& ah, const CUtensorMap& al, const CUtensorMap& bh,
-                  const CUtensorMap& bl, int64_t rows_pad, int split) {
+                  const CUtensorMap& bl, int64_t rows_pad, int split, double* eslot_of_pass) {
     P.split = split; P.rows_pad = (int)rows_pad; P.part = part;
     online_pass_kernel<<<dim3((unsigned)(rows_pad / OL_M), (unsigned)split), OL_THREADS, OL_SMEM, st>>>(ah, al, bh,
                                                                                                        bl, P);
     if (split > 1) online_finalize_kernel<<<(unsigned)((rows_pad + 255) / 256), 256, 0, st>>>(P);
+    // the L1 error: the row slots summed in a fixed order (the same value in every run)
+    if (P.err) slot_sum_kernel<1024><<<1, 1024, 0, st>>>(P.err, P.n_rows, eslot_of_pass);
   };
   neg_kernel<<<256, 256, 0, st>>>(xn2, n, nx);
   neg_kernel<<<256, 256, 0, st>>>(yn2, m, ny);
@@ -490,13 +481,12 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
   for (int it = 0; it < p->max_iter; ++it) {
     const bool check = (it > 0) && (it % 10 == 0);  // error of iteration it-1 ((it-1)+1) % 10 == 0
     double* eslot = errs + (nchk % 60);
-    if (check && cudaMemsetAsync(eslot, 0, 8, st) != cudaSuccess) return OTG_ERR_CUDA;
     // f pass: rows = X, streamed = Y (h = g2 - |y|^2 k2)
     OnlinePass A{};
     A.n_rows = (int)n; A.col_tiles = (int)(mp / OL_N); A.k_tiles = dp / OL_K; A.alpha = alpha;
     A.h = hy; A.rterm = nx; A.logw2 = la2; A.pot2 = f2[cur]; A.w = p->a; A.pot_out2 = f2[cur ^ 1];
-    A.other_norm2 = xn2; A.h_out = hx; A.err = check ? eslot : nullptr; A.abort_flag = flag; A.timeout_ns = tmo;
-    pass(A, mxh, mxl, myh, myl, np, split_f);
+    A.other_norm2 = xn2; A.h_out = hx; A.err = check ? erow : nullptr; A.abort_flag = flag; A.timeout_ns = tmo;
+    pass(A, mxh, mxl, myh, myl, np, split_f, eslot);
     if (check) {
       double e = 0;
       if (cudaMemcpyAsync(&e, eslot, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return OTG_ERR_CUDA;
@@ -511,18 +501,17 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     B.n_rows = (int)m; B.col_tiles = (int)(np / OL_N); B.k_tiles = dp / OL_K; B.alpha = alpha;
     B.h = hx; B.rterm = ny; B.logw2 = lb2; B.pot2 = g2; B.w = p->b; B.pot_out2 = g2;
     B.other_norm2 = yn2; B.h_out = hy; B.err = nullptr; B.abort_flag = flag; B.timeout_ns = tmo;
-    pass(B, myh, myl, mxh, mxl, mp, split_g);
+    pass(B, myh, myl, mxh, mxl, mp, split_g, nullptr);
     if (cudaGetLastError() != cudaSuccess) return OTG_ERR_CUDA;
   }
   // a last check at max_iter when (max_iter) % 10 == 0 is done by the next f pass
   if (status == OTG_STATUS_MAXITER && p->max_iter > 0 && p->max_iter % 10 == 0) {
     double* eslot = errs + (nchk % 60);
-    cudaMemsetAsync(eslot, 0, 8, st);
     OnlinePass A{};
     A.n_rows = (int)n; A.col_tiles = (int)(mp / OL_N); A.k_tiles = dp / OL_K; A.alpha = alpha;
     A.h = hy; A.rterm = nx; A.logw2 = la2; A.pot2 = f2[cur]; A.w = p->a; A.pot_out2 = f2[cur ^ 1];
-    A.other_norm2 = xn2; A.h_out = hx; A.err = eslot; A.abort_flag = flag; A.timeout_ns = tmo;
-    pass(A, mxh, mxl, myh, myl, np, split_f);
+    A.other_norm2 = xn2; A.h_out = hx; A.err = erow; A.abort_flag = flag; A.timeout_ns = tmo;
+    pass(A, mxh, mxl, myh, myl, np, split_f, eslot);
     double e = 0;
     cudaMemcpyAsync(&e, eslot, 8, cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);

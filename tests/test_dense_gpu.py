@@ -191,3 +191,26 @@ def test_precomputed_gibbs_kernel_is_bit_identical(cuda, dtype, shape):
     np.testing.assert_array_equal(r0.errs, r1.errs)
     np.testing.assert_array_equal(r0.u.cpu().numpy(), r1.u.cpu().numpy())
     np.testing.assert_array_equal(r0.v.cpu().numpy(), r1.v.cpu().numpy())
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("method", ["sinkhorn", "sinkhorn_log"])
+def test_error_history_is_reproducible(cuda, dtype, method):
+    """The squared marginal error of a check is summed over fixed slots in a
+    fixed order (which CTA merges a slab varies from run to run, the order
+    of the sum does not): ten solves give bit-identical error histories,
+    stop indices and potentials."""
+    from pot_gb300 import bregman, _lib
+    n, m = 700, 3000
+    rng = np.random.default_rng(11)
+    M = oracle.sqeuclidean(rng.normal(size=(n, 2)), rng.normal(size=(m, 2)) + 1.0)
+    M = torch.tensor(M / M.max(), dtype=dtype, device=cuda)
+    a = torch.tensor(rng.dirichlet(np.ones(n)), dtype=dtype, device=cuda)
+    b = torch.tensor(rng.dirichlet(np.ones(m)), dtype=dtype, device=cuda)
+    code = _lib.OTG_METHOD_LOG if method == "sinkhorn_log" else _lib.OTG_METHOD_KNOPP
+    stop = 1e-9 if dtype == torch.float64 else 1e-6
+    runs = [bregman.solve_dense(M, a, b, 0.02, code, 2000, stop, gibbs=False) for _ in range(10)]
+    for r in runs[1:]:
+        assert r.niter == runs[0].niter and r.status == runs[0].status
+        np.testing.assert_array_equal(r.errs, runs[0].errs)
+        assert torch.equal(r.u, runs[0].u) and torch.equal(r.v, runs[0].v)

@@ -5,8 +5,9 @@ memory at solve time (a host whose allocator owns the device pool, or a
 latency-bound loop that must not pay cudaMalloc/cudaFree): its scratch is a
 static device array inside the library.  Both entry points are called here
 through the C ABI on the same problem; the allocation-free one is called
-twice in a row, because every call reuses the array and must not see the
-previous call's contents.  Tolerances are the float64 ones of the dense
+twice, with a call on a different problem (other shape, other form) in
+between, because every call reuses the array and must not depend on what
+the previous call left in it.  Tolerances are the float64 ones of the dense
 parity tests (potentials rtol 1e-8, error history rtol 1e-6) and an
 identical status and last iteration index.
 
@@ -80,7 +81,15 @@ def test_no_alloc_matches_allocating_entry_point(cuda, name, dtype, method, stop
     reg = float(g["reg"])
     ref_u, ref_v, ref_h, ref_i = _with_alloc(lib, M, a, b, reg, method, 2000, stop)
     rtol = 1e-8 if dtype == torch.float64 else 1e-5
-    for _ in range(2):  # two calls in a row share the static scratch
+    # another problem that leaves different contents in the shared array
+    g2 = golden("dense_31x33_reg0.5")
+    M2 = torch.tensor(g2["M"], dtype=dtype, device=cuda)
+    a2 = torch.tensor(g2["a"], dtype=dtype, device=cuda)
+    b2 = torch.tensor(g2["b"], dtype=dtype, device=cuda)
+    other = _lib.OTG_METHOD_KNOPP if method == _lib.OTG_METHOD_LOG else _lib.OTG_METHOD_LOG
+    for k in range(2):  # two checked calls share the static scratch
+        if k == 1:
+            _no_alloc(lib, M2, a2, b2, float(g2["reg"]), other, 37, 1e-12)
         u, v, h, info = _no_alloc(lib, M, a, b, reg, method, 2000, stop)
         assert list(info[:4]) == list(ref_i[:4])
         nchk = int(info[2])
