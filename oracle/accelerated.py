@@ -17,6 +17,13 @@ with the acceleration switched off, are ``sinkhorn_log`` (``:880-899``).
   with ``sum alpha = 1`` (normal equations with a Tikhonov term
   ``lam * trace / depth``).  The stop test measures the pair (mixed u, last
   v), which is what the next column pass sees.
+- ``sinkhorn_log_anderson_v``: the iteration of ``otg_sinkhorn_multi`` with
+  ``anderson_depth``: Anderson mixing of the map ``F(v) = colT(rowT(v))``
+  with ``u`` always the exact row update of the mixed ``v`` (so the stop
+  test is the plain one on a pair with an exact row marginal), history in
+  ``depth`` slots filled round-robin, the weights from the slot-ordered Gram
+  matrix by Gaussian elimination with partial pivoting, a restart with the
+  plain step when the solve fails or ``sum |alpha|`` exceeds 1e4.
 """
 import numpy as np
 
@@ -87,3 +94,78 @@ def sinkhorn_log_anderson(a, b, M, reg, depth=5, numItermax=1000, stopThr=1e-9, 
         w = np.linalg.solve(A, np.ones(k))
         u = np.stack(gs, 1) @ (w / w.sum())
     return u, v, ii, errs
+
+
+AND_LAMBDA = 1e-10
+AND_MAX_L1 = 1e4
+
+
+def _anderson_weights(G, nh, s):
+    """Mixing weights of the slot-ordered history (None: restart)."""
+    if nh < 2:
+        return None
+    tr = float(np.trace(G[:nh, :nh]))
+    if not tr > 0.0:
+        return None
+    A = G[:nh, :nh] + AND_LAMBDA * tr / nh * np.eye(nh)
+    Mx = np.concatenate([A, np.ones((nh, 1))], 1)
+    for c in range(nh):
+        piv = c + int(np.argmax(np.abs(Mx[c:, c])))
+        if not abs(Mx[piv, c]) > 0.0:
+            return None
+        Mx[[c, piv]] = Mx[[piv, c]]
+        for i in range(c + 1, nh):
+            Mx[i, c:] -= Mx[i, c] / Mx[c, c] * Mx[c, c:]
+    w = np.zeros(nh)
+    for i in range(nh - 1, -1, -1):
+        w[i] = (Mx[i, nh] - Mx[i, i + 1:nh] @ w[i + 1:nh]) / Mx[i, i]
+    w = w / w.sum()
+    l1 = float(np.abs(w).sum())
+    if not (np.isfinite(l1) and l1 < AND_MAX_L1):
+        return None
+    return w
+
+
+def sinkhorn_log_anderson_v(a, b, M, reg, depth=5, numItermax=1000, stopThr=1e-9, warm_u=None, check_period=1):
+    """Anderson-mixed log-domain Sinkhorn on v (``otg_sinkhorn_multi`` with
+    ``anderson_depth``); returns (log_u, log_v, niter, errs) with niter the
+    last loop index and (log_u, log_v) the pair that met the test."""
+    Mr, la, lb, b = _setup(a, b, M, reg)
+    m = Mr.shape[1]
+    u = np.zeros(Mr.shape[0]) if warm_u is None else _f64(warm_u).copy()
+    F = np.zeros((depth, m))
+    R = np.zeros((depth, m))
+    G = np.zeros((depth, depth))
+    cnt = 0
+    v = None
+    errs = []
+    prev_check = False
+    for ii in range(numItermax + 1):
+        L = logsumexp(Mr + u[:, None], 0)
+        if prev_check:
+            errs.append(float(np.linalg.norm(np.exp(v + L) - b)))
+            if errs[-1] < stopThr:
+                return u, v, ii - 1, errs
+        if ii == numItermax:
+            break
+        f = lb - L
+        if v is None:
+            vn = f
+        else:
+            s = cnt % depth
+            nh = min(cnt + 1, depth)
+            F[s] = f
+            R[s] = f - v
+            for q in range(nh):
+                G[s, q] = G[q, s] = float(R[s] @ R[q])
+            w = _anderson_weights(G, nh, s)
+            if w is None:
+                vn = f
+                cnt = cnt + 1 if nh == 1 else 0
+            else:
+                vn = w @ F[:nh]
+                cnt += 1
+        v = vn
+        u = la - logsumexp(Mr + v[None, :], 1)
+        prev_check = ii % check_period == 0
+    return u, v, numItermax - 1, errs

@@ -145,13 +145,15 @@ def _tail_enabled(dtype):
 
 def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
               events=None, omega=1.0, check_period=10, schedule=None, tail_problems=0, info=None, joint=False,
-              scaling=False):
+              scaling=False, anderson=0):
     """Work-balanced persistent launch (csrc/multi.cu) in the sinkhorn_log
     order (v first, column-marginal test).  Returns (u, v, status, niter,
     err, reg).  ``joint`` stops the whole batch together on the largest
     error (ot.batch's rule); otherwise every problem stops on its own.
     ``scaling`` runs the scaling form (u, v are then scalings, not natural
-    logs).  ``omega != 1`` over-relaxes the potential updates and
+    logs).  ``anderson`` > 0 mixes the v updates over that many iterates
+    (Anderson acceleration; u stays the exact row update of the v in use).
+    ``omega != 1`` over-relaxes the potential updates and
     ``check_period`` other than 10 moves the stop tests (no reference
     counterpart for either; the stop criterion is unchanged).  ``schedule``
     (a ``tune.Schedule``) divides the work; by default the autotuner's cached
@@ -160,12 +162,12 @@ def run_multi(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=N
     ``info`` the call synchronises and reports the handoff iteration (-1:
     none)."""
     return _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u, grid, timeout_ms,
-                           events, omega, check_period, schedule, tail_problems, info, joint, scaling)
+                           events, omega, check_period, schedule, tail_problems, info, joint, scaling, anderson)
 
 
 def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, warm_u=None, grid=0, timeout_ms=0,
                     events=None, omega=1.0, check_period=10, schedule=None, tail_problems=0, info=None,
-                    joint=False, scaling=False):
+                    joint=False, scaling=False, anderson=0):
     lib = _lib.load()
     if schedule is None:
         schedule = tune.lookup(layout) or tune.DEFAULT
@@ -191,6 +193,8 @@ def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, wa
     status = torch.empty(B, dtype=torch.int32, device=dev)
     niter = torch.empty(B, dtype=torch.int32, device=dev)
     err = torch.empty(B, dtype=torch.float64, device=dev)
+    awb = lib.otg_multi_anderson_bytes(dcode, B, layout.total_c, int(anderson)) if anderson else 0
+    aws = torch.empty(max(awb, 1), dtype=torch.uint8, device=dev)
     q = _lib.OtgMultiProblem(
         dtype=dcode, nprob=B, M=M_packed.data_ptr(), m_off=layout.m_off.data_ptr(), rows=layout.rows.data_ptr(),
         cols=layout.cols.data_ptr(), ldm=layout.ldm.data_ptr(), r_off=layout.r_off.data_ptr(),
@@ -202,12 +206,13 @@ def _run_multi_once(layout, M_packed, a_packed, b_packed, reg, max_iter, tol, wa
         err=err.data_ptr(), workspace=ws.data_ptr(), workspace_bytes=wsb, timeout_ms=int(timeout_ms),
         omega=float(omega), check_period=int(check_period), units_per_warp=int(schedule.units_per_warp),
         split_cap_fill=int(schedule.cap_fill), split_cap_tail=int(schedule.cap_tail),
-        tail_problems=int(tail_problems), joint_stop=int(bool(joint)), scaling=int(bool(scaling)))
+        tail_problems=int(tail_problems), joint_stop=int(bool(joint)), scaling=int(bool(scaling)),
+        anderson_depth=int(anderson), anderson_ws=aws.data_ptr() if awb else None, anderson_ws_bytes=awb)
     if events is not None:
         events[0].record()
     _lib.check(lib.otg_sinkhorn_multi(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_multi")
-    if (not joint and not scaling and (tail_problems > 0 or (tail_problems == 0 and dt == torch.float32))
-            and _tail_enabled(dt)):
+    if (not joint and not scaling and not anderson
+            and (tail_problems > 0 or (tail_problems == 0 and dt == torch.float32)) and _tail_enabled(dt)):
         _lib.LAUNCHES[0] += 1  # the tail kernel launched behind the batch kernel
     if events is not None:
         events[1].record()

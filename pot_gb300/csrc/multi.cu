@@ -15,6 +15,17 @@
 // summed per problem in a fixed order, so a problem's error, and with it
 // its stop index, is the same in every run.
 //
+// Anderson mixing (no reference counterpart; the warm-start refinement).
+// The map F(v) = colT(rowT(v)) (a row update followed by a column update)
+// has the Sinkhorn potentials as fixed points.  With and_depth = D > 0 the v
+// of the next row pass is  sum_k alpha_k F(v_k)  over the last D iterates,
+// alpha minimising |sum_k alpha_k (F(v_k) - v_k)|_2 with sum alpha = 1
+// (normal equations of the residual Gram matrix with a Tikhonov term
+// 1e-10 trace / D; a non-finite or wildly extrapolating solution restarts
+// the history with the plain step).  u is always the exact row update of the
+// v in use, so the stop test measures exactly what it measures for plain
+// sinkhorn_log: the column marginal of (u, v) with u = rowT(v).
+//
 // One persistent cooperative launch.  Each iteration:
 //   column pass : units (problem, row chunk, slab of 32*VW columns) over all
 //                 active problems -> partial (max, sum) per column  | barrier
@@ -82,6 +93,15 @@ struct MultiArgs {
   double* err2;             // per problem: squared error of the last check (joint stop)
   double* e2col;            // per column: squared marginal error (check passes), packed like b
   bool joint;               // whole-batch stop on the largest error
+  // Anderson mixing of the v update (depth 0: off): history slots of F(v)
+  // and of the residual F(v) - v, [depth][total_cols] each (slot-major,
+  // packed like b), residual Gram matrices [nprob][depth][depth] and the
+  // number of iterates taken so far per problem
+  int and_depth;
+  int64_t total_cols;
+  T* and_F; T* and_R;
+  double* and_G;
+  int32_t* and_cnt;
   int32_t* active;          // active problem ids [nprob]
   int64_t* ucol_pre;        // prefix of column-pass units over the active list [nprob+1]
   int64_t* urow_pre;        // prefix of row-pass units
@@ -422,6 +442,107 @@ __device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leavi
   __syncthreads();
 }
 
+// Anderson step (one CTA per active problem): insert F(v_k) (in vnxt) and
+// the residual F(v_k) - v_k (vcur) into the history, update the residual
+// Gram matrix, solve for the mixing weights and write the mixed v into vnxt.
+// Kept out of line, like the joint decision: it must not weigh on the
+// registers of the passes.
+constexpr double AND_LAMBDA = 1e-10;   // Tikhonov term, relative to trace / D
+constexpr double AND_MAX_L1 = 1e4;     // larger sum |alpha|: restart with the plain step
+
+template <typename T>
+__device__ __noinline__ void mt_anderson(const MultiArgs<T>& A, int nact, const T* vcur, T* vnxt) {
+  constexpr int MD = OTG_ANDERSON_MAX_DEPTH;
+  __shared__ double s_dot[MD];
+  __shared__ double s_alpha[MD];
+  __shared__ int s_keep;
+  const int D = A.and_depth;
+  for (int k = blockIdx.x; k < nact; k += gridDim.x) {
+    const int p = __ldcg(A.active + k);
+    const int m = A.cols[p];
+    const int64_t co = A.c_off[p];
+    const int cnt = __ldcg(A.and_cnt + p);
+    const int s = cnt % D;                       // slot of the new iterate
+    const int nh = cnt + 1 < D ? cnt + 1 : D;    // slots in use after the insert
+    // insert, and this thread's share of the dots <r_new, R_q>
+    double acc[MD];
+#pragma unroll
+    for (int q = 0; q < MD; ++q) acc[q] = 0.0;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+      const T f = __ldcg(vnxt + co + j);
+      const T r = f - __ldcg(vcur + co + j);
+      A.and_F[(int64_t)s * A.total_cols + co + j] = f;
+      A.and_R[(int64_t)s * A.total_cols + co + j] = r;
+#pragma unroll
+      for (int q = 0; q < MD; ++q) {
+        if (q < nh) {
+          const T rq = q == s ? r : __ldcg(A.and_R + (int64_t)q * A.total_cols + co + j);
+          acc[q] += (double)r * (double)rq;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < MD; ++q) {
+      if (q < nh) {
+        const double d = block_sum_fixed(acc[q]);
+        if (threadIdx.x == 0) s_dot[q] = d;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double* G = A.and_G + (int64_t)p * D * D;
+      for (int q = 0; q < nh; ++q) { G[s * D + q] = s_dot[q]; G[q * D + s] = s_dot[q]; }
+      // (G + lambda I) w = 1 by Gaussian elimination with partial pivoting
+      double Mx[MD][MD + 1];
+      double tr = 0.0;
+      for (int i = 0; i < nh; ++i) tr += G[i * D + i];
+      const double lam = AND_LAMBDA * tr / nh;
+      for (int i = 0; i < nh; ++i) {
+        for (int j = 0; j < nh; ++j) Mx[i][j] = G[i * D + j] + (i == j ? lam : 0.0);
+        Mx[i][nh] = 1.0;
+      }
+      bool ok = nh > 1 && tr > 0.0;
+      for (int c = 0; ok && c < nh; ++c) {
+        int piv = c;
+        for (int i = c + 1; i < nh; ++i) if (fabs(Mx[i][c]) > fabs(Mx[piv][c])) piv = i;
+        if (!(fabs(Mx[piv][c]) > 0.0)) { ok = false; break; }
+        if (piv != c) for (int j = c; j <= nh; ++j) { const double t = Mx[c][j]; Mx[c][j] = Mx[piv][j]; Mx[piv][j] = t; }
+        for (int i = c + 1; i < nh; ++i) {
+          const double f = Mx[i][c] / Mx[c][c];
+          for (int j = c; j <= nh; ++j) Mx[i][j] -= f * Mx[c][j];
+        }
+      }
+      double w[MD];
+      double sw = 0.0, l1 = 0.0;
+      for (int i = nh - 1; ok && i >= 0; --i) {
+        double t = Mx[i][nh];
+        for (int j = i + 1; j < nh; ++j) t -= Mx[i][j] * w[j];
+        w[i] = t / Mx[i][i];
+        sw += w[i];
+      }
+      if (ok) {
+        for (int i = 0; i < nh; ++i) { w[i] /= sw; l1 += fabs(w[i]); }
+        ok = isfinite(l1) && l1 < AND_MAX_L1;
+      }
+      for (int i = 0; i < MD; ++i) s_alpha[i] = ok && i < nh ? w[i] : (i == s ? 1.0 : 0.0);
+      // a first iterate, or a failed solve: the plain step; after a failure
+      // the history restarts from this iterate alone
+      s_keep = ok;
+      A.and_cnt[p] = ok || nh == 1 ? cnt + 1 : 0;
+    }
+    __syncthreads();
+    if (s_keep) {
+      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        double vm = 0.0;
+        for (int q = 0; q < nh; ++q) vm += s_alpha[q] * (double)__ldcg(A.and_F + (int64_t)q * A.total_cols + co + j);
+        vnxt[co + j] = (T)vm;
+      }
+    }
+    // after a restart vnxt keeps F(v_k): the plain step
+    __syncthreads();
+  }
+}
+
 // Whole-batch stop decision (joint mode): every problem's error into
 // err2[p] (its column slots summed in a fixed order), then the largest over
 // the batch (a max: the same in any order).  Returns 1 when the batch stops,
@@ -471,7 +592,11 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
       else A.u[ri] = A.warm_u ? exp(A.warm_u[ri]) : T(1);
     }
     for (int j = threadIdx.x; j < m; j += blockDim.x) A.v0[A.c_off[p] + j] = LOGF ? T(0) : T(1);
-    if (threadIdx.x == 0) { leaving[p] = 0; A.err2[p] = 0.0; }
+    if (threadIdx.x == 0) {
+      leaving[p] = 0;
+      A.err2[p] = 0.0;
+      if (A.and_depth > 0) A.and_cnt[p] = 0;
+    }
   }
   if (blockIdx.x == 0) {
     for (int k = threadIdx.x; k < A.nprob; k += blockDim.x) A.active[k] = k;
@@ -545,6 +670,14 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
           A.ctl[5] = 1;
         }
         break;
+      }
+    }
+    if constexpr (LOGF) {
+      // Anderson mixing of the new v (from the second iteration on: the first
+      // v comes from u alone and is not an iterate of the map)
+      if (A.and_depth > 0 && ii >= 1) {
+        mt_anderson<T>(A, ld_acquire_i(A.ctl), vcur, vnxt);
+        if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
       }
     }
     { T* t = vcur; vcur = vnxt; vnxt = t; }
@@ -872,6 +1005,12 @@ TailCfg tail_config() {
   return tc;
 }
 
+// Device bytes of the Anderson history: F and residual slots, Gram matrices, counts.
+size_t anderson_ws_bytes(size_t es, int64_t nprob, int64_t cols, int depth) {
+  auto r = [](size_t b) { return (b + 255) / 256 * 256; };
+  return 2 * r(es * (size_t)depth * (size_t)cols) + r(8 * (size_t)nprob * depth * depth) + r(4 * (size_t)nprob);
+}
+
 template <typename T, bool LOGF>
 int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   MultiArgs<T> A{};
@@ -883,7 +1022,9 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   A.out_u = static_cast<T*>(q->out_u); A.out_v = static_cast<T*>(q->out_v);
   A.status = q->status; A.niter = q->niter; A.err = q->err;
   A.timeout_ns = q->timeout_ms > 0 ? (uint64_t)q->timeout_ms * 1000000ull : 4000000000ull;
-  A.relax = LOGF && q->omega != 0.0 && q->omega != 1.0;
+  A.and_depth = LOGF ? q->anderson_depth : 0;
+  A.total_cols = q->total_cols;
+  A.relax = LOGF && A.and_depth == 0 && q->omega != 0.0 && q->omega != 1.0;
   A.joint = q->joint_stop != 0;
   A.omega = (T)q->omega;
   A.period = q->check_period > 0 ? q->check_period : 10;
@@ -897,8 +1038,9 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   // kernel supplies and one cluster per problem does not: no default handoff
   const int def_tail = sizeof(T) == 8 ? 0 : 3 * tc.max;
   A.tail_max = q->tail_problems < 0 || tc.cl == 0 ? 0 : (q->tail_problems > 0 ? q->tail_problems : def_tail);
-  // the whole-batch stop keeps every problem to the end; the tail kernel runs the log form only
-  if (A.joint || !LOGF) A.tail_max = 0;
+  // the whole-batch stop keeps every problem to the end; the tail kernel runs
+  // the plain or over-relaxed log form only
+  if (A.joint || !LOGF || A.and_depth > 0) A.tail_max = 0;
   // carve the workspace
   char* w = static_cast<char*>(q->workspace);
   size_t off = 0;
@@ -920,6 +1062,17 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   A.ctl = reinterpret_cast<int32_t*>(ctlp);
   A.bar = reinterpret_cast<unsigned*>(ctlp + 32);
   if (off > q->workspace_bytes) return OTG_ERR_WORKSPACE;
+  if (A.and_depth > 0) {
+    if (!q->anderson_ws || q->anderson_ws_bytes < anderson_ws_bytes(sizeof(T), q->nprob, q->total_cols, A.and_depth))
+      return OTG_ERR_WORKSPACE;
+    char* aw = static_cast<char*>(q->anderson_ws);
+    size_t ao = 0;
+    auto atake = [&](size_t bytes) { char* p = aw + ao; ao += (bytes + 255) / 256 * 256; return p; };
+    A.and_F = reinterpret_cast<T*>(atake(sizeof(T) * (size_t)A.and_depth * (size_t)q->total_cols));
+    A.and_R = reinterpret_cast<T*>(atake(sizeof(T) * (size_t)A.and_depth * (size_t)q->total_cols));
+    A.and_G = reinterpret_cast<double*>(atake(sizeof(double) * (size_t)q->nprob * A.and_depth * A.and_depth));
+    A.and_cnt = reinterpret_cast<int32_t*>(atake(sizeof(int32_t) * (size_t)q->nprob));
+  }
   if (cudaMemsetAsync(ctlp, 0, 64, st) != cudaSuccess) return OTG_ERR_CUDA;
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
@@ -968,8 +1121,8 @@ size_t otg_multi_workspace_bytes(int dtype, int32_t nprob, int64_t total_rows, i
 }
 
 size_t otg_multi_anderson_bytes(int dtype, int32_t nprob, int64_t total_cols, int32_t depth) {
-  (void)dtype; (void)nprob; (void)total_cols; (void)depth;
-  return 0;
+  if (depth <= 0) return 0;
+  return anderson_ws_bytes(dtype == OTG_F64 ? 8 : 4, nprob, total_cols, depth);
 }
 
 int otg_multi_tail_config(int dtype, int32_t* cluster_ctas, int32_t* max_clusters, int64_t* tile_bytes,
@@ -993,7 +1146,7 @@ int otg_sinkhorn_multi(const OtgMultiProblem* q, cudaStream_t stream) {
     return OTG_ERR_ARG;
   if (q->nprob < 1 || q->max_iter < 1) return OTG_ERR_ARG;
   if (q->anderson_depth < 0 || q->anderson_depth > OTG_ANDERSON_MAX_DEPTH) return OTG_ERR_ARG;
-  if (q->anderson_depth > 0) return OTG_ERR_UNSUPPORTED;
+  if (q->anderson_depth > 0 && q->scaling != 0) return OTG_ERR_UNSUPPORTED;
   const bool logf = q->scaling == 0;
   if (q->dtype == OTG_F64) return logf ? launch_multi<double, true>(q, stream) : launch_multi<double, false>(q, stream);
   if (q->dtype == OTG_F32) return logf ? launch_multi<float, true>(q, stream) : launch_multi<float, false>(q, stream);

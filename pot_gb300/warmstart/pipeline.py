@@ -59,16 +59,17 @@ class PairSolver:
                   else b.reshape(-1).float().contiguous())
 
     def solve(self, reg_rel, tol, max_iter=100000, warm_u=None, engine="multi", events=None, omega=1.0,
-              check_period=10):
+              check_period=10, anderson=0):
         """Log-domain solve of every pair (sinkhorn_log order and stop test);
-        with `warm_u` the first half-step (the c-transform) derives v from it."""
+        with `warm_u` the first half-step (the c-transform) derives v from it.
+        `anderson` > 0 mixes the v updates over that many iterates."""
         reg = self.maxc.double() * reg_rel
         if warm_u is not None:
             warm_u = warm_u.reshape(-1).contiguous()
         if engine == "multi":
             u, v, status, niter, err, _ = pb.run_multi(self.layout, self.M, self.a, self.b, reg, max_iter, tol,
                                                        warm_u=warm_u, events=events, omega=omega,
-                                                       check_period=check_period)
+                                                       check_period=check_period, anderson=anderson)
         else:
             wv = None if warm_u is None else torch.zeros(self.P * self.m, dtype=torch.float32, device=self.M.device)
             u, v, status, niter, err, _ = pb.run_batched(self.layout, self.M, self.a, self.b, reg,
@@ -300,25 +301,65 @@ def train_default(device=None, n_train=8192, steps=4000, verbose=True, out=None)
 
 
 REFINE_OMEGA = 1.4  # over-relaxation of the warm-started solve (measured: 1.8 and above diverge on some pairs)
+REFINE_ANDERSON = 5  # Anderson window of the warm-started solve (0: over-relaxation by REFINE_OMEGA instead)
 
 
-def solve_cloud_pairs(X, Y, reg_rel=0.02, tol=1e-6, max_iter=100000, warm=True, net=None, omega=REFINE_OMEGA):
+class CloudPairsResult(tuple):
+    """Result of `solve_cloud_pairs`: (log_u, log_v, niter, status, err,
+    fallback), in the caller's array type.  status 0 means the pair's
+    column-marginal error met `tol`; `fallback` flags the pairs that were
+    re-solved from zero with the plain iteration because their warm solve
+    did not meet it."""
+
+    def __new__(cls, *items):
+        return super().__new__(cls, items)
+
+    log_u = property(lambda self: self[0])
+    log_v = property(lambda self: self[1])
+    niter = property(lambda self: self[2])
+    status = property(lambda self: self[3])
+    err = property(lambda self: self[4])
+    fallback = property(lambda self: self[5])
+
+
+def solve_cloud_pairs(X, Y, reg_rel=0.02, tol=1e-6, max_iter=100000, warm=True, net=None, omega=REFINE_OMEGA,
+                      anderson=REFINE_ANDERSON, check_period=10, warm_max_iter=None):
     """Public entry point for batches of equal-size cloud pairs: X (P, n, d),
-    Y (P, m, d) (numpy or torch); returns (log_u, log_v, niter) in the
-    caller's array type.  reg = reg_rel x each pair's max squared distance;
-    sinkhorn_log order and stop test per pair.  With `warm` the source
-    potential starts from the learned warm start and the solve over-relaxes
-    its updates by `omega` (the stop test is unchanged: every pair ends with
-    its column-marginal error below `tol`); without it the solve is the plain
+    Y (P, m, d) (numpy or torch); returns a `CloudPairsResult` (log_u, log_v,
+    niter, status, err, fallback) in the caller's array type.  reg =
+    reg_rel x each pair's max squared distance; sinkhorn_log order and stop
+    test per pair (every `check_period` iterations).
+
+    With `warm` the source potential starts from the learned warm start and
+    the solve is accelerated: Anderson mixing over `anderson` iterates, or,
+    with anderson=0, updates over-relaxed by `omega`.  The stop test is the
+    plain one: a pair ends only when the column-marginal error of its (u, v)
+    pair, u the exact row update of v, is below `tol`.  Zero start is the
+    fallback: any pair whose warm solve ends without meeting the test (after
+    `warm_max_iter` iterations, default `max_iter`) is solved again from zero
+    with the plain iteration.  Without `warm` every pair runs the plain
     zero-started iteration."""
     from .._arrays import Boundary
     bd = Boundary(X, Y)
     Xd = bd.to_dev(X, torch.float32).contiguous()
     Yd = bd.to_dev(Y, torch.float32).contiguous()
     ps = PairSolver(Xd, Yd)
-    wu = None
     if warm:
         net = net or default_net(Xd.device)
         wu = warm_potential(net, Xd, Yd, ps, reg_rel)
-    u, v, status, niter, err = ps.solve(reg_rel, tol, max_iter, warm_u=wu, omega=omega if warm else 1.0)
-    return bd.out(u), bd.out(v), bd.out(niter)
+        u, v, status, niter, err = ps.solve(reg_rel, tol, warm_max_iter or max_iter, warm_u=wu,
+                                            omega=1.0 if anderson else omega, check_period=check_period,
+                                            anderson=anderson)
+    else:
+        u, v, status, niter, err = ps.solve(reg_rel, tol, max_iter, check_period=check_period)
+    fallback = torch.zeros(ps.P, dtype=torch.bool, device=Xd.device)
+    if warm:
+        bad = torch.nonzero(status != 0).flatten()
+        if bad.numel():
+            # zero start, plain iteration, for the pairs the warm solve left unconverged
+            idx = bad.to(Xd.device)
+            sub = PairSolver(Xd[idx].contiguous(), Yd[idx].contiguous())
+            u2, v2, s2, n2, e2 = sub.solve(reg_rel, tol, max_iter, check_period=check_period)
+            u[idx], v[idx], status[idx], niter[idx], err[idx] = u2, v2, s2, n2, e2
+            fallback[idx] = True
+    return CloudPairsResult(bd.out(u), bd.out(v), bd.out(niter), bd.out(status), bd.out(err), bd.out(fallback))

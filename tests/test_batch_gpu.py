@@ -423,3 +423,65 @@ def test_float64_batches_keep_every_sm_by_default(cuda):
     assert info["handoff_ii"] == -1
     pb.run_multi(layout, Mp, a, b, 0.05, 1000, 1e-9, tail_problems=4, info=info)
     assert info["handoff_ii"] == 1
+
+
+def _small_batch(seed, B, lo, hi, dtype, cuda):
+    rng = np.random.default_rng(seed)
+    rows = rng.integers(lo, hi, B)
+    cols = rng.integers(lo, hi, B)
+    layout = pb.RaggedLayout(rows, cols, dtype, cuda)
+    Ms = []
+    for n, m in zip(rows, cols):
+        M = oracle.sqeuclidean(rng.random((n, 3)), rng.random((m, 3)))
+        Ms.append(M / M.max())
+    Mp = pb.pack_dense(layout, [torch.tensor(M, dtype=dtype, device=cuda) for M in Ms])
+    a = torch.cat([torch.full((int(n),), 1.0 / n, dtype=dtype, device=cuda) for n in rows])
+    b = torch.cat([torch.full((int(m),), 1.0 / m, dtype=dtype, device=cuda) for m in cols])
+    return layout, Ms, Mp, a, b, rows, cols
+
+
+@pytest.mark.parametrize("depth", [3, 5, 8])
+def test_multi_anderson_matches_oracle(cuda, depth):
+    """Anderson mixing of the v update (anderson_depth): float64 stop indices
+    equal to the oracle's restatement of the same iteration, potentials to
+    1e-8; the stop test is the plain one (column marginal below tol, row
+    marginal exact), reached in fewer iterations than the plain solve."""
+    from oracle import accelerated as acc
+    layout, Ms, Mp, a, b, rows, cols = _small_batch(41, 6, 30, 160, torch.float64, cuda)
+    reg, tol = 0.02, 1e-9
+    res = pb.run_multi(layout, Mp, a, b, reg, 20000, tol, check_period=1, anderson=depth)
+    plain = pb.run_multi(layout, Mp, a, b, reg, 20000, tol, check_period=1)
+    assert (res[2] == 0).all()
+    assert res[3].sum() < plain[3].sum()
+    for p in range(layout.B):
+        n, m = int(rows[p]), int(cols[p])
+        u, v, it, errs = acc.sinkhorn_log_anderson_v(np.full(n, 1 / n), np.full(m, 1 / m), Ms[p], reg, depth=depth,
+                                                     numItermax=20000, stopThr=tol, check_period=1)
+        assert int(res[3][p]) == it, (p, int(res[3][p]), it)
+        r0, c0 = int(layout.r_off_np[p]), int(layout.c_off_np[p])
+        np.testing.assert_allclose(res[0][r0:r0 + n].cpu().numpy(), u, rtol=1e-8, atol=1e-8)
+        np.testing.assert_allclose(res[1][c0:c0 + m].cpu().numpy(), v, rtol=1e-8, atol=1e-8)
+        P = np.exp(u[:, None] - Ms[p] / reg + v[None, :])
+        assert np.linalg.norm(P.sum(0) - 1 / m) < tol
+        assert np.abs(P.sum(1) - 1 / n).max() < 1e-14
+
+
+def test_multi_anderson_float32_meets_the_plain_test(cuda):
+    """float32 with Anderson mixing: every problem converges with its float64
+    column-marginal error below 2 tol, and its plan is within 1e-4 (relative
+    L1) of the converged float64 solution (a stop at tol = 1e-6 itself leaves
+    1e-5 to 4e-5 there, for the plain iteration as well)."""
+    layout, Ms, Mp, a, b, rows, cols = _small_batch(43, 8, 100, 700, torch.float32, cuda)
+    reg, tol = 0.02, 1e-6
+    res = pb.run_multi(layout, Mp, a, b, reg, 20000, tol, check_period=1, anderson=5)
+    assert (res[2] == 0).all()
+    for p in range(layout.B):
+        n, m = int(rows[p]), int(cols[p])
+        Pref, _ = oracle.sinkhorn_log(np.full(n, 1 / n), np.full(m, 1 / m), Ms[p], reg, numItermax=20000,
+                                      stopThr=1e-12)
+        r0, c0 = int(layout.r_off_np[p]), int(layout.c_off_np[p])
+        u = res[0][r0:r0 + n].double().cpu().numpy()
+        v = res[1][c0:c0 + m].double().cpu().numpy()
+        P = np.exp(u[:, None] - Ms[p] / reg + v[None, :])
+        assert np.linalg.norm(P.sum(0) - 1 / m) < 2 * tol
+        assert np.abs(P - Pref).sum() / Pref.sum() < 1e-4
