@@ -156,23 +156,28 @@ def run_warmstart(args, pk):
     st = torch.cuda.current_stream()
 
     OM = wp.REFINE_OMEGA
-    # arms: the headline warm start (multiscale prior + learned residual,
-    # over-relaxed solve), the plain solve, and the ablations; (start, omega,
-    # iterations between stop tests: 10 is the reference's schedule, 1 tests
-    # every iteration with the same criterion)
-    ARMS = {"warm": ("net", OM, 10), "plain": (None, 1.0, 10), "prior_relaxed": ("prior", OM, 10),
-            "net_plain": ("net", 1.0, 10), "prior_plain": ("prior", 1.0, 10), "zero_relaxed": (None, OM, 10),
-            "plain_check1": (None, 1.0, 1), "warm_check1": ("net", OM, 1), "prior_relaxed_check1": ("prior", OM, 1)}
+    AD = wp.REFINE_ANDERSON
+    # arms: (start, omega, iterations between stop tests, Anderson window).
+    # Headline: the multiscale prior with Anderson-mixed updates against the
+    # plain zero-started iteration, both testing the reference's criterion
+    # (column-marginal L2 error < 1e-6) at every iteration.  Ablations: the
+    # learned residual network on top of the prior, each component alone,
+    # over-relaxation instead of Anderson mixing, and the reference's
+    # every-10th-iteration test schedule.
+    ARMS = {"warm": ("prior", 1.0, 1, AD), "plain": (None, 1.0, 1, 0),
+            "learned_anderson": ("net", 1.0, 1, AD), "zero_anderson": (None, 1.0, 1, AD),
+            "prior_plain": ("prior", 1.0, 1, 0), "prior_relaxed": ("prior", OM, 1, 0),
+            "plain_ref_schedule": (None, 1.0, 10, 0), "warm_ref_schedule": ("prior", 1.0, 10, AD)}
 
     def step(arm, ev=None):
-        init, om, per = ARMS[arm]
+        init, om, per, ad = ARMS[arm]
         ps = wp.PairSolver(X, Y)
         wu = None
         if init == "net":
             wu = wp.warm_potential(net, X, Y, ps, WS_REG)
         elif init == "prior":
-            wu = wp.coarse_potential(X, Y, ps.maxc, WS_REG, wp.COARSE_K) / WS_REG
-        out = ps.solve(WS_REG, WS_TOL, warm_u=wu, events=ev, omega=om, check_period=per)
+            wu = wp.prior_potential(X, Y, ps, WS_REG)
+        out = ps.solve(WS_REG, WS_TOL, warm_u=wu, events=ev, omega=om, check_period=per, anderson=ad)
         return ps, out
 
     for _ in range(args.warmup):
@@ -216,8 +221,9 @@ def run_warmstart(args, pk):
     replica_barrier()
     t = time.perf_counter()
     for _ in range(e2e_steps):
-        lu, lv, ni = wp.solve_cloud_pairs(Xh, Yh, WS_REG, WS_TOL, warm=True, net=net)
+        e2e_res = wp.solve_cloud_pairs(Xh, Yh, WS_REG, WS_TOL, warm=True, check_period=1)
     e2e_s = replica_max((time.perf_counter() - t) / e2e_steps)
+    lu, lv, ni = e2e_res[0], e2e_res[1], e2e_res[2]
     W = _WS["world"]
     return {
         "value": W * B / (w["ms"] * 1e-3), "unit": "solves/s", "ms_per_step": w["ms"], "dtype": "f32",
@@ -226,17 +232,18 @@ def run_warmstart(args, pk):
         "warm": {"niter_mean": w["niter_mean"], "niter_max": w["niter_max"], "converged": w["converged"],
                  "max_marginal_err": w["max_err"]},
         "speedup_warm_vs_plain": p["ms"] / w["ms"],
-        "warm_pipeline": "coarse multiscale prior (Voronoi-weighted 256-point problem + c-transform) + learned "
-                         "residual network, then the solve over-relaxed with omega=%.2f; every pair stops on the "
-                         "same column-marginal test (err < %g, checked every 10 iterations)" % (OM, WS_TOL),
+        "warm_pipeline": "coarse multiscale prior (Voronoi-weighted 256-point problem solved on the GPU + one "
+                         "c-transform to every source point), then the solve with Anderson-mixed v updates over "
+                         "the last %d iterates (u the exact row update of the mixed v); every pair of both arms "
+                         "stops at the first iteration whose column-marginal L2 error is below %g" % (AD, WS_TOL),
         "ablation": {k: {"value": W * B / (res[k]["ms"] * 1e-3), "niter_mean": res[k]["niter_mean"],
-                         "speedup_vs_plain": p["ms"] / res[k]["ms"], "check_period": ARMS[k][2],
+                         "speedup_vs_plain": p["ms"] / res[k]["ms"], "start": ARMS[k][0] or "zero",
+                         "omega": ARMS[k][1], "check_period": ARMS[k][2], "anderson": ARMS[k][3],
                          "max_marginal_err": res[k]["max_err"], "converged": res[k]["converged"]}
-                     for k in ("prior_relaxed", "net_plain", "prior_plain", "zero_relaxed", "plain_check1",
-                               "warm_check1", "prior_relaxed_check1")},
-        # both arms stop at the first iteration whose column-marginal error is
-        # below the tolerance (stop test every iteration)
-        "speedup_warm_vs_plain_check1": res["plain_check1"]["ms"] / res["warm_check1"]["ms"],
+                     for k in ARMS if k not in ("warm", "plain")},
+        # the reference's own schedule (stop test every 10th iteration) for both arms
+        "speedup_warm_vs_plain_ref_schedule": res["plain_ref_schedule"]["ms"] / res["warm_ref_schedule"]["ms"],
+        "speedup_warm_vs_plain_ref_schedule_plain": res["plain_ref_schedule"]["ms"] / w["ms"],
         "config": {"workload": "learned warm start vs plain log-Sinkhorn, %d GMM cloud pairs n=m=%d d=%d, "
                                "reg=%.2f x max cost, stopThr=%g, float32" % (B, WS_N, WS_D, WS_REG, WS_TOL),
                    "pairs_per_step": W * B, "replicas": W, "l2": "inputs larger than L2 (%.1f GiB of cost blocks)" % (
@@ -316,6 +323,71 @@ def run_online(args, pk):
                          "frac": achieved / pk["bf16_tflops"], "issued_multiplier": 3,
                          "issued_frac": 3 * achieved / pk["bf16_tflops"], "traffic": None,
                          "kernel": "online_pass_kernel", "alg_flop_per_iteration": flop}}
+
+
+def aux_online(pk, n=65536, iters=20):
+    """The online-cost workload's iteration (n = m = 65536 points in R^64,
+    8-component mixture, reg = 0.01 x median cost): `iters` iterations timed
+    with CUDA events, algorithmic tensor FLOP 4 n m d per iteration."""
+    import torch
+    from pot_gb300.empirical import online_sinkhorn
+    dev = torch.device("cuda", _WS["local"])
+    d = 64
+    X, Y, _ = gmm_clouds(n, d, 8, 2.0, 0.5 ** 0.5, 7, dev)
+    a = torch.full((n,), 1.0 / n, device=dev)
+    k = min(4096, n)
+    reg = 0.01 * float(torch.cdist(X[:k].double(), Y[:k].double()).pow(2).median())
+    st = torch.cuda.current_stream()
+    online_sinkhorn(X, Y, reg, a, a, 2, 0.0)
+    _, ms = _timed(lambda: online_sinkhorn(X, Y, reg, a, a, iters, 0.0), st)
+    per_it = ms / iters
+    flop = 4.0 * n * n * d
+    achieved = flop / (per_it * 1e-3) / 1e12
+    return {"workload": "online log-Sinkhorn iteration, n=m=%d d=64 GMM(8), reg=0.01 x median cost" % n,
+            "value": 1000.0 / per_it, "unit": "iterations/s", "ms_per_iteration": per_it, "timed_iterations": iters,
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                         "frac": achieved / pk["bf16_tflops"], "issued_multiplier": 3,
+                         "issued_frac": 3 * achieved / pk["bf16_tflops"], "traffic": None,
+                         "kernel": "online_pass_kernel (+ online_finalize_kernel)",
+                         "alg_flop_per_iteration": flop}}
+
+
+def aux_gw(pk, n=8192, reps=5):
+    """The entropic-GW workload's gradient (n = m = 8192, C1 / C2 from
+    N(0, I3) / N(0, I8) points, each / max): both tensor-core GEMMs of
+    constC - C1 T hC2^T, median of `reps` CUDA-event timings, algorithmic
+    FLOP 4 n^3."""
+    import torch
+    from pot_gb300 import gromov as pgw
+    dev = torch.device("cuda", _WS["local"])
+    g = torch.Generator(device=dev)
+    g.manual_seed(3)
+    xs = torch.randn(n, 3, generator=g, device=dev, dtype=torch.float64)
+    xt = torch.randn(n, 8, generator=g, device=dev, dtype=torch.float64)
+    C1 = torch.cdist(xs, xs).pow(2)
+    C1 /= C1.max()
+    C2 = torch.cdist(xt, xt).pow(2)
+    C2 /= C2.max()
+    C1, C2 = C1.float().contiguous(), C2.float().contiguous()
+    del xs, xt
+    st = torch.cuda.current_stream()
+    pd = torch.full((n,), 1.0 / n, device=dev)
+    tp = pgw.TensorProduct(C1, C2, pd, pd)
+    T = torch.outer(pd, pd)
+    M = torch.empty(n, n, device=dev)
+    tp.grad(T, M)
+    kms = [_timed(lambda: tp.grad(T, M), st)[1] for _ in range(reps)]
+    tp.check_abort()
+    gemm_ms = statistics.median(kms)
+    flop = 4.0 * n ** 3
+    achieved = flop / (gemm_ms * 1e-3) / 1e12
+    return {"workload": "entropic-GW gradient constC - C1 T hC2^T, n=m=%d" % n, "value": 1000.0 / gemm_ms,
+            "unit": "gradients/s", "ms_per_gradient": gemm_ms,
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                         "frac": achieved / pk["bf16_tflops"], "issued_multiplier": 3,
+                         "issued_frac": 3 * achieved / pk["bf16_tflops"], "traffic": None,
+                         "kernel": "gemm_split3_kernel (both GEMMs of one gradient)",
+                         "alg_flop_per_gradient": flop}}
 
 
 def run_gw(args, pk):
@@ -497,12 +569,13 @@ def run_small(args, pk):
 
 
 def run_warm_eval(args, pk):
-    """Held-out evaluation of the learned warm start: 10 batches of 1024 pairs
-    (seeds EVAL_SEED .. EVAL_SEED + 10239, never used in training), warm
-    start (prior + network, over-relaxed) against the plain zero-started solve,
-    both stopping on the same column-marginal test (1e-6, every 10
-    iterations); mean stop index, relative error of the predicted potential,
-    and wall time per batch."""
+    """Held-out evaluation of the warm start on 10 batches of 1024 pairs
+    (seeds after the headline batch's): the warm arm (multiscale prior +
+    Anderson-mixed updates) against the plain iteration, both testing the
+    column-marginal error (1e-6) at every iteration; mean stop index,
+    relative error of the prior and of prior + learned residual against each
+    batch's converged potential, and device time per batch (seeds EVAL_SEED
+    .. EVAL_SEED + 10239, never used in training)."""
     import torch
     from pot_gb300.warmstart import pipeline as wp
     dev = torch.device("cuda:0")
@@ -514,8 +587,9 @@ def run_warm_eval(args, pk):
 
     def arm_run(X, Y, arm):
         ps = wp.PairSolver(X, Y)
-        wu = wp.warm_potential(net, X, Y, ps, WS_REG) if arm == "warm" else None
-        return ps, ps.solve(WS_REG, WS_TOL, warm_u=wu, omega=wp.REFINE_OMEGA if arm == "warm" else 1.0)
+        wu = wp.prior_potential(X, Y, ps, WS_REG) if arm == "warm" else None
+        return ps, ps.solve(WS_REG, WS_TOL, warm_u=wu, check_period=1,
+                            anderson=wp.REFINE_ANDERSON if arm == "warm" else 0)
 
     X, Y = wp.gen_pairs(EVAL_SEED, B, WS_N, WS_D, dev)
     for _ in range(max(1, args.warmup)):  # untimed: module loads, allocator pools
@@ -550,6 +624,8 @@ def run_warm_eval(args, pk):
             "mean_stop_index": {"warm": float(np.mean(res["warm"])), "plain": float(np.mean(res["plain"]))},
             "median_rel_error_potential": {"prior_plus_network": float(np.mean(res["err"])),
                                            "prior_only": float(np.mean(res["prior_err"]))},
+            "warm_pipeline": "multiscale prior + Anderson(%d), stop test every iteration (both arms)"
+                             % wp.REFINE_ANDERSON,
             "config": {"workload": "%d held-out GMM cloud pairs n=m=%d d=%d, reg=%.2f x max cost, stopThr=%g, "
                                    "seeds %d..%d, device time per batch (CUDA events) incl. cost blocks and warm "
                                    "start"
@@ -704,6 +780,7 @@ def main():
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-aux", action="store_true")
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--iters", type=int, default=20)
     ap.add_argument("--full", type=int, default=0)
@@ -739,6 +816,9 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "data": "synthetic (seeded Gaussian-mixture clouds generated on the device)"}
     line.update(res)
+    if not args.no_aux:
+        # the tensor-core kernels of the other workloads, measured in the same run
+        line["aux"] = {"online": aux_online(pk), "gw_gradient": aux_gw(pk)}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(1, 3)
     if rank == 0:

@@ -107,6 +107,7 @@ struct MultiArgs {
   int64_t* urow_pre;        // prefix of row-pass units
   int64_t* colpre;          // prefix of columns (merge) over the active list
   int32_t* ctl;             // [0] n active, [1] abort
+  int32_t* leave_cnt;       // [2] problems leaving at a decision (alternate decisions)
   unsigned* bar;
   // outputs
   T* out_u; T* out_v;
@@ -414,19 +415,49 @@ __device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leavi
     A.nsr[p] = (n + rc - 1) / rc;
   }
   __syncthreads();
-  // prefix sums of units and columns over the new list (serial, one thread)
-  if (threadIdx.x == 0) {
-    const int na = s_base;
-    int64_t uc = 0, ur = 0, cc = 0;
-    for (int k = 0; k < na; ++k) {
+  // prefix sums of units and columns over the new list: block-wide scans
+  // (warp shuffles, then the warp totals), chunk by chunk with running bases
+  __shared__ int64_t s_wt[3][MT_THREADS / 32];
+  __shared__ int64_t s_run[3];
+  if (threadIdx.x == 0) { s_run[0] = 0; s_run[1] = 0; s_run[2] = 0; }
+  __syncthreads();
+  const int na = s_base;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  for (int c0 = 0; c0 < na; c0 += blockDim.x) {
+    const int k = c0 + threadIdx.x;
+    int64_t own[3] = {0, 0, 0};
+    if (k < na) {
       const int p = A.active[k];
       const int m = A.cols[p];
-      A.ucol_pre[k] = uc; A.urow_pre[k] = ur; A.colpre[k] = cc;
-      uc += (int64_t)((m + 32 * VW - 1) / (32 * VW)) * A.nsr[p];
-      ur += (A.rows[p] + MT_RW - 1) / MT_RW;
-      cc += m;
+      own[0] = (int64_t)((m + 32 * VW - 1) / (32 * VW)) * A.nsr[p];
+      own[1] = (A.rows[p] + MT_RW - 1) / MT_RW;
+      own[2] = m;
     }
-    A.ucol_pre[na] = uc; A.urow_pre[na] = ur; A.colpre[na] = cc;
+    int64_t inc[3] = {own[0], own[1], own[2]};
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int64_t up = __shfl_up_sync(0xffffffffu, inc[q], o);
+        if (lane >= o) inc[q] += up;
+      }
+    }
+    if (lane == 31) { s_wt[0][wid] = inc[0]; s_wt[1][wid] = inc[1]; s_wt[2][wid] = inc[2]; }
+    __syncthreads();
+    int64_t before[3] = {s_run[0], s_run[1], s_run[2]};
+    for (int w = 0; w < wid; ++w) { before[0] += s_wt[0][w]; before[1] += s_wt[1][w]; before[2] += s_wt[2][w]; }
+    if (k < na) {
+      A.ucol_pre[k] = before[0] + inc[0] - own[0];
+      A.urow_pre[k] = before[1] + inc[1] - own[1];
+      A.colpre[k] = before[2] + inc[2] - own[2];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int w = 0; w < nwb; ++w) { s_run[0] += s_wt[0][w]; s_run[1] += s_wt[1][w]; s_run[2] += s_wt[2][w]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    A.ucol_pre[na] = s_run[0]; A.urow_pre[na] = s_run[1]; A.colpre[na] = s_run[2];
     // hand the rest to the tail kernel when every remaining block fits a cluster
     int tail = A.tail_max > 0 && na > 0 && na <= A.tail_max;
     for (int k = 0; tail && k < na; ++k) {
@@ -608,6 +639,7 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
   T* vcur = A.v0;
   T* vnxt = A.v1;
   bool prev_check = false;
+  int ndec = 0;  // decisions taken (the same count in every CTA)
   for (int ii = 0;; ++ii) {
     const int nact = ld_acquire_i(A.ctl);
     if (nact == 0) break;
@@ -636,6 +668,7 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
         joint_conv = jc == 1;
       }
       // decide per problem, write out the leaving ones (state of iteration ii-1)
+      int nleave = 0;
       for (int k = blockIdx.x; k < nact; k += gridDim.x) {
         const int p = __ldcg(A.active + k);
         double e = -1.0;
@@ -654,11 +687,20 @@ __global__ void __launch_bounds__(MT_THREADS, MtBlocks<T>::value) multi_sinkhorn
             A.err[p] = e;
           }
           leaving[p] = leave ? 1 : 0;
+          nleave += leave ? 1 : 0;
         }
       }
+      if (threadIdx.x == 0 && nleave) atomicAdd(A.leave_cnt + (ndec & 1), nleave);
       if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
-      if (blockIdx.x == 0) mt_rebuild<T>(A, nact, leaving, s_scan, nwarps);
-      if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+      // the active list and its prefix sums change only when a problem left
+      const bool changed = ld_acquire_i(A.leave_cnt + (ndec & 1)) != 0;
+      // the other counter was last read a decision ago: ready for the next one
+      if (blockIdx.x == 0 && threadIdx.x == 0) A.leave_cnt[(ndec + 1) & 1] = 0;
+      ++ndec;
+      if (changed) {
+        if (blockIdx.x == 0) mt_rebuild<T>(A, nact, leaving, s_scan, nwarps);
+        if (!grid_barrier(A.bar, gridDim.x, abort_flag, A.timeout_ns)) return;
+      }
       if (ld_acquire_i(A.ctl) == 0) break;
       if (ld_acquire_i(A.ctl + 2)) {
         // handoff: v of iteration ii is in vnxt, u of ii-1 in A.u; the tail
@@ -1061,6 +1103,7 @@ int launch_multi(const OtgMultiProblem* q, cudaStream_t st) {
   char* ctlp = take(64);
   A.ctl = reinterpret_cast<int32_t*>(ctlp);
   A.bar = reinterpret_cast<unsigned*>(ctlp + 32);
+  A.leave_cnt = reinterpret_cast<int32_t*>(ctlp + 48);
   if (off > q->workspace_bytes) return OTG_ERR_WORKSPACE;
   if (A.and_depth > 0) {
     if (!q->anderson_ws || q->anderson_ws_bytes < anderson_ws_bytes(sizeof(T), q->nprob, q->total_cols, A.and_depth))

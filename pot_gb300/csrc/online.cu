@@ -197,30 +197,50 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
       const int qlast = tile * P.k_tiles + P.k_tiles - 1;
       const float* h = hbuf + (qlast % OL_STAGES) * OL_N;
       {
-        float v[32];
+        // packed fp32x2 arithmetic (one instruction per column pair, each
+        // lane rounded as the scalar op) and three-input max: the epilogue
+        // is bound by instruction issue, and the partial sums group the
+        // terms exactly as four scalar accumulators would
+        uint32_t v[32];
         const int col = cgrp * 32;
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * OL_N + col), v);
+        tmem_ld32u(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * OL_N + col), v);
+        const ulonglong2* hv = reinterpret_cast<const ulonglong2*>(h + col);
+        const uint64_t a2 = pack2(P.alpha, P.alpha);
+        uint64_t t2[16];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const ulonglong2 hh = hv[i];
+          t2[2 * i] = fma2(pack2u(v[4 * i], v[4 * i + 1]), a2, hh.x);
+          t2[2 * i + 1] = fma2(pack2u(v[4 * i + 2], v[4 * i + 3]), a2, hh.y);
+        }
         float t[32];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) t[i] = fmaf(v[i], P.alpha, h[col + i]);
-        // max and sum as trees / independent accumulators: serial 32-long
-        // chains would expose the FP latency on every element
-        float mm[16];
+        for (int i = 0; i < 16; ++i) unpack2(t2[i], t[2 * i], t[2 * i + 1]);
+        float m1[11];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) mm[i] = fmaxf(t[i], t[i + 16]);
-#pragma unroll
-        for (int w = 8; w > 0; w >>= 1)
-#pragma unroll
-          for (int i = 0; i < w; ++i) mm[i] = fmaxf(mm[i], mm[i + w]);
-        const float nm = fmaxf(mx, mm[0]);
+        for (int i = 0; i < 10; ++i) m1[i] = fmax3(t[3 * i], t[3 * i + 1], t[3 * i + 2]);
+        m1[10] = fmaxf(t[30], t[31]);
+        const float n0 = fmax3(m1[0], m1[1], m1[2]), n1 = fmax3(m1[3], m1[4], m1[5]);
+        const float n2 = fmax3(m1[6], m1[7], m1[8]), n3 = fmaxf(m1[9], m1[10]);
+        const float nm = fmax3(mx, fmax3(n0, n1, n2), n3);
         if (nm != -INFINITY) {
           const float r = ex2(mx - nm);
           sm *= r;
           sc *= r;
-          float ps[4] = {0.f, 0.f, 0.f, 0.f};
+          const uint64_t nm2 = pack2(nm, nm);
+          uint64_t acc0 = 0ull, acc1 = 0ull;  // columns 4k, 4k+1 and 4k+2, 4k+3
 #pragma unroll
-          for (int i = 0; i < 32; ++i) ps[i & 3] += ex2(t[i] - nm);
-          const float part = (ps[0] + ps[1]) + (ps[2] + ps[3]);
+          for (int i = 0; i < 16; ++i) {
+            float x0, x1;
+            unpack2(sub2(t2[i], nm2), x0, x1);
+            const uint64_t e2 = pack2(ex2(x0), ex2(x1));
+            if (i & 1) acc1 = add2(acc1, e2);
+            else acc0 = add2(acc0, e2);
+          }
+          float p0, p1, p2, p3;
+          unpack2(acc0, p0, p1);
+          unpack2(acc1, p2, p3);
+          const float part = (p0 + p1) + (p2 + p3);
           const float y = part - sc;
           const float tt = sm + y;
           sc = (tt - sm) - y;

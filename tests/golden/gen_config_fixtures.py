@@ -1,9 +1,10 @@
 """Float64 oracle fixtures at the benchmark configurations (run on a CPU).
 
-    python tests/golden/gen_config_fixtures.py [online|gw|ragged|all]
+    python tests/golden/gen_config_fixtures.py [online|ragged|all]
 
 Each fixture holds seeded synthetic inputs of one benchmark configuration,
-at a size the float64 oracle solves in minutes, and the oracle's results:
+at a size the float64 oracle solves in minutes (too slow to run inside a
+test), and the oracle's results:
 
 - ``online_gmm4096_d64``: the online-cost workload (8-component Gaussian
   mixture in R^64, means ~ N(0, 4 I), covariances 0.5 I; weights uniform
@@ -11,10 +12,6 @@ at a size the float64 oracle solves in minutes, and the oracle's results:
   cost) on its 4096-point subsample; oracle ``sinkhorn_log`` on the stored
   float64 cost (the reference's log-domain solver, ``ot/bregman/
   _sinkhorn.py:690-918``) at stopThr 1e-6 and converged (1e-10).
-- ``gw_gauss1024``: the entropic Gromov-Wasserstein workload (C1 = squared
-  distances of N(0, I_3) points, C2 of N(0, I_8) points, each divided by its
-  maximum, uniform weights, epsilon = 5e-3) at n = m = 1024: a few outer
-  iterations of the log-domain inner variant (``oracle.entropic_gw_log_inner``).
 - ``ragged_cfg3``: a sample of the uneven-batch workload (n, m ~ U{32..1024},
   d in {3, 16}, points ~ U[0,1]^d, a, b ~ Dirichlet(1), reg = 10^U[-3,-1] x
   max cost) with each problem's oracle ``sinkhorn_log`` at stopThr 1e-6.
@@ -62,21 +59,6 @@ def online(path):
     np.savez_compressed(path, **out)
 
 
-def gw(path):
-    rng = np.random.default_rng(5)
-    n = 1024
-    xs = rng.standard_normal((n, 3)).astype(np.float32)
-    xt = rng.standard_normal((n, 8)).astype(np.float32)
-    C1 = oracle.sqeuclidean(xs.astype(np.float64), xs.astype(np.float64))
-    C2 = oracle.sqeuclidean(xt.astype(np.float64), xt.astype(np.float64))
-    C1 /= C1.max()
-    C2 /= C2.max()
-    t = time.time()
-    T, lg = oracle.entropic_gw_log_inner(C1, C2, epsilon=5e-3, max_iter=5, numItermax=100000, stopThr=1e-7)
-    print("gw: %.0f s, gw_dist %.6e" % (time.time() - t, lg["gw_dist"]), flush=True)
-    np.savez_compressed(path, xs=xs, xt=xt, T=T, gw_dist=lg["gw_dist"], max_iter=5, epsilon=5e-3, stopThr=1e-7)
-
-
 def ragged(path):
     rng = np.random.default_rng(3)
     B = 24
@@ -103,7 +85,5 @@ if __name__ == "__main__":
     which = sys.argv[1] if len(sys.argv) > 1 else "all"
     if which in ("online", "all"):
         online(os.path.join(HERE, "online_gmm4096_d64.npz"))
-    if which in ("gw", "all"):
-        gw(os.path.join(HERE, "gw_gauss1024.npz"))
     if which in ("ragged", "all"):
         ragged(os.path.join(HERE, "ragged_cfg3.npz"))

@@ -5,8 +5,8 @@ through ``ref_import.py``); the GPU machine never runs this script, it only reads
 the ``.npz`` files it writes.  Every case records its inputs, the reference's
 outputs and, where the reference warns, the warnings it raised.
 
-    python tests/golden/gen_golden.py            # every section
-    python tests/golden/gen_golden.py next       # one section
+    POT_REFERENCE_SRC=<reference tree> python tests/golden/gen_golden.py        # every section
+    POT_REFERENCE_SRC=<reference tree> python tests/golden/gen_golden.py next   # one section
 """
 import os
 import sys

@@ -16,7 +16,7 @@ import subprocess
 import sys
 import types
 
-REF_SRC = os.environ.get("POT_REFERENCE_SRC", "/root/reference")
+REF_SRC = os.environ.get("POT_REFERENCE_SRC")  # the read-only reference tree: required, no default
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 DEST = os.path.join(REPO, "baseline", "_ref", "pot")
@@ -40,8 +40,8 @@ def build():
         have = [f for f in os.listdir(os.path.join(DEST, "ot", "lp")) if f.startswith("emd_wrap") and f.endswith(".so")]
         if have:
             return DEST
-    if not os.path.isdir(REF_SRC):
-        raise RuntimeError("reference source tree not found: %s" % REF_SRC)
+    if not REF_SRC or not os.path.isdir(REF_SRC):
+        raise RuntimeError("set POT_REFERENCE_SRC to the reference (PythonOT/POT) source tree; got %r" % REF_SRC)
     if os.path.exists(DEST):
         shutil.rmtree(DEST)
     shutil.copytree(REF_SRC, DEST, ignore=shutil.ignore_patterns(".git", "docs", "data", "examples"))
