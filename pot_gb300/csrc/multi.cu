@@ -54,6 +54,7 @@
 #include <algorithm>
 #include <cooperative_groups.h>
 #include "common.cuh"
+#include "anderson.cuh"
 #include "../../include/pot_gb300.h"
 
 namespace cg = cooperative_groups;
@@ -473,104 +474,15 @@ __device__ void mt_rebuild(const MultiArgs<T>& A, int nact, const int32_t* leavi
   __syncthreads();
 }
 
-// Anderson step (one CTA per active problem): insert F(v_k) (in vnxt) and
-// the residual F(v_k) - v_k (vcur) into the history, update the residual
-// Gram matrix, solve for the mixing weights and write the mixed v into vnxt.
-// Kept out of line, like the joint decision: it must not weigh on the
-// registers of the passes.
-constexpr double AND_LAMBDA = 1e-10;   // Tikhonov term, relative to trace / D
-constexpr double AND_MAX_L1 = 1e4;     // larger sum |alpha|: restart with the plain step
-
+// Anderson step (one CTA per active problem, anderson.cuh): the new v of
+// every active problem is mixed over its history.  Kept out of line, like
+// the joint decision: it must not weigh on the registers of the passes.
 template <typename T>
 __device__ __noinline__ void mt_anderson(const MultiArgs<T>& A, int nact, const T* vcur, T* vnxt) {
-  constexpr int MD = OTG_ANDERSON_MAX_DEPTH;
-  __shared__ double s_dot[MD];
-  __shared__ double s_alpha[MD];
-  __shared__ int s_keep;
-  const int D = A.and_depth;
   for (int k = blockIdx.x; k < nact; k += gridDim.x) {
     const int p = __ldcg(A.active + k);
-    const int m = A.cols[p];
-    const int64_t co = A.c_off[p];
-    const int cnt = __ldcg(A.and_cnt + p);
-    const int s = cnt % D;                       // slot of the new iterate
-    const int nh = cnt + 1 < D ? cnt + 1 : D;    // slots in use after the insert
-    // insert, and this thread's share of the dots <r_new, R_q>
-    double acc[MD];
-#pragma unroll
-    for (int q = 0; q < MD; ++q) acc[q] = 0.0;
-    for (int j = threadIdx.x; j < m; j += blockDim.x) {
-      const T f = __ldcg(vnxt + co + j);
-      const T r = f - __ldcg(vcur + co + j);
-      A.and_F[(int64_t)s * A.total_cols + co + j] = f;
-      A.and_R[(int64_t)s * A.total_cols + co + j] = r;
-#pragma unroll
-      for (int q = 0; q < MD; ++q) {
-        if (q < nh) {
-          const T rq = q == s ? r : __ldcg(A.and_R + (int64_t)q * A.total_cols + co + j);
-          acc[q] += (double)r * (double)rq;
-        }
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < MD; ++q) {
-      if (q < nh) {
-        const double d = block_sum_fixed(acc[q]);
-        if (threadIdx.x == 0) s_dot[q] = d;
-      }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double* G = A.and_G + (int64_t)p * D * D;
-      for (int q = 0; q < nh; ++q) { G[s * D + q] = s_dot[q]; G[q * D + s] = s_dot[q]; }
-      // (G + lambda I) w = 1 by Gaussian elimination with partial pivoting
-      double Mx[MD][MD + 1];
-      double tr = 0.0;
-      for (int i = 0; i < nh; ++i) tr += G[i * D + i];
-      const double lam = AND_LAMBDA * tr / nh;
-      for (int i = 0; i < nh; ++i) {
-        for (int j = 0; j < nh; ++j) Mx[i][j] = G[i * D + j] + (i == j ? lam : 0.0);
-        Mx[i][nh] = 1.0;
-      }
-      bool ok = nh > 1 && tr > 0.0;
-      for (int c = 0; ok && c < nh; ++c) {
-        int piv = c;
-        for (int i = c + 1; i < nh; ++i) if (fabs(Mx[i][c]) > fabs(Mx[piv][c])) piv = i;
-        if (!(fabs(Mx[piv][c]) > 0.0)) { ok = false; break; }
-        if (piv != c) for (int j = c; j <= nh; ++j) { const double t = Mx[c][j]; Mx[c][j] = Mx[piv][j]; Mx[piv][j] = t; }
-        for (int i = c + 1; i < nh; ++i) {
-          const double f = Mx[i][c] / Mx[c][c];
-          for (int j = c; j <= nh; ++j) Mx[i][j] -= f * Mx[c][j];
-        }
-      }
-      double w[MD];
-      double sw = 0.0, l1 = 0.0;
-      for (int i = nh - 1; ok && i >= 0; --i) {
-        double t = Mx[i][nh];
-        for (int j = i + 1; j < nh; ++j) t -= Mx[i][j] * w[j];
-        w[i] = t / Mx[i][i];
-        sw += w[i];
-      }
-      if (ok) {
-        for (int i = 0; i < nh; ++i) { w[i] /= sw; l1 += fabs(w[i]); }
-        ok = isfinite(l1) && l1 < AND_MAX_L1;
-      }
-      for (int i = 0; i < MD; ++i) s_alpha[i] = ok && i < nh ? w[i] : (i == s ? 1.0 : 0.0);
-      // a first iterate, or a failed solve: the plain step; after a failure
-      // the history restarts from this iterate alone
-      s_keep = ok;
-      A.and_cnt[p] = ok || nh == 1 ? cnt + 1 : 0;
-    }
-    __syncthreads();
-    if (s_keep) {
-      for (int j = threadIdx.x; j < m; j += blockDim.x) {
-        double vm = 0.0;
-        for (int q = 0; q < nh; ++q) vm += s_alpha[q] * (double)__ldcg(A.and_F + (int64_t)q * A.total_cols + co + j);
-        vnxt[co + j] = (T)vm;
-      }
-    }
-    // after a restart vnxt keeps F(v_k): the plain step
-    __syncthreads();
+    anderson_step<T>(A.and_depth, A.cols[p], A.c_off[p], A.total_cols, vcur, vnxt, A.and_F, A.and_R,
+                     A.and_G + (int64_t)p * A.and_depth * A.and_depth, A.and_cnt + p);
   }
 }
 

@@ -63,8 +63,24 @@ struct OnlinePass {
   int split;
   int rows_pad;
   float* part;
+  // batch of pairs (active == null: one problem).  CTA blockIdx.x takes row
+  // block blockIdx.x % nrb of the pair in active slot blockIdx.x / nrb; slots
+  // at or beyond *count have left the batch and their CTAs return at once.
+  // Planes and per-row vectors hold pair p's rows from p * rows_per_pair
+  // (resident side) and p * cols_per_pair (streamed side); alpha_p is the
+  // pair's alpha.  err_sq: the check error of a row is the squared violation
+  // (the L2 test of sinkhorn_log) instead of the absolute one (L1).
+  const int* active;
+  const int* count;
+  int nrb;
+  int64_t rows_per_pair, cols_per_pair;
+  const float* alpha_p;
+  int err_sq;
 };
 
+// MAXP: instead of the log-sum-exp, each row's max of t (the max cost of a
+// pair batch, which sets its regularisation): no exponentials.
+template <bool MAXP>
 __global__ void __launch_bounds__(OL_THREADS, 1)
 online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                    const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, OnlinePass P) {
@@ -83,7 +99,15 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
   float* red = reinterpret_cast<float*>(tslot + 4);                 // [3][2][128] (mx, s) of column groups 1-3
   unsigned* relcnt = reinterpret_cast<unsigned*>(red + 6 * OL_M);   // [OL_STAGES] epilogue warps done
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r0 = blockIdx.x * OL_M;
+  int pair = 0, rblk = blockIdx.x;
+  if (P.active) {
+    const int slot = blockIdx.x / P.nrb;
+    if (slot >= __ldcg(P.count)) return;  // the whole CTA, before any barrier or TMEM allocation
+    pair = __ldcg(P.active + slot);
+    rblk = blockIdx.x % P.nrb;
+  }
+  const int64_t rbase = (int64_t)pair * P.rows_per_pair, cbase = (int64_t)pair * P.cols_per_pair;
+  const int r0 = rblk * OL_M;
   const int cs = blockIdx.y;
   const int t0 = (int)((int64_t)cs * P.col_tiles / P.split), t1 = (int)((int64_t)(cs + 1) * P.col_tiles / P.split);
   const int ntl = t1 - t0;                     // this CTA's streamed tiles
@@ -108,8 +132,8 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
     if (lane == 0) {
       mbar_arrive_expect_tx(res_full, 2 * OL_TILE * P.k_tiles);
       for (int kt = 0; kt < P.k_tiles; ++kt) {
-        tma_load_2d(resident + (2 * kt) * OL_TILE, &tAh, kt * OL_K, r0, res_full);
-        tma_load_2d(resident + (2 * kt + 1) * OL_TILE, &tAl, kt * OL_K, r0, res_full);
+        tma_load_2d(resident + (2 * kt) * OL_TILE, &tAh, kt * OL_K, (int)(rbase + r0), res_full);
+        tma_load_2d(resident + (2 * kt + 1) * OL_TILE, &tAl, kt * OL_K, (int)(rbase + r0), res_full);
       }
       int issued = 0;
       for (int q = 0; q < nsteps; ++q) {
@@ -118,9 +142,9 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
         const int tile = t0 + q / P.k_tiles, kt = q % P.k_tiles;
         unsigned char* st = ring + s * OL_STAGE;
         mbar_arrive_expect_tx(full + s, 2 * OL_TILE + OL_HVEC);
-        tma_load_2d(st, &tBh, kt * OL_K, tile * OL_N, full + s);
-        tma_load_2d(st + OL_TILE, &tBl, kt * OL_K, tile * OL_N, full + s);
-        bulk_g2s(hbuf + s * OL_N, P.h + (int64_t)tile * OL_N, OL_HVEC, full + s);
+        tma_load_2d(st, &tBh, kt * OL_K, (int)(cbase + tile * OL_N), full + s);
+        tma_load_2d(st + OL_TILE, &tBl, kt * OL_K, (int)(cbase + tile * OL_N), full + s);
+        bulk_g2s(hbuf + s * OL_N, P.h + cbase + (int64_t)tile * OL_N, OL_HVEC, full + s);
         ++issued;
       }
       const int lo = issued > OL_STAGES ? issued - OL_STAGES : 0;
@@ -205,7 +229,8 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
         const int col = cgrp * 32;
         tmem_ld32u(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * OL_N + col), v);
         const ulonglong2* hv = reinterpret_cast<const ulonglong2*>(h + col);
-        const uint64_t a2 = pack2(P.alpha, P.alpha);
+        const float alpha = P.alpha_p ? __ldg(P.alpha_p + pair) : P.alpha;
+        const uint64_t a2 = pack2(alpha, alpha);
         uint64_t t2[16];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
@@ -223,7 +248,9 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
         const float n0 = fmax3(m1[0], m1[1], m1[2]), n1 = fmax3(m1[3], m1[4], m1[5]);
         const float n2 = fmax3(m1[6], m1[7], m1[8]), n3 = fmaxf(m1[9], m1[10]);
         const float nm = fmax3(mx, fmax3(n0, n1, n2), n3);
-        if (nm != -INFINITY) {
+        if (MAXP) {
+          mx = nm;
+        } else if (nm != -INFINITY) {
           const float r = ex2(mx - nm);
           sm *= r;
           sc *= r;
@@ -264,17 +291,23 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
     if (cgrp == 0 && ok) {
       for (int g = 0; g < 3; ++g) lse_merge(mx, sm, red[g * 2 * OL_M + row_local], red[g * 2 * OL_M + OL_M + row_local]);
       const int row = r0 + row_local;
-      if (P.split > 1) {
+      const int64_t ri = rbase + row;  // the row in the packed vectors
+      if (MAXP) {
+        if (row < P.n_rows) P.pot_out2[ri] = mx + P.rterm[ri];
+      } else if (P.split > 1) {
         P.part[((size_t)cs * 2) * P.rows_pad + row] = mx;
         P.part[((size_t)cs * 2 + 1) * P.rows_pad + row] = sm;
       } else if (row < P.n_rows) {
-        const float L = lse_value(mx, sm) + P.rterm[row];  // base-2 LSE_j(g2_j - C_ij log2e/reg)
-        const float pnew = P.logw2[row] - L;
-        P.pot_out2[row] = pnew;
-        P.h_out[row] = pnew - P.other_norm2[row];
-        if (P.err) P.err[row] = fabs((double)ex2(P.pot2[row] + L) - (double)P.w[row]);
+        const float L = lse_value(mx, sm) + P.rterm[ri];  // base-2 LSE_j(g2_j - C_ij log2e/reg)
+        const float pnew = P.logw2[ri] - L;
+        if (P.err) {
+          const double e = (double)ex2(P.pot2[ri] + L) - (double)P.w[ri];
+          P.err[ri] = P.err_sq ? e * e : fabs(e);
+        }
+        P.pot_out2[ri] = pnew;
+        P.h_out[ri] = pnew - P.other_norm2[ri];
       } else {
-        P.h_out[row] = -INFINITY;  // padding rows of the resident side
+        P.h_out[ri] = -INFINITY;  // padding rows of the resident side
       }
     }
   }
@@ -467,7 +500,8 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     return OTG_ERR_CUDA;
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(online_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) != cudaSuccess)
+    if (cudaFuncSetAttribute(online_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) !=
+        cudaSuccess)
       return OTG_ERR_CUDA;
     attr = true;
   }
@@ -487,7 +521,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
   auto pass = [&](OnlinePass& P, const CUtensorMap& ah, const CUtensorMap& al, const CUtensorMap& bh,
                   const CUtensorMap& bl, int64_t rows_pad, int split, double* eslot_of_pass) {
     P.split = split; P.rows_pad = (int)rows_pad; P.part = part;
-    online_pass_kernel<<<dim3((unsigned)(rows_pad / OL_M), (unsigned)split), OL_THREADS, OL_SMEM, st>>>(ah, al, bh,
+    online_pass_kernel<false><<<dim3((unsigned)(rows_pad / OL_M), (unsigned)split), OL_THREADS, OL_SMEM, st>>>(ah, al, bh,
                                                                                                        bl, P);
     if (split > 1) online_finalize_kernel<<<(unsigned)((rows_pad + 255) / 256), 256, 0, st>>>(P);
     // the L1 error: the row slots summed in a fixed order (the same value in every run)

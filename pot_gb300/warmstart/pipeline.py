@@ -215,8 +215,9 @@ def predict(net, X, Y, maxc, F, chunk=1024):
 
 
 # encoder widths h1, h2 and head width h3 of the shipped network: the learned
-# residual does not beat the prior (measured), so the network is kept small
-# (about 13k multiply-adds per point instead of 46k at 64/64/128)
+# residual explains only a few per cent of the prior's error (measured), so
+# the network is kept small (about 13k multiply-adds per point instead of 46k
+# at 64/64/128)
 NET_SIZES = (32, 32, 64)
 
 

@@ -2,12 +2,14 @@
 
 - online-cost workload (8-component Gaussian mixture in R^64, Dirichlet(50)
   weights, reg = 0.01 x median cost) on its 4096-point subsample: the float32
-  online solver (tensor-core cost tiles, fp16 hi/lo x3) at stopThr 1e-6
-  against the oracle's converged sinkhorn_log (stored fixture,
+  online solver (tensor-core cost tiles, fp16 hi/lo x3) against the
+  oracle's converged sinkhorn_log (stored fixture,
   tests/golden/gen_config_fixtures.py): plan relative L1 <= 1e-5.  The loss
-  and the exact-cost marginals are within 1e-5 (relative / L1), not 1e-6: at
-  this regularisation the exponent arguments are ~100 in magnitude, where one
-  float32 ulp is 7.6e-6, which bounds every float32 potential's accuracy;
+  and the exact-cost marginals are within 1e-5 (relative / L1), not 1e-6, and
+  the solver's own float32 L1 error estimate levels off at 1.3e-6, so it is
+  run to stopThr 2e-6: at this regularisation the exponent arguments are
+  ~100 in magnitude, where one float32 ulp is 7.6e-6, which bounds the
+  accuracy of every float32 potential;
 - entropic Gromov-Wasserstein (C1, C2 from N(0, I3) / N(0, I8) points, each
   divided by its maximum, epsilon = 5e-3) at n = m = 1024, five outer
   iterations: the float32 tensor-core path against the float64 oracle run
@@ -37,7 +39,7 @@ def test_online_config_subsample_vs_converged_oracle(cuda):
     C = oracle.sqeuclidean(X.astype(np.float64), Y.astype(np.float64))
     Pref = np.exp(g["conv_log_u"][:, None] - C / reg + g["conv_log_v"][None, :])
     f32 = lambda z: torch.tensor(z, dtype=torch.float32, device=cuda)  # noqa: E731
-    f, gg, st, nit, errs = online_sinkhorn(f32(X), f32(Y), reg, f32(a), f32(b), 5000, 1e-6)
+    f, gg, st, nit, errs = online_sinkhorn(f32(X), f32(Y), reg, f32(a), f32(b), 5000, 2e-6)
     P = np.exp(f.double().cpu().numpy()[:, None] - C / reg + gg.double().cpu().numpy()[None, :])
     rel = np.abs(P - Pref).sum() / Pref.sum()
     loss, loss_ref = float((P * C).sum()), float((Pref * C).sum())
@@ -46,7 +48,7 @@ def test_online_config_subsample_vs_converged_oracle(cuda):
     print("online 4096 d=64 reg=0.01 median: status %d niter %d (oracle %d at 1e-6), plan rel L1 %.2e, "
           "loss rel %.2e, row L1 %.2e, col L2 %.2e, last errors %s"
           % (st, nit, int(g["niter"]), rel, abs(loss - loss_ref) / loss_ref, row_l1, col_l2, errs[-3:]))
-    assert st == 0 and errs[-1] <= 1e-6
+    assert st == 0 and errs[-1] <= 2e-6
     assert rel <= 1e-5
     assert abs(loss - loss_ref) <= 1e-5 * loss_ref
     assert row_l1 <= 1e-5 and col_l2 <= 1e-5
