@@ -323,6 +323,54 @@ int otg_multi_tail_config(int dtype, int32_t* cluster_ctas, int32_t* max_cluster
                           int32_t* cuda_error);
 
 /* ------------------------------------------------------------------------
+ * Batched point-cloud solves on the tensor cores: P pairs of clouds X_p
+ * (n x d) and Y_p (m x d), fp32, the same n, m, d for every pair, packed
+ * pair after pair, squared-Euclidean cost that is never stored: every pass
+ * rebuilds the cost tiles from the points (tcgen05, fp16 hi/lo x3, as
+ * otg_sinkhorn_online) and folds them into per-row log-sum-exps, so a pass
+ * reads points instead of a cost block (16 MiB per 2048 x 2048 pair).  Per
+ * pair the iteration, stop test and outputs are those of otg_sinkhorn_multi
+ * on the stored cost: sinkhorn_log order (ot/bregman/_sinkhorn.py:880-899,
+ * v first), column-marginal L2 error every check_period iterations (0: 10),
+ * each pair stopping on its own, optional Anderson mixing of the v update
+ * (anderson_depth, at most OTG_ANDERSON_MAX_DEPTH).  reg: one absolute value
+ * per pair (otg_pairs_max_cost gives each pair's largest cost, to set it
+ * relative to that).  a, b: P x n, P x m weights; warm_u: P x n natural-log
+ * source potentials or NULL; out_u, out_v: P x n, P x m natural-log
+ * potentials; status, niter, err per pair as otg_sinkhorn_multi.  No
+ * reference counterpart for the batching; replaces the stored-cost passes of
+ * the pair solver of the warm-start workload.
+ * ---------------------------------------------------------------------- */
+typedef struct OtgPairsProblem {
+  const float* X;
+  const float* Y;
+  int32_t npairs;
+  int32_t d;
+  int64_t n, m;
+  const float* a;
+  const float* b;
+  const double* reg;
+  const float* warm_u;
+  int32_t max_iter;
+  int32_t check_period;
+  double stop_thr;
+  int32_t anderson_depth;
+  int32_t timeout_ms;
+  float* out_u;
+  float* out_v;
+  int32_t* status;
+  int32_t* niter;
+  double* err;
+  void* workspace;
+  size_t workspace_bytes;
+} OtgPairsProblem;
+size_t otg_pairs_workspace_bytes(int32_t npairs, int64_t n, int64_t m, int32_t d, int32_t anderson_depth);
+/* Each pair's largest squared distance max_ij |x_i - y_j|^2 (device, P
+ * doubles), from one max-only pass on the tensor cores. */
+int otg_pairs_max_cost(const OtgPairsProblem* q, double* maxc, cudaStream_t stream);
+int otg_sinkhorn_pairs(const OtgPairsProblem* q, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
  * Online ("lazy") log-domain Sinkhorn on point clouds with squared-Euclidean
  * cost that is never stored: cost tiles |x|^2 + |y|^2 - 2 x.y come from
  * tcgen05 MMAs on high/low half planes of the points (prescaled by the

@@ -52,6 +52,14 @@ class OtgMultiProblem(ctypes.Structure):
                 ("anderson_ws_bytes", c_sz)]
 
 
+class OtgPairsProblem(ctypes.Structure):
+    _fields_ = [("X", c_vp), ("Y", c_vp), ("npairs", c_i32), ("d", c_i32), ("n", c_i64), ("m", c_i64), ("a", c_vp),
+                ("b", c_vp), ("reg", c_vp), ("warm_u", c_vp), ("max_iter", c_i32), ("check_period", c_i32),
+                ("stop_thr", c_dbl), ("anderson_depth", c_i32), ("timeout_ms", c_i32), ("out_u", c_vp),
+                ("out_v", c_vp), ("status", c_vp), ("niter", c_vp), ("err", c_vp), ("workspace", c_vp),
+                ("workspace_bytes", c_sz)]
+
+
 class OtgCostTable(ctypes.Structure):
     _fields_ = [("dtype", c_i32), ("nprob", c_i32), ("X", c_vp), ("Y", c_vp), ("x_off", c_vp), ("y_off", c_vp),
                 ("rows", c_vp), ("cols", c_vp), ("dim", c_vp), ("max_dim", c_i32), ("M", c_vp), ("m_off", c_vp),
@@ -113,6 +121,9 @@ SIGNATURES = {
     "otg_multi_workspace_bytes": (c_sz, [ctypes.c_int, c_i32, c_i64, c_i64, c_i64]),
     "otg_sinkhorn_multi": (ctypes.c_int, [ctypes.POINTER(OtgMultiProblem), c_vp]),
     "otg_multi_anderson_bytes": (c_sz, [ctypes.c_int, c_i32, c_i64, c_i32]),
+    "otg_pairs_workspace_bytes": (c_sz, [c_i32, c_i64, c_i64, c_i32, c_i32]),
+    "otg_pairs_max_cost": (ctypes.c_int, [ctypes.POINTER(OtgPairsProblem), c_vp, c_vp]),
+    "otg_sinkhorn_pairs": (ctypes.c_int, [ctypes.POINTER(OtgPairsProblem), c_vp]),
     "otg_online_workspace_bytes": (c_sz, [c_i64, c_i64, c_i32]),
     "otg_sinkhorn_online": (ctypes.c_int, [ctypes.POINTER(OtgOnlineProblem), c_vp]),
     "otg_batched_sqdist": (ctypes.c_int, [ctypes.POINTER(OtgCostTable), c_i32, c_vp]),

@@ -475,6 +475,67 @@ def solve_sample_ragged(Xs, Ys, reg, as_=None, bs=None, reg_relative=False, max_
 
 
 # ---------------------------------------------------------------------------
+# Equal-size cloud pairs with the cost rebuilt on the tensor cores
+# ---------------------------------------------------------------------------
+def _pairs_problem(X, Y, anderson=0):
+    lib = _lib.load()
+    P, n, d = X.shape
+    m = Y.shape[1]
+    wsb = lib.otg_pairs_workspace_bytes(P, n, m, d, int(anderson))
+    ws = torch.empty(wsb, dtype=torch.uint8, device=X.device)
+    q = _lib.OtgPairsProblem(X=X.data_ptr(), Y=Y.data_ptr(), npairs=P, d=d, n=n, m=m, anderson_depth=int(anderson),
+                             workspace=ws.data_ptr(), workspace_bytes=wsb)
+    return lib, q, ws
+
+
+def pairs_max_cost(X, Y):
+    """Largest squared distance max_ij |x_i - y_j|^2 of every pair of X
+    (P, n, d) and Y (P, m, d), float32 device tensors: (P,) float64, from
+    one max-only pass on the tensor cores (otg_pairs_max_cost)."""
+    X, Y = X.float().contiguous(), Y.float().contiguous()
+    lib, q, ws = _pairs_problem(X, Y)
+    out = torch.empty(X.shape[0], dtype=torch.float64, device=X.device)
+    _lib.check(lib.otg_pairs_max_cost(ctypes.byref(q), _lib.ptr(out), _lib.stream_handle(X.device)),
+               "otg_pairs_max_cost")
+    return out
+
+
+def run_pairs(X, Y, reg, a=None, b=None, max_iter=100000, tol=1e-6, warm_u=None, check_period=10, anderson=0,
+              timeout_ms=0):
+    """Log-domain solves of P equal-size cloud pairs, X (P, n, d), Y (P, m, d)
+    float32 on the device, squared-Euclidean cost never stored: every pass
+    rebuilds cost tiles from the points on the tensor cores
+    (otg_sinkhorn_pairs).  Per pair the iteration and stop test of
+    ``run_multi`` (sinkhorn_log order, column-marginal L2 error every
+    ``check_period`` iterations, each pair on its own; ``anderson`` > 0 mixes
+    the v updates).  ``reg``: (P,) absolute values.  Returns (u, v, status,
+    niter, err) with u (P, n), v (P, m) natural-log potentials."""
+    X, Y = X.float().contiguous(), Y.float().contiguous()
+    P, n, _ = X.shape
+    m = Y.shape[1]
+    dev = X.device
+    lib, q, ws = _pairs_problem(X, Y, anderson)
+    reg_t = torch.as_tensor(reg, dtype=torch.float64, device=dev).reshape(-1)
+    if reg_t.numel() == 1:
+        reg_t = reg_t.expand(P).contiguous()
+    a = torch.full((P, n), 1.0 / n, dtype=torch.float32, device=dev) if a is None else a.float().contiguous()
+    b = torch.full((P, m), 1.0 / m, dtype=torch.float32, device=dev) if b is None else b.float().contiguous()
+    u = torch.empty((P, n), dtype=torch.float32, device=dev)
+    v = torch.empty((P, m), dtype=torch.float32, device=dev)
+    status = torch.empty(P, dtype=torch.int32, device=dev)
+    niter = torch.empty(P, dtype=torch.int32, device=dev)
+    err = torch.empty(P, dtype=torch.float64, device=dev)
+    wu = None if warm_u is None else warm_u.float().reshape(P, n).contiguous()
+    q.a, q.b, q.reg = a.data_ptr(), b.data_ptr(), reg_t.data_ptr()
+    q.warm_u = wu.data_ptr() if wu is not None else None
+    q.max_iter, q.check_period, q.stop_thr, q.timeout_ms = int(max_iter), int(check_period), float(tol), int(timeout_ms)
+    q.out_u, q.out_v = u.data_ptr(), v.data_ptr()
+    q.status, q.niter, q.err = status.data_ptr(), niter.data_ptr(), err.data_ptr()
+    _lib.check(lib.otg_sinkhorn_pairs(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_pairs")
+    return u, v, status, niter, err
+
+
+# ---------------------------------------------------------------------------
 # Batched (fused) Gromov-Wasserstein
 # ---------------------------------------------------------------------------
 def _bgemm(A, B, ta, tb, out, alpha=1.0, beta=0.0):

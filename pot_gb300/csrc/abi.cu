@@ -211,6 +211,30 @@ namespace {
   X(ld_add) \
   X(s_add)
 
+#define OTG_FIELDS_OtgPairsProblem(X) \
+  X(X) \
+  X(Y) \
+  X(npairs) \
+  X(d) \
+  X(n) \
+  X(m) \
+  X(a) \
+  X(b) \
+  X(reg) \
+  X(warm_u) \
+  X(max_iter) \
+  X(check_period) \
+  X(stop_thr) \
+  X(anderson_depth) \
+  X(timeout_ms) \
+  X(out_u) \
+  X(out_v) \
+  X(status) \
+  X(niter) \
+  X(err) \
+  X(workspace) \
+  X(workspace_bytes)
+
 template <typename S>
 int write_layout(int64_t* out, int32_t cap, const size_t* offs, int nf) {
   if (cap < nf + 1) return OTG_ERR_ARG;
@@ -270,6 +294,12 @@ extern "C" int otg_abi_layout(const char* name, int64_t* out, int32_t cap) {
     static const size_t offs[] = {OTG_FIELDS_OtgSplitGemm(X)};
 #undef X
     return write_layout<OtgSplitGemm>(out, cap, offs, (int)(sizeof(offs) / sizeof(offs[0])));
+  }
+  if (std::strcmp(name, "OtgPairsProblem") == 0) {
+#define X(fld) offsetof(OtgPairsProblem, fld),
+    static const size_t offs[] = {OTG_FIELDS_OtgPairsProblem(X)};
+#undef X
+    return write_layout<OtgPairsProblem>(out, cap, offs, (int)(sizeof(offs) / sizeof(offs[0])));
   }
   return OTG_ERR_ARG;
 }

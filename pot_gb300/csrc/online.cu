@@ -24,10 +24,12 @@
 #include <cuda_fp16.h>
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include "common.cuh"
 #include "tma.cuh"
 #include "tc.cuh"
+#include "anderson.cuh"
 #include "../../include/pot_gb300.h"
 
 namespace otg {
@@ -380,6 +382,185 @@ __global__ void neg_kernel(const float* x, int64_t n, float* out) {
     out[i] = -x[i];
 }
 
+// ---------------------------------------------------------------------------
+// Batched pair solves (otg_sinkhorn_pairs): the cost of every pass rebuilt
+// from the points by online_pass_kernel over the active pairs.
+// ---------------------------------------------------------------------------
+struct PairsState {
+  int P;
+  int n, m;                   // valid rows per pair (X side, Y side)
+  int64_t n_pad, m_pad;       // padded rows per pair
+  const float* a; const float* b;     // caller's weights, P x n, P x m
+  float* u2;                  // X side potential, base 2, P x n_pad
+  float* v2[2];               // Y side potential, base 2, double-buffered
+  float* xk; float* yk;       // |x|^2 log2(e)/reg_p, |y|^2 log2(e)/reg_p
+  float* hx; float* hy;       // streamed-side vectors of the next pass
+  double* erow;               // per-row squared column-marginal violations (Y side)
+  const int* act; const int* cnt;     // active pair list in use and its length
+  int* act_next; int* cnt_next;       // the list after a decision
+  int* flag;                  // per active slot: leaves at this decision
+  float* out_u; float* out_v;
+  int32_t* status; int32_t* niter; double* err;
+  double stop_thr;
+  // Anderson history
+  int depth;
+  float* aF; float* aR; double* aG; int32_t* acnt;
+};
+
+// One warp per point: fp16 high/low planes of scale * x (pair p's rows from
+// p * ld_rows) and the raw squared norm |x|^2.
+__global__ void prep_pairs_kernel(const float* __restrict__ X, int P, int n, int d, int64_t n_pad, float scale,
+                                  __half* hi, __half* lo, int64_t ld, float* norm) {
+  const int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (g >= (int64_t)P * n) return;
+  const int64_t p = g / n, i = g % n, row = p * n_pad + i;
+  float s = 0.f;
+  for (int k = lane; k < d; k += 32) {
+    const float x = X[g * d + k];
+    s = fmaf(x, x, s);
+    const float xs = x * scale;
+    const __half h = __float2half_rn(xs);
+    hi[row * ld + k] = h;
+    lo[row * ld + k] = __float2half_rn(xs - __half2float(h));
+  }
+  s = warp_sum(s);
+  if (lane == 0) norm[row] = s;
+}
+
+// max-only pass inputs: h = |y|^2 (-inf on padding rows)
+__global__ void pairs_hmax_kernel(const float* __restrict__ yn, int P, int m, int64_t m_pad, float* h) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)P * m_pad;
+       e += (int64_t)gridDim.x * blockDim.x)
+    h[e] = (e % m_pad) < m ? yn[e] : -INFINITY;
+}
+
+// Per pair: the largest row max (one CTA per pair).
+__global__ void pairs_max_finish_kernel(const float* __restrict__ rowmax, int n, int64_t n_pad, double* maxc) {
+  __shared__ float red[32];
+  float x = -INFINITY;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x = fmaxf(x, rowmax[(int64_t)blockIdx.x * n_pad + i]);
+  x = warp_max(x);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = -INFINITY;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t = fmaxf(t, red[k]);
+    maxc[blockIdx.x] = (double)t;
+  }
+}
+
+// Per pair: k2 = log2(e) / reg and the pass factor alpha = 2 k2 / (sx sy).
+__global__ void pairs_scale_kernel(const double* __restrict__ reg, int P, double sxy, float* k2, float* alpha) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+    const double k = OTG_LOG2E / reg[p];
+    k2[p] = (float)k;
+    alpha[p] = (float)(2.0 * k / sxy);
+  }
+}
+
+// One side's per-row vectors: scaled norms nk = |x|^2 k2 and -nk, log2 of
+// the weights, the starting potential (base 2; warm: natural log) and the h
+// of the first pass that streams this side (pot - nk; -inf on padding rows).
+__global__ void pairs_side_kernel(const float* __restrict__ norm, const float* __restrict__ k2, const float* w,
+                                  const float* warm, int P, int n, int64_t n_pad, float* nk, float* neg_nk,
+                                  float* logw2, float* pot2, float* h) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)P * n_pad;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = e / n_pad, i = e % n_pad;
+    if (i < n) {
+      const float v = norm[e] * k2[p];
+      nk[e] = v;
+      neg_nk[e] = -v;
+      logw2[e] = lg2(w[p * n + i]);
+      const float u0 = warm ? warm[p * n + i] * (float)OTG_LOG2E : 0.f;
+      if (pot2) pot2[e] = u0;
+      if (h) h[e] = u0 - v;
+    } else {
+      nk[e] = 0.f;
+      neg_nk[e] = 0.f;
+      logw2[e] = -INFINITY;
+      if (pot2) pot2[e] = 0.f;
+      if (h) h[e] = -INFINITY;
+    }
+  }
+}
+
+// Decision at a check (one CTA per active slot): the pair's error (its row
+// slots summed in a fixed order), convergence, and for a leaving pair its
+// outputs (the pair (u, v_old) in natural logs).  check = 0: no error was
+// measured (the pairs leave only at max_iter).
+__global__ void pairs_decide_kernel(PairsState S, const float* __restrict__ vold, int ii, int check, int at_max) {
+  const int slot = blockIdx.x;
+  if (slot >= __ldcg(S.cnt)) return;
+  const int p = __ldcg(S.act + slot);
+  double e = -1.0;
+  bool conv = false;
+  if (check) {
+    e = sqrt(block_sum_slots(S.erow + (int64_t)p * S.m_pad, S.m));
+    conv = e < S.stop_thr;
+  }
+  const bool leave = conv || at_max;
+  if (leave) {
+    const float LN2 = (float)OTG_LN2;
+    for (int i = threadIdx.x; i < S.n; i += blockDim.x) S.out_u[(int64_t)p * S.n + i] = S.u2[(int64_t)p * S.n_pad + i] * LN2;
+    for (int j = threadIdx.x; j < S.m; j += blockDim.x) S.out_v[(int64_t)p * S.m + j] = vold[(int64_t)p * S.m_pad + j] * LN2;
+    if (threadIdx.x == 0) {
+      S.status[p] = conv ? OTG_STATUS_CONVERGED : OTG_STATUS_MAXITER;
+      S.niter[p] = ii - 1;
+      S.err[p] = e;
+    }
+  }
+  if (threadIdx.x == 0) S.flag[slot] = leave ? 1 : 0;
+}
+
+// The active list without the leaving pairs (one CTA, block-wide scan).
+__global__ void __launch_bounds__(1024) pairs_compact_kernel(PairsState S) {
+  __shared__ int s_warp[32];
+  __shared__ int s_base;
+  const int n = __ldcg(S.cnt);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_base = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+    const int k = c0 + threadIdx.x;
+    const int keep = k < n && !__ldcg(S.flag + k);
+    int inc = keep;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int up = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += up;
+    }
+    if (lane == 31) s_warp[wid] = inc;
+    __syncthreads();
+    int before = s_base;
+    for (int w = 0; w < wid; ++w) before += s_warp[w];
+    if (keep) S.act_next[before + inc - 1] = __ldcg(S.act + k);
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s_base += s_warp[w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *S.cnt_next = s_base;
+}
+
+// Anderson mixing of the new v of every active pair, then the h of the next
+// pass (which streams the Y side) from the mixed v.
+__global__ void pairs_anderson_kernel(PairsState S, const float* __restrict__ vold, float* vnew) {
+  const int slot = blockIdx.x;
+  if (slot >= __ldcg(S.cnt)) return;
+  const int p = __ldcg(S.act + slot);
+  const int64_t co = (int64_t)p * S.m_pad;
+  anderson_step<float>(S.depth, S.m, co, (int64_t)S.P * S.m_pad, vold, vnew, S.aF, S.aR,
+                       S.aG + (int64_t)p * S.depth * S.depth, S.acnt + p);
+  for (int64_t j = threadIdx.x; j < S.m_pad; j += blockDim.x)
+    S.hy[co + j] = j < S.m ? vnew[co + j] - S.yk[co + j] : -INFINITY;
+}
+
+__global__ void fill_int_kernel(int* x, int n, int v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = v < 0 ? i : v;
+}
+
 }  // namespace otg
 
 using namespace otg;
@@ -583,6 +764,292 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
   p->info[1] = niter;
   p->info[2] = nchk;
   return OTG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched pair solves: host side
+// ---------------------------------------------------------------------------
+namespace {
+
+struct PairsLayout {
+  int64_t n_pad, m_pad;
+  int dp;
+  size_t xh, xl, yh, yl, xn, yn, xk, nxk, la2, wa, u2, hx, yk, nyk, lb2, wb, v0, v1, hy, erow, k2, alpha, act0,
+      act1, cnt, flag, aF, aR, aG, acnt, total;
+};
+
+PairsLayout pairs_layout(int64_t P, int64_t n, int64_t m, int d, int depth) {
+  PairsLayout L{};
+  L.n_pad = (n + 127) / 128 * 128;
+  L.m_pad = (m + 127) / 128 * 128;
+  L.dp = (d + 63) / 64 * 64;
+  size_t off = 0;
+  auto take = [&](size_t bytes) { const size_t o = off; off += a16(bytes); return o; };
+  const size_t nx = (size_t)(P * L.n_pad), ny = (size_t)(P * L.m_pad);
+  L.xh = take(2 * nx * L.dp); L.xl = take(2 * nx * L.dp);
+  L.yh = take(2 * ny * L.dp); L.yl = take(2 * ny * L.dp);
+  L.xn = take(4 * nx); L.yn = take(4 * ny);
+  L.xk = take(4 * nx); L.nxk = take(4 * nx); L.la2 = take(4 * nx); L.wa = take(4 * nx); L.u2 = take(4 * nx);
+  L.hx = take(4 * nx);
+  L.yk = take(4 * ny); L.nyk = take(4 * ny); L.lb2 = take(4 * ny); L.wb = take(4 * ny); L.v0 = take(4 * ny);
+  L.v1 = take(4 * ny); L.hy = take(4 * ny);
+  L.erow = take(8 * ny);
+  L.k2 = take(4 * (size_t)P); L.alpha = take(4 * (size_t)P);
+  L.act0 = take(4 * (size_t)P); L.act1 = take(4 * (size_t)P); L.cnt = take(64); L.flag = take(4 * (size_t)P);
+  if (depth > 0) {
+    L.aF = take(4 * (size_t)depth * ny); L.aR = take(4 * (size_t)depth * ny);
+    L.aG = take(8 * (size_t)P * depth * depth); L.acnt = take(4 * (size_t)P);
+  }
+  L.total = off;
+  return L;
+}
+
+int pairs_check(const OtgPairsProblem* q) {
+  if (!q || !q->X || !q->Y || !q->workspace) return OTG_ERR_ARG;
+  if (q->npairs < 1 || q->n < 1 || q->m < 1 || q->d < 1 || q->d > 64 * OL_MAXKT) return OTG_ERR_ARG;
+  if ((int64_t)q->npairs * ((q->n + 127) / 128 * 128) > INT32_MAX ||
+      (int64_t)q->npairs * ((q->m + 127) / 128 * 128) > INT32_MAX)
+    return OTG_ERR_ARG;  // TMA row coordinates are 32-bit
+  if (q->anderson_depth < 0 || q->anderson_depth > OTG_ANDERSON_MAX_DEPTH) return OTG_ERR_ARG;
+  if (q->workspace_bytes < pairs_layout(q->npairs, q->n, q->m, q->d, q->anderson_depth).total) return OTG_ERR_WORKSPACE;
+  return OTG_OK;
+}
+
+bool pairs_attr() {
+  static bool done = false;
+  if (done) return true;
+  if (cudaFuncSetAttribute(online_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(online_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) !=
+          cudaSuccess)
+    return false;
+  done = true;
+  return true;
+}
+
+// Planes and raw norms of both sides; returns the prescales through sx, sy.
+int pairs_prep(const OtgPairsProblem* q, const PairsLayout& L, char* w, float* max_abs_host, cudaStream_t st,
+               CUtensorMap* mx_h, CUtensorMap* mx_l, CUtensorMap* my_h, CUtensorMap* my_l) {
+  const int P = q->npairs, d = q->d;
+  __half* xh = reinterpret_cast<__half*>(w + L.xh);
+  __half* xl = reinterpret_cast<__half*>(w + L.xl);
+  __half* yh = reinterpret_cast<__half*>(w + L.yh);
+  __half* yl = reinterpret_cast<__half*>(w + L.yl);
+  // planes are zero beyond the data
+  if (cudaMemsetAsync(w + L.xh, 0, L.xn - L.xh, st) != cudaSuccess) return OTG_ERR_CUDA;
+  const float sx = max_abs_host[0], sy = max_abs_host[1];
+  const int64_t gx = (int64_t)P * q->n, gy = (int64_t)P * q->m;
+  prep_pairs_kernel<<<(unsigned)((gx + 7) / 8), 256, 0, st>>>(q->X, P, (int)q->n, d, L.n_pad, sx, xh, xl, L.dp,
+                                                             reinterpret_cast<float*>(w + L.xn));
+  prep_pairs_kernel<<<(unsigned)((gy + 7) / 8), 256, 0, st>>>(q->Y, P, (int)q->m, d, L.m_pad, sy, yh, yl, L.dp,
+                                                             reinterpret_cast<float*>(w + L.yn));
+  if (cudaGetLastError() != cudaSuccess) return OTG_ERR_CUDA;
+  if (!ol_plane_map(mx_h, xh, (int64_t)P * L.n_pad, L.dp) || !ol_plane_map(mx_l, xl, (int64_t)P * L.n_pad, L.dp) ||
+      !ol_plane_map(my_h, yh, (int64_t)P * L.m_pad, L.dp) || !ol_plane_map(my_l, yl, (int64_t)P * L.m_pad, L.dp))
+    return OTG_ERR_CUDA;
+  return OTG_OK;
+}
+
+// Power-of-two prescale of a cloud set from its largest magnitude (the
+// planes' high parts then sit near 2^14).
+float pow2_prescale(float max_abs) {
+  if (!(max_abs > 0.f)) return 1.f;
+  return std::ldexp(1.0f, 14 - (int)std::ceil(std::log2((double)max_abs)));
+}
+
+__global__ void absmax_kernel(const float* __restrict__ x, int64_t n, unsigned* out) {
+  float m = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[i]));
+  m = warp_max(m);
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));  // max of non-negative floats
+}
+
+int pairs_scales(const OtgPairsProblem* q, char* w, const PairsLayout& L, cudaStream_t st, float* sxy) {
+  unsigned* tmp = reinterpret_cast<unsigned*>(w + L.cnt) + 8;  // two scratch words of the control block
+  if (cudaMemsetAsync(tmp, 0, 8, st) != cudaSuccess) return OTG_ERR_CUDA;
+  absmax_kernel<<<304, 256, 0, st>>>(q->X, (int64_t)q->npairs * q->n * q->d, tmp);
+  absmax_kernel<<<304, 256, 0, st>>>(q->Y, (int64_t)q->npairs * q->m * q->d, tmp + 1);
+  unsigned hb[2] = {0u, 0u};
+  if (cudaMemcpyAsync(hb, tmp, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return OTG_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return OTG_ERR_CUDA;
+  float fx, fy;
+  std::memcpy(&fx, hb, 4);
+  std::memcpy(&fy, hb + 1, 4);
+  sxy[0] = pow2_prescale(fx);
+  sxy[1] = pow2_prescale(fy);
+  return OTG_OK;
+}
+
+OnlinePass pairs_pass(const PairsLayout& L, char* w, bool x_resident, int n_rows, int tiles, int kt,
+                      const int* act, const int* cnt, int* abort_flag, uint64_t tmo) {
+  OnlinePass A{};
+  A.n_rows = n_rows;
+  A.col_tiles = tiles;
+  A.k_tiles = kt;
+  A.active = act;
+  A.count = cnt;
+  A.nrb = (int)((x_resident ? L.n_pad : L.m_pad) / OL_M);
+  A.rows_per_pair = x_resident ? L.n_pad : L.m_pad;
+  A.cols_per_pair = x_resident ? L.m_pad : L.n_pad;
+  A.rows_pad = (int)A.rows_per_pair;
+  A.split = 1;
+  A.alpha_p = reinterpret_cast<const float*>(w + L.alpha);
+  A.abort_flag = abort_flag;
+  A.timeout_ns = tmo;
+  return A;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t otg_pairs_workspace_bytes(int32_t npairs, int64_t n, int64_t m, int32_t d, int32_t anderson_depth) {
+  return pairs_layout(npairs, n, m, d, anderson_depth).total;
+}
+
+int otg_pairs_max_cost(const OtgPairsProblem* q, double* maxc, cudaStream_t st) {
+  int rc = pairs_check(q);
+  if (rc != OTG_OK) return rc;
+  if (!maxc) return OTG_ERR_ARG;
+  if (!ol_encode_fn() || !pairs_attr()) return OTG_ERR_CUDA;
+  const PairsLayout L = pairs_layout(q->npairs, q->n, q->m, q->d, q->anderson_depth);
+  char* w = static_cast<char*>(q->workspace);
+  const int P = q->npairs;
+  float sxy[2];
+  if ((rc = pairs_scales(q, w, L, st, sxy)) != OTG_OK) return rc;
+  CUtensorMap mxh, mxl, myh, myl;
+  if ((rc = pairs_prep(q, L, w, sxy, st, &mxh, &mxl, &myh, &myl)) != OTG_OK) return rc;
+  int* cnt = reinterpret_cast<int*>(w + L.cnt);
+  int* abort_flag = cnt + 4;
+  int* act = reinterpret_cast<int*>(w + L.act0);
+  if (cudaMemsetAsync(cnt, 0, 32, st) != cudaSuccess) return OTG_ERR_CUDA;
+  fill_int_kernel<<<(P + 255) / 256, 256, 0, st>>>(act, P, -1);
+  fill_int_kernel<<<1, 32, 0, st>>>(cnt, 1, P);
+  float* h = reinterpret_cast<float*>(w + L.hy);
+  pairs_hmax_kernel<<<1024, 256, 0, st>>>(reinterpret_cast<const float*>(w + L.yn), P, (int)q->m, L.m_pad, h);
+  // t = |y|^2 - 2 x.y, row max + |x|^2 = max_j |x_i - y_j|^2
+  OnlinePass A = pairs_pass(L, w, true, (int)q->n, (int)(L.m_pad / OL_N), L.dp / OL_K, act, cnt, abort_flag,
+                            q->timeout_ms > 0 ? (uint64_t)q->timeout_ms * 1000000ull : 4000000000ull);
+  A.alpha_p = nullptr;
+  A.alpha = (float)(-2.0 / ((double)sxy[0] * (double)sxy[1]));
+  A.h = h;
+  A.rterm = reinterpret_cast<const float*>(w + L.xn);
+  float* rowmax = reinterpret_cast<float*>(w + L.u2);
+  A.pot_out2 = rowmax;
+  online_pass_kernel<true><<<(unsigned)(P * A.nrb), OL_THREADS, OL_SMEM, st>>>(mxh, mxl, myh, myl, A);
+  pairs_max_finish_kernel<<<P, 256, 0, st>>>(rowmax, (int)q->n, L.n_pad, maxc);
+  int hflag = 0;
+  if (cudaMemcpyAsync(&hflag, abort_flag, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return OTG_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return OTG_ERR_CUDA;
+  return hflag ? OTG_ERR_CUDA : OTG_OK;
+}
+
+int otg_sinkhorn_pairs(const OtgPairsProblem* q, cudaStream_t st) {
+  int rc = pairs_check(q);
+  if (rc != OTG_OK) return rc;
+  if (!q->a || !q->b || !q->reg || !q->out_u || !q->out_v || !q->status || !q->niter || !q->err || q->max_iter < 1)
+    return OTG_ERR_ARG;
+  if (!ol_encode_fn() || !pairs_attr()) return OTG_ERR_CUDA;
+  const PairsLayout L = pairs_layout(q->npairs, q->n, q->m, q->d, q->anderson_depth);
+  char* w = static_cast<char*>(q->workspace);
+  const int P = q->npairs, D = q->anderson_depth;
+  const int period = q->check_period > 0 ? q->check_period : 10;
+  const uint64_t tmo = q->timeout_ms > 0 ? (uint64_t)q->timeout_ms * 1000000ull : 4000000000ull;
+  float sxy[2];
+  if ((rc = pairs_scales(q, w, L, st, sxy)) != OTG_OK) return rc;
+  CUtensorMap mxh, mxl, myh, myl;
+  if ((rc = pairs_prep(q, L, w, sxy, st, &mxh, &mxl, &myh, &myl)) != OTG_OK) return rc;
+  auto F = [&](size_t off) { return reinterpret_cast<float*>(w + off); };
+  int* cnt = reinterpret_cast<int*>(w + L.cnt);  // [0], [1] list lengths, [4] abort flag
+  int* abort_flag = cnt + 4;
+  int* act[2] = {reinterpret_cast<int*>(w + L.act0), reinterpret_cast<int*>(w + L.act1)};
+  if (cudaMemsetAsync(cnt, 0, 32, st) != cudaSuccess) return OTG_ERR_CUDA;
+  pairs_scale_kernel<<<(P + 255) / 256, 256, 0, st>>>(q->reg, P, (double)sxy[0] * (double)sxy[1], F(L.k2),
+                                                     F(L.alpha));
+  pairs_side_kernel<<<1024, 256, 0, st>>>(F(L.xn), F(L.k2), q->a, q->warm_u, P, (int)q->n, L.n_pad, F(L.xk),
+                                          F(L.nxk), F(L.la2), F(L.u2), F(L.hx));
+  pairs_side_kernel<<<1024, 256, 0, st>>>(F(L.yn), F(L.k2), q->b, nullptr, P, (int)q->m, L.m_pad, F(L.yk),
+                                          F(L.nyk), F(L.lb2), F(L.v0), nullptr);
+  // weights in the padded layout (the check reads them per resident row)
+  {
+    // logw2 = log2 w on valid rows: w = 2^logw2 exactly enough for the check
+    // would round twice; copy the weights themselves instead
+    const int64_t ex = (int64_t)P * L.n_pad, ey = (int64_t)P * L.m_pad;
+    float* wa = F(L.wa);
+    float* wb = F(L.wb);
+    if (cudaMemsetAsync(wa, 0, 4 * ex, st) != cudaSuccess || cudaMemsetAsync(wb, 0, 4 * ey, st) != cudaSuccess)
+      return OTG_ERR_CUDA;
+    if (cudaMemcpy2DAsync(wa, 4 * L.n_pad, q->a, 4 * q->n, 4 * q->n, P, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+        cudaMemcpy2DAsync(wb, 4 * L.m_pad, q->b, 4 * q->m, 4 * q->m, P, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return OTG_ERR_CUDA;
+  }
+  fill_int_kernel<<<(P + 255) / 256, 256, 0, st>>>(act[0], P, -1);
+  fill_int_kernel<<<1, 32, 0, st>>>(cnt, 1, P);
+  if (D > 0 && cudaMemsetAsync(w + L.acnt, 0, 4 * (size_t)P, st) != cudaSuccess) return OTG_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return OTG_ERR_CUDA;
+
+  PairsState S{};
+  S.P = P; S.n = (int)q->n; S.m = (int)q->m; S.n_pad = L.n_pad; S.m_pad = L.m_pad;
+  S.a = q->a; S.b = q->b;
+  S.u2 = F(L.u2); S.v2[0] = F(L.v0); S.v2[1] = F(L.v1);
+  S.xk = F(L.xk); S.yk = F(L.yk); S.hx = F(L.hx); S.hy = F(L.hy);
+  S.erow = reinterpret_cast<double*>(w + L.erow);
+  S.flag = reinterpret_cast<int*>(w + L.flag);
+  S.out_u = q->out_u; S.out_v = q->out_v; S.status = q->status; S.niter = q->niter; S.err = q->err;
+  S.stop_thr = q->stop_thr;
+  S.depth = D;
+  if (D > 0) {
+    S.aF = F(L.aF); S.aR = F(L.aR); S.aG = reinterpret_cast<double*>(w + L.aG);
+    S.acnt = reinterpret_cast<int32_t*>(w + L.acnt);
+  }
+  const int kt = L.dp / OL_K;
+  const int nrb_x = (int)(L.n_pad / OL_M), nrb_y = (int)(L.m_pad / OL_M);
+  int nact = P, sel = 0, cur = 0;
+  bool prev_check = false;
+  for (int ii = 0;; ++ii) {
+    const bool at_max = ii == q->max_iter;
+    S.act = act[sel]; S.cnt = cnt + sel; S.act_next = act[sel ^ 1]; S.cnt_next = cnt + (sel ^ 1);
+    if (at_max && !prev_check) {
+      // every pair left ends without a final check (state of iteration ii-1)
+      pairs_decide_kernel<<<nact, 256, 0, st>>>(S, S.v2[cur], ii, 0, 1);
+      break;
+    }
+    // column update (resident Y, streamed X): v_new; on check iterations the
+    // squared column-marginal violation of (u, v_old) per row
+    OnlinePass G = pairs_pass(L, w, false, (int)q->m, nrb_x, kt, S.act, S.cnt, abort_flag, tmo);
+    G.h = S.hx; G.rterm = F(L.nyk); G.logw2 = F(L.lb2); G.pot2 = S.v2[cur]; G.w = F(L.wb);
+    G.pot_out2 = S.v2[cur ^ 1]; G.other_norm2 = S.yk; G.h_out = S.hy; G.err = prev_check ? S.erow : nullptr;
+    G.err_sq = 1;
+    online_pass_kernel<false><<<(unsigned)(nact * nrb_y), OL_THREADS, OL_SMEM, st>>>(myh, myl, mxh, mxl, G);
+    if (prev_check || at_max) {
+      pairs_decide_kernel<<<nact, 256, 0, st>>>(S, S.v2[cur], ii, prev_check ? 1 : 0, at_max ? 1 : 0);
+      pairs_compact_kernel<<<1, 1024, 0, st>>>(S);
+      sel ^= 1;
+      S.act = act[sel]; S.cnt = cnt + sel; S.act_next = act[sel ^ 1]; S.cnt_next = cnt + (sel ^ 1);
+      int hc[8];
+      if (cudaMemcpyAsync(hc, cnt, 32, cudaMemcpyDeviceToHost, st) != cudaSuccess) return OTG_ERR_CUDA;
+      if (cudaStreamSynchronize(st) != cudaSuccess) return OTG_ERR_CUDA;
+      if (hc[4]) return OTG_ERR_CUDA;  // a bounded device wait ran out
+      nact = hc[sel];
+      if (nact == 0 || at_max) break;
+    }
+    if (D > 0 && ii >= 1) pairs_anderson_kernel<<<nact, 256, 0, st>>>(S, S.v2[cur], S.v2[cur ^ 1]);
+    // row update (resident X, streamed Y): u, and the h of the next column update
+    OnlinePass Fp = pairs_pass(L, w, true, (int)q->n, nrb_y, kt, S.act, S.cnt, abort_flag, tmo);
+    Fp.h = S.hy; Fp.rterm = F(L.nxk); Fp.logw2 = F(L.la2); Fp.pot2 = S.u2; Fp.w = F(L.wa);
+    Fp.pot_out2 = S.u2; Fp.other_norm2 = S.xk; Fp.h_out = S.hx;
+    online_pass_kernel<false><<<(unsigned)(nact * nrb_x), OL_THREADS, OL_SMEM, st>>>(mxh, mxl, myh, myl, Fp);
+    if (cudaGetLastError() != cudaSuccess) return OTG_ERR_CUDA;
+    cur ^= 1;
+    prev_check = ii % period == 0;
+  }
+  int hflag = 0;
+  if (cudaMemcpyAsync(&hflag, abort_flag, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return OTG_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return OTG_ERR_CUDA;
+  return hflag ? OTG_ERR_CUDA : OTG_OK;
 }
 
 }  // extern "C"

@@ -40,17 +40,28 @@ def gen_pairs(seed, count, n=2048, d=16, device=None):
 
 
 class PairSolver:
-    """Uniform-size batch of cloud pairs on the device: cost blocks, per-pair
-    max cost, and log-domain solves (zero or warm start)."""
+    """Uniform-size batch of cloud pairs on the device: per-pair max cost and
+    log-domain solves (zero or warm start).  engine "multi": the cost blocks
+    are stored (16 MiB per 2048 x 2048 pair) and every pass reads them
+    (otg_sinkhorn_multi); engine "online": nothing is stored, every pass
+    rebuilds the cost tiles from the points on the tensor cores
+    (otg_sinkhorn_pairs)."""
 
-    def __init__(self, X, Y, maxc=None, a=None, b=None):
+    def __init__(self, X, Y, maxc=None, a=None, b=None, engine="multi"):
         self.P, self.n, self.d = X.shape
         self.m = Y.shape[1]
+        self.engine = engine
+        self.X, self.Y = X, Y
         self.layout = pb.RaggedLayout([self.n] * self.P, [self.m] * self.P, torch.float32, X.device)
-        xo = np.arange(self.P) * self.n * self.d
-        yo = np.arange(self.P) * self.m * self.d
-        self.M, self.maxc = pb.batched_sqdist(self.layout, X.reshape(-1).contiguous(), Y.reshape(-1).contiguous(),
-                                              xo, yo, [self.d] * self.P, want_max=True)
+        if engine == "online":
+            self.M = None
+            self.maxc = pb.pairs_max_cost(X, Y).float() if maxc is None else maxc
+        else:
+            xo = np.arange(self.P) * self.n * self.d
+            yo = np.arange(self.P) * self.m * self.d
+            self.M, self.maxc = pb.batched_sqdist(self.layout, X.reshape(-1).contiguous(),
+                                                  Y.reshape(-1).contiguous(), xo, yo, [self.d] * self.P,
+                                                  want_max=True)
         if maxc is not None:  # cost scale of an enclosing problem (sub-sampled clouds)
             self.maxc = maxc
         self.a = (torch.full((self.P * self.n,), 1.0 / self.n, dtype=torch.float32, device=X.device) if a is None
@@ -66,6 +77,15 @@ class PairSolver:
         reg = self.maxc.double() * reg_rel
         if warm_u is not None:
             warm_u = warm_u.reshape(-1).contiguous()
+        if self.engine == "online":
+            if events is not None:
+                events[0].record()
+            u, v, status, niter, err = pb.run_pairs(self.X, self.Y, reg, self.a.view(self.P, self.n),
+                                                    self.b.view(self.P, self.m), max_iter, tol, warm_u=warm_u,
+                                                    check_period=check_period, anderson=anderson)
+            if events is not None:
+                events[1].record()
+            return u, v, status, niter, err
         if engine == "multi":
             u, v, status, niter, err, _ = pb.run_multi(self.layout, self.M, self.a, self.b, reg, max_iter, tol,
                                                        warm_u=warm_u, events=events, omega=omega,

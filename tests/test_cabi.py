@@ -69,6 +69,8 @@ def test_invalid_arguments_are_rejected_before_any_device_work():
     assert lib.otg_sinkhorn_dense(None, None, None) == ERR_ARG
     assert lib.otg_sinkhorn_dense_noalloc(None, None, None, None) == ERR_ARG
     assert lib.otg_sinkhorn_multi(None, None) == ERR_ARG
+    assert lib.otg_sinkhorn_pairs(None, None) == ERR_ARG
+    assert lib.otg_pairs_max_cost(None, None, None) == ERR_ARG
     assert lib.otg_batched_sqdist(None, 1, None) == ERR_ARG
     assert lib.otg_dense_plan(0, 1, None, 4, 4, 4, None, None, 1.0, None, 0, None, None) == ERR_ARG
     assert lib.otg_gibbs_kernel(0, None, 4, 4, 4, 1.0, None, 4, None) == ERR_ARG
