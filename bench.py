@@ -574,6 +574,39 @@ def run_small(args, pk):
                          "alg_bytes_per_launch": alg}}
 
 
+def run_solve(args, pk):
+    """One arm of the warm-start workload alone (profiling runs): `args.batch`
+    cloud pairs (n = m = 2048, d = 16), plain zero-started solve or (with
+    --warm) prior + Anderson, stop test every iteration, on the stored-cost
+    engine (multi_sinkhorn_kernel) or the online engine (otg_sinkhorn_pairs);
+    the first `warmup` solves are untimed."""
+    import torch
+    from pot_gb300.warmstart import pipeline as wp
+    dev = torch.device("cuda", _WS["local"])
+    X, Y = wp.gen_pairs(EVAL_SEED, args.batch, WS_N, WS_D, dev)
+    st = torch.cuda.current_stream()
+
+    def one():
+        ps = wp.PairSolver(X, Y, engine=args.engine)
+        wu = wp.prior_potential(X, Y, ps, WS_REG) if args.warm else None
+        return ps.solve(WS_REG, WS_TOL, warm_u=wu, check_period=1, anderson=wp.REFINE_ANDERSON if args.warm else 0)
+
+    for _ in range(args.warmup):
+        one()
+    ms = []
+    for _ in range(args.steps):
+        out, t = _timed(one, st)
+        ms.append(t)
+    per = statistics.median(ms)
+    return {"metric": "cloud-pair solves/s (one arm)", "value": args.batch / (per * 1e-3), "unit": "solves/s",
+            "ms_per_step": per, "dtype": "f32",
+            "config": {"workload": "%s arm, %d GMM cloud pairs n=m=%d d=%d, reg=%.2f x max cost, stopThr=%g, "
+                                   "test every iteration, engine %s" % ("warm" if args.warm else "plain",
+                                                                         args.batch, WS_N, WS_D, WS_REG, WS_TOL,
+                                                                         args.engine),
+                       "niter_mean": float(out[3].double().mean()), "converged": int((out[2] == 0).sum())}}
+
+
 def run_warm_eval(args, pk):
     """Held-out evaluation of the warm start on 10 batches of 1024 pairs
     (seeds after the headline batch's): the warm arm (multiscale prior +
@@ -788,6 +821,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-aux", action="store_true")
     ap.add_argument("--arms", default="", help="warm-start workload: comma list of ablation arms to run")
+    ap.add_argument("--engine", default="multi", help="solve workload: multi (stored cost) or online")
+    ap.add_argument("--warm", action="store_true", help="solve workload: prior + Anderson instead of plain")
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--iters", type=int, default=20)
     ap.add_argument("--full", type=int, default=0)
@@ -811,7 +846,7 @@ def main():
     pk = peaks()
     if args.workload != "warmstart":
         fn = {"online": run_online, "gw": run_gw, "ragged": run_ragged, "dense": run_dense,
-              "batch": run_batch, "small": run_small, "tail": run_tail,
+              "batch": run_batch, "small": run_small, "tail": run_tail, "solve": run_solve,
               "warm_eval": run_warm_eval}[args.workload]
         line = {"n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                 "data": "synthetic"}
