@@ -39,7 +39,7 @@ def test_max_cost_matches_float64(cuda, n, m, d):
 @pytest.mark.parametrize("n,m,d", [(200, 333, 3), (256, 128, 16)])
 @pytest.mark.parametrize("anderson", [0, 5])
 def test_pairs_vs_oracle(cuda, n, m, d, anderson):
-    P, reg_rel, tol = 6, 0.05, 1e-6
+    P, reg_rel, tol = 4, 0.05, 1e-6
     X, Y = _clouds(2 + d, P, n, m, d, cuda)
     g = torch.Generator(device="cpu").manual_seed(9)
     a = torch.distributions.Dirichlet(torch.ones(n)).sample((P,)).float().to(cuda)
@@ -57,7 +57,7 @@ def test_pairs_vs_oracle(cuda, n, m, d, anderson):
         Pg = np.exp(u[p].double().cpu().numpy()[:, None] - C / regs[p] + v[p].double().cpu().numpy()[None, :])
         assert np.linalg.norm(Pg.sum(0) - bp) < 2 * tol, p
         assert np.abs(Pg.sum(1) - ap).sum() < 1e-5, p
-        Pref, lg = oracle.sinkhorn_log(ap, bp, C, regs[p], numItermax=20000, stopThr=1e-12)
+        Pref, lg = oracle.sinkhorn_log(ap, bp, C, regs[p], numItermax=20000, stopThr=1e-9)
         assert np.abs(Pg - Pref).sum() / Pref.sum() < 1e-4, p
 
 
