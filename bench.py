@@ -164,18 +164,22 @@ def run_warmstart(args, pk):
     # learned residual network on top of the prior, each component alone,
     # over-relaxation instead of Anderson mixing, and the reference's
     # every-10th-iteration test schedule.
-    ARMS = {"warm": ("prior", 1.0, 1, AD), "plain": (None, 1.0, 1, 0),
-            "learned_anderson": ("net", 1.0, 1, AD), "zero_anderson": (None, 1.0, 1, AD),
-            "prior_plain": ("prior", 1.0, 1, 0), "prior_relaxed": ("prior", OM, 1, 0),
-            "plain_ref_schedule": (None, 1.0, 10, 0), "warm_ref_schedule": ("prior", 1.0, 10, AD)}
+    # The last field is the engine: "multi" reads stored cost blocks (the
+    # headline, HBM-bound), "online" rebuilds the cost tiles from the points on
+    # the tensor cores every pass (otg_sinkhorn_pairs).
+    ARMS = {"warm": ("prior", 1.0, 1, AD, "multi"), "plain": (None, 1.0, 1, 0, "multi"),
+            "online_warm": ("prior", 1.0, 1, AD, "online"), "online_plain": (None, 1.0, 1, 0, "online"),
+            "learned_anderson": ("net", 1.0, 1, AD, "multi"), "zero_anderson": (None, 1.0, 1, AD, "multi"),
+            "prior_plain": ("prior", 1.0, 1, 0, "multi"), "prior_relaxed": ("prior", OM, 1, 0, "multi"),
+            "plain_ref_schedule": (None, 1.0, 10, 0, "multi"), "warm_ref_schedule": ("prior", 1.0, 10, AD, "multi")}
 
     if args.arms:  # a subset (profiling runs); the headline needs both warm and plain
         keep = set(args.arms.split(",")) | {"warm", "plain"}
         ARMS = {k: v for k, v in ARMS.items() if k in keep}
 
     def step(arm, ev=None):
-        init, om, per, ad = ARMS[arm]
-        ps = wp.PairSolver(X, Y)
+        init, om, per, ad, eng = ARMS[arm]
+        ps = wp.PairSolver(X, Y, engine=eng)
         wu = None
         if init == "net":
             wu = wp.warm_potential(net, X, Y, ps, WS_REG)
@@ -243,6 +247,7 @@ def run_warmstart(args, pk):
         "ablation": {k: {"value": W * B / (res[k]["ms"] * 1e-3), "niter_mean": res[k]["niter_mean"],
                          "speedup_vs_plain": p["ms"] / res[k]["ms"], "start": ARMS[k][0] or "zero",
                          "omega": ARMS[k][1], "check_period": ARMS[k][2], "anderson": ARMS[k][3],
+                         "engine": ARMS[k][4],
                          "max_marginal_err": res[k]["max_err"], "converged": res[k]["converged"]}
                      for k in ARMS if k not in ("warm", "plain")},
         # the reference's own schedule (stop test every 10th iteration) for both arms
@@ -250,6 +255,11 @@ def run_warmstart(args, pk):
                                                if "warm_ref_schedule" in res else None),
         "speedup_warm_vs_plain_ref_schedule_plain": (res["plain_ref_schedule"]["ms"] / w["ms"]
                                                      if "plain_ref_schedule" in res else None),
+        # the same two arms on the online engine (no cost blocks; cost tiles from the points)
+        "engine_online": ({"warm": W * B / (res["online_warm"]["ms"] * 1e-3),
+                           "plain": W * B / (res["online_plain"]["ms"] * 1e-3),
+                           "speedup_warm_vs_plain": res["online_plain"]["ms"] / res["online_warm"]["ms"],
+                           "unit": "solves/s"} if "online_warm" in res and "online_plain" in res else None),
         "config": {"workload": "learned warm start vs plain log-Sinkhorn, %d GMM cloud pairs n=m=%d d=%d, "
                                "reg=%.2f x max cost, stopThr=%g, float32" % (B, WS_N, WS_D, WS_REG, WS_TOL),
                    "pairs_per_step": W * B, "replicas": W, "l2": "inputs larger than L2 (%.1f GiB of cost blocks)" % (

@@ -36,6 +36,7 @@ namespace otg {
 
 constexpr int OL_M = 128, OL_N = 128, OL_K = 64, OL_STAGES = 4;
 constexpr uint32_t OL_TILE = OL_M * OL_K * 2;          // one half plane tile (16 KiB)
+constexpr uint32_t OL_TILE_NARROW = OL_M * 16 * 2;     // a narrow (16-wide) plane tile (4 KiB)
 constexpr uint32_t OL_HVEC = OL_N * 4;                 // h slice of a tile (512 B)
 constexpr uint32_t OL_STAGE = 2 * OL_TILE;             // streamed hi, lo (1024-aligned tiles)
 constexpr int OL_MAXKT = 2;                            // d <= 128
@@ -78,6 +79,10 @@ struct OnlinePass {
   int64_t rows_per_pair, cols_per_pair;
   const float* alpha_p;
   int err_sq;
+  // narrow planes (d <= 16): one K-tile of 16 values, 32-byte rows written by
+  // TMA with the 32-byte swizzle, one k-step (three MMAs) per streamed tile;
+  // the tiles keep their 16 KiB shared-memory slots (only 4 KiB are used)
+  int narrow;
 };
 
 // MAXP: instead of the log-sum-exp, each row's max of t (the max cost of a
@@ -132,7 +137,8 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
   if (warp == OL_EPI) {
     // producer
     if (lane == 0) {
-      mbar_arrive_expect_tx(res_full, 2 * OL_TILE * P.k_tiles);
+      const uint32_t tbytes = P.narrow ? OL_TILE_NARROW : OL_TILE;  // bytes of one plane tile
+      mbar_arrive_expect_tx(res_full, 2 * tbytes * P.k_tiles);
       for (int kt = 0; kt < P.k_tiles; ++kt) {
         tma_load_2d(resident + (2 * kt) * OL_TILE, &tAh, kt * OL_K, (int)(rbase + r0), res_full);
         tma_load_2d(resident + (2 * kt + 1) * OL_TILE, &tAl, kt * OL_K, (int)(rbase + r0), res_full);
@@ -143,7 +149,7 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
         if (!mbar_wait(empty + s, ((q / OL_STAGES) & 1u) ^ 1u, P.abort_flag, P.timeout_ns)) break;
         const int tile = t0 + q / P.k_tiles, kt = q % P.k_tiles;
         unsigned char* st = ring + s * OL_STAGE;
-        mbar_arrive_expect_tx(full + s, 2 * OL_TILE + OL_HVEC);
+        mbar_arrive_expect_tx(full + s, 2 * tbytes + OL_HVEC);
         tma_load_2d(st, &tBh, kt * OL_K, (int)(cbase + tile * OL_N), full + s);
         tma_load_2d(st + OL_TILE, &tBl, kt * OL_K, (int)(cbase + tile * OL_N), full + s);
         bulk_g2s(hbuf + s * OL_N, P.h + cbase + (int64_t)tile * OL_N, OL_HVEC, full + s);
@@ -175,16 +181,25 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
           if (!mbar_wait(full + s, (q / OL_STAGES) & 1u, P.abort_flag, P.timeout_ns)) { ok = false; break; }
           tc_fence_after();
           unsigned char* st = ring + s * OL_STAGE;
-          const uint64_t ah = umma_desc_k128(resident + (2 * kt) * OL_TILE);
-          const uint64_t al = umma_desc_k128(resident + (2 * kt + 1) * OL_TILE);
-          const uint64_t bh = umma_desc_k128(st), bl = umma_desc_k128(st + OL_TILE);
+          if (P.narrow) {
+            // one 16-wide k-step: 32-byte swizzled rows
+            const uint64_t ah = umma_desc_k32(resident), al = umma_desc_k32(resident + OL_TILE);
+            const uint64_t bh = umma_desc_k32(st), bl = umma_desc_k32(st + OL_TILE);
+            umma_f16(dst, ah, bh, idesc, 0);
+            umma_f16(dst, ah, bl, idesc, 1);
+            umma_f16(dst, al, bh, idesc, 1);
+          } else {
+            const uint64_t ah = umma_desc_k128(resident + (2 * kt) * OL_TILE);
+            const uint64_t al = umma_desc_k128(resident + (2 * kt + 1) * OL_TILE);
+            const uint64_t bh = umma_desc_k128(st), bl = umma_desc_k128(st + OL_TILE);
 #pragma unroll
-          for (int kk = 0; kk < OL_K / 16; ++kk) {
-            const uint64_t o = (uint64_t)(kk * 32) >> 4;
-            umma_f16(dst, ah + o, bh + o, idesc, acc);
-            acc = 1;
-            umma_f16(dst, ah + o, bl + o, idesc, 1);
-            umma_f16(dst, al + o, bh + o, idesc, 1);
+            for (int kk = 0; kk < OL_K / 16; ++kk) {
+              const uint64_t o = (uint64_t)(kk * 32) >> 4;
+              umma_f16(dst, ah + o, bh + o, idesc, acc);
+              acc = 1;
+              umma_f16(dst, ah + o, bl + o, idesc, 1);
+              umma_f16(dst, al + o, bh + o, idesc, 1);
+            }
           }
           // the stage's h slice is read by the epilogue: release the stage only
           // after the epilogue is done with this tile (see below), except for
@@ -584,17 +599,24 @@ EncodeTiledFn2 ol_encode_fn() {
   return fn;
 }
 
+// Plane tensor map: ld = 16 (narrow planes, d <= 16): 16 x 128 boxes with
+// the 32-byte swizzle; otherwise 64 x 128 boxes with the 128-byte swizzle.
 bool ol_plane_map(CUtensorMap* m, const void* base, int64_t rows, int64_t ld) {
   EncodeTiledFn2 fn = ol_encode_fn();
   if (!fn) return false;
+  const bool narrow = ld == 16;
   cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-  cuuint32_t box[2] = {OL_K, OL_M};
+  cuuint32_t box[2] = {narrow ? 16u : (cuuint32_t)OL_K, OL_M};
   cuuint32_t estr[2] = {1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+            CU_TENSOR_MAP_INTERLEAVE_NONE, narrow ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+
+// Width of the planes of d-dimensional points: 16 for d <= 16 (narrow),
+// else a multiple of 64.
+int ol_plane_width(int d) { return d <= 16 ? 16 : (d + 63) / 64 * 64; }
 
 constexpr size_t OL_SMEM = (size_t)OL_MAXKT * 2 * OL_TILE + (size_t)OL_STAGES * OL_STAGE + OL_STAGES * OL_HVEC +
                            1024 /*align*/ + 256 /*barriers*/ + 6 * OL_M * 4 /*red*/ + 64 /*counters*/;
@@ -625,7 +647,7 @@ extern "C" {
 
 size_t otg_online_workspace_bytes(int64_t n, int64_t m, int32_t d) {
   const int64_t np = (n + 127) / 128 * 128, mp = (m + 127) / 128 * 128;
-  const int64_t dp = (d + 63) / 64 * 64;
+  const int64_t dp = ol_plane_width(d);
   size_t b = 0;
   b += 2 * a16(2 * np * dp) + 2 * a16(2 * mp * dp);          // half planes
   b += 5 * a16(4 * np) + 4 * a16(4 * mp);                    // norms, log2 w, potentials, h
@@ -643,7 +665,8 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
   if (p->workspace_bytes < otg_online_workspace_bytes(p->n, p->m, p->d)) return OTG_ERR_WORKSPACE;
   const int64_t n = p->n, m = p->m;
   const int64_t np = (n + 127) / 128 * 128, mp = (m + 127) / 128 * 128;
-  const int dp = (p->d + 63) / 64 * 64;
+  const int dp = ol_plane_width(p->d);
+  const int nkt = dp == 16 ? 1 : dp / OL_K;  // K-tiles per streamed tile
   char* w = static_cast<char*>(p->workspace);
   size_t off = 0;
   auto take = [&](size_t bytes) { char* q = w + off; off += a16(bytes); return q; };
@@ -718,7 +741,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     double* eslot = errs + (nchk % 60);
     // f pass: rows = X, streamed = Y (h = g2 - |y|^2 k2)
     OnlinePass A{};
-    A.n_rows = (int)n; A.col_tiles = (int)(mp / OL_N); A.k_tiles = dp / OL_K; A.alpha = alpha;
+    A.n_rows = (int)n; A.col_tiles = (int)(mp / OL_N); A.k_tiles = nkt; A.narrow = dp == 16; A.alpha = alpha;
     A.h = hy; A.rterm = nx; A.logw2 = la2; A.pot2 = f2[cur]; A.w = p->a; A.pot_out2 = f2[cur ^ 1];
     A.other_norm2 = xn2; A.h_out = hx; A.err = check ? erow : nullptr; A.abort_flag = flag; A.timeout_ns = tmo;
     pass(A, mxh, mxl, myh, myl, np, split_f, eslot);
@@ -733,7 +756,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     cur ^= 1;
     // g pass: rows = Y, streamed = X (h = f2 - |x|^2 k2)
     OnlinePass B{};
-    B.n_rows = (int)m; B.col_tiles = (int)(np / OL_N); B.k_tiles = dp / OL_K; B.alpha = alpha;
+    B.n_rows = (int)m; B.col_tiles = (int)(np / OL_N); B.k_tiles = nkt; B.narrow = dp == 16; B.alpha = alpha;
     B.h = hx; B.rterm = ny; B.logw2 = lb2; B.pot2 = g2; B.w = p->b; B.pot_out2 = g2;
     B.other_norm2 = yn2; B.h_out = hy; B.err = nullptr; B.abort_flag = flag; B.timeout_ns = tmo;
     pass(B, myh, myl, mxh, mxl, mp, split_g, nullptr);
@@ -743,7 +766,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
   if (status == OTG_STATUS_MAXITER && p->max_iter > 0 && p->max_iter % 10 == 0) {
     double* eslot = errs + (nchk % 60);
     OnlinePass A{};
-    A.n_rows = (int)n; A.col_tiles = (int)(mp / OL_N); A.k_tiles = dp / OL_K; A.alpha = alpha;
+    A.n_rows = (int)n; A.col_tiles = (int)(mp / OL_N); A.k_tiles = nkt; A.narrow = dp == 16; A.alpha = alpha;
     A.h = hy; A.rterm = nx; A.logw2 = la2; A.pot2 = f2[cur]; A.w = p->a; A.pot_out2 = f2[cur ^ 1];
     A.other_norm2 = xn2; A.h_out = hx; A.err = erow; A.abort_flag = flag; A.timeout_ns = tmo;
     pass(A, mxh, mxl, myh, myl, np, split_f, eslot);
@@ -784,7 +807,7 @@ PairsLayout pairs_layout(int64_t P, int64_t n, int64_t m, int d, int depth) {
   PairsLayout L{};
   L.n_pad = (n + 127) / 128 * 128;
   L.m_pad = (m + 127) / 128 * 128;
-  L.dp = (d + 63) / 64 * 64;
+  L.dp = ol_plane_width(d);
   size_t off = 0;
   auto take = [&](size_t bytes) { const size_t o = off; off += a16(bytes); return o; };
   const size_t nx = (size_t)(P * L.n_pad), ny = (size_t)(P * L.m_pad);
@@ -889,6 +912,7 @@ OnlinePass pairs_pass(const PairsLayout& L, char* w, bool x_resident, int n_rows
   A.n_rows = n_rows;
   A.col_tiles = tiles;
   A.k_tiles = kt;
+  A.narrow = L.dp == 16;
   A.active = act;
   A.count = cnt;
   A.nrb = (int)((x_resident ? L.n_pad : L.m_pad) / OL_M);
@@ -931,7 +955,7 @@ int otg_pairs_max_cost(const OtgPairsProblem* q, double* maxc, cudaStream_t st) 
   float* h = reinterpret_cast<float*>(w + L.hy);
   pairs_hmax_kernel<<<1024, 256, 0, st>>>(reinterpret_cast<const float*>(w + L.yn), P, (int)q->m, L.m_pad, h);
   // t = |y|^2 - 2 x.y, row max + |x|^2 = max_j |x_i - y_j|^2
-  OnlinePass A = pairs_pass(L, w, true, (int)q->n, (int)(L.m_pad / OL_N), L.dp / OL_K, act, cnt, abort_flag,
+  OnlinePass A = pairs_pass(L, w, true, (int)q->n, (int)(L.m_pad / OL_N), L.dp == 16 ? 1 : L.dp / OL_K, act, cnt, abort_flag,
                             q->timeout_ms > 0 ? (uint64_t)q->timeout_ms * 1000000ull : 4000000000ull);
   A.alpha_p = nullptr;
   A.alpha = (float)(-2.0 / ((double)sxy[0] * (double)sxy[1]));
@@ -1005,7 +1029,7 @@ int otg_sinkhorn_pairs(const OtgPairsProblem* q, cudaStream_t st) {
     S.aF = F(L.aF); S.aR = F(L.aR); S.aG = reinterpret_cast<double*>(w + L.aG);
     S.acnt = reinterpret_cast<int32_t*>(w + L.acnt);
   }
-  const int kt = L.dp / OL_K;
+  const int kt = L.dp == 16 ? 1 : L.dp / OL_K;
   const int nrb_x = (int)(L.n_pad / OL_M), nrb_y = (int)(L.m_pad / OL_M);
   int nact = P, sel = 0, cur = 0;
   bool prev_check = false;

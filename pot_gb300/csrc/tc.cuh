@@ -38,6 +38,19 @@ __device__ __forceinline__ uint64_t umma_desc_k128(const void* tile) {
   return d;
 }
 
+// The same for a K-major tile of 32-byte rows (16 half-precision values)
+// written by TMA with the 32-byte swizzle: groups of 8 rows 256 bytes apart,
+// layout 6 (32-byte swizzle), base 256-aligned.
+__device__ __forceinline__ uint64_t umma_desc_k32(const void* tile) {
+  const uint64_t addr = smem_addr(tile);
+  uint64_t d = (addr >> 4) & 0x3FFFull;
+  d |= 1ull << 16;
+  d |= (uint64_t)(256 >> 4) << 32;
+  d |= 1ull << 46;
+  d |= 6ull << 61;
+  return d;
+}
+
 // Instruction descriptor for kind::f16 with fp32 accumulation, both operands
 // K-major: [4,6) D format (1 = f32), [7,10) A format (0 = f16, 1 = bf16),
 // [10,13) B format, [17,23) N >> 3, [24,29) M >> 4.

@@ -352,7 +352,7 @@ class CloudPairsResult(tuple):
 
 
 def solve_cloud_pairs(X, Y, reg_rel=0.02, tol=1e-6, max_iter=100000, warm=True, net=None, omega=REFINE_OMEGA,
-                      anderson=REFINE_ANDERSON, check_period=10, warm_max_iter=None, start="prior"):
+                      anderson=REFINE_ANDERSON, check_period=10, warm_max_iter=None, start="prior", engine="multi"):
     """Public entry point for batches of equal-size cloud pairs: X (P, n, d),
     Y (P, m, d) (numpy or torch); returns a `CloudPairsResult` (log_u, log_v,
     niter, status, err, fallback) in the caller's array type.  reg =
@@ -364,7 +364,9 @@ def solve_cloud_pairs(X, Y, reg_rel=0.02, tol=1e-6, max_iter=100000, warm=True, 
     (`start="learned"`; it measures no faster on the Gaussian-mixture
     workload, whose residual the network does not predict better than the
     prior), and the solve is accelerated: Anderson mixing over `anderson`
-    iterates, or, with anderson=0, updates over-relaxed by `omega`.  The stop test is the
+    iterates, or, with anderson=0, updates over-relaxed by `omega`.  `engine`
+    "online" solves without storing the cost blocks (cost tiles rebuilt from
+    the points on the tensor cores; anderson only, no omega).  The stop test is the
     plain one: a pair ends only when the column-marginal error of its (u, v)
     pair, u the exact row update of v, is below `tol`.  Zero start is the
     fallback: any pair whose warm solve ends without meeting the test (after
@@ -375,7 +377,7 @@ def solve_cloud_pairs(X, Y, reg_rel=0.02, tol=1e-6, max_iter=100000, warm=True, 
     bd = Boundary(X, Y)
     Xd = bd.to_dev(X, torch.float32).contiguous()
     Yd = bd.to_dev(Y, torch.float32).contiguous()
-    ps = PairSolver(Xd, Yd)
+    ps = PairSolver(Xd, Yd, engine=engine)
     if warm:
         if start == "learned":
             net = net or default_net(Xd.device)
@@ -395,7 +397,7 @@ def solve_cloud_pairs(X, Y, reg_rel=0.02, tol=1e-6, max_iter=100000, warm=True, 
         if bad.numel():
             # zero start, plain iteration, for the pairs the warm solve left unconverged
             idx = bad.to(Xd.device)
-            sub = PairSolver(Xd[idx].contiguous(), Yd[idx].contiguous())
+            sub = PairSolver(Xd[idx].contiguous(), Yd[idx].contiguous(), maxc=ps.maxc[idx], engine=engine)
             u2, v2, s2, n2, e2 = sub.solve(reg_rel, tol, max_iter, check_period=check_period)
             u[idx], v[idx], status[idx], niter[idx], err[idx] = u2, v2, s2, n2, e2
             fallback[idx] = True
