@@ -85,135 +85,248 @@ struct OnlinePass {
   int narrow;
 };
 
-// MAXP: instead of the log-sum-exp, each row's max of t (the max cost of a
-// pair batch, which sets its regularisation): no exponentials.
+// One tile of the epilogue for one warp: its 32 columns of the tile's
+// accumulator (TMEM address taddr) and of the h slice fold into the running
+// base-2 (max, sum) of the warp's rows; the TMEM buffer (acce_b) and, from
+// the last epilogue warp, the stage holding h (empty_s, counted in relcnt_s)
+// are handed back as soon as their contents are in registers.  MAXP: only
+// the running max.
 template <bool MAXP>
+__device__ __forceinline__ void ol_epi_tile(uint32_t taddr, const float* hcol, uint64_t a2, uint64_t* acce_b,
+                                            unsigned* relcnt_s, uint64_t* empty_s, int lane, float& mx, float& sm,
+                                            float& sc) {
+  // packed fp32x2 arithmetic (one instruction per column pair, each lane
+  // rounded as the scalar op) and three-input max: fewer instructions for
+  // the same arithmetic, and the partial sums group the terms exactly as
+  // four scalar accumulators would
+  uint32_t v[32];
+  tmem_ld32u(taddr, v);
+  const ulonglong2* hv = reinterpret_cast<const ulonglong2*>(hcol);
+  uint64_t t2[16];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const ulonglong2 hh = hv[i];
+    t2[2 * i] = fma2(pack2u(v[4 * i], v[4 * i + 1]), a2, hh.x);
+    t2[2 * i + 1] = fma2(pack2u(v[4 * i + 2], v[4 * i + 3]), a2, hh.y);
+  }
+  // the accumulator and the h slice are in registers now: hand the TMEM
+  // buffer back to the MMA warp and the stage to the producer before the
+  // arithmetic
+  tc_fence_before();
+  __syncwarp();
+  if (lane == 0) {
+    mbar_arrive(acce_b);
+    // the stage is released once all epilogue warps have read its h slice
+    if (atomicAdd(relcnt_s, 1u) == (unsigned)(OL_EPI - 1)) { atomicExch(relcnt_s, 0u); mbar_arrive(empty_s); }
+  }
+  float t[32];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) unpack2(t2[i], t[2 * i], t[2 * i + 1]);
+  float m1[11];
+#pragma unroll
+  for (int i = 0; i < 10; ++i) m1[i] = fmax3(t[3 * i], t[3 * i + 1], t[3 * i + 2]);
+  m1[10] = fmaxf(t[30], t[31]);
+  const float n0 = fmax3(m1[0], m1[1], m1[2]), n1 = fmax3(m1[3], m1[4], m1[5]);
+  const float n2 = fmax3(m1[6], m1[7], m1[8]), n3 = fmaxf(m1[9], m1[10]);
+  const float nm = fmax3(mx, fmax3(n0, n1, n2), n3);
+  if (MAXP) {
+    mx = nm;
+  } else if (nm != -INFINITY) {
+    const float r = ex2(mx - nm);
+    sm *= r;
+    sc *= r;
+    const uint64_t nm2 = pack2(nm, nm);
+    uint64_t acc0 = 0ull, acc1 = 0ull;  // columns 4k, 4k+1 and 4k+2, 4k+3
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      float x0, x1;
+      unpack2(sub2(t2[i], nm2), x0, x1);
+      const uint64_t e2 = pack2(ex2(x0), ex2(x1));
+      if (i & 1) acc1 = add2(acc1, e2);
+      else acc0 = add2(acc0, e2);
+    }
+    float p0, p1, p2, p3;
+    unpack2(acc0, p0, p1);
+    unpack2(acc1, p2, p3);
+    // each tile adds one Kahan-compensated partial sum of 32 terms, so
+    // rounding does not grow with the number of streamed points
+    const float part = (p0 + p1) + (p2 + p3);
+    const float y = part - sc;
+    const float tt = sm + y;
+    sc = (tt - sm) - y;
+    sm = tt;
+    mx = nm;
+  }
+}
+
+// The MMAs of one streamed (tile, k-tile) step into TMEM column dst.
+__device__ __forceinline__ void ol_mma_step(const OnlinePass& P, uint32_t dst, const unsigned char* resident,
+                                            const unsigned char* st, int kt, uint32_t idesc) {
+  if (P.narrow) {
+    // one 16-wide k-step: 32-byte swizzled rows
+    const uint64_t ah = umma_desc_k32(resident), al = umma_desc_k32(resident + OL_TILE);
+    const uint64_t bh = umma_desc_k32(st), bl = umma_desc_k32(st + OL_TILE);
+    umma_f16(dst, ah, bh, idesc, 0);
+    umma_f16(dst, ah, bl, idesc, 1);
+    umma_f16(dst, al, bh, idesc, 1);
+  } else {
+    const uint64_t ah = umma_desc_k128(resident + (2 * kt) * OL_TILE);
+    const uint64_t al = umma_desc_k128(resident + (2 * kt + 1) * OL_TILE);
+    const uint64_t bh = umma_desc_k128(st), bl = umma_desc_k128(st + OL_TILE);
+#pragma unroll
+    for (int kk = 0; kk < OL_K / 16; ++kk) {
+      const uint64_t o = (uint64_t)(kk * 32) >> 4;
+      umma_f16(dst, ah + o, bh + o, idesc, (kt | kk) ? 1u : 0u);
+      umma_f16(dst, ah + o, bl + o, idesc, 1);
+      umma_f16(dst, al + o, bh + o, idesc, 1);
+    }
+  }
+}
+
+// The rows' results after the last tile: column groups 1-3 hand their
+// (max, sum) to group 0 through `red` (the caller's named barrier sits
+// between the two halves), group 0 merges and writes the row outputs.
+template <bool MAXP>
+__device__ __forceinline__ void ol_rows_out(const OnlinePass& P, const float* red, int row_local, float mx, float sm,
+                                            int r0, int64_t rbase, int cs) {
+  for (int g = 0; g < 3; ++g) lse_merge(mx, sm, red[g * 2 * OL_M + row_local], red[g * 2 * OL_M + OL_M + row_local]);
+  const int row = r0 + row_local;
+  const int64_t ri = rbase + row;  // the row in the packed vectors
+  if (MAXP) {
+    if (row < P.n_rows) P.pot_out2[ri] = mx + P.rterm[ri];
+  } else if (P.split > 1) {
+    P.part[((size_t)cs * 2) * P.rows_pad + row] = mx;
+    P.part[((size_t)cs * 2 + 1) * P.rows_pad + row] = sm;
+  } else if (row < P.n_rows) {
+    const float L = lse_value(mx, sm) + P.rterm[ri];  // base-2 LSE_j(g2_j - C_ij log2e/reg)
+    const float pnew = P.logw2[ri] - L;
+    if (P.err) {
+      const double e = (double)ex2(P.pot2[ri] + L) - (double)P.w[ri];
+      P.err[ri] = P.err_sq ? e * e : fabs(e);
+    }
+    P.pot_out2[ri] = pnew;
+    P.h_out[ri] = pnew - P.other_norm2[ri];
+  } else {
+    P.h_out[ri] = -INFINITY;  // padding rows of the resident side
+  }
+}
+
+// Shared-memory carve-up of both pass kernels.
+struct OlSmem {
+  unsigned char* resident; unsigned char* ring; float* hbuf;
+  uint64_t *res_full, *full, *empty, *accf, *acce, *res_empty;
+  uint32_t* tslot; float* red; unsigned* relcnt;
+};
+__device__ __forceinline__ OlSmem ol_carve(unsigned char* smem_raw) {
+  OlSmem S;
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  S.resident = smem;                                          // [kt][hi, lo] tiles
+  S.ring = smem + OL_MAXKT * 2 * OL_TILE;                     // [stage][hi, lo] of one k-tile
+  S.hbuf = reinterpret_cast<float*>(S.ring + OL_STAGES * OL_STAGE);  // [stage][128] h slices
+  uint64_t* bars = reinterpret_cast<uint64_t*>(S.hbuf + OL_STAGES * OL_N);
+  S.res_full = bars;                     // resident operand landed
+  S.full = bars + 1;                     // [OL_STAGES]
+  S.empty = S.full + OL_STAGES;          // [OL_STAGES]
+  S.accf = S.empty + OL_STAGES;          // [OL_NBUF]
+  S.acce = S.accf + OL_NBUF;             // [OL_NBUF]
+  S.res_empty = S.acce + OL_NBUF;        // resident operand no longer read (batch kernel)
+  S.tslot = reinterpret_cast<uint32_t*>(S.res_empty + 1);
+  S.red = reinterpret_cast<float*>(S.tslot + 4);              // [3][2][128] (mx, s) of column groups 1-3
+  S.relcnt = reinterpret_cast<unsigned*>(S.red + 6 * OL_M);   // [OL_STAGES] epilogue warps done
+  return S;
+}
+
+__device__ __forceinline__ void ol_setup(const OlSmem& S, const CUtensorMap* tAh, const CUtensorMap* tAl,
+                                         const CUtensorMap* tBh, const CUtensorMap* tBl) {
+  if (threadIdx.x == 0) {
+    mbar_init(S.res_full, 1);
+    mbar_init(S.res_empty, 1);
+    for (int s = 0; s < OL_STAGES; ++s) { mbar_init(S.full + s, 1); mbar_init(S.empty + s, 1); }
+    for (int b = 0; b < OL_NBUF; ++b) { mbar_init(S.accf + b, 1); mbar_init(S.acce + b, OL_EPI); }
+    for (int s2 = 0; s2 < OL_STAGES; ++s2) S.relcnt[s2] = 0u;
+    fence_mbar_init();
+    prefetch_tmap(tAh); prefetch_tmap(tAl); prefetch_tmap(tBh); prefetch_tmap(tBl);
+  }
+  if ((threadIdx.x >> 5) == OL_EPI + 1) tmem_alloc(S.tslot, OL_NBUF * OL_N);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+}
+
+// One problem: CTA (blockIdx.x, blockIdx.y) takes row block blockIdx.x and
+// the streamed tiles of column range blockIdx.y, one unit per CTA.
 __global__ void __launch_bounds__(OL_THREADS, 1)
 online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                    const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, OnlinePass P) {
   extern __shared__ unsigned char smem_raw[];
-  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* resident = smem;                                   // [kt][hi, lo] tiles
-  unsigned char* ring = smem + OL_MAXKT * 2 * OL_TILE;              // [stage][hi, lo] of one k-tile
-  float* hbuf = reinterpret_cast<float*>(ring + OL_STAGES * OL_STAGE);  // [stage][128] h slices
-  uint64_t* bars = reinterpret_cast<uint64_t*>(hbuf + OL_STAGES * OL_N);
-  uint64_t* res_full = bars;            // resident operand landed
-  uint64_t* full = bars + 1;            // [OL_STAGES]
-  uint64_t* empty = full + OL_STAGES;   // [OL_STAGES]
-  uint64_t* accf = empty + OL_STAGES;   // [OL_NBUF]
-  uint64_t* acce = accf + OL_NBUF;      // [OL_NBUF]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(acce + OL_NBUF);
-  float* red = reinterpret_cast<float*>(tslot + 4);                 // [3][2][128] (mx, s) of column groups 1-3
-  unsigned* relcnt = reinterpret_cast<unsigned*>(red + 6 * OL_M);   // [OL_STAGES] epilogue warps done
+  const OlSmem S = ol_carve(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int pair = 0, rblk = blockIdx.x;
-  if (P.active) {
-    const int slot = blockIdx.x / P.nrb;
-    if (slot >= __ldcg(P.count)) return;  // the whole CTA, before any barrier or TMEM allocation
-    pair = __ldcg(P.active + slot);
-    rblk = blockIdx.x % P.nrb;
-  }
-  const int64_t rbase = (int64_t)pair * P.rows_per_pair, cbase = (int64_t)pair * P.cols_per_pair;
-  const int r0 = rblk * OL_M;
+  const int r0 = blockIdx.x * OL_M;
   const int cs = blockIdx.y;
   const int t0 = (int)((int64_t)cs * P.col_tiles / P.split), t1 = (int)((int64_t)(cs + 1) * P.col_tiles / P.split);
   const int ntl = t1 - t0;                     // this CTA's streamed tiles
   const int nsteps = ntl * P.k_tiles;          // streamed (tile, k-tile) steps
-
-  if (threadIdx.x == 0) {
-    mbar_init(res_full, 1);
-    for (int s = 0; s < OL_STAGES; ++s) { mbar_init(full + s, 1); mbar_init(empty + s, 1); }
-    for (int b = 0; b < OL_NBUF; ++b) { mbar_init(accf + b, 1); mbar_init(acce + b, OL_EPI); }
-    for (int s2 = 0; s2 < OL_STAGES; ++s2) relcnt[s2] = 0u;
-    fence_mbar_init();
-    prefetch_tmap(&tAh); prefetch_tmap(&tAl); prefetch_tmap(&tBh); prefetch_tmap(&tBl);
-  }
-  if (warp == OL_EPI + 1) tmem_alloc(tslot, OL_NBUF * OL_N);
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tslot;
+  ol_setup(S, &tAh, &tAl, &tBh, &tBl);
+  const uint32_t tmem = *S.tslot;
 
   if (warp == OL_EPI) {
     // producer
     if (lane == 0) {
       const uint32_t tbytes = P.narrow ? OL_TILE_NARROW : OL_TILE;  // bytes of one plane tile
-      mbar_arrive_expect_tx(res_full, 2 * tbytes * P.k_tiles);
+      mbar_arrive_expect_tx(S.res_full, 2 * tbytes * P.k_tiles);
       for (int kt = 0; kt < P.k_tiles; ++kt) {
-        tma_load_2d(resident + (2 * kt) * OL_TILE, &tAh, kt * OL_K, (int)(rbase + r0), res_full);
-        tma_load_2d(resident + (2 * kt + 1) * OL_TILE, &tAl, kt * OL_K, (int)(rbase + r0), res_full);
+        tma_load_2d(S.resident + (2 * kt) * OL_TILE, &tAh, kt * OL_K, r0, S.res_full);
+        tma_load_2d(S.resident + (2 * kt + 1) * OL_TILE, &tAl, kt * OL_K, r0, S.res_full);
       }
       int issued = 0;
       for (int q = 0; q < nsteps; ++q) {
         const int s = q % OL_STAGES;
-        if (!mbar_wait(empty + s, ((q / OL_STAGES) & 1u) ^ 1u, P.abort_flag, P.timeout_ns)) break;
+        if (!mbar_wait(S.empty + s, ((q / OL_STAGES) & 1u) ^ 1u, P.abort_flag, P.timeout_ns)) break;
         const int tile = t0 + q / P.k_tiles, kt = q % P.k_tiles;
-        unsigned char* st = ring + s * OL_STAGE;
-        mbar_arrive_expect_tx(full + s, 2 * tbytes + OL_HVEC);
-        tma_load_2d(st, &tBh, kt * OL_K, (int)(cbase + tile * OL_N), full + s);
-        tma_load_2d(st + OL_TILE, &tBl, kt * OL_K, (int)(cbase + tile * OL_N), full + s);
-        bulk_g2s(hbuf + s * OL_N, P.h + cbase + (int64_t)tile * OL_N, OL_HVEC, full + s);
+        unsigned char* st = S.ring + s * OL_STAGE;
+        mbar_arrive_expect_tx(S.full + s, 2 * tbytes + OL_HVEC);
+        tma_load_2d(st, &tBh, kt * OL_K, tile * OL_N, S.full + s);
+        tma_load_2d(st + OL_TILE, &tBl, kt * OL_K, tile * OL_N, S.full + s);
+        bulk_g2s(S.hbuf + s * OL_N, P.h + (int64_t)tile * OL_N, OL_HVEC, S.full + s);
         ++issued;
       }
+      // copies still in flight land before the CTA leaves
       const int lo = issued > OL_STAGES ? issued - OL_STAGES : 0;
       for (int q = lo; q < issued; ++q) {
-        const uint64_t t0 = globaltimer();
-        while (!mbar_try_wait(full + q % OL_STAGES, (q / OL_STAGES) & 1u))
-          if (globaltimer() - t0 > P.timeout_ns) break;
+        const uint64_t w0 = globaltimer();
+        while (!mbar_try_wait(S.full + q % OL_STAGES, (q / OL_STAGES) & 1u))
+          if (globaltimer() - w0 > P.timeout_ns) break;
       }
-      const uint64_t t0 = globaltimer();
-      while (!mbar_try_wait(res_full, 0)) if (globaltimer() - t0 > P.timeout_ns) break;
+      const uint64_t w0 = globaltimer();
+      while (!mbar_try_wait(S.res_full, 0)) if (globaltimer() - w0 > P.timeout_ns) break;
     }
   } else if (warp == OL_EPI + 1) {
     // MMA issuer: one accumulator tile per streamed tile, TMEM buffers in turn
     if (lane == 0) {
       const uint32_t idesc = umma_idesc_f16(OL_M, OL_N, false);
-      bool ok = mbar_wait(res_full, 0, P.abort_flag, P.timeout_ns);
+      bool ok = mbar_wait(S.res_full, 0, P.abort_flag, P.timeout_ns);
       int q = 0, committed = 0;
       for (int tile = 0; tile < ntl && ok; ++tile) {
         const int b = tile % OL_NBUF;
-        if (!mbar_wait(acce + b, ((tile / OL_NBUF) & 1) ^ 1, P.abort_flag, P.timeout_ns)) break;
+        if (!mbar_wait(S.acce + b, ((tile / OL_NBUF) & 1) ^ 1, P.abort_flag, P.timeout_ns)) break;
         tc_fence_after();
-        const uint32_t dst = tmem + (uint32_t)(b * OL_N);
-        uint32_t acc = 0;
         for (int kt = 0; kt < P.k_tiles; ++kt, ++q) {
           const int s = q % OL_STAGES;
-          if (!mbar_wait(full + s, (q / OL_STAGES) & 1u, P.abort_flag, P.timeout_ns)) { ok = false; break; }
+          if (!mbar_wait(S.full + s, (q / OL_STAGES) & 1u, P.abort_flag, P.timeout_ns)) { ok = false; break; }
           tc_fence_after();
-          unsigned char* st = ring + s * OL_STAGE;
-          if (P.narrow) {
-            // one 16-wide k-step: 32-byte swizzled rows
-            const uint64_t ah = umma_desc_k32(resident), al = umma_desc_k32(resident + OL_TILE);
-            const uint64_t bh = umma_desc_k32(st), bl = umma_desc_k32(st + OL_TILE);
-            umma_f16(dst, ah, bh, idesc, 0);
-            umma_f16(dst, ah, bl, idesc, 1);
-            umma_f16(dst, al, bh, idesc, 1);
-          } else {
-            const uint64_t ah = umma_desc_k128(resident + (2 * kt) * OL_TILE);
-            const uint64_t al = umma_desc_k128(resident + (2 * kt + 1) * OL_TILE);
-            const uint64_t bh = umma_desc_k128(st), bl = umma_desc_k128(st + OL_TILE);
-#pragma unroll
-            for (int kk = 0; kk < OL_K / 16; ++kk) {
-              const uint64_t o = (uint64_t)(kk * 32) >> 4;
-              umma_f16(dst, ah + o, bh + o, idesc, acc);
-              acc = 1;
-              umma_f16(dst, ah + o, bl + o, idesc, 1);
-              umma_f16(dst, al + o, bh + o, idesc, 1);
-            }
-          }
-          // the stage's h slice is read by the epilogue: release the stage only
-          // after the epilogue is done with this tile (see below), except for
-          // stages of earlier k-tiles of the same tile, which only the MMAs read
-          if (kt + 1 < P.k_tiles) umma_commit(empty + s);
+          ol_mma_step(P, tmem + (uint32_t)(b * OL_N), S.resident, S.ring + s * OL_STAGE, kt, idesc);
+          // the stage's h slice is read by the epilogue, which releases the
+          // tile's last stage; earlier k-tiles' stages only the MMAs read
+          if (kt + 1 < P.k_tiles) umma_commit(S.empty + s);
         }
         if (!ok) break;
-        umma_commit(accf + b);
+        umma_commit(S.accf + b);
         committed = tile + 1;
       }
       if (committed > 0) {
         const int c = committed - 1;
-        const uint64_t t0 = globaltimer();
-        while (!mbar_try_wait(accf + (c % OL_NBUF), (c / OL_NBUF) & 1)) if (globaltimer() - t0 > P.timeout_ns) break;
+        const uint64_t w0 = globaltimer();
+        while (!mbar_try_wait(S.accf + (c % OL_NBUF), (c / OL_NBUF) & 1)) if (globaltimer() - w0 > P.timeout_ns) break;
       }
     }
   } else {
@@ -221,111 +334,165 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
     // and columns 32 (w / 4) .. +31 of each tile
     const int quarter = warp & 3, cgrp = warp >> 2;
     const int row_local = quarter * 32 + lane;
-    // running (max, sum) per row; the sum is Kahan-compensated (sc) and each
-    // tile adds one partial sum of 32 terms, so rounding does not grow with
-    // the number of streamed points
     float mx = -INFINITY, sm = 0.f, sc = 0.f;
     int ok = 1;
+    const uint64_t a2 = pack2(P.alpha, P.alpha);
     for (int tile = 0; tile < ntl && ok; ++tile) {
       const int b = tile % OL_NBUF;
-      if (lane == 0) ok = (mbar_wait(accf + b, (tile / OL_NBUF) & 1, P.abort_flag, P.timeout_ns) &&
-                           !*(volatile int*)P.abort_flag) ? 1 : 0;
+      // (mbar_wait itself polls the abort flag while it spins)
+      if (lane == 0) ok = mbar_wait(S.accf + b, (tile / OL_NBUF) & 1, P.abort_flag, P.timeout_ns) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       __syncwarp();
       if (!ok) break;
       tc_fence_after();
       // the last k-step's stage holds this tile's h slice
-      const int qlast = tile * P.k_tiles + P.k_tiles - 1;
-      const float* h = hbuf + (qlast % OL_STAGES) * OL_N;
-      {
-        // packed fp32x2 arithmetic (one instruction per column pair, each
-        // lane rounded as the scalar op) and three-input max: the epilogue
-        // is bound by instruction issue, and the partial sums group the
-        // terms exactly as four scalar accumulators would
-        uint32_t v[32];
-        const int col = cgrp * 32;
-        tmem_ld32u(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * OL_N + col), v);
-        const ulonglong2* hv = reinterpret_cast<const ulonglong2*>(h + col);
-        const float alpha = P.alpha_p ? __ldg(P.alpha_p + pair) : P.alpha;
-        const uint64_t a2 = pack2(alpha, alpha);
-        uint64_t t2[16];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const ulonglong2 hh = hv[i];
-          t2[2 * i] = fma2(pack2u(v[4 * i], v[4 * i + 1]), a2, hh.x);
-          t2[2 * i + 1] = fma2(pack2u(v[4 * i + 2], v[4 * i + 3]), a2, hh.y);
-        }
-        float t[32];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) unpack2(t2[i], t[2 * i], t[2 * i + 1]);
-        float m1[11];
-#pragma unroll
-        for (int i = 0; i < 10; ++i) m1[i] = fmax3(t[3 * i], t[3 * i + 1], t[3 * i + 2]);
-        m1[10] = fmaxf(t[30], t[31]);
-        const float n0 = fmax3(m1[0], m1[1], m1[2]), n1 = fmax3(m1[3], m1[4], m1[5]);
-        const float n2 = fmax3(m1[6], m1[7], m1[8]), n3 = fmaxf(m1[9], m1[10]);
-        const float nm = fmax3(mx, fmax3(n0, n1, n2), n3);
-        if (MAXP) {
-          mx = nm;
-        } else if (nm != -INFINITY) {
-          const float r = ex2(mx - nm);
-          sm *= r;
-          sc *= r;
-          const uint64_t nm2 = pack2(nm, nm);
-          uint64_t acc0 = 0ull, acc1 = 0ull;  // columns 4k, 4k+1 and 4k+2, 4k+3
-#pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            float x0, x1;
-            unpack2(sub2(t2[i], nm2), x0, x1);
-            const uint64_t e2 = pack2(ex2(x0), ex2(x1));
-            if (i & 1) acc1 = add2(acc1, e2);
-            else acc0 = add2(acc0, e2);
-          }
-          float p0, p1, p2, p3;
-          unpack2(acc0, p0, p1);
-          unpack2(acc1, p2, p3);
-          const float part = (p0 + p1) + (p2 + p3);
-          const float y = part - sc;
-          const float tt = sm + y;
-          sc = (tt - sm) - y;
-          sm = tt;
-          mx = nm;
-        }
-      }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) {
-        mbar_arrive(acce + b);
-        // the tile's last stage (its h slice) is released once all
-        // epilogue warps have read it
-        const int s = qlast % OL_STAGES;
-        if (atomicAdd(relcnt + s, 1u) == (unsigned)(OL_EPI - 1)) { atomicExch(relcnt + s, 0u); mbar_arrive(empty + s); }
-      }
+      const int s = (tile * P.k_tiles + P.k_tiles - 1) % OL_STAGES;
+      ol_epi_tile<false>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * OL_N + cgrp * 32),
+                         S.hbuf + s * OL_N + cgrp * 32, a2, S.acce + b, S.relcnt + s, S.empty + s, lane, mx, sm, sc);
     }
     // merge the four column groups of each row
-    if (cgrp > 0) { red[(cgrp - 1) * 2 * OL_M + row_local] = mx; red[(cgrp - 1) * 2 * OL_M + OL_M + row_local] = sm; }
+    if (cgrp > 0) { S.red[(cgrp - 1) * 2 * OL_M + row_local] = mx; S.red[(cgrp - 1) * 2 * OL_M + OL_M + row_local] = sm; }
     named_bar(1, OL_EPI * 32);
-    if (cgrp == 0 && ok) {
-      for (int g = 0; g < 3; ++g) lse_merge(mx, sm, red[g * 2 * OL_M + row_local], red[g * 2 * OL_M + OL_M + row_local]);
-      const int row = r0 + row_local;
-      const int64_t ri = rbase + row;  // the row in the packed vectors
-      if (MAXP) {
-        if (row < P.n_rows) P.pot_out2[ri] = mx + P.rterm[ri];
-      } else if (P.split > 1) {
-        P.part[((size_t)cs * 2) * P.rows_pad + row] = mx;
-        P.part[((size_t)cs * 2 + 1) * P.rows_pad + row] = sm;
-      } else if (row < P.n_rows) {
-        const float L = lse_value(mx, sm) + P.rterm[ri];  // base-2 LSE_j(g2_j - C_ij log2e/reg)
-        const float pnew = P.logw2[ri] - L;
-        if (P.err) {
-          const double e = (double)ex2(P.pot2[ri] + L) - (double)P.w[ri];
-          P.err[ri] = P.err_sq ? e * e : fabs(e);
+    if (cgrp == 0 && ok) ol_rows_out<false>(P, S.red, row_local, mx, sm, r0, 0, cs);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == OL_EPI + 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, OL_NBUF * OL_N);
+  }
+}
+
+// A batch of pairs: units (active slot, row block), taken by the CTAs in
+// turn (one CTA per SM keeps its TMEM, barriers and pipeline across its
+// units; the stage and tile counters run on).  Slot k's pair is active[k],
+// k < *count.  MAXP: instead of the log-sum-exp, each row's max of t (the
+// max cost of a pair, which sets its regularisation): no exponentials.
+template <bool MAXP>
+__global__ void __launch_bounds__(OL_THREADS, 1)
+online_batch_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
+                    const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, OnlinePass P) {
+  extern __shared__ unsigned char smem_raw[];
+  const OlSmem S = ol_carve(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nunits = __ldcg(P.count) * P.nrb;
+  if ((int)blockIdx.x >= nunits) return;  // the whole CTA, before any barrier or TMEM allocation
+  const int ntl = P.col_tiles;                 // streamed tiles per unit
+  const int nsteps = ntl * P.k_tiles;          // streamed (tile, k-tile) steps per unit
+  // unit u -> pair, resident rows (offset of the pair and of the row block)
+  auto unit_rows = [&](int u, int& pair, int64_t& rbase, int64_t& cbase, int& r0) {
+    pair = __ldcg(P.active + u / P.nrb);
+    rbase = (int64_t)pair * P.rows_per_pair;
+    cbase = (int64_t)pair * P.cols_per_pair;
+    r0 = (u % P.nrb) * OL_M;
+  };
+  ol_setup(S, &tAh, &tAl, &tBh, &tBl);
+  const uint32_t tmem = *S.tslot;
+
+  if (warp == OL_EPI) {
+    // producer: per unit the resident tile (once the previous unit's MMAs
+    // are done with it), then the streamed stages; the stage counter q runs
+    // on across units
+    if (lane == 0) {
+      const uint32_t tbytes = P.narrow ? OL_TILE_NARROW : OL_TILE;  // bytes of one plane tile
+      int q = 0, lu = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x, ++lu) {
+        int pair, r0;
+        int64_t rbase, cbase;
+        unit_rows(u, pair, rbase, cbase, r0);
+        if (lu > 0 && !mbar_wait(S.res_empty, (lu - 1) & 1, P.abort_flag, P.timeout_ns)) break;
+        mbar_arrive_expect_tx(S.res_full, 2 * tbytes * P.k_tiles);
+        for (int kt = 0; kt < P.k_tiles; ++kt) {
+          tma_load_2d(S.resident + (2 * kt) * OL_TILE, &tAh, kt * OL_K, (int)(rbase + r0), S.res_full);
+          tma_load_2d(S.resident + (2 * kt + 1) * OL_TILE, &tAl, kt * OL_K, (int)(rbase + r0), S.res_full);
         }
-        P.pot_out2[ri] = pnew;
-        P.h_out[ri] = pnew - P.other_norm2[ri];
-      } else {
-        P.h_out[ri] = -INFINITY;  // padding rows of the resident side
+        for (int qs = 0; qs < nsteps; ++qs, ++q) {
+          const int s = q % OL_STAGES;
+          if (!mbar_wait(S.empty + s, ((q / OL_STAGES) & 1u) ^ 1u, P.abort_flag, P.timeout_ns)) { ok = false; break; }
+          const int tile = qs / P.k_tiles, kt = qs % P.k_tiles;
+          unsigned char* st = S.ring + s * OL_STAGE;
+          mbar_arrive_expect_tx(S.full + s, 2 * tbytes + OL_HVEC);
+          tma_load_2d(st, &tBh, kt * OL_K, (int)(cbase + tile * OL_N), S.full + s);
+          tma_load_2d(st + OL_TILE, &tBl, kt * OL_K, (int)(cbase + tile * OL_N), S.full + s);
+          bulk_g2s(S.hbuf + s * OL_N, P.h + cbase + (int64_t)tile * OL_N, OL_HVEC, S.full + s);
+        }
       }
+      // copies still in flight land before the CTA leaves
+      const int lo = q > OL_STAGES ? q - OL_STAGES : 0;
+      for (int qq = lo; qq < q; ++qq) {
+        const uint64_t w0 = globaltimer();
+        while (!mbar_try_wait(S.full + qq % OL_STAGES, (qq / OL_STAGES) & 1u))
+          if (globaltimer() - w0 > P.timeout_ns) break;
+      }
+      if (lu > 0) {
+        const uint64_t w0 = globaltimer();
+        while (!mbar_try_wait(S.res_full, (lu - 1) & 1)) if (globaltimer() - w0 > P.timeout_ns) break;
+      }
+    }
+  } else if (warp == OL_EPI + 1) {
+    // MMA issuer: the tile counter T and the stage counter q run on across units
+    if (lane == 0) {
+      const uint32_t idesc = umma_idesc_f16(OL_M, OL_N, false);
+      int q = 0, T = 0, committed = 0, lu = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x, ++lu) {
+        if (!mbar_wait(S.res_full, lu & 1, P.abort_flag, P.timeout_ns)) break;
+        tc_fence_after();
+        for (int tile = 0; tile < ntl && ok; ++tile, ++T) {
+          const int b = T % OL_NBUF;
+          if (!mbar_wait(S.acce + b, ((T / OL_NBUF) & 1) ^ 1, P.abort_flag, P.timeout_ns)) { ok = false; break; }
+          tc_fence_after();
+          for (int kt = 0; kt < P.k_tiles; ++kt, ++q) {
+            const int s = q % OL_STAGES;
+            if (!mbar_wait(S.full + s, (q / OL_STAGES) & 1u, P.abort_flag, P.timeout_ns)) { ok = false; break; }
+            tc_fence_after();
+            ol_mma_step(P, tmem + (uint32_t)(b * OL_N), S.resident, S.ring + s * OL_STAGE, kt, idesc);
+            if (kt + 1 < P.k_tiles) umma_commit(S.empty + s);
+          }
+          if (!ok) break;
+          umma_commit(S.accf + b);
+          committed = T + 1;
+        }
+        // the resident tile is free once this unit's MMAs have completed
+        if (ok) umma_commit(S.res_empty);
+      }
+      if (committed > 0) {
+        const int c = committed - 1;
+        const uint64_t w0 = globaltimer();
+        while (!mbar_try_wait(S.accf + (c % OL_NBUF), (c / OL_NBUF) & 1)) if (globaltimer() - w0 > P.timeout_ns) break;
+      }
+    }
+  } else {
+    // epilogue: warp w reads TMEM lane quarter w % 4 (rows 32 (w % 4) + lane)
+    // and columns 32 (w / 4) .. +31 of each tile
+    const int quarter = warp & 3, cgrp = warp >> 2;
+    const int row_local = quarter * 32 + lane;
+    int ok = 1, T = 0;
+    for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+      int pair, r0;
+      int64_t rbase, cbase;
+      unit_rows(u, pair, rbase, cbase, r0);
+      float mx = -INFINITY, sm = 0.f, sc = 0.f;
+      const float alpha = P.alpha_p ? __ldg(P.alpha_p + pair) : P.alpha;
+      const uint64_t a2 = pack2(alpha, alpha);
+      for (int tile = 0; tile < ntl; ++tile, ++T) {
+        const int b = T % OL_NBUF;
+        if (lane == 0) ok = mbar_wait(S.accf + b, (T / OL_NBUF) & 1, P.abort_flag, P.timeout_ns) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        __syncwarp();
+        if (!ok) break;
+        tc_fence_after();
+        const int s = (T * P.k_tiles + P.k_tiles - 1) % OL_STAGES;
+        ol_epi_tile<MAXP>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * OL_N + cgrp * 32),
+                          S.hbuf + s * OL_N + cgrp * 32, a2, S.acce + b, S.relcnt + s, S.empty + s, lane, mx, sm,
+                          sc);
+      }
+      if (cgrp > 0) { S.red[(cgrp - 1) * 2 * OL_M + row_local] = mx; S.red[(cgrp - 1) * 2 * OL_M + OL_M + row_local] = sm; }
+      named_bar(1, OL_EPI * 32);
+      if (cgrp == 0 && ok) ol_rows_out<MAXP>(P, S.red, row_local, mx, sm, r0, rbase, 0);
+      // the partials are read before the next unit writes them again
+      named_bar(1, OL_EPI * 32);
     }
   }
   tc_fence_before();
@@ -704,8 +871,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     return OTG_ERR_CUDA;
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(online_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(online_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) != cudaSuccess)
       return OTG_ERR_CUDA;
     attr = true;
   }
@@ -725,7 +891,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
   auto pass = [&](OnlinePass& P, const CUtensorMap& ah, const CUtensorMap& al, const CUtensorMap& bh,
                   const CUtensorMap& bl, int64_t rows_pad, int split, double* eslot_of_pass) {
     P.split = split; P.rows_pad = (int)rows_pad; P.part = part;
-    online_pass_kernel<false><<<dim3((unsigned)(rows_pad / OL_M), (unsigned)split), OL_THREADS, OL_SMEM, st>>>(ah, al, bh,
+    online_pass_kernel<<<dim3((unsigned)(rows_pad / OL_M), (unsigned)split), OL_THREADS, OL_SMEM, st>>>(ah, al, bh,
                                                                                                        bl, P);
     if (split > 1) online_finalize_kernel<<<(unsigned)((rows_pad + 255) / 256), 256, 0, st>>>(P);
     // the L1 error: the row slots summed in a fixed order (the same value in every run)
@@ -840,12 +1006,25 @@ int pairs_check(const OtgPairsProblem* q) {
   return OTG_OK;
 }
 
+// CTAs of a batch pass: one per SM (each keeps its TMEM and pipeline across
+// the (pair, row block) units it takes), fewer when there are fewer units.
+int pairs_grid(int64_t units) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
+  }
+  return (int)std::min<int64_t>(units, sms);
+}
+
 bool pairs_attr() {
   static bool done = false;
   if (done) return true;
-  if (cudaFuncSetAttribute(online_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) !=
+  if (cudaFuncSetAttribute(online_batch_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) !=
           cudaSuccess ||
-      cudaFuncSetAttribute(online_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) !=
+      cudaFuncSetAttribute(online_batch_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OL_SMEM) !=
           cudaSuccess)
     return false;
   done = true;
@@ -963,7 +1142,7 @@ int otg_pairs_max_cost(const OtgPairsProblem* q, double* maxc, cudaStream_t st) 
   A.rterm = reinterpret_cast<const float*>(w + L.xn);
   float* rowmax = reinterpret_cast<float*>(w + L.u2);
   A.pot_out2 = rowmax;
-  online_pass_kernel<true><<<(unsigned)(P * A.nrb), OL_THREADS, OL_SMEM, st>>>(mxh, mxl, myh, myl, A);
+  online_batch_kernel<true><<<(unsigned)pairs_grid(P * A.nrb), OL_THREADS, OL_SMEM, st>>>(mxh, mxl, myh, myl, A);
   pairs_max_finish_kernel<<<P, 256, 0, st>>>(rowmax, (int)q->n, L.n_pad, maxc);
   int hflag = 0;
   if (cudaMemcpyAsync(&hflag, abort_flag, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return OTG_ERR_CUDA;
@@ -1047,7 +1226,7 @@ int otg_sinkhorn_pairs(const OtgPairsProblem* q, cudaStream_t st) {
     G.h = S.hx; G.rterm = F(L.nyk); G.logw2 = F(L.lb2); G.pot2 = S.v2[cur]; G.w = F(L.wb);
     G.pot_out2 = S.v2[cur ^ 1]; G.other_norm2 = S.yk; G.h_out = S.hy; G.err = prev_check ? S.erow : nullptr;
     G.err_sq = 1;
-    online_pass_kernel<false><<<(unsigned)(nact * nrb_y), OL_THREADS, OL_SMEM, st>>>(myh, myl, mxh, mxl, G);
+    online_batch_kernel<false><<<(unsigned)pairs_grid(nact * nrb_y), OL_THREADS, OL_SMEM, st>>>(myh, myl, mxh, mxl, G);
     if (prev_check || at_max) {
       pairs_decide_kernel<<<nact, 256, 0, st>>>(S, S.v2[cur], ii, prev_check ? 1 : 0, at_max ? 1 : 0);
       pairs_compact_kernel<<<1, 1024, 0, st>>>(S);
@@ -1065,7 +1244,7 @@ int otg_sinkhorn_pairs(const OtgPairsProblem* q, cudaStream_t st) {
     OnlinePass Fp = pairs_pass(L, w, true, (int)q->n, nrb_y, kt, S.act, S.cnt, abort_flag, tmo);
     Fp.h = S.hy; Fp.rterm = F(L.nxk); Fp.logw2 = F(L.la2); Fp.pot2 = S.u2; Fp.w = F(L.wa);
     Fp.pot_out2 = S.u2; Fp.other_norm2 = S.xk; Fp.h_out = S.hx;
-    online_pass_kernel<false><<<(unsigned)(nact * nrb_x), OL_THREADS, OL_SMEM, st>>>(mxh, mxl, myh, myl, Fp);
+    online_batch_kernel<false><<<(unsigned)pairs_grid(nact * nrb_x), OL_THREADS, OL_SMEM, st>>>(mxh, mxl, myh, myl, Fp);
     if (cudaGetLastError() != cudaSuccess) return OTG_ERR_CUDA;
     cur ^= 1;
     prev_check = ii % period == 0;
