@@ -542,10 +542,25 @@ typedef struct OtgSplitGemm {
    * ld_add; may alias out) -- the (1 - alpha) M term of fused GW,
    * ot/gromov/_bregman.py:1184-1190 */
   const float* addend; int64_t ld_add; float s_add;
+  /* batched form (batch > 1; 0 or 1: one product): `batch` independent
+   * products of equal shape, one per grid z-slice.  The planes stack the
+   * problems' padded planes (A: batch * a_rows rows, B: batch * b_rows
+   * rows); problem z reads rows z*a_rows.. of A and z*b_rows.. of B and
+   * writes mode-0 planes from row z*a_rows.  Mode 1: problem z writes
+   * out + z*o_bstride, reads rowv + z*rowv_bstride, colv + z*colv_bstride
+   * and addend + z*addend_bstride (element strides).  Replaces the batched
+   * einsum chains of ot/batch/_quadratic.py:535-572 (tensor_product_batch). */
+  int64_t batch;
+  int64_t o_bstride, rowv_bstride, colv_bstride, addend_bstride;
 } OtgSplitGemm;
 int otg_split_half(const float* X, int64_t rows, int64_t cols, int64_t ldx, float scale, int transpose, void* hi,
                    void* lo, int64_t ld_out, cudaStream_t stream);
 int otg_gemm_split3(const OtgSplitGemm* g, cudaStream_t stream);
+/* otg_split_half over `batch` problems: problem z reads X + z*sx and writes
+ * its planes at hi/lo + z*so (element strides). */
+int otg_split_half_batched(const float* X, int64_t rows, int64_t cols, int64_t ldx, int64_t sx, float scale,
+                           int transpose, void* hi, void* lo, int64_t ld_out, int64_t so, int64_t batch,
+                           cudaStream_t stream);
 /* Batched tiled GEMM (CUDA cores), C_z = alpha op(A_z) op(B_z) + beta C_z for z < batch with
  * element strides sA, sB, sC between batch members; replaces the einsum chains of
  * ot/batch/_quadratic.py:535-572 (tensor_product_batch). */

@@ -78,7 +78,8 @@ class OtgSplitGemm(ctypes.Structure):
                 ("s_acc", ctypes.c_float), ("s_vec", ctypes.c_float), ("out_hi", c_vp), ("out_lo", c_vp),
                 ("ld_h", c_i64), ("out", c_vp), ("ld_o", c_i64), ("M", c_i64), ("N", c_i64), ("rowv", c_vp),
                 ("colv", c_vp), ("abort_flag", c_vp), ("timeout_ms", c_i32), ("addend", c_vp), ("ld_add", c_i64),
-                ("s_add", ctypes.c_float)]
+                ("s_add", ctypes.c_float), ("batch", c_i64), ("o_bstride", c_i64), ("rowv_bstride", c_i64),
+                ("colv_bstride", c_i64), ("addend_bstride", c_i64)]
 
 
 class OtgBaryProblem(ctypes.Structure):
@@ -146,6 +147,8 @@ SIGNATURES = {
     "otg_split_half": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, ctypes.c_float, ctypes.c_int, c_vp, c_vp, c_i64,
                                       c_vp]),
     "otg_gemm_split3": (ctypes.c_int, [ctypes.POINTER(OtgSplitGemm), c_vp]),
+    "otg_split_half_batched": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_i64, ctypes.c_float, ctypes.c_int, c_vp,
+                                              c_vp, c_i64, c_i64, c_i64, c_vp]),
     "otg_mlp_relu_bwd": (ctypes.c_int, [c_vp, c_vp, c_i64, c_vp]),
     "otg_mlp_colsum": (ctypes.c_int, [c_vp, c_i64, c_i64, c_vp, c_vp]),
     "otg_mlp_segment_mean": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, c_vp]),

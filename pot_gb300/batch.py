@@ -552,6 +552,84 @@ def _bgemm(A, B, ta, tb, out, alpha=1.0, beta=0.0):
     return out
 
 
+class _BatchPlanes:
+    """High/low half planes of a batch of equal-shape operands, each padded
+    to whole 128 tiles and stacked (problem z from row z * rows)."""
+
+    def __init__(self, B, rows, cols, device):
+        self.B, self.rows, self.cols = B, -(-rows // 128) * 128, -(-cols // 128) * 128
+        self.hi = torch.zeros(B * self.rows, self.cols, dtype=torch.float16, device=device)
+        self.lo = torch.zeros_like(self.hi)
+
+    def fill(self, X, scale=1.0, transpose=False):
+        """planes of scale * X_z (or its transpose) for X of shape (B, r, c)."""
+        lib = _lib.load()
+        X = X.contiguous()
+        _, r, c = X.shape
+        _lib.check(lib.otg_split_half_batched(_lib.ptr(X), r, c, c, r * c, float(scale), int(transpose),
+                                              _lib.ptr(self.hi), _lib.ptr(self.lo), self.cols, self.rows * self.cols,
+                                              self.B, _lib.stream_handle(X.device)), "otg_split_half_batched")
+        return self
+
+
+class _BatchTensorProduct:
+    """``out_z = s_acc hC1_z T_z hC2_z^T + s_vec (rowv_z,i + colv_z,j)
+    [+ s_add addend_z]`` for a float32 batch of equal-shape problems: two
+    tcgen05 split-GEMM launches per product over the whole batch (one grid
+    z-slice per problem), the operands as stacked high/low half planes with
+    exact power-of-two prescales (the batch's largest entries), fp32-grade
+    products.  ``hC1^T T hC2`` (asymmetric costs) uses the transposed planes.
+    Replaces the einsum chain of ``tensor_product_batch``
+    (``ot/batch/_quadratic.py:535-572``)."""
+
+    def __init__(self, hC1, hC2, qmax, tmax, transposed=False):
+        from .gromov import pow2_scale
+        self.B, self.n, self.m = hC1.shape[0], hC1.shape[1], hC2.shape[1]
+        dev = hC1.device
+        B, n, m = self.B, self.n, self.m
+        self.lib = _lib.load()
+        c1max = float(hC1.abs().max())
+        self.s1 = pow2_scale(c1max)
+        self.s2 = pow2_scale(float(hC2.abs().max()))
+        self.sT = pow2_scale(tmax)
+        # (hC1 T)_ij <= max|hC1| sum_k T_kj = max|hC1| q_j
+        self.e1 = pow2_scale(self.s1 * c1max * qmax * self.sT)
+        self.A1 = _BatchPlanes(B, n, n, dev).fill(hC1, self.s1)
+        self.B2 = _BatchPlanes(B, m, m, dev).fill(hC2, self.s2)
+        self.A1t = _BatchPlanes(B, n, n, dev).fill(hC1, self.s1, transpose=True) if transposed else None
+        self.B2t = _BatchPlanes(B, m, m, dev).fill(hC2, self.s2, transpose=True) if transposed else None
+        self.Tt = _BatchPlanes(B, m, n, dev)
+        self.P1 = _BatchPlanes(B, n, m, dev)
+        self.flag = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def _gemm(self, A, Bp, k, **kw):
+        g = _lib.OtgSplitGemm(a_hi=_lib.ptr(A.hi), a_lo=_lib.ptr(A.lo), a_rows=A.rows, lda=A.cols,
+                              b_hi=_lib.ptr(Bp.hi), b_lo=_lib.ptr(Bp.lo), b_rows=Bp.rows, ldb=Bp.cols,
+                              k_alloc=-(-k // 64) * 64, abort_flag=_lib.ptr(self.flag), timeout_ms=0,
+                              batch=self.B, **kw)
+        _lib.check(self.lib.otg_gemm_split3(ctypes.byref(g), _lib.stream_handle(self.flag.device)),
+                   "otg_gemm_split3")
+
+    def product(self, T, out, s_acc, s_vec, rowv, colv, addend=None, s_add=0.0, transposed=False):
+        n, m = self.n, self.m
+        A1, B2 = (self.A1t, self.B2t) if transposed else (self.A1, self.B2)
+        self.Tt.fill(T, self.sT, transpose=True)
+        # P1 = e1 (s1 hC1)(sT T) as planes; acc of the second GEMM = e1 s1 sT s2 (hC1 T hC2^T)
+        self._gemm(A1, self.Tt, n, mode=0, scale=self.e1, out_hi=_lib.ptr(self.P1.hi),
+                   out_lo=_lib.ptr(self.P1.lo), ld_h=self.P1.cols, M=n, N=m)
+        rowv, colv = rowv.contiguous(), colv.contiguous()
+        self._gemm(self.P1, B2, m, mode=1, scale=1.0, s_acc=s_acc / (self.s1 * self.sT * self.e1 * self.s2),
+                   s_vec=s_vec, out=_lib.ptr(out), ld_o=m, M=n, N=m, rowv=_lib.ptr(rowv), colv=_lib.ptr(colv),
+                   o_bstride=n * m, rowv_bstride=n, colv_bstride=m,
+                   addend=_lib.ptr(addend) if addend is not None else None, ld_add=m if addend is not None else 0,
+                   addend_bstride=n * m if addend is not None else 0, s_add=float(s_add))
+        return out
+
+    def check_abort(self):
+        if int(self.flag.item()) != 0:
+            raise RuntimeError("pot_gb300: a device-side wait of the tensor-core GEMM timed out")
+
+
 def solve_gromov_batch(C1, C2, reg=1e-2, a=None, b=None, loss="sqeuclidean", symmetric=None, M=None, alpha=None,
                        T_init=None, max_iter=50, tol=1e-5, max_iter_inner=50, tol_inner=1e-5, grad="envelope",
                        logits=None, per_problem=False):
@@ -596,32 +674,69 @@ def solve_gromov_batch(C1, C2, reg=1e-2, a=None, b=None, loss="sqeuclidean", sym
         if alpha < 0 or alpha > 1:
             raise ValueError("Alpha must be in [0, 1] for Fused Gromov-Wasserstein problem")
 
+    def const_parts(p, q):
+        return torch.einsum("bij,bj->bi", fC1, p), torch.einsum("bij,bj->bi", fC2, q)
+
     def const_of(p, q):
-        return (torch.einsum("bij,bj->bi", fC1, p)[:, :, None] + torch.einsum("bij,bj->bi", fC2, q)[:, None, :])
+        r, c = const_parts(p, q)
+        return r[:, :, None] + c[:, None, :]
 
-    tmp = torch.empty((B, n, m), dtype=dt, device=dev)
-    dotb = torch.empty((B, n, m), dtype=dt, device=dev)
-
-    def dot(T):
-        _bgemm(hC1, T, 0, 0, tmp)
-        _bgemm(tmp, hC2, 0, 1, dotb)                 # hC1 T hC2^T
-        if not symmetric:
-            _bgemm(hC1t, T, 0, 0, tmp)
-            _bgemm(tmp, hC2t, 0, 1, dotb, 0.5, 0.5)  # average with hC1^T T hC2
-        return dotb
-
-    constC = const_of(ad, bv)
     if T_init is None:
         const = torch.sqrt(ad.sum(1) * bv.sum(1))
         T = torch.einsum("bi,bj->bij", ad, bv) / const[:, None, None]
     else:
         T = bd.to_dev(T_init, dt).contiguous()
+
+    if dt == torch.float32:
+        # tensor cores: the fused products write s_acc dot + s_vec constC (+ addend) directly
+        tp = _BatchTensorProduct(hC1, hC2, float(bv.max()), min(float(ad.max()), float(bv.max())),
+                                 transposed=not symmetric)
+        buf = torch.empty((B, n, m), dtype=dt, device=dev)
+
+        def lin_minus_dot(T, s_dot, s_const, rowv, colv, addend=None, s_add=0.0):
+            """s_dot * dot(T) + s_const * (rowv_i + colv_j) [+ s_add addend]"""
+            Tc = T.contiguous()
+            if symmetric:
+                return tp.product(Tc, buf, s_dot, s_const, rowv, colv, addend, s_add)
+            tp.product(Tc, buf, 0.5 * s_dot, s_const, rowv, colv, addend, s_add)
+            return tp.product(Tc, buf, 0.5 * s_dot, 0.0, rowv, colv, buf, 1.0, transposed=True)
+
+        rv0, cv0 = const_parts(ad, bv)
+        has_lin = alpha != 1
+
+        def cost_of(T):   # Mk = (1 - alpha) M + 2 alpha (constC - dot)
+            return lin_minus_dot(T, -2.0 * alpha, 2.0 * alpha, rv0, cv0, Md if has_lin else None,
+                                 (1 - alpha) if has_lin else 0.0)
+
+        def quad_of(T):   # const_of(T marginals) - dot(T)
+            r, c = const_parts(T.sum(2), T.sum(1))
+            return lin_minus_dot(T, -1.0, 1.0, r, c)
+    else:
+        tmp = torch.empty((B, n, m), dtype=dt, device=dev)
+        dotb = torch.empty((B, n, m), dtype=dt, device=dev)
+
+        def dot(T):
+            _bgemm(hC1, T, 0, 0, tmp)
+            _bgemm(tmp, hC2, 0, 1, dotb)                 # hC1 T hC2^T
+            if not symmetric:
+                _bgemm(hC1t, T, 0, 0, tmp)
+                _bgemm(tmp, hC2t, 0, 1, dotb, 0.5, 0.5)  # average with hC1^T T hC2
+            return dotb
+
+        constC = const_of(ad, bv)
+
+        def cost_of(T):
+            return (1 - alpha) * Md + 2 * alpha * (constC - dot(T))
+
+        def quad_of(T):
+            return const_of(T.sum(2), T.sum(1)) - dot(T)
+
     log_T = torch.log(T + 1e-15)
     it = 0
     u = v = None
     for it in range(max_iter):
         T_prev = T
-        Mk = (1 - alpha) * Md + 2 * alpha * (constC - dot(T))
+        Mk = cost_of(T)
         K = -Mk / reg + log_T
         T, u, v, _, _, _ = _solve_uniform((-K).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_LOG, max_iter_inner,
                                           tol_inner, False, per_problem)
@@ -629,7 +744,9 @@ def solve_gromov_batch(C1, C2, reg=1e-2, a=None, b=None, loss="sqeuclidean", sym
         if float(torch.amax(torch.mean(torch.abs(T_prev - T), dim=(1, 2)))) < tol:
             break
     vl = (Md * T).sum((1, 2))
-    vq = ((const_of(T.sum(2), T.sum(1)) - dot(T)) * T).sum((1, 2))
+    vq = (quad_of(T) * T).sum((1, 2))
+    if dt == torch.float32:
+        tp.check_abort()
     return OTResult(value=bd.out((1 - alpha) * vl + alpha * vq), value_linear=bd.out((1 - alpha) * vl),
                     value_quad=bd.out(alpha * vq), plan=bd.out(T), potentials=(bd.out(u), bd.out(v)),
                     log={"n_iter": it})

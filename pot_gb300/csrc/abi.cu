@@ -209,7 +209,12 @@ namespace {
   X(timeout_ms) \
   X(addend) \
   X(ld_add) \
-  X(s_add)
+  X(s_add) \
+  X(batch) \
+  X(o_bstride) \
+  X(rowv_bstride) \
+  X(colv_bstride) \
+  X(addend_bstride)
 
 #define OTG_FIELDS_OtgPairsProblem(X) \
   X(X) \

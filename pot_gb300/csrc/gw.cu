@@ -53,6 +53,8 @@ struct GemmEpi {
   float* out; int64_t ld_o;
   const float* rowv; const float* colv;
   const float* addend; int64_t ld_add; float s_add;  // mode 1, optional
+  int64_t a_rows, b_rows;       // rows per problem of the stacked planes (batched form)
+  int64_t o_bs, rv_bs, cv_bs, add_bs;  // mode 1: element strides between problems
   int k_tiles;
   int* abort_flag;
   uint64_t timeout_ns;
@@ -70,6 +72,10 @@ gemm_split3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
   uint32_t* tslot = reinterpret_cast<uint32_t*>(acce + 2);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
+  // problem z of a batch: its rows of the stacked planes start at z a_rows
+  // (A, mode-0 output) and z b_rows (B)
+  const int z = blockIdx.z;
+  const int am0 = (int)(z * ep.a_rows) + m0, bn0 = (int)(z * ep.b_rows) + n0;
   const int nchunks = (ep.k_tiles + GB_CHUNK - 1) / GB_CHUNK;
 
   if (threadIdx.x == 0) {
@@ -93,10 +99,10 @@ gemm_split3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
         if (!mbar_wait(empty + s, (round & 1u) ^ 1u, ep.abort_flag, ep.timeout_ns)) break;
         unsigned char* st = smem + s * GB_STAGE;
         mbar_arrive_expect_tx(full + s, GB_STAGE);
-        tma_load_2d(st, &tAh, kt * GB_K, m0, full + s);
-        tma_load_2d(st + GB_TILE_A, &tAl, kt * GB_K, m0, full + s);
-        tma_load_2d(st + 2 * GB_TILE_A, &tBh, kt * GB_K, n0, full + s);
-        tma_load_2d(st + 2 * GB_TILE_A + GB_TILE_B, &tBl, kt * GB_K, n0, full + s);
+        tma_load_2d(st, &tAh, kt * GB_K, am0, full + s);
+        tma_load_2d(st + GB_TILE_A, &tAl, kt * GB_K, am0, full + s);
+        tma_load_2d(st + 2 * GB_TILE_A, &tBh, kt * GB_K, bn0, full + s);
+        tma_load_2d(st + 2 * GB_TILE_A + GB_TILE_B, &tBl, kt * GB_K, bn0, full + s);
         ++issued;
       }
       // copies still in flight must land before the CTA can leave
@@ -188,29 +194,31 @@ gemm_split3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
             h[i] = __float2half_rn(x);
             l[i] = __float2half_rn(x - __half2float(h[i]));
           }
-          uint4* dh = reinterpret_cast<uint4*>(ep.out_hi + row * ep.ld_h + col0);
-          uint4* dl = reinterpret_cast<uint4*>(ep.out_lo + row * ep.ld_h + col0);
+          const int64_t prow = z * ep.a_rows + row;  // row of the stacked output planes
+          uint4* dh = reinterpret_cast<uint4*>(ep.out_hi + prow * ep.ld_h + col0);
+          uint4* dl = reinterpret_cast<uint4*>(ep.out_lo + prow * ep.ld_h + col0);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             dh[q] = reinterpret_cast<const uint4*>(h)[q];
             dl[q] = reinterpret_cast<const uint4*>(l)[q];
           }
         } else if (row < ep.M) {
-          const float rv = ep.rowv[row];
-          float* dst = ep.out + row * ep.ld_o;
+          const float rv = ep.rowv[z * ep.rv_bs + row];
+          const float* colv = ep.colv + z * ep.cv_bs;
+          float* dst = ep.out + z * ep.o_bs + row * ep.ld_o;
           if (ep.addend) {
-            const float* add = ep.addend + row * ep.ld_add;
+            const float* add = ep.addend + z * ep.add_bs + row * ep.ld_add;
 #pragma unroll
             for (int i = 0; i < 32; ++i) {
               const int64_t col = col0 + i;
               if (col < ep.N)
-                dst[col] = fmaf(ep.s_add, add[col], ep.s_acc * acc[c0 + i] + ep.s_vec * (rv + ep.colv[col]));
+                dst[col] = fmaf(ep.s_add, add[col], ep.s_acc * acc[c0 + i] + ep.s_vec * (rv + colv[col]));
             }
           } else {
 #pragma unroll
             for (int i = 0; i < 32; ++i) {
               const int64_t col = col0 + i;
-              if (col < ep.N) dst[col] = ep.s_acc * acc[c0 + i] + ep.s_vec * (rv + ep.colv[col]);
+              if (col < ep.N) dst[col] = ep.s_acc * acc[c0 + i] + ep.s_vec * (rv + colv[col]);
             }
           }
         }
@@ -227,12 +235,17 @@ gemm_split3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
 
 // hi/lo half planes of scale*X (transpose = 0) or scale*X^T (transpose = 1).
 // X is rows x cols (ldx); out has ld_out columns.  32x32 tiles through
-// shared memory keep both the read and the write coalesced.
+// shared memory keep both the read and the write coalesced.  Batched form:
+// blockIdx.z selects the problem, sx and so are the element strides between
+// problems of X and of the planes.
 __global__ void __launch_bounds__(256) split_half_kernel(const float* __restrict__ X, int64_t rows, int64_t cols,
                                                          int64_t ldx, float scale, int transpose,
                                                          __half* __restrict__ hi, __half* __restrict__ lo,
-                                                         int64_t ld_out) {
+                                                         int64_t ld_out, int64_t sx, int64_t so) {
   __shared__ float tile[32][33];
+  X += blockIdx.z * sx;
+  hi += blockIdx.z * so;
+  lo += blockIdx.z * so;
   const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   for (int k = ty; k < 32; k += 8) {
@@ -299,7 +312,20 @@ int otg_split_half(const float* X, int64_t rows, int64_t cols, int64_t ldx, floa
   dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
   if (grid.y > 65535) return OTG_ERR_UNSUPPORTED;
   split_half_kernel<<<grid, 256, 0, stream>>>(X, rows, cols, ldx, scale, transpose, static_cast<__half*>(hi),
-                                              static_cast<__half*>(lo), ld_out);
+                                              static_cast<__half*>(lo), ld_out, 0, 0);
+  return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
+}
+
+int otg_split_half_batched(const float* X, int64_t rows, int64_t cols, int64_t ldx, int64_t sx, float scale,
+                           int transpose, void* hi, void* lo, int64_t ld_out, int64_t so, int64_t batch,
+                           cudaStream_t stream) {
+  if (!X || !hi || !lo || rows < 1 || cols < 1 || ldx < cols || batch < 1) return OTG_ERR_ARG;
+  if (ld_out < (transpose ? rows : cols)) return OTG_ERR_ARG;
+  if (batch > 1 && (sx < rows * ldx || so < (transpose ? cols : rows) * ld_out)) return OTG_ERR_ARG;
+  dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32), (unsigned)batch);
+  if (grid.y > 65535 || batch > 65535) return OTG_ERR_UNSUPPORTED;
+  split_half_kernel<<<grid, 256, 0, stream>>>(X, rows, cols, ldx, scale, transpose, static_cast<__half*>(hi),
+                                              static_cast<__half*>(lo), ld_out, sx, so);
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
 }
 
@@ -317,6 +343,12 @@ int otg_gemm_split3(const OtgSplitGemm* g, cudaStream_t stream) {
   ep.out_hi = static_cast<__half*>(g->out_hi); ep.out_lo = static_cast<__half*>(g->out_lo); ep.ld_h = g->ld_h;
   ep.out = g->out; ep.ld_o = g->ld_o; ep.rowv = g->rowv; ep.colv = g->colv;
   ep.addend = g->addend; ep.ld_add = g->ld_add; ep.s_add = g->s_add;
+  const int64_t batch = g->batch > 1 ? g->batch : 1;
+  if (batch > 65535) return OTG_ERR_UNSUPPORTED;
+  ep.a_rows = batch > 1 ? g->a_rows : 0;
+  ep.b_rows = batch > 1 ? g->b_rows : 0;
+  ep.o_bs = g->o_bstride; ep.rv_bs = g->rowv_bstride; ep.cv_bs = g->colv_bstride; ep.add_bs = g->addend_bstride;
+  if (batch > 1 && (g->a_rows * batch > INT32_MAX || g->b_rows * batch > INT32_MAX)) return OTG_ERR_UNSUPPORTED;
   ep.k_tiles = (int)(g->k_alloc / GB_K);
   ep.abort_flag = g->abort_flag;
   ep.timeout_ns = g->timeout_ms > 0 ? (uint64_t)g->timeout_ms * 1000000ull : 4000000000ull;
@@ -327,10 +359,15 @@ int otg_gemm_split3(const OtgSplitGemm* g, cudaStream_t stream) {
   } else {
     if (!ep.out || !ep.rowv || !ep.colv || ep.ld_o < ep.N || ep.M > g->a_rows || ep.N > g->b_rows) return OTG_ERR_ARG;
     if (ep.addend && ep.ld_add < ep.N) return OTG_ERR_ARG;
+    // problems' outputs and addends must not overlap one another
+    if (batch > 1 && (ep.o_bs < ep.M * ep.ld_o || ep.rv_bs < ep.M || ep.cv_bs < ep.N ||
+                      (ep.addend && ep.add_bs < ep.M * ep.ld_add)))
+      return OTG_ERR_ARG;
   }
   CUtensorMap mah, mal, mbh, mbl;
-  if (!make_plane_map(&mah, g->a_hi, g->a_rows, g->lda) || !make_plane_map(&mal, g->a_lo, g->a_rows, g->lda) ||
-      !make_plane_map(&mbh, g->b_hi, g->b_rows, g->ldb) || !make_plane_map(&mbl, g->b_lo, g->b_rows, g->ldb))
+  const int64_t ar = g->a_rows * batch, br = g->b_rows * batch;  // rows of the stacked planes
+  if (!make_plane_map(&mah, g->a_hi, ar, g->lda) || !make_plane_map(&mal, g->a_lo, ar, g->lda) ||
+      !make_plane_map(&mbh, g->b_hi, br, g->ldb) || !make_plane_map(&mbl, g->b_lo, br, g->ldb))
     return OTG_ERR_CUDA;
   static bool attr_set = false;
   if (!attr_set) {
@@ -339,7 +376,7 @@ int otg_gemm_split3(const OtgSplitGemm* g, cudaStream_t stream) {
       return OTG_ERR_CUDA;
     attr_set = true;
   }
-  dim3 grid((unsigned)(g->b_rows / GB_N), (unsigned)(g->a_rows / GB_M));
+  dim3 grid((unsigned)(g->b_rows / GB_N), (unsigned)(g->a_rows / GB_M), (unsigned)batch);
   if (grid.y > 65535) return OTG_ERR_UNSUPPORTED;
   gemm_split3_kernel<<<grid, GB_THREADS, GB_SMEM, stream>>>(mah, mal, mbh, mbl, ep);
   return cudaGetLastError() == cudaSuccess ? OTG_OK : OTG_ERR_CUDA;
