@@ -380,7 +380,9 @@ int otg_sinkhorn_pairs(const OtgPairsProblem* q, cudaStream_t stream);
  * error after iterations with (i+1) % 10 == 0, compared with <=.  The host
  * loop runs inside the call (one synchronisation per check), so the call
  * returns with the results; info[0] status, info[1] niter, info[2] number
- * of logged errors (err_hist is HOST memory, hist_cap doubles).  X: n x d,
+ * of logged errors, info[3] row blocks recomputed by fix-up passes (rows
+ * whose shifted sums left their range; info is HOST memory, 4 int32;
+ * err_hist is HOST memory, hist_cap doubles).  X: n x d,
  * Y: m x d fp32 row-major, d <= 128; a, b weights; warm_f, warm_g optional
  * natural-log potentials.
  * ---------------------------------------------------------------------- */

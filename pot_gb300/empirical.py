@@ -22,6 +22,10 @@ from . import bregman
 from . import batch as pb
 from .gromov import pow2_scale
 
+# statistics of the last online_sinkhorn call: fixup_units = row blocks that a
+# fix-up pass recomputed (their shifted sums left the representable range)
+LAST_STATS = {"fixup_units": 0}
+
 NONCONV_MSG = bregman.NONCONV_MSG
 
 
@@ -54,7 +58,7 @@ def online_sinkhorn(X, Y, reg, a, b, numIterMax, stopThr, warm_f=None, warm_g=No
     g = torch.empty(m, dtype=torch.float32, device=X.device)
     cap = max(2, numIterMax // 10 + 2)
     hist = (ctypes.c_double * cap)()
-    info = (ctypes.c_int32 * 3)()
+    info = (ctypes.c_int32 * 4)()
     p = _lib.OtgOnlineProblem(X=X.data_ptr(), Y=Y.data_ptr(), n=n, m=m, d=d, max_iter=int(numIterMax),
                               a=a.data_ptr(), b=b.data_ptr(),
                               warm_f=warm_f.data_ptr() if warm_f is not None else None,
@@ -66,6 +70,7 @@ def online_sinkhorn(X, Y, reg, a, b, numIterMax, stopThr, warm_f=None, warm_g=No
     _lib.check(lib.otg_sinkhorn_online(ctypes.byref(p), _lib.stream_handle(X.device)), "otg_sinkhorn_online")
     if info[0] == _lib.STATUS_ABORTED:
         raise RuntimeError("pot_gb300: a device-side wait of the online kernel timed out")
+    LAST_STATS["fixup_units"] = int(info[3])
     return f, g, info[0], info[1], [hist[k] for k in range(min(info[2], cap))]
 
 
