@@ -234,11 +234,56 @@ def sinkhorn_log(a, b, M, reg, numItermax=1000, stopThr=1e-9, verbose=False, log
 
 
 def _log_multi(bd, a, B, M, reg, numItermax, stopThr, verbose, log, warmstart):
-    """Several target histograms: one solve per column, as the reference's
-    recursion (``_sinkhorn.py:819-854``) does; returns the per-histogram
-    losses and a log holding only the potentials."""
+    """Several target histograms: every histogram is its own sinkhorn_log
+    solve, as in the reference's recursion (``_sinkhorn.py:819-854``), all of
+    them in one work-balanced launch of the batch kernel (the histograms
+    share the cost block; each stops on its own test).  Returns the
+    per-histogram losses and a log holding only the potentials.  With
+    ``verbose`` the histograms are solved one after another (the error
+    tables are printed per solve, as the reference does)."""
     H = B.shape[1]
     ws = warmstart if warmstart is not None else [None] * H
+    if verbose:
+        return _log_multi_sequential(bd, a, B, M, reg, numItermax, stopThr, verbose, log, ws)
+    from . import batch as pb
+    n, m = M.shape
+    dt, dev = M.dtype, M.device
+    lay = pb.RaggedLayout([n] * H, [m] * H, dt, dev)
+    ld = int(lay.ldm_np[0])
+    if ld == m and M.is_contiguous():
+        Mp = M.reshape(-1)
+    else:
+        Mp = torch.full((n, ld), float("inf"), dtype=dt, device=dev)
+        Mp[:, :m].copy_(M)
+        Mp = Mp.reshape(-1)
+    # one shared cost block: every histogram's problem reads it
+    lay.m_off.zero_()
+    lay.m_off_np = np.zeros(H, dtype=np.int64)
+    a_p = a.repeat(H).contiguous()
+    b_p = B.t().contiguous().reshape(-1)
+    warm_u = None
+    if warmstart is not None:
+        warm_u = torch.cat([_warm(bd, ws[k], dt)[0] for k in range(H)]).contiguous()
+    u, v, st, _, _, _ = pb.run_multi(lay, Mp, a_p, b_p, reg, numItermax, stopThr, warm_u=warm_u)
+    U, V = u.view(H, n).t(), v.view(H, m).t()
+    for k in range(H):
+        if int(st[k]) == _lib.STATUS_MAXITER:
+            warnings.warn(NONCONV_MSG)
+    losses = []
+    for k in range(H):
+        r = DenseResult()
+        r.u, r.v = U[:, k].contiguous(), V[:, k].contiguous()
+        losses.append(_loss(M, r, reg, _lib.OTG_METHOD_LOG))
+    res = torch.stack(losses)
+    if log:
+        lu, lv = U.contiguous(), V.contiguous()
+        return bd.out(res), {"log_u": bd.out(lu), "log_v": bd.out(lv), "u": bd.out(torch.exp(lu)),
+                             "v": bd.out(torch.exp(lv))}
+    return bd.out(res)
+
+
+def _log_multi_sequential(bd, a, B, M, reg, numItermax, stopThr, verbose, log, ws):
+    H = B.shape[1]
     losses, lus, lvs = [], [], []
     for k in range(H):
         r, _ = _run_single(bd, a, B[:, k].contiguous(), M, reg, _lib.OTG_METHOD_LOG, numItermax,
@@ -259,35 +304,42 @@ def _knopp_multi(bd, a, B, M, reg, numItermax, stopThr, verbose, log, warn, warm
     with ``n_hists``): the histograms evolve independently and interact only
     through the joint stop (Frobenius norm of all column-marginal errors) and
     the joint revert on numerical errors.  Each histogram is iterated on the
-    GPU with its error history; the joint stop index is found from the
-    histories, and every histogram is re-run to exactly that index."""
+    GPU with its error history, first over a short horizon that grows four
+    times until the joint stop (or a numerical error, or numItermax) falls
+    inside it; every histogram is then re-run to exactly that index (a run
+    that ended there already is kept)."""
     H = B.shape[1]
     wu = wv = None
     if warmstart is not None:
         wu = bd.to_dev(warmstart[0], M.dtype)
         wv = bd.to_dev(warmstart[1], M.dtype)
     warm = lambda k: (None, None) if wu is None else (wu[:, k].contiguous(), wv[:, k].contiguous())  # noqa: E731
-    runs = [solve_dense(M, a, B[:, k].contiguous(), reg, _lib.OTG_METHOD_KNOPP, numItermax, 0.0, *warm(k))
-            for k in range(H)]
-    nan_at = min([r.niter for r in runs if r.status == _lib.STATUS_NUMERICAL], default=None)
-    nchk = min(len(r.errs) for r in runs)
-    joint = [float(np.sqrt(sum(r.errs[k] ** 2 for r in runs))) for k in range(nchk)]
-    stop_ii, errs = None, []
-    for k, e in enumerate(joint):
-        ii = 10 * k
-        if nan_at is not None and ii >= nan_at:
+    horizon = min(numItermax, 64)
+    while True:
+        runs = [solve_dense(M, a, B[:, k].contiguous(), reg, _lib.OTG_METHOD_KNOPP, horizon, 0.0, *warm(k))
+                for k in range(H)]
+        nan_at = min([r.niter for r in runs if r.status == _lib.STATUS_NUMERICAL], default=None)
+        nchk = min(len(r.errs) for r in runs)
+        joint = [float(np.sqrt(sum(r.errs[k] ** 2 for r in runs))) for k in range(nchk)]
+        stop_ii, errs = None, []
+        for k, e in enumerate(joint):
+            ii = 10 * k
+            if nan_at is not None and ii >= nan_at:
+                break
+            errs.append(e)
+            if e < stopThr:
+                stop_ii = ii
+                break
+        if stop_ii is not None or nan_at is not None or horizon == numItermax:
             break
-        errs.append(e)
-        if e < stopThr:
-            stop_ii = ii
-            break
+        horizon = min(numItermax, 4 * horizon)
     if stop_ii is not None:
         final_iters, niter, status = stop_ii + 1, stop_ii, _lib.STATUS_CONVERGED
     elif nan_at is not None:
         final_iters, niter, status = nan_at, nan_at, _lib.STATUS_NUMERICAL
     else:
         final_iters, niter, status = numItermax, numItermax - 1, _lib.STATUS_MAXITER
-    if final_iters == numItermax and nan_at is None:
+    if final_iters == horizon and nan_at is None:
         final = runs
     else:
         final = [solve_dense(M, a, B[:, k].contiguous(), reg, _lib.OTG_METHOD_KNOPP, final_iters, 0.0, *warm(k))

@@ -160,6 +160,27 @@ def test_log_multi_histogram(cuda):
     np.testing.assert_allclose(lg["u"], g["log_u"], rtol=1e-7)
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_log_multi_histogram_matches_single_solves(cuda, dtype):
+    """Several histograms in one batch launch: every histogram exactly as its
+    own sinkhorn_log solve (the reference's recursion), warm starts per
+    histogram included; float32 with 7 columns exercises the padded block."""
+    rng = np.random.default_rng(5)
+    n, m, H = 90, 7 if dtype == np.float32 else 40, 4
+    M = rng.random((n, m)).astype(dtype)
+    a = np.full(n, 1.0 / n, dtype=dtype)
+    B = rng.dirichlet(np.ones(m), size=H).T.astype(dtype)
+    ws = [(rng.standard_normal(n).astype(dtype) * 0.1, np.zeros(m, dtype=dtype)) for _ in range(H)]
+    thr = 1e-9 if dtype == np.float64 else 1e-6
+    loss, lg = pg.sinkhorn2(a, B, M, 0.2, method="sinkhorn_log", log=True, stopThr=thr, warmstart=ws)
+    for k in range(H):
+        lk, lgk = pg.sinkhorn2(a, B[:, k], M, 0.2, method="sinkhorn_log", log=True, stopThr=thr, warmstart=ws[k])
+        tol = 1e-12 if dtype == np.float64 else 2e-5
+        np.testing.assert_allclose(loss[k], lk, rtol=tol)
+        np.testing.assert_allclose(lg["log_u"][:, k], lgk["log_u"], rtol=tol, atol=tol)
+        np.testing.assert_allclose(lg["log_v"][:, k], lgk["log_v"], rtol=tol, atol=tol)
+
+
 def test_knopp_multi_histogram(cuda):
     g = golden("multib_31x3")
     loss, lg = pg.sinkhorn2(g["a"], g["b"], g["M"], 1.0, method="sinkhorn", log=True, stopThr=1e-10)
