@@ -362,16 +362,21 @@ __global__ void __launch_bounds__(256) softmin_features_kernel(const float* __re
 
 // Soft-min of every source point over the k weighted atoms of its pair, the
 // squared distances computed on the fly (no cost block): one thread per
-// point, the pair's atoms in shared memory (stride D + 1: conflict-free).
-// Two sweeps over the atoms -- the maxima, then the sums -- so every term
-// costs one exponential; the squared distances are recomputed in the second
-// sweep (FMAs are cheaper than storing them).  Column 0 of the result is the
-// c-transform of the atoms' potential g at temperature g_tau (if g is given),
-// columns 1.. the soft-mins of the zero potential at taus[]; all in units of
-// scale[p], as softmin_features_kernel computes them from a cost block.
-// Every thread reads the same atom at the same time (broadcast), so the atoms
-// are stored densely and read as float4 when D is a multiple of 4.
-template <int D>
+// point, the pair's atoms in shared memory.  One sweep over the atoms in
+// chunks of SP_CHUNK: the chunk's distances, then per temperature one
+// rescale of the running (max, sum) to the chunk's max and the chunk's
+// exponentials (1 + 1/SP_CHUNK exponentials and one distance per term).
+// Slot 0 of the result is the c-transform of the atoms' potential g at
+// temperature g_tau (if g is given), slots 1.. the soft-mins of the zero
+// potential at taus[]; all in units of scale[p], as softmin_features_kernel
+// computes them from a cost block.  NT: the temperature slots handled (1:
+// slot 0 only).  Every thread reads the same atom at the same time
+// (broadcast), so the atoms are stored densely and read as float4 when D is
+// a multiple of 4.
+constexpr int SP_CHUNK = 8;
+constexpr int SP_PTS_PRIOR = 2;  // points per thread of the c-transform-only form
+
+template <int D, int NT, int PTS>
 __global__ void __launch_bounds__(256) softmin_points_kernel(const float* __restrict__ X, const float* __restrict__ C,
                                                              int n, int k, int64_t sx, int64_t sc,
                                                              const float* __restrict__ bw,
@@ -392,95 +397,161 @@ __global__ void __launch_bounds__(256) softmin_points_kernel(const float* __rest
     lg[c] = gw ? l + gw[(int64_t)p * k + c] * (float)OTG_LOG2E : l;
   }
   __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float x[D];
+  // points i0 + r * blockDim.x, r < PTS: every atom read from shared memory
+  // serves all of them
+  const int i0 = blockIdx.x * blockDim.x * PTS + threadIdx.x;
+  if (i0 >= n) return;
+  float x[PTS][D];
 #pragma unroll
-  for (int q = 0; q < D; ++q) x[q] = X[p * sx + (int64_t)i * D + q];
-  const int nt = ntau + 1;                     // slot 0: the c-transform of g
-  float ck[SM_MAXTAU + 1], mx[SM_MAXTAU + 1], s[SM_MAXTAU + 1];
+  for (int r = 0; r < PTS; ++r) {
+    const int i = min(i0 + r * (int)blockDim.x, n - 1);
 #pragma unroll
-  for (int t = 0; t <= SM_MAXTAU; ++t) {
+    for (int q = 0; q < D; ++q) x[r][q] = X[p * sx + (int64_t)i * D + q];
+  }
+  const int nt = NT == 1 ? 1 : ntau + 1;       // slot 0: the c-transform of g
+  float ck[NT], mx[PTS][NT], s[PTS][NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
     const float tau = t == 0 ? g_tau : (t <= ntau ? taus[t - 1] : 1.f);
     ck[t] = -(float)OTG_LOG2E / (scale[p] * tau);
-    mx[t] = -INFINITY;
-    s[t] = 0.f;
-  }
-  auto dist = [&](int c) {
-    const float* y = cs + c * D;
-    float d2 = 0.f;
-    if (D % 4 == 0) {
 #pragma unroll
-      for (int q = 0; q < D; q += 4) {
-        const float4 w = *reinterpret_cast<const float4*>(y + q);
-        float df = x[q] - w.x; d2 = fmaf(df, df, d2);
-        df = x[q + 1] - w.y; d2 = fmaf(df, df, d2);
-        df = x[q + 2] - w.z; d2 = fmaf(df, df, d2);
-        df = x[q + 3] - w.w; d2 = fmaf(df, df, d2);
+    for (int r = 0; r < PTS; ++r) { mx[r][t] = -INFINITY; s[r][t] = 0.f; }
+  }
+  for (int c0 = 0; c0 < k; c0 += SP_CHUNK) {
+    float d2[PTS][SP_CHUNK];
+#pragma unroll
+    for (int j = 0; j < SP_CHUNK; ++j) {
+      const int c = min(c0 + j, k - 1);
+      const float* y = cs + c * D;
+#pragma unroll
+      for (int r = 0; r < PTS; ++r) d2[r][j] = 0.f;
+      if (D % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < D; q += 4) {
+          const float4 w = *reinterpret_cast<const float4*>(y + q);
+#pragma unroll
+          for (int r = 0; r < PTS; ++r) {
+            float df = x[r][q] - w.x; d2[r][j] = fmaf(df, df, d2[r][j]);
+            df = x[r][q + 1] - w.y; d2[r][j] = fmaf(df, df, d2[r][j]);
+            df = x[r][q + 2] - w.z; d2[r][j] = fmaf(df, df, d2[r][j]);
+            df = x[r][q + 3] - w.w; d2[r][j] = fmaf(df, df, d2[r][j]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < D; ++q) {
+          const float yq = y[q];
+#pragma unroll
+          for (int r = 0; r < PTS; ++r) { const float df = x[r][q] - yq; d2[r][j] = fmaf(df, df, d2[r][j]); }
+        }
       }
-    } else {
-#pragma unroll
-      for (int q = 0; q < D; ++q) { const float df = x[q] - y[q]; d2 = fmaf(df, df, d2); }
     }
-    return d2;
-  };
-  for (int c = 0; c < k; ++c) {
-    const float d2 = dist(c);
-    mx[0] = fmaxf(mx[0], fmaf(d2, ck[0], lg[c]));
 #pragma unroll
-    for (int t = 1; t <= SM_MAXTAU; ++t)
-      if (t < nt) mx[t] = fmaxf(mx[t], fmaf(d2, ck[t], lb[c]));
+    for (int t = 0; t < NT; ++t) {
+      if (NT > 1 && t >= nt) break;
+      const float* l = t == 0 ? lg : lb;
+      float lc[SP_CHUNK];
+#pragma unroll
+      for (int j = 0; j < SP_CHUNK; ++j) lc[j] = c0 + j < k ? l[c0 + j] : -INFINITY;
+#pragma unroll
+      for (int r = 0; r < PTS; ++r) {
+        float v[SP_CHUNK];
+        float cm = -INFINITY;
+#pragma unroll
+        for (int j = 0; j < SP_CHUNK; ++j) {
+          v[j] = fmaf(d2[r][j], ck[t], lc[j]);
+          cm = fmaxf(cm, v[j]);
+        }
+        const float nm = fmaxf(mx[r][t], cm);
+        if (nm > -INFINITY) {  // (atoms of zero mass add nothing)
+          float acc = s[r][t] * ex2(mx[r][t] - nm);
+#pragma unroll
+          for (int j = 0; j < SP_CHUNK; ++j) acc += ex2(v[j] - nm);
+          s[r][t] = acc;
+          mx[r][t] = nm;
+        }
+      }
+    }
   }
-  for (int c = 0; c < k; ++c) {
-    const float d2 = dist(c);
-    s[0] += ex2(fmaf(d2, ck[0], lg[c]) - mx[0]);
 #pragma unroll
-    for (int t = 1; t <= SM_MAXTAU; ++t)
-      if (t < nt) s[t] += ex2(fmaf(d2, ck[t], lb[c]) - mx[t]);
+  for (int r = 0; r < PTS; ++r) {
+    const int i = i0 + r * (int)blockDim.x;
+    if (i >= n) break;
+    const int64_t row = (int64_t)p * n + i;
+    if (out_f) out_f[row] = -g_tau * (float)OTG_LN2 * lse_value(mx[r][0], s[r][0]);
+#pragma unroll
+    for (int t = 1; t < NT; ++t)
+      if (t < nt) out_F[row * ntau + (t - 1)] = -taus[t - 1] * (float)OTG_LN2 * lse_value(mx[r][t], s[r][t]);
   }
-  const int64_t row = (int64_t)p * n + i;
-  if (out_f) out_f[row] = -g_tau * (float)OTG_LN2 * lse_value(mx[0], s[0]);
-#pragma unroll
-  for (int t = 1; t <= SM_MAXTAU; ++t)
-    if (t < nt) out_F[row * ntau + (t - 1)] = -taus[t - 1] * (float)OTG_LN2 * lse_value(mx[t], s[t]);
 }
 
 // Voronoi cell masses: for every point of cloud p (n points, rows of X), the
 // nearest of its k centres (the first k points of the paired centre cloud)
-// gains weight 1/n.  Centres are staged in shared memory; one thread per point.
+// gains weight 1/n.  Centres and their squared norms are staged in shared
+// memory; each thread ranks the centres for NM_PTS points (every centre read
+// from shared memory serves them all) by |c|^2 - 2 x.c (|x - c|^2 less the
+// point's own |x|^2: one FMA per coordinate; the first of equal values wins).
+constexpr int NM_PTS = 2;
+
 template <int D>
 __global__ void __launch_bounds__(256) nearest_mass_kernel(const float* __restrict__ X, const float* __restrict__ Cc,
                                                            int n, int k, int64_t sx, int64_t sc, float* w) {
   extern __shared__ __align__(16) float cs[];
+  float* cn = cs + (size_t)k * D;  // [k] squared norms
   const int p = blockIdx.y;
   const float* C = Cc + p * sc;
   for (int e = threadIdx.x; e < k * D; e += blockDim.x) cs[e] = C[e];
   __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float x[D];
+  for (int c = threadIdx.x; c < k; c += blockDim.x) {
+    float q2 = 0.f;
+    for (int q = 0; q < D; ++q) q2 = fmaf(cs[c * D + q], cs[c * D + q], q2);
+    cn[c] = q2;
+  }
+  __syncthreads();
+  // points i0 + r * blockDim.x, r < NM_PTS (coalesced rows of X per r)
+  const int i0 = blockIdx.x * blockDim.x * NM_PTS + threadIdx.x;
+  float x[NM_PTS][D];
 #pragma unroll
-  for (int q = 0; q < D; ++q) x[q] = X[p * sx + (int64_t)i * D + q];
-  float best = INFINITY;
-  int arg = 0;
+  for (int r = 0; r < NM_PTS; ++r) {
+    const int i = min(i0 + r * (int)blockDim.x, n - 1);
+#pragma unroll
+    for (int q = 0; q < D; ++q) x[r][q] = -2.f * X[p * sx + (int64_t)i * D + q];
+  }
+  float best[NM_PTS];
+  int arg[NM_PTS];
+#pragma unroll
+  for (int r = 0; r < NM_PTS; ++r) { best[r] = INFINITY; arg[r] = 0; }
   for (int c = 0; c < k; ++c) {
-    float d2 = 0.f;
+    float v[NM_PTS];
+#pragma unroll
+    for (int r = 0; r < NM_PTS; ++r) v[r] = cn[c];
     if (D % 4 == 0) {  // every thread reads centre c: broadcast float4 loads
 #pragma unroll
       for (int q = 0; q < D; q += 4) {
-        const float4 w = *reinterpret_cast<const float4*>(cs + c * D + q);
-        float df = x[q] - w.x; d2 = fmaf(df, df, d2);
-        df = x[q + 1] - w.y; d2 = fmaf(df, df, d2);
-        df = x[q + 2] - w.z; d2 = fmaf(df, df, d2);
-        df = x[q + 3] - w.w; d2 = fmaf(df, df, d2);
+        const float4 y = *reinterpret_cast<const float4*>(cs + c * D + q);
+#pragma unroll
+        for (int r = 0; r < NM_PTS; ++r) {
+          v[r] = fmaf(x[r][q], y.x, v[r]);
+          v[r] = fmaf(x[r][q + 1], y.y, v[r]);
+          v[r] = fmaf(x[r][q + 2], y.z, v[r]);
+          v[r] = fmaf(x[r][q + 3], y.w, v[r]);
+        }
       }
     } else {
 #pragma unroll
-      for (int q = 0; q < D; ++q) { const float df = x[q] - cs[c * D + q]; d2 = fmaf(df, df, d2); }
+      for (int q = 0; q < D; ++q) {
+        const float y = cs[c * D + q];
+#pragma unroll
+        for (int r = 0; r < NM_PTS; ++r) v[r] = fmaf(x[r][q], y, v[r]);
+      }
     }
-    if (d2 < best) { best = d2; arg = c; }
+#pragma unroll
+    for (int r = 0; r < NM_PTS; ++r)
+      if (v[r] < best[r]) { best[r] = v[r]; arg[r] = c; }
   }
-  atomicAdd(w + (int64_t)p * k + arg, 1.0f / (float)n);
+#pragma unroll
+  for (int r = 0; r < NM_PTS; ++r)
+    if (i0 + r * (int)blockDim.x < n) atomicAdd(w + (int64_t)p * k + arg[r], 1.0f / (float)n);
 }
 
 // Loss of a lazy plan: sum_ij C_ij exp(f_i + g_j - C_ij / reg) with C the
@@ -581,8 +652,8 @@ int otg_nearest_mass(const float* X, const float* C, int32_t nprob, int32_t n, i
                      int64_t sc, float* w, cudaStream_t stream) {
   if (!X || !C || !w || nprob < 1 || nprob > 65535 || n < 1 || k < 1) return OTG_ERR_ARG;
   if (cudaMemsetAsync(w, 0, sizeof(float) * (size_t)nprob * k, stream) != cudaSuccess) return OTG_ERR_CUDA;
-  dim3 grid((unsigned)((n + 255) / 256), (unsigned)nprob);
-  const size_t sm = sizeof(float) * (size_t)k * d;
+  dim3 grid((unsigned)((n + 256 * NM_PTS - 1) / (256 * NM_PTS)), (unsigned)nprob);
+  const size_t sm = sizeof(float) * ((size_t)k * d + (size_t)k);
   if (sm > 48 * 1024) return OTG_ERR_UNSUPPORTED;
   if (d == 16) nearest_mass_kernel<16><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, w);
   else if (d == 8) nearest_mass_kernel<8><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, w);
@@ -600,10 +671,16 @@ int otg_softmin_points(const float* X, const float* C, int32_t nprob, int32_t n,
   if (out_f && !(g_tau > 0)) return OTG_ERR_ARG;
   const size_t sm = sizeof(float) * ((size_t)k * d + 2 * (size_t)k);
   if (sm > 48 * 1024) return OTG_ERR_UNSUPPORTED;
-  dim3 grid((unsigned)((n + 255) / 256), (unsigned)nprob);
+  const int pts = ntau == 0 ? SP_PTS_PRIOR : 1;  // points per thread
+  dim3 grid((unsigned)((n + 256 * pts - 1) / (256 * pts)), (unsigned)nprob);
   const float gt = out_f ? g_tau : 1.f;
-#define OTG_SOFTMIN_POINTS(DD) \
-  softmin_points_kernel<DD><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, b, g, gt, scale, taus, ntau, out_f, out_F)
+#define OTG_SOFTMIN_POINTS(DD)                                                                                     \
+  if (ntau == 0)                                                                                                   \
+    softmin_points_kernel<DD, 1, SP_PTS_PRIOR><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, b, g, gt, scale, taus,  \
+                                                                          ntau, out_f, out_F);                      \
+  else                                                                                                             \
+    softmin_points_kernel<DD, SM_MAXTAU + 1, 1><<<grid, 256, sm, stream>>>(X, C, n, k, sx, sc, b, g, gt, scale,     \
+                                                                           taus, ntau, out_f, out_F)
   if (d == 16) OTG_SOFTMIN_POINTS(16);
   else if (d == 8) OTG_SOFTMIN_POINTS(8);
   else if (d == 3) OTG_SOFTMIN_POINTS(3);
