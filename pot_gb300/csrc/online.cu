@@ -153,6 +153,27 @@ __device__ __forceinline__ void ext_put(__half* ext, int64_t row, float v, bool 
   ph[1] = make_uint4(0u, 0u, 0u, 0u);
 }
 
+// Shifted-sum arithmetic of one warp's 32 columns (accumulator values t - s
+// already in registers): the exponentials summed as packed pairs (columns
+// 4k, 4k+1 and 4k+2, 4k+3), one Kahan-compensated partial per tile.
+__device__ __forceinline__ void ol_fsum_acc(const uint32_t* v, float& sm, float& sc) {
+  uint64_t acc0 = 0ull, acc1 = 0ull;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const uint64_t e2 = pack2(ex2(__uint_as_float(v[2 * i])), ex2(__uint_as_float(v[2 * i + 1])));
+    if (i & 1) acc1 = add2(acc1, e2);
+    else acc0 = add2(acc0, e2);
+  }
+  float p0, p1, p2, p3;
+  unpack2(acc0, p0, p1);
+  unpack2(acc1, p2, p3);
+  const float part = (p0 + p1) + (p2 + p3);
+  const float y = part - sc;
+  const float tt = sm + y;
+  sc = (tt - sm) - y;
+  sm = tt;
+}
+
 // One tile of the epilogue for one warp: its 32 columns of the tile's
 // accumulator (TMEM address taddr) fold into the running base-2 (max, sum)
 // (OL_FSUM: sum) of the warp's rows.  The TMEM buffer (acce_b) is handed
@@ -169,22 +190,7 @@ __device__ __forceinline__ void ol_epi_tile(uint32_t taddr, const float* hcol, u
     tc_fence_before();
     __syncwarp();
     if (lane == 0) mbar_arrive(acce_b);
-    // the exponentials summed as packed pairs: columns 4k, 4k+1 and 4k+2, 4k+3
-    uint64_t acc0 = 0ull, acc1 = 0ull;
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const uint64_t e2 = pack2(ex2(__uint_as_float(v[2 * i])), ex2(__uint_as_float(v[2 * i + 1])));
-      if (i & 1) acc1 = add2(acc1, e2);
-      else acc0 = add2(acc0, e2);
-    }
-    float p0, p1, p2, p3;
-    unpack2(acc0, p0, p1);
-    unpack2(acc1, p2, p3);
-    const float part = (p0 + p1) + (p2 + p3);
-    const float y = part - sc;
-    const float tt = sm + y;
-    sc = (tt - sm) - y;
-    sm = tt;
+    ol_fsum_acc(v, sm, sc);
     return;
   }
   // packed fp32x2 arithmetic (one instruction per column pair, each lane
@@ -292,9 +298,26 @@ __device__ __forceinline__ void ol_mma_step(const OnlinePass& P, uint32_t dst, c
 // Returns false for a row that failed (OL_FSUM: its sum left the range; it
 // writes nothing and is marked for the fix-up).  A fix-up launch
 // (P.fixup) writes only the rows marked, and clears the marks.
+// A row's inputs for its finish, loaded by the finishing thread when the
+// unit starts (their memory latency then hides behind the unit's tiles).
+struct OlRowIn { float shift, rterm, logw2, onorm, pot2, w; };
+
+template <int MODE>
+__device__ __forceinline__ OlRowIn ol_row_in(const OnlinePass& P, int64_t ri, bool valid) {
+  OlRowIn v{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (!valid) return v;
+  v.rterm = P.rterm[ri];
+  if (MODE == OL_MAXP) return v;
+  if (MODE == OL_FMAX || MODE == OL_FSUM) v.shift = P.shift[ri];
+  v.logw2 = P.logw2[ri];
+  v.onorm = P.other_norm2[ri];
+  if (P.err) { v.pot2 = P.pot2[ri]; v.w = P.w[ri]; }
+  return v;
+}
+
 template <int MODE>
 __device__ __forceinline__ bool ol_rows_out(const OnlinePass& P, const float* red, int row_local, float mx, float sm,
-                                            int r0, int64_t rbase, int cs) {
+                                            int r0, int64_t rbase, int cs, const OlRowIn& in) {
   constexpr bool FOLD = MODE == OL_FMAX || MODE == OL_FSUM;
   if constexpr (MODE == OL_FSUM) {
     for (int g = 0; g < 3; ++g) sm += red[g * 2 * OL_M + OL_M + row_local];
@@ -304,7 +327,7 @@ __device__ __forceinline__ bool ol_rows_out(const OnlinePass& P, const float* re
   const int row = r0 + row_local;
   const int64_t ri = rbase + row;  // the row in the packed vectors
   if constexpr (MODE == OL_MAXP) {
-    if (row < P.n_rows) P.pot_out2[ri] = mx + P.rterm[ri];
+    if (row < P.n_rows) P.pot_out2[ri] = mx + in.rterm;
     return true;
   }
   if (MODE != OL_FSUM && P.split > 1) {
@@ -323,20 +346,20 @@ __device__ __forceinline__ bool ol_rows_out(const OnlinePass& P, const float* re
       P.fail[ri] = 1;
       return false;
     }
-    lse_t = P.shift[ri] + lg2(sm);
+    lse_t = in.shift + lg2(sm);
   } else if constexpr (MODE == OL_FMAX) {
-    lse_t = P.shift[ri] + lse_value(mx, sm);
+    lse_t = in.shift + lse_value(mx, sm);
   } else {
     lse_t = lse_value(mx, sm);
   }
-  const float L = lse_t + P.rterm[ri];  // base-2 LSE_j(g2_j - C_ij log2e/reg)
-  const float pnew = P.logw2[ri] - L;
+  const float L = lse_t + in.rterm;  // base-2 LSE_j(g2_j - C_ij log2e/reg)
+  const float pnew = in.logw2 - L;
   if (P.err) {
-    const double e = (double)ex2(P.pot2[ri] + L) - (double)P.w[ri];
+    const double e = (double)ex2(in.pot2 + L) - (double)in.w;
     P.err[ri] = P.err_sq ? e * e : fabs(e);
   }
   P.pot_out2[ri] = pnew;
-  const float hn = pnew - P.other_norm2[ri];
+  const float hn = pnew - in.onorm;
   if constexpr (FOLD) {
     ext_put(P.ext_str, ri, hn, true);
     ext_put(P.ext_row, ri, -lse_t, false);
@@ -538,6 +561,7 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
     // and columns 32 (w / 4) .. +31 of each tile
     const int quarter = warp & 3, cgrp = warp >> 2;
     const int row_local = quarter * 32 + lane;
+    const OlRowIn rin = ol_row_in<MODE>(P, r0 + row_local, cgrp == 0 && r0 + row_local < P.n_rows);
     float mx = -INFINITY, sm = 0.f, sc = 0.f;
     int ok = 1;
     const uint64_t a2 = pack2(P.alpha, P.alpha);
@@ -557,7 +581,7 @@ online_pass_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constan
     // merge the four column groups of each row
     if (cgrp > 0) { S.red[(cgrp - 1) * 2 * OL_M + row_local] = mx; S.red[(cgrp - 1) * 2 * OL_M + OL_M + row_local] = sm; }
     named_bar(1, OL_EPI * 32);
-    if (cgrp == 0 && ok && !ol_rows_out<MODE>(P, S.red, row_local, mx, sm, r0, 0, cs)) *S.uflag = 1;
+    if (cgrp == 0 && ok && !ol_rows_out<MODE>(P, S.red, row_local, mx, sm, r0, 0, cs, rin)) *S.uflag = 1;
     if constexpr (MODE == OL_FSUM) {
       named_bar(1, OL_EPI * 32);
       if (warp == 0 && lane == 0) ol_note_unit(P, S.uflag, 0, r0);
@@ -708,6 +732,7 @@ online_batch_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_consta
       int pair, r0;
       int64_t rbase, cbase;
       unit_rows(u, pair, rbase, cbase, r0);
+      const OlRowIn rin = ol_row_in<MODE>(P, rbase + r0 + row_local, cgrp == 0 && r0 + row_local < P.n_rows);
       float mx = -INFINITY, sm = 0.f, sc = 0.f;
       const float alpha = P.alpha_p ? __ldg(P.alpha_p + pair) : P.alpha;
       const uint64_t a2 = pack2(alpha, alpha);
@@ -725,7 +750,7 @@ online_batch_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_consta
       }
       if (cgrp > 0) { S.red[(cgrp - 1) * 2 * OL_M + row_local] = mx; S.red[(cgrp - 1) * 2 * OL_M + OL_M + row_local] = sm; }
       named_bar(1, OL_EPI * 32);
-      if (cgrp == 0 && ok && !ol_rows_out<MODE>(P, S.red, row_local, mx, sm, r0, rbase, 0)) *S.uflag = 1;
+      if (cgrp == 0 && ok && !ol_rows_out<MODE>(P, S.red, row_local, mx, sm, r0, rbase, 0, rin)) *S.uflag = 1;
       // the partials are read (and the unit's failures marked) before the
       // next unit writes them again
       named_bar(1, OL_EPI * 32);
