@@ -75,6 +75,30 @@ def test_non_lazy_matches_dense(cuda):
     np.testing.assert_allclose(P, Pref, rtol=1e-9, atol=1e-14)
 
 
+def test_online_small_reg_vs_oracle(cuda):
+    """reg = 0.02 x median cost from a zero start (the shifted sums of the
+    folded passes start from the running-max first pass; a row's LSE moves by
+    a few units of log2 per iteration here, well inside the range the
+    shifted sums hold, so no fix-up is needed): the oracle's plan."""
+    from pot_gb300.empirical import online_sinkhorn, LAST_STATS
+    n, m, d = 600, 520, 8
+    rng = np.random.default_rng(21)
+    X = rng.standard_normal((n, d))
+    Y = rng.standard_normal((m, d)) + 0.3
+    C = oracle.sqeuclidean(X, Y)
+    reg = 0.02 * float(np.median(C))
+    a, b = np.full(n, 1.0 / n), np.full(m, 1.0 / m)
+    fr, gr, lr = oracle.empirical_sinkhorn_lazy(X, Y, reg, a, b, numIterMax=5000, stopThr=1e-7, batchSize=512)
+    assert lr["niter"] < 4999
+    f32 = lambda z: torch.tensor(z, dtype=torch.float32, device=cuda)  # noqa: E731
+    f, g, st, nit, errs = online_sinkhorn(f32(X), f32(Y), reg, f32(a), f32(b), 5000, 1e-6)
+    assert LAST_STATS["fixup_units"] == 0
+    assert st == 0
+    P = plan(X, Y, f.double().cpu().numpy(), g.double().cpu().numpy(), reg)
+    Pref = plan(X, Y, fr, gr, reg)
+    assert np.abs(P - Pref).sum() / Pref.sum() <= 2e-5
+
+
 def test_online_column_split_vs_oracle(cuda):
     """n = m = 8192: enough row blocks and streamed tiles that each pass
     is split over column ranges (partials merged by online_finalize_kernel)."""

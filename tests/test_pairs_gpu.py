@@ -61,6 +61,30 @@ def test_pairs_vs_oracle(cuda, n, m, d, anderson):
         assert np.abs(Pg - Pref).sum() / Pref.sum() < 1e-4, p
 
 
+def test_pairs_far_start(cuda):
+    """A warm start far from the solution (random potentials of size 400 in
+    natural-log units): the first passes keep the running max, the later ones
+    sum under shifts taken from them, and every pair still reaches the float64
+    oracle's plan."""
+    P, n, m, d, tol = 4, 256, 384, 16, 1e-6
+    X, Y = _clouds(31, P, n, m, d, cuda)
+    regs = []
+    for p in range(P):
+        C = oracle.sqeuclidean(X[p].double().cpu().numpy(), Y[p].double().cpu().numpy())
+        regs.append(0.05 * C.max())
+    g = torch.Generator(device="cpu").manual_seed(4)
+    far = (torch.randn(P, n, generator=g) * 400.0).to(cuda)  # natural-log units, far from any solution
+    u, v, st, nit, err = pb.run_pairs(X, Y, regs, None, None, 20000, tol, warm_u=far, check_period=1)
+    assert (st == 0).all() and (err < tol).all()
+    for p in range(P):
+        Xp, Yp = X[p].double().cpu().numpy(), Y[p].double().cpu().numpy()
+        C = oracle.sqeuclidean(Xp, Yp)
+        Pg = np.exp(u[p].double().cpu().numpy()[:, None] - C / regs[p] + v[p].double().cpu().numpy()[None, :])
+        Pref, _ = oracle.sinkhorn_log(np.full(n, 1 / n), np.full(m, 1 / m), C, regs[p], numItermax=20000,
+                                      stopThr=1e-9)
+        assert np.abs(Pg - Pref).sum() / Pref.sum() < 1e-4, p
+
+
 def test_pairs_match_the_stored_cost_solver(cuda):
     """The same pairs through both engines of the pair solver: stop indices
     within one check, potentials to float32 precision."""
