@@ -363,6 +363,7 @@ typedef struct OtgPairsProblem {
   double* err;
   void* workspace;
   size_t workspace_bytes;
+  float sum_window_log2;  /* as in OtgOnlineProblem (0: default) */
 } OtgPairsProblem;
 size_t otg_pairs_workspace_bytes(int32_t npairs, int64_t n, int64_t m, int32_t d, int32_t anderson_depth);
 /* Each pair's largest squared distance max_ij |x_i - y_j|^2 (device, P
@@ -398,9 +399,14 @@ typedef struct OtgOnlineProblem {
   float scale_x, scale_y;
   float* out_f; float* out_g;
   double* err_hist; int32_t hist_cap;
-  int32_t* info;         /* HOST, 3 ints */
+  int32_t* info;         /* HOST, 4 ints */
   void* workspace; size_t workspace_bytes;
   int32_t timeout_ms;
+  /* shifted-sum acceptance window of the folded passes, in log2 units: a
+   * row's sum outside [2^-w, 2^w] is recomputed by the fix-up pass.  0: the
+   * default [2^-70, 2^100]; a narrow window sends most rows through the
+   * fix-up (a test of that path; the results are the same). */
+  float sum_window_log2;
 } OtgOnlineProblem;
 size_t otg_online_workspace_bytes(int64_t n, int64_t m, int32_t d);
 int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t stream);

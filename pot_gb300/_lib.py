@@ -57,7 +57,7 @@ class OtgPairsProblem(ctypes.Structure):
                 ("b", c_vp), ("reg", c_vp), ("warm_u", c_vp), ("max_iter", c_i32), ("check_period", c_i32),
                 ("stop_thr", c_dbl), ("anderson_depth", c_i32), ("timeout_ms", c_i32), ("out_u", c_vp),
                 ("out_v", c_vp), ("status", c_vp), ("niter", c_vp), ("err", c_vp), ("workspace", c_vp),
-                ("workspace_bytes", c_sz)]
+                ("workspace_bytes", c_sz), ("sum_window_log2", ctypes.c_float)]
 
 
 class OtgCostTable(ctypes.Structure):
@@ -94,7 +94,8 @@ class OtgOnlineProblem(ctypes.Structure):
                 ("a", c_vp), ("b", c_vp), ("warm_f", c_vp), ("warm_g", c_vp), ("reg", c_dbl), ("stop_thr", c_dbl),
                 ("scale_x", ctypes.c_float), ("scale_y", ctypes.c_float), ("out_f", c_vp), ("out_g", c_vp),
                 ("err_hist", ctypes.POINTER(c_dbl)), ("hist_cap", c_i32), ("info", ctypes.POINTER(c_i32)),
-                ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32)]
+                ("workspace", c_vp), ("workspace_bytes", c_sz), ("timeout_ms", c_i32),
+                ("sum_window_log2", ctypes.c_float)]
 
 
 # name -> (restype, argtypes)

@@ -501,15 +501,17 @@ def pairs_max_cost(X, Y):
 
 
 def run_pairs(X, Y, reg, a=None, b=None, max_iter=100000, tol=1e-6, warm_u=None, check_period=10, anderson=0,
-              timeout_ms=0):
+              timeout_ms=0, sum_window_log2=0.0):
     """Log-domain solves of P equal-size cloud pairs, X (P, n, d), Y (P, m, d)
     float32 on the device, squared-Euclidean cost never stored: every pass
     rebuilds cost tiles from the points on the tensor cores
     (otg_sinkhorn_pairs).  Per pair the iteration and stop test of
     ``run_multi`` (sinkhorn_log order, column-marginal L2 error every
     ``check_period`` iterations, each pair on its own; ``anderson`` > 0 mixes
-    the v updates).  ``reg``: (P,) absolute values.  Returns (u, v, status,
-    niter, err) with u (P, n), v (P, m) natural-log potentials."""
+    the v updates).  ``reg``: (P,) absolute values.  ``sum_window_log2`` > 0
+    narrows the acceptance window of the shifted sums (rows outside it go
+    through the fix-up pass; the results are the same).  Returns (u, v,
+    status, niter, err) with u (P, n), v (P, m) natural-log potentials."""
     X, Y = X.float().contiguous(), Y.float().contiguous()
     P, n, _ = X.shape
     m = Y.shape[1]
@@ -529,6 +531,7 @@ def run_pairs(X, Y, reg, a=None, b=None, max_iter=100000, tol=1e-6, warm_u=None,
     q.a, q.b, q.reg = a.data_ptr(), b.data_ptr(), reg_t.data_ptr()
     q.warm_u = wu.data_ptr() if wu is not None else None
     q.max_iter, q.check_period, q.stop_thr, q.timeout_ms = int(max_iter), int(check_period), float(tol), int(timeout_ms)
+    q.sum_window_log2 = float(sum_window_log2)
     q.out_u, q.out_v = u.data_ptr(), v.data_ptr()
     q.status, q.niter, q.err = status.data_ptr(), niter.data_ptr(), err.data_ptr()
     _lib.check(lib.otg_sinkhorn_pairs(ctypes.byref(q), _lib.stream_handle(dev)), "otg_sinkhorn_pairs")

@@ -146,7 +146,8 @@ namespace {
   X(info) \
   X(workspace) \
   X(workspace_bytes) \
-  X(timeout_ms)
+  X(timeout_ms) \
+  X(sum_window_log2)
 #define OTG_FIELDS_OtgCostTable(X) \
   X(dtype) \
   X(nprob) \
@@ -238,7 +239,8 @@ namespace {
   X(niter) \
   X(err) \
   X(workspace) \
-  X(workspace_bytes)
+  X(workspace_bytes) \
+  X(sum_window_log2)
 
 template <typename S>
 int write_layout(int64_t* out, int32_t cap, const size_t* offs, int nf) {

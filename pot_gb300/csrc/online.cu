@@ -112,6 +112,7 @@ struct OnlinePass {
   unsigned char* fail;
   int* fail_list; int* fail_cnt; unsigned* done_cnt;
   int fixup, units_enc;
+  float sum_lo, sum_hi;  // acceptance range of the shifted sums
 };
 
 // Epilogue modes of a pass.
@@ -342,7 +343,7 @@ __device__ __forceinline__ bool ol_rows_out(const OnlinePass& P, const float* re
   if (P.fixup && !P.fail[ri]) return true;
   float lse_t;  // base-2 LSE_j(t_ij), without the row term
   if constexpr (MODE == OL_FSUM) {
-    if (!(sm >= 0x1p-70f && sm <= 0x1p100f)) {
+    if (!(sm >= P.sum_lo && sm <= P.sum_hi)) {
       P.fail[ri] = 1;
       return false;
     }
@@ -1111,6 +1112,20 @@ int choose_split(int nb, int tiles, int sms) {
   return best;
 }
 
+// Acceptance range of the shifted sums: [2^-w, 2^w] for a window w > 0,
+// else [2^-70, 2^100] (terms below 2^-126 flush to zero, so a sum of at
+// least 2^-70 loses at most 2^-40 of itself to them; at most 2^100 leaves no
+// term near the float range's end).
+void ol_sum_window(float w, float& lo, float& hi) {
+  if (w > 0.f) {
+    lo = std::exp2(-std::min(w, 70.f));
+    hi = std::exp2(std::min(w, 100.f));
+  } else {
+    lo = 0x1p-70f;
+    hi = 0x1p100f;
+  }
+}
+
 // Dynamic shared memory of every pass kernel instantiation (once).
 bool online_attr() {
   static std::once_flag once;
@@ -1265,6 +1280,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     if (fold) {
       A.ext_row = xe[0]; A.ext_str = xe[1];
       A.shift = shx; A.shift_out = shx; A.fail = fax; A.fail_list = flist; A.fail_cnt = fcnt; A.done_cnt = fdone;
+      ol_sum_window(p->sum_window_log2, A.sum_lo, A.sum_hi);
     }
   };
   int cur = 0, nchk = 0, status = OTG_STATUS_MAXITER, niter = p->max_iter - 1;
@@ -1291,6 +1307,7 @@ int otg_sinkhorn_online(const OtgOnlineProblem* p, cudaStream_t st) {
     if (fold) {
       B.ext_row = ye[0]; B.ext_str = ye[1];
       B.shift = shy; B.shift_out = shy; B.fail = fay; B.fail_list = flist; B.fail_cnt = fcnt; B.done_cnt = fdone;
+      ol_sum_window(p->sum_window_log2, B.sum_lo, B.sum_hi);
     }
     pass(B, myh, myl, mxh, mxl, eyr, exs, mp, split_g, it == 0, nullptr);
     if (cudaGetLastError() != cudaSuccess) return OTG_ERR_CUDA;
@@ -1612,6 +1629,7 @@ int otg_sinkhorn_pairs(const OtgPairsProblem* q, cudaStream_t st) {
     A.shift = x_res ? F(L.shx) : F(L.shy); A.shift_out = const_cast<float*>(A.shift);
     A.fail = reinterpret_cast<unsigned char*>(w + (x_res ? L.fax : L.fay));
     A.fail_list = reinterpret_cast<int*>(w + L.flist); A.fail_cnt = fcnt; A.done_cnt = fdone;
+    ol_sum_window(q->sum_window_log2, A.sum_lo, A.sum_hi);
     if (first) {
       online_batch_kernel<OL_FMAX><<<grid, OL_THREADS, OL_SMEM, st>>>(ah, al, bh, bl, rx, sx2, A);
       return;

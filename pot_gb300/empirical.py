@@ -47,8 +47,10 @@ class LazyPlan:
         return self._out(P.to(self.f.dtype))
 
 
-def online_sinkhorn(X, Y, reg, a, b, numIterMax, stopThr, warm_f=None, warm_g=None):
-    """Device float32 tensors in; (f, g, status, niter, errs) out."""
+def online_sinkhorn(X, Y, reg, a, b, numIterMax, stopThr, warm_f=None, warm_g=None, sum_window_log2=0.0):
+    """Device float32 tensors in; (f, g, status, niter, errs) out.
+    ``sum_window_log2`` > 0 narrows the acceptance window of the folded
+    passes' shifted sums (rows outside it go through the fix-up pass)."""
     lib = _lib.load()
     n, d = X.shape
     m = Y.shape[0]
@@ -66,7 +68,7 @@ def online_sinkhorn(X, Y, reg, a, b, numIterMax, stopThr, warm_f=None, warm_g=No
                               stop_thr=float(stopThr), scale_x=pow2_scale(float(X.abs().max())),
                               scale_y=pow2_scale(float(Y.abs().max())), out_f=f.data_ptr(), out_g=g.data_ptr(),
                               err_hist=hist, hist_cap=cap, info=info, workspace=ws.data_ptr(),
-                              workspace_bytes=wsb, timeout_ms=0)
+                              workspace_bytes=wsb, timeout_ms=0, sum_window_log2=float(sum_window_log2))
     _lib.check(lib.otg_sinkhorn_online(ctypes.byref(p), _lib.stream_handle(X.device)), "otg_sinkhorn_online")
     if info[0] == _lib.STATUS_ABORTED:
         raise RuntimeError("pot_gb300: a device-side wait of the online kernel timed out")

@@ -99,6 +99,34 @@ def test_online_small_reg_vs_oracle(cuda):
     assert np.abs(P - Pref).sum() / Pref.sum() <= 2e-5
 
 
+def test_online_fixup_path(cuda):
+    """A narrow acceptance window (2^-0.5 .. 2^0.5) for the shifted sums
+    sends every row whose LSE moved by more than half a unit of log2 since
+    the last pass in its direction through the fix-up launch (the
+    running-max recomputation of its row block): fix-ups happen (info[3])
+    and the result is the default run's and the oracle's."""
+    from pot_gb300.empirical import online_sinkhorn, LAST_STATS
+    n, m, d = 600, 520, 8
+    rng = np.random.default_rng(23)
+    X = rng.standard_normal((n, d))
+    Y = rng.standard_normal((m, d)) + 0.3
+    C = oracle.sqeuclidean(X, Y)
+    reg = 0.05 * float(np.median(C))
+    a, b = np.full(n, 1.0 / n), np.full(m, 1.0 / m)
+    fr, gr, lr = oracle.empirical_sinkhorn_lazy(X, Y, reg, a, b, numIterMax=5000, stopThr=1e-7, batchSize=512)
+    f32 = lambda z: torch.tensor(z, dtype=torch.float32, device=cuda)  # noqa: E731
+    f0, g0, st0, nit0, _ = online_sinkhorn(f32(X), f32(Y), reg, f32(a), f32(b), 5000, 1e-6)
+    assert LAST_STATS["fixup_units"] == 0
+    f1, g1, st1, nit1, _ = online_sinkhorn(f32(X), f32(Y), reg, f32(a), f32(b), 5000, 1e-6, sum_window_log2=0.5)
+    assert LAST_STATS["fixup_units"] > 0
+    assert st0 == 0 and st1 == 0 and abs(nit1 - nit0) <= 10
+    P0 = plan(X, Y, f0.double().cpu().numpy(), g0.double().cpu().numpy(), reg)
+    P1 = plan(X, Y, f1.double().cpu().numpy(), g1.double().cpu().numpy(), reg)
+    Pref = plan(X, Y, fr, gr, reg)
+    assert np.abs(P1 - P0).sum() / P0.sum() <= 1e-5
+    assert np.abs(P1 - Pref).sum() / Pref.sum() <= 2e-5
+
+
 def test_online_column_split_vs_oracle(cuda):
     """n = m = 8192: enough row blocks and streamed tiles that each pass
     is split over column ranges (partials merged by online_finalize_kernel)."""

@@ -85,6 +85,26 @@ def test_pairs_far_start(cuda):
         assert np.abs(Pg - Pref).sum() / Pref.sum() < 1e-4, p
 
 
+def test_pairs_fixup_path(cuda):
+    """A narrow acceptance window for the shifted sums sends most row blocks
+    of the early passes through the fix-up launch (explicit unit lists over
+    the pairs); the result is the default run's."""
+    P, n, m, d, tol = 4, 256, 384, 16, 1e-6
+    X, Y = _clouds(33, P, n, m, d, cuda)
+    mx = pb.pairs_max_cost(X, Y)
+    regs = mx.double() * 0.05
+    u0, v0, st0, nit0, _ = pb.run_pairs(X, Y, regs, None, None, 20000, tol, check_period=1)
+    u1, v1, st1, nit1, _ = pb.run_pairs(X, Y, regs, None, None, 20000, tol, check_period=1, sum_window_log2=0.5)
+    assert (st0 == 0).all() and (st1 == 0).all()
+    assert (nit1 - nit0).abs().max() <= 2
+    for p in range(P):
+        C = oracle.sqeuclidean(X[p].double().cpu().numpy(), Y[p].double().cpu().numpy())
+        r = float(regs[p])
+        Pa = np.exp(u0[p].double().cpu().numpy()[:, None] - C / r + v0[p].double().cpu().numpy()[None, :])
+        Pb = np.exp(u1[p].double().cpu().numpy()[:, None] - C / r + v1[p].double().cpu().numpy()[None, :])
+        assert np.abs(Pb - Pa).sum() / Pa.sum() < 1e-5, p
+
+
 def test_pairs_match_the_stored_cost_solver(cuda):
     """The same pairs through both engines of the pair solver: stop indices
     within one check, potentials to float32 precision."""
