@@ -589,6 +589,63 @@ def run_small(args, pk):
                          "alg_bytes_per_launch": alg}}
 
 
+def run_greenkhorn(args, pk):
+    """Greenkhorn (ot.sinkhorn(method='greenkhorn')) on the reference's
+    CPU-sized dense case: n = m = 1024 in R^2, x ~ N(0, I), y ~ N((1,1), 0.5 I),
+    a = b uniform, cost / max, reg = 0.05, stopThr = 1e-9, float64, step
+    budget 10^5 so that every problem converges.  The step chain runs in one
+    CTA (latency-bound: a step is a dependent sequence of block reductions);
+    wall time per solve on the host, plan and log read back.  The CPU baseline
+    is the numpy restatement of the reference's loop on one problem."""
+    import torch
+    import pot_gb300 as pg
+    dev = torch.device("cuda:0")
+    n, reg, P = 1024, 0.05, 8
+    g = torch.Generator(device=dev); g.manual_seed(1)
+    probs = []
+    for _ in range(P):
+        x = torch.randn(n, 2, generator=g, device=dev, dtype=torch.float64)
+        y = torch.randn(n, 2, generator=g, device=dev, dtype=torch.float64) * 0.5 ** 0.5 + 1.0
+        M = torch.cdist(x, y).pow(2); M /= M.max()
+        probs.append(M.contiguous())
+    a = torch.full((n,), 1.0 / n, device=dev, dtype=torch.float64)
+
+    def solve(M):
+        Pl, lg = pg.greenkhorn(a, a, M, reg, numItermax=100000, stopThr=1e-9, log=True)
+        return lg["n_iter"]
+
+    for _ in range(args.warmup):
+        solve(probs[0])
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    steps = []
+    for _ in range(args.steps):
+        for M in probs:
+            steps.append(solve(M) + 1)
+    torch.cuda.synchronize()
+    s = (time.perf_counter() - t) / (args.steps * P)
+    st = np.array(steps, dtype=np.float64)
+    out = {"metric": "greenkhorn solves/s (n=m=1024, float64)", "value": 1.0 / s, "unit": "solves/s",
+           "ms_per_step": s * 1e3, "dtype": "f64",
+           "coordinate_steps_per_s": float(st.mean() / s), "us_per_coordinate_step": float(s / st.mean() * 1e6),
+           "config": {"workload": "ot.sinkhorn(method='greenkhorn') n=m=1024 in R^2, reg=0.05, stopThr=1e-9, "
+                                  "float64, %d seeded problems resident on the device; K and its transpose built "
+                                  "per solve, step chain in one CTA, plan + log read back" % P,
+                      "steps_mean": float(st.mean()), "l2": "K and K^T 16 MiB, L2-resident (latency-bound)"}}
+    if not args.no_cpu:
+        import oracle
+        Mh = probs[0].cpu().numpy()
+        ah = np.full(n, 1.0 / n)
+        t = time.perf_counter()
+        _, lo = oracle.greenkhorn(ah, ah, Mh, reg, numItermax=100000, stopThr=1e-9)
+        cs = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": 1.0 / cs, "unit": "solves/s", "cores": 1, "kind": "port",
+                               "sample": "1 problem of the workload, numpy restatement of the reference loop, "
+                                         "%d steps (%.1f us per step)" % (lo["n_iter"] + 1,
+                                                                          cs / (lo["n_iter"] + 1) * 1e6)}
+    return out
+
+
 def run_solve(args, pk):
     """One arm of the warm-start workload alone (profiling runs): `args.batch`
     cloud pairs (n = m = 2048, d = 16), plain zero-started solve or (with
@@ -862,7 +919,7 @@ def main():
     if args.workload != "warmstart":
         fn = {"online": run_online, "gw": run_gw, "ragged": run_ragged, "dense": run_dense,
               "batch": run_batch, "small": run_small, "tail": run_tail, "solve": run_solve,
-              "warm_eval": run_warm_eval}[args.workload]
+              "warm_eval": run_warm_eval, "greenkhorn": run_greenkhorn}[args.workload]
         line = {"n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                 "data": "synthetic"}
         line.update(fn(args, pk))

@@ -139,6 +139,23 @@ int otg_gibbs_kernel(int dtype, const void* M, int64_t n, int64_t m, int64_t ldm
 int otg_dense_marginals(int dtype, const void* M, int64_t n, int64_t m, int64_t ldm, const void* u, const void* v,
                         double reg, double* rowsum, double* colsum, cudaStream_t stream);
 
+/* Greenkhorn, the greedy coordinate Sinkhorn, on one dense problem.
+ * Replaces ot/bregman/_sinkhorn.py:1034-1102 (greenkhorn, reached through
+ * ot.sinkhorn(method='greenkhorn'), :192-204).  K = exp(-M/reg) and its
+ * transpose are built in the workspace; u, v start at 1/n, 1/m, or at
+ * exp(warm_u), exp(warm_v) (both or neither); each of at most num_iter_max
+ * steps rescales the row or column with the largest |marginal violation|,
+ * the whole chain in one CTA.  Outputs: the scalings u (n) and v (m), the
+ * plan G_ij = u_i K_ij v_j when G is not NULL (leading dimension ldg), and
+ * info[0] = last step index (the reference's log["n_iter"]; -1 when
+ * num_iter_max is 0), info[1] = OTG_STATUS_CONVERGED or OTG_STATUS_MAXITER.
+ * All pointers are device pointers of the dtype; info is device int32[2]. */
+size_t otg_greenkhorn_workspace_bytes(int dtype, int64_t n, int64_t m);
+int otg_greenkhorn(int dtype, const void* M, int64_t n, int64_t m, int64_t ldm, const void* a, const void* b,
+                   double reg, const void* warm_u, const void* warm_v, int32_t num_iter_max, double stop_thr,
+                   void* G, int64_t ldg, void* u, void* v, int32_t* info, void* workspace, size_t workspace_bytes,
+                   cudaStream_t stream);
+
 /* Loss of a lazy plan, sum_ij C_ij exp(f_i + g_j - C_ij/reg) with
  * C_ij = |x_i - y_j|^2 (X: n x d, Y: m x d row-major; f, g natural-log
  * potentials), fp64 accumulation.  Replaces the block loop of

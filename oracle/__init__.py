@@ -17,6 +17,7 @@ from .entropic import (  # noqa: F401
     logsumexp,
     sinkhorn_knopp,
     sinkhorn_log,
+    greenkhorn,
     sinkhorn,
     sinkhorn2,
     sinkhorn_stabilized,

@@ -174,12 +174,65 @@ def sinkhorn_log(a, b, M, reg, numItermax=1000, stopThr=1e-9, warmstart=None):
                "u": np.exp(u), "v": np.exp(v), "_warnings": warns}
 
 
+def greenkhorn(a, b, M, reg, numItermax=10000, stopThr=1e-9, warmstart=None):
+    """Greedy coordinate Sinkhorn, ``ot/bregman/_sinkhorn.py:1034-1102``.
+
+    K = exp(-M / reg); u, v start at 1/n, 1/m (or exp of the warm start);
+    each step picks the row and the column whose marginal violation is the
+    largest in absolute value (first index on ties), rescales the row when
+    its violation is strictly larger, else the column, updates both
+    violation vectors incrementally, and stops after the step whose chosen
+    maximum is <= stopThr.  Returns (plan, log) with log keys n_iter, u, v."""
+    M = _f64(M)
+    a, b = _uniform_if_empty(a, b, M)
+    K = np.exp(-M / reg)
+    if warmstart is None:
+        u = np.full(M.shape[0], 1.0 / M.shape[0])
+        v = np.full(M.shape[1], 1.0 / M.shape[1])
+    else:
+        u, v = np.exp(_f64(warmstart[0])), np.exp(_f64(warmstart[1]))
+    G = u[:, None] * K * v[None, :]
+    viol = G.sum(1) - a
+    viol_2 = G.sum(0) - b
+    warns = []
+    ii = -1
+    for ii in range(numItermax):
+        i_1 = int(np.argmax(np.abs(viol)))
+        i_2 = int(np.argmax(np.abs(viol_2)))
+        m_viol_1 = abs(viol[i_1])
+        m_viol_2 = abs(viol_2[i_2])
+        stop_val = np.maximum(m_viol_1, m_viol_2)
+        if m_viol_1 > m_viol_2:
+            old_u = u[i_1]
+            new_u = a[i_1] / np.dot(K[i_1, :], v)
+            G[i_1, :] = new_u * K[i_1, :] * v
+            viol[i_1] = np.dot(new_u * K[i_1, :], v) - a[i_1]
+            viol_2 += K[i_1, :] * (new_u - old_u) * v
+            u[i_1] = new_u
+        else:
+            old_v = v[i_2]
+            dot = np.dot(K[:, i_2], u)
+            new_v = b[i_2] / dot
+            G[:, i_2] = u * K[:, i_2] * new_v
+            viol += (-old_v + new_v) * K[:, i_2] * u
+            viol_2[i_2] = new_v * dot - b[i_2]
+            v[i_2] = new_v
+        if stop_val <= stopThr:
+            break
+    else:
+        warns.append(NONCONV)
+    return G, {"n_iter": ii, "u": u, "v": v, "_warnings": warns}
+
+
 def sinkhorn(a, b, M, reg, method="sinkhorn", **kw):
     """Method dispatch of ``ot/bregman/_sinkhorn.py:164-234``."""
     if method.lower() == "sinkhorn":
         return sinkhorn_knopp(a, b, M, reg, **kw)
     if method.lower() == "sinkhorn_log":
         return sinkhorn_log(a, b, M, reg, **kw)
+    if method.lower() == "greenkhorn":
+        kw.setdefault("numItermax", 1000)  # the dispatcher's default, not greenkhorn's
+        return greenkhorn(a, b, M, reg, **kw)
     if method.lower() == "sinkhorn_stabilized":
         return sinkhorn_stabilized(a, b, M, reg, **kw)
     if method.lower() == "sinkhorn_epsilon_scaling":

@@ -2,14 +2,14 @@
 
 Drop-in GPU implementations of PythonOT/POT's entropic-OT hot path:
 ``sinkhorn`` / ``sinkhorn2`` (methods 'sinkhorn', 'sinkhorn_log',
-'sinkhorn_stabilized', 'sinkhorn_epsilon_scaling'), the ``ot.batch`` solvers,
+'sinkhorn_stabilized', 'sinkhorn_epsilon_scaling', 'greenkhorn'), the ``ot.batch`` solvers,
 entropic Gromov-Wasserstein, the lazy empirical Sinkhorn, and the entropic
 branches of ``solve`` / ``solve_sample``.  All arithmetic runs in hand-written
 CUDA kernels for sm_103a (``pot_gb300/csrc``) behind the C ABI of
 ``include/pot_gb300.h``; there is no CPU fallback.
 """
 from .bregman import sinkhorn, sinkhorn2, sinkhorn_knopp, sinkhorn_log  # noqa: F401
-from .bregman import sinkhorn_stabilized, sinkhorn_epsilon_scaling  # noqa: F401
+from .bregman import sinkhorn_stabilized, sinkhorn_epsilon_scaling, greenkhorn  # noqa: F401
 from . import batch  # noqa: F401
 from .batch import solve_batch, solve_sample_batch, dist_batch  # noqa: F401
 from . import gromov  # noqa: F401

@@ -116,7 +116,10 @@ SIGNATURES = {
     "otg_gibbs_kernel": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_dbl, c_vp, c_i64, c_vp]),
     "otg_dense_marginals": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_dbl, c_vp, c_vp,
                                            c_vp]),
-    "otg_sinkhorn_dense_noalloc": (ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp, c_vp]),
+    "otg_greenkhorn_workspace_bytes": (c_sz, [ctypes.c_int, c_i64, c_i64]),
+    "otg_greenkhorn": (ctypes.c_int, [ctypes.c_int, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_dbl, c_vp, c_vp, c_i32,
+                                      c_dbl, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "otg_sinkhorn_dense_noalloc":(ctypes.c_int, [ctypes.POINTER(OtgDenseProblem), c_vp, c_vp, c_vp]),
     "otg_batch_limits": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
                                         ctypes.POINTER(c_i32)]),
     "otg_sinkhorn_batched": (ctypes.c_int, [ctypes.POINTER(OtgBatchProblem), c_vp]),

@@ -1,12 +1,13 @@
 """Drop-in replacements for ``ot.sinkhorn``, ``ot.sinkhorn2``,
 ``ot.bregman.sinkhorn_knopp``, ``ot.bregman.sinkhorn_log``,
-``ot.bregman.sinkhorn_stabilized`` and ``ot.bregman.sinkhorn_epsilon_scaling``.
+``ot.bregman.sinkhorn_stabilized``, ``ot.bregman.sinkhorn_epsilon_scaling``
+and ``ot.bregman.greenkhorn``.
 
 Signatures, defaults, return values, log-dict keys and warnings follow
 PythonOT/POT ``ot/bregman/_sinkhorn.py`` (``sinkhorn`` :21-234, ``sinkhorn2``
 :237-484, ``sinkhorn_knopp`` :487-687, ``sinkhorn_log`` :690-918,
 ``sinkhorn_stabilized`` :1105-1368, ``sinkhorn_epsilon_scaling``
-:1371-1575).  The
+:1371-1575, ``greenkhorn`` :921-1102).  The
 iteration loop runs on the GPU in one persistent kernel
 (``csrc/dense.cu``); the host only reads the result block once per solve.
 """
@@ -486,6 +487,39 @@ def sinkhorn_epsilon_scaling(a, b, M, reg, numItermax=100, epsilon0=1e4, numInne
     return bd.out(P)
 
 
+def greenkhorn(a, b, M, reg, numItermax=10000, stopThr=1e-9, verbose=False, log=False, warn=True,
+               warmstart=None):
+    """GPU ``ot.bregman.greenkhorn`` (``_sinkhorn.py:921-1102``): greedy
+    coordinate steps, each rescaling the row or column with the largest
+    marginal violation, run as one chain in a single CTA
+    (``otg_greenkhorn``).  Returns the plan; with ``log=True`` also a dict
+    with ``n_iter`` (last step index), ``u`` and ``v``.  ``warmstart`` is the
+    pair of log-scalings, as in the reference."""
+    bd, Md, ad, bdv = _prep(a, b, M)
+    if bdv.dim() > 1:
+        raise ValueError("greenkhorn takes one target histogram (1-D b)")
+    n, m = Md.shape
+    wu, wv = _warm(bd, warmstart, Md.dtype)
+    lib = _lib.load()
+    code = _lib.dtype_code(Md.dtype)
+    dev = Md.device
+    u = torch.empty(n, dtype=Md.dtype, device=dev)
+    v = torch.empty(m, dtype=Md.dtype, device=dev)
+    P = torch.empty((n, m), dtype=Md.dtype, device=dev)
+    info = torch.zeros(2, dtype=torch.int32, device=dev)
+    ws = torch.empty(lib.otg_greenkhorn_workspace_bytes(code, n, m), dtype=torch.uint8, device=dev)
+    _lib.check(lib.otg_greenkhorn(code, _lib.ptr(Md), n, m, Md.stride(0), _lib.ptr(ad), _lib.ptr(bdv), float(reg),
+                                  _lib.ptr(wu), _lib.ptr(wv), max(0, int(numItermax)), float(stopThr), _lib.ptr(P),
+                                  P.stride(0), _lib.ptr(u), _lib.ptr(v), _lib.ptr(info), _lib.ptr(ws), ws.numel(),
+                                  _lib.stream_handle(dev)), "otg_greenkhorn")
+    niter, status = (int(x) for x in info.tolist())
+    if status == _lib.STATUS_MAXITER and warn:
+        warnings.warn(NONCONV_MSG)
+    if log:
+        return bd.out(P), {"n_iter": niter, "u": bd.out(u), "v": bd.out(v)}
+    return bd.out(P)
+
+
 def sinkhorn(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, verbose=False,
              log=False, warn=True, warmstart=None, **kwargs):
     """GPU ``ot.sinkhorn``: dispatch on ``method`` (``_sinkhorn.py:164-234``)."""
@@ -503,7 +537,8 @@ def sinkhorn(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, ver
         return sinkhorn_epsilon_scaling(a, b, M, reg, numItermax=numItermax, stopThr=stopThr,
                                         warmstart=warmstart, verbose=verbose, log=log, warn=warn, **kwargs)
     if meth == "greenkhorn":
-        raise NotImplementedError("pot_gb300: method='greenkhorn' is not on the GPU path")
+        return greenkhorn(a, b, M, reg, numItermax=numItermax, stopThr=stopThr, verbose=verbose, log=log,
+                          warn=warn, warmstart=warmstart)
     raise ValueError("Unknown method '%s'." % method)
 
 

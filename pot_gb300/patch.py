@@ -6,10 +6,10 @@ replaces the hot-path names in every module that imported them:
 
     ot/__init__.py:56            sinkhorn, sinkhorn2
     ot/bregman/__init__.py:13    sinkhorn, sinkhorn2, sinkhorn_knopp, sinkhorn_log, sinkhorn_stabilized,
-                                 sinkhorn_epsilon_scaling, empirical_sinkhorn, empirical_sinkhorn2,
+                                 sinkhorn_epsilon_scaling, greenkhorn, empirical_sinkhorn, empirical_sinkhorn2,
                                  barycenter, barycenter_sinkhorn
     ot/bregman/_sinkhorn.py      sinkhorn_knopp, sinkhorn_log, sinkhorn_stabilized,
-                                 sinkhorn_epsilon_scaling (the dispatcher's callees)
+                                 sinkhorn_epsilon_scaling, greenkhorn (the dispatcher's callees)
     ot/bregman/_empirical.py:18  sinkhorn, sinkhorn2
     ot/gromov/_bregman.py:17     sinkhorn
     ot/gromov/__init__.py        entropic_gromov_wasserstein(2), entropic_fused_gromov_wasserstein(2)
@@ -37,6 +37,7 @@ GPU = {
     "sinkhorn_log": bregman.sinkhorn_log,
     "sinkhorn_stabilized": bregman.sinkhorn_stabilized,
     "sinkhorn_epsilon_scaling": bregman.sinkhorn_epsilon_scaling,
+    "greenkhorn": bregman.greenkhorn,
     "empirical_sinkhorn2": solvers.empirical_sinkhorn2,
     "empirical_sinkhorn_divergence": solvers.empirical_sinkhorn_divergence,
     "barycenter": barycenters.barycenter,
@@ -59,9 +60,10 @@ GPU = {
 MODULES = {
     "": ["sinkhorn", "sinkhorn2"],
     ".bregman": ["sinkhorn", "sinkhorn2", "sinkhorn_knopp", "sinkhorn_log", "sinkhorn_stabilized",
-                 "sinkhorn_epsilon_scaling", "empirical_sinkhorn", "empirical_sinkhorn2", "barycenter",
+                 "sinkhorn_epsilon_scaling", "greenkhorn", "empirical_sinkhorn", "empirical_sinkhorn2", "barycenter",
                  "barycenter_sinkhorn", "empirical_sinkhorn_divergence"],
-    ".bregman._sinkhorn": ["sinkhorn_knopp", "sinkhorn_log", "sinkhorn_stabilized", "sinkhorn_epsilon_scaling"],
+    ".bregman._sinkhorn": ["sinkhorn_knopp", "sinkhorn_log", "sinkhorn_stabilized", "sinkhorn_epsilon_scaling",
+                           "greenkhorn"],
     ".bregman._empirical": ["sinkhorn", "sinkhorn2"],
     ".gromov": ["entropic_gromov_wasserstein", "entropic_gromov_wasserstein2", "entropic_fused_gromov_wasserstein",
                 "entropic_fused_gromov_wasserstein2"],

@@ -414,6 +414,48 @@ def unbalanced():
 SECTIONS = {"core": core, "next": next_rows, "fgw": fused_gw, "bary": barycenters, "unbal": unbalanced}
 
 
+def greenkhorn():
+    # 12. greedy coordinate Sinkhorn (ot/bregman/_sinkhorn.py:921-1102): the
+    # doctest, a symmetric uniform problem (ties between rows and columns), a
+    # rectangular weighted one, a warm start, a short budget, empty weights
+    def case(name, a, b, M, reg, **kw):
+        (G, lg), w = call_warn(ot.sinkhorn, a, b, M, reg, method="greenkhorn", log=True, **kw)
+        out = dict(a=a, b=b, M=M, reg=reg, plan=G, n_iter=lg["n_iter"], u=lg["u"], v=lg["v"],
+                   warn_nonconv=int(any("did not converge" in s for s in w)))
+        for k, val in kw.items():
+            if k == "warmstart":
+                out["ws_u"], out["ws_v"] = val
+            else:
+                out["kw_" + k] = val
+        save(name, **out)
+
+    a = np.array([0.5, 0.5])
+    case("green_doctest_2x2", a, a, np.array([[0.0, 1.0], [1.0, 0.0]]), 1.0)
+    rng = np.random.default_rng(41)
+    x = rng.standard_normal((100, 2))
+    M = ot.dist(x, x)
+    u = ot.unif(100)
+    case("green_sym_100", u, u, M, 1.0, stopThr=1e-10)
+    x = rng.standard_normal((31, 2))
+    y = rng.standard_normal((33, 2)) + 0.5
+    M = ot.dist(x, y)
+    M /= M.max()
+    a = rng.random(31) + 0.1
+    a /= a.sum()
+    b = rng.random(33) + 0.1
+    b /= b.sum()
+    case("green_31x33_reg0.1", a, b, M, 0.1, stopThr=1e-9)
+    case("green_31x33_warm", a, b, M, 0.1, stopThr=1e-9,
+         warmstart=(rng.standard_normal(31) * 0.1 - np.log(31), rng.standard_normal(33) * 0.1 - np.log(33)))
+    case("green_31x33_iter25", a, b, M, 0.05, numItermax=25)
+    case("green_empty_40x50", np.array([]), np.array([]), ot.dist(rng.standard_normal((40, 3)),
+                                                                rng.standard_normal((50, 3))), 1.0,
+         stopThr=1e-10)
+
+
+SECTIONS["green"] = greenkhorn
+
+
 def main(names):
     for k in names or list(SECTIONS):
         SECTIONS[k]()

@@ -21,6 +21,21 @@ def test_unknown_method_raises_before_any_device_work():
         pg.sinkhorn2([0.5, 0.5], [0.5, 0.5], [[0.0, 1.0], [1.0, 0.0]], 1.0, method="new_method")
 
 
+def test_one_histogram_methods_have_no_loss_form():
+    """test/test_bregman.py:1404-1407: sinkhorn2 accepts neither 'greenkhorn'
+    nor 'sinkhorn_epsilon_scaling' (ValueError, before any device work)."""
+    for method in ("greenkhorn", "sinkhorn_epsilon_scaling"):
+        with pytest.raises(ValueError):
+            pg.sinkhorn2([0.5, 0.5], [0.5, 0.5], [[0.0, 1.0], [1.0, 0.0]], 1.0, method=method)
+
+
+def test_greenkhorn_without_gpu_raises():
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(RuntimeError, match="CUDA"):
+        pg.sinkhorn([0.5, 0.5], [0.5, 0.5], [[0.0, 1.0], [1.0, 0.0]], 1.0, method="greenkhorn")
+
+
 def test_is_empty():
     assert is_empty([]) and is_empty(np.array([])) and is_empty(torch.tensor([]))
     assert not is_empty([1.0])

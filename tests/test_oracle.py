@@ -315,3 +315,29 @@ def test_accelerated_oracles_reach_the_solution_faster():
         P = np.exp(-M / reg + u[:, None] + v[None, :])
         P0 = np.exp(-M / reg + lg["log_u"][:, None] + lg["log_v"][None, :])
         assert np.abs(P - P0).sum() / P0.sum() < 1e-6
+
+
+def _green_kw(g):
+    kw = {k[3:]: g[k].item() for k in g if k.startswith("kw_")}
+    if "ws_u" in g:
+        kw["warmstart"] = (g["ws_u"], g["ws_v"])
+    return kw
+
+
+@pytest.mark.parametrize("name", golden_names("green_"))
+def test_greenkhorn(name):
+    """The greedy coordinate restatement follows the reference step by step:
+    same choices, so the same plan, scalings and last index, bit for bit."""
+    g = golden(name)
+    P, lg = oracle.sinkhorn(g["a"], g["b"], g["M"], float(g["reg"]), method="greenkhorn", **_green_kw(g))
+    assert lg["n_iter"] == int(g["n_iter"])
+    np.testing.assert_array_equal(P, g["plan"])
+    np.testing.assert_array_equal(lg["u"], g["u"])
+    np.testing.assert_array_equal(lg["v"], g["v"])
+    assert (oracle.NONCONV in lg["_warnings"]) == bool(g["warn_nonconv"])
+
+
+def test_greenkhorn_doctest():
+    """ot/bregman/_sinkhorn.py:995-1001."""
+    P, _ = oracle.greenkhorn([0.5, 0.5], [0.5, 0.5], [[0.0, 1.0], [1.0, 0.0]], 1.0)
+    np.testing.assert_allclose(P, [[0.36552929, 0.13447071], [0.13447071, 0.36552929]], atol=1e-8)

@@ -6,8 +6,8 @@ reference's suite (the reference itself is not available where the GPU tests
 run, so its scenarios are restated here in this project's code):
 
 - ``test/test_bregman.py:284`` test_sinkhorn_variants: the 'sinkhorn',
-  'sinkhorn_log', 'sinkhorn_stabilized' and 'sinkhorn_epsilon_scaling'
-  plans agree to 1e-5 ('greenkhorn' is not on the GPU path);
+  'sinkhorn_log', 'sinkhorn_stabilized', 'sinkhorn_epsilon_scaling' and
+  'greenkhorn' plans agree to 1e-5;
 - ``test/test_bregman.py:1197`` test_lazy_empirical_sinkhorn (squared
   Euclidean parts): marginals of the lazy plans against ``sinkhorn`` to
   1e-5, ``empirical_sinkhorn2`` against ``sinkhorn2`` to 1e-5, the lazy plan
@@ -46,10 +46,12 @@ def test_sinkhorn_variants(cuda):
     G0 = pg.sinkhorn(ub, ub, Mb, 1, method="sinkhorn", stopThr=1e-10).cpu().numpy()
     Gs = pg.sinkhorn(ub, ub, Mb, 1, method="sinkhorn_stabilized", stopThr=1e-10).cpu().numpy()
     Ges = pg.sinkhorn(ub, ub, Mb, 1, method="sinkhorn_epsilon_scaling", stopThr=1e-10).cpu().numpy()
+    G_green = pg.sinkhorn(ub, ub, Mb, 1, method="greenkhorn", stopThr=1e-10).cpu().numpy()
     np.testing.assert_allclose(G, G0, atol=1e-05)
     np.testing.assert_allclose(G, Gl, atol=1e-05)
     np.testing.assert_allclose(G0, Gs, atol=1e-05)
     np.testing.assert_allclose(G0, Ges, atol=1e-05)
+    np.testing.assert_allclose(G0, G_green, atol=1e-5)
 
 
 def test_lazy_empirical_sinkhorn(cuda):
