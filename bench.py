@@ -227,6 +227,8 @@ def run_warmstart(args, pk):
     # region; results come back as host tensors)
     Xh, Yh = X.cpu().pin_memory(), Y.cpu().pin_memory()
     e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(args.warmup):  # untimed, like the device arms (first-call allocations)
+        wp.solve_cloud_pairs(Xh, Yh, WS_REG, WS_TOL, warm=True, check_period=1)
     torch.cuda.synchronize()
     replica_barrier()
     t = time.perf_counter()

@@ -100,13 +100,17 @@ __global__ void __launch_bounds__(256) batched_sqdist_kernel(OtgCostTable t) {
 }
 
 // Register-tiled float32 cost blocks for the common point dimensions: a CTA
-// computes 64 rows x 256 columns of one problem, both point tiles staged in
-// shared memory dimension-major; each thread owns 8 rows x (4 + 4) columns --
-// columns 4l..4l+3 and 128+4l..128+4l+3 for lane l -- so each 16-byte store
-// of a warp covers 512 contiguous bytes (64 accumulators per thread).  Same arithmetic as
-// the kernel above: sum_k (x_k - y_k)^2 in order of k, +inf padding.
+// computes 64 rows x 128 columns of one problem, both point tiles staged in
+// shared memory dimension-major; each thread owns 8 rows x (2 + 2) columns --
+// columns 2l, 2l+1 and 64+2l, 64+2l+1 for lane l -- so each 8-byte store of a
+// warp covers 256 contiguous bytes.  Same arithmetic as the kernel above:
+// sum_k (x_k - y_k)^2 in order of k, +inf padding.  The tile is sized for
+// occupancy: at 32 accumulators a thread fits four CTAs per SM, which hide
+// one another's point staging (64 x 256 tiles with 64 accumulators, two CTAs
+// per SM: 6.0 ms for 1024 blocks of 2048 x 2048 at d = 16; this shape 4.7 ms,
+// bit-identical).
 // grid = (column-tile stride, row tiles, problems).
-constexpr int SQ_R = 64, SQ_C = 256;
+constexpr int SQ_R = 64, SQ_C = 128, SQ_CSTRIDE = 16;
 // shared-memory row strides of the staged tiles: +4 floats keeps 16-byte
 // alignment and spreads the transposing stores over the banks
 constexpr int SQ_RP = SQ_R + 4, SQ_CP = SQ_C + 4;
@@ -152,67 +156,58 @@ __device__ __forceinline__ void sqdist_regtile(const float* __restrict__ X, cons
     __syncthreads();
     // column pairs (j, j+1) in packed fp32x2 registers: one sub.f32x2 and one
     // fma.f32x2 per pair and dimension, each lane rounding as the scalar ops
-    unsigned long long acc2[8][4];
+    unsigned long long acc2[8][2];
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) acc2[i][j] = 0ull;
+    for (int i = 0; i < 8; ++i) acc2[i][0] = acc2[i][1] = 0ull;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
       const float4 xa = *reinterpret_cast<const float4*>(xt + k * SQ_RP + warp * 8);
       const float4 xb = *reinterpret_cast<const float4*>(xt + k * SQ_RP + warp * 8 + 4);
-      const ulonglong2 ya = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_CP + lane * 4);
-      const ulonglong2 yb = *reinterpret_cast<const ulonglong2*>(yt + k * SQ_CP + SQ_C / 2 + lane * 4);
+      const unsigned long long yp[2] = {*reinterpret_cast<const unsigned long long*>(yt + k * SQ_CP + lane * 2),
+                                        *reinterpret_cast<const unsigned long long*>(yt + k * SQ_CP + SQ_C / 2 +
+                                                                                     lane * 2)};
       const float xv[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
-      const unsigned long long yp[4] = {ya.x, ya.y, yb.x, yb.y};
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const unsigned long long xx =
             (unsigned long long)__float_as_uint(xv[i]) | ((unsigned long long)__float_as_uint(xv[i]) << 32);
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < 2; ++j) {
           unsigned long long df;
           asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(df) : "l"(xx), "l"(yp[j]));
           asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i][j]) : "l"(df));
         }
       }
     }
-    float acc[8][8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        acc[i][2 * j] = __uint_as_float((unsigned)(acc2[i][j] & 0xffffffffull));
-        acc[i][2 * j + 1] = __uint_as_float((unsigned)(acc2[i][j] >> 32));
-      }
-    // columns of acc[i][0..3]: ca + 0..3; of acc[i][4..7]: cz + 0..3 (ldm is a
-    // multiple of 4, so a group starting below ldm ends within it)
-    const int ca = c0 + lane * 4, cz = c0 + SQ_C / 2 + lane * 4;
+    // columns of acc2[i][0]: ca, ca + 1; of acc2[i][1]: cz, cz + 1 (ldm is a
+    // multiple of 4, so a pair starting below ldm ends within it)
+    const int ca = c0 + lane * 2, cz = c0 + SQ_C / 2 + lane * 2;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int row = r0 + warp * 8 + i;
       if (row >= n) break;
-      float v[8];
+      float v[4];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int col = (j < 4 ? ca : cz) + (j & 3);
-        if (col < m) { v[j] = acc[i][j]; local_max = fmaxf(local_max, acc[i][j]); }
+      for (int j = 0; j < 4; ++j) {
+        const float x = __uint_as_float((unsigned)(j & 1 ? acc2[i][j >> 1] >> 32 : acc2[i][j >> 1] & 0xffffffffull));
+        const int col = (j < 2 ? ca : cz) + (j & 1);
+        if (col < m) { v[j] = x; local_max = fmaxf(local_max, x); }
         else v[j] = INFINITY;
       }
       float* dst = M + (int64_t)row * ldm;
-      if (ca < ldm) *reinterpret_cast<float4*>(dst + ca) = make_float4(v[0], v[1], v[2], v[3]);
-      if (cz < ldm) *reinterpret_cast<float4*>(dst + cz) = make_float4(v[4], v[5], v[6], v[7]);
+      if (ca < ldm) *reinterpret_cast<float2*>(dst + ca) = make_float2(v[0], v[1]);
+      if (cz < ldm) *reinterpret_cast<float2*>(dst + cz) = make_float2(v[2], v[3]);
     }
   }
 }
 
-__global__ void __launch_bounds__(256) sqdist_regtile_kernel(OtgCostTable t) {
+__global__ void __launch_bounds__(256, 4) sqdist_regtile_kernel(OtgCostTable t) {
   extern __shared__ __align__(16) float sq_smem[];
   const int p = blockIdx.z;
   if (p >= t.nprob) return;
   const int n = t.rows[p], m = t.cols[p], d = t.dim[p], ldm = t.ldm[p];
   const int r0 = blockIdx.y * SQ_R;
-  if (r0 >= n) return;
+  if (r0 >= n || (int)blockIdx.x * SQ_C >= ldm) return;  // no tile of this problem for this CTA
   const float* X = static_cast<const float*>(t.X) + t.x_off[p];
   const float* Y = static_cast<const float*>(t.Y) + t.y_off[p];
   float* M = static_cast<float*>(t.M) + t.m_off[p];
@@ -620,7 +615,7 @@ int otg_batched_sqdist(const OtgCostTable* t, int32_t max_rows, cudaStream_t str
   } else if (t->dtype == OTG_F32 && t->fixed_dim &&
              (t->fixed_dim % 4 != 0 || ((uintptr_t)t->X % 16 == 0 && (uintptr_t)t->Y % 16 == 0))) {
     // every problem has the same dimension, one of 2, 3, 8, 16: register tiles
-    const dim3 g2(8, (unsigned)((max_rows + SQ_R - 1) / SQ_R), (unsigned)t->nprob);
+    const dim3 g2(SQ_CSTRIDE, (unsigned)((max_rows + SQ_R - 1) / SQ_R), (unsigned)t->nprob);
     sqdist_regtile_kernel<<<g2, 256, (SQ_RP + SQ_CP) * t->max_dim * sizeof(float), stream>>>(*t);
   } else if (t->dtype == OTG_F32) {
     batched_sqdist_kernel<float><<<grid, 256, 32 * t->max_dim * sizeof(float), stream>>>(*t);
