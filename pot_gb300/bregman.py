@@ -508,9 +508,10 @@ def greenkhorn(a, b, M, reg, numItermax=10000, stopThr=1e-9, verbose=False, log=
     P = torch.empty((n, m), dtype=Md.dtype, device=dev)
     info = torch.zeros(2, dtype=torch.int32, device=dev)
     ws = torch.empty(lib.otg_greenkhorn_workspace_bytes(code, n, m), dtype=torch.uint8, device=dev)
+    steps = min(max(0, int(numItermax)), 2 ** 31 - 1)
     _lib.check(lib.otg_greenkhorn(code, _lib.ptr(Md), n, m, Md.stride(0), _lib.ptr(ad), _lib.ptr(bdv), float(reg),
-                                  _lib.ptr(wu), _lib.ptr(wv), max(0, int(numItermax)), float(stopThr), _lib.ptr(P),
-                                  P.stride(0), _lib.ptr(u), _lib.ptr(v), _lib.ptr(info), _lib.ptr(ws), ws.numel(),
+                                  _lib.ptr(wu), _lib.ptr(wv), steps, float(stopThr), _lib.ptr(P), P.stride(0),
+                                  _lib.ptr(u), _lib.ptr(v), _lib.ptr(info), _lib.ptr(ws), ws.numel(),
                                   _lib.stream_handle(dev)), "otg_greenkhorn")
     niter, status = (int(x) for x in info.tolist())
     if status == _lib.STATUS_MAXITER and warn:
