@@ -21,6 +21,9 @@ replaces the hot-path names in every module that imported them:
                                  entropic branches of ot.solve / ot.solve_sample)
     ot/unbalanced/__init__.py    sinkhorn_unbalanced(2), sinkhorn_knopp_unbalanced
     ot/unbalanced/_sinkhorn.py   sinkhorn_knopp_unbalanced (the dispatcher's callee)
+    ot/bregman/_barycenter.py:20, ot/da.py:19, ot/optim.py:14, ot/lowrank.py:13, ot/factored.py:12,
+    ot/coot.py:14, ot/gromov/_estimators.py:14
+                                 sinkhorn (consumers that bound it at import)
 
 Calls the GPU path does not cover (other methods, metrics or losses) raise
 NotImplementedError from the GPU function; ``unpatch_pot`` restores the
@@ -75,6 +78,14 @@ MODULES = {
     ".solvers": ["sinkhorn_log", "empirical_sinkhorn2", "sinkhorn_knopp_unbalanced"],
     ".unbalanced": ["sinkhorn_unbalanced", "sinkhorn_unbalanced2", "sinkhorn_knopp_unbalanced"],
     ".unbalanced._sinkhorn": ["sinkhorn_knopp_unbalanced"],
+    # consumers that bind `sinkhorn` at import (their Sinkhorn calls then run on the GPU)
+    ".bregman._barycenter": ["sinkhorn"],
+    ".da": ["sinkhorn"],
+    ".optim": ["sinkhorn"],
+    ".lowrank": ["sinkhorn"],
+    ".factored": ["sinkhorn"],
+    ".coot": ["sinkhorn"],
+    ".gromov._estimators": ["sinkhorn"],
 }
 
 _saved = {}
