@@ -11,18 +11,20 @@
 // memory otherwise): no grid-wide barrier and no host round trip per step;
 // the host reads the step count once at the end.
 //
-// GB300 issues FP64 at a few lanes per clock per SM, so the chain keeps FP64
-// work to the arithmetic the reference itself does per element: the argmax
-// runs on integer keys (the bit pattern of |x| orders non-negative floats,
-// and NaN patterns sit above +inf, as numpy's argmax ranks NaN first), each
-// sum is one partial per thread folded by a single warp, and the division
+// GB300 issues FP64 at a few lanes per clock per SM, and FP64 issue bounds
+// the chain, so it keeps FP64 work per entry to three operations: the dot
+// product of the rescaled line (one fused multiply-add) and the violation
+// update (a rounded product, then a fused multiply-add; the reference rounds
+// both products, a difference in the last place, as is the order of its BLAS
+// dot products).  The argmax runs on integer keys (the bit pattern of |x|
+// orders non-negative floats, and NaN patterns sit above +inf, as numpy's
+// argmax ranks NaN first), as do the row/column choice and the stop test;
+// each sum is one partial per thread folded by a single warp; the division
 // of a rescaling is done once, by one thread, and broadcast.
 //
 // Reductions run in a fixed order (per-thread sequential partial, then warp 0
 // folds the partials in slot order and by xor butterfly), so two runs are
-// bit-identical.  Argmax ties go to the lowest index.  The elementwise updates
-// keep the reference's operation order with rounded multiplies and adds (no
-// contraction into fused multiply-adds).
+// bit-identical.  Argmax ties go to the lowest index.
 #include <algorithm>
 #include <climits>
 #include <cstdint>
@@ -57,7 +59,6 @@ struct GkKey<double> {
     const unsigned long long k = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
     return k > kInf ? 0x7ff8000000000000ull : k;
   }
-  static __device__ __forceinline__ double value(unsigned long long k) { return __longlong_as_double((long long)k); }
 };
 template <>
 struct GkKey<float> {
@@ -66,7 +67,6 @@ struct GkKey<float> {
     const unsigned k = __float_as_uint(x) & 0x7fffffffu;
     return k > 0x7f800000u ? 0x7fc00000ull : (unsigned long long)k;
   }
-  static __device__ __forceinline__ double value(unsigned long long k) { return (double)__uint_as_float((unsigned)k); }
 };
 
 struct GkArg {
@@ -247,13 +247,18 @@ __global__ void __launch_bounds__(GK_THREADS, 1)
   GkArg g1 = own1, g2 = own2;
   gk_block_argmax(sh, g1, g2, buf);
   int32_t last = -1, status = OTG_STATUS_MAXITER;
+  // the stop test on keys: |x| <= thr for non-negative thr (a negative or NaN
+  // threshold never stops, as in the reference)
+  const T thr = (T)stop_thr;
+  const bool thr_ok = thr >= T(0);
+  const unsigned long long thr_key = thr_ok ? GkKey<T>::of(thr) : 0ull;
   for (int32_t ii = 0; ii < num_iter_max; ++ii) {
     last = ii;
     const bool nan1 = g1.k > GkKey<T>::kInf, nan2 = g2.k > GkKey<T>::kInf;
-    const double m1 = GkKey<T>::value(g1.k), m2 = GkKey<T>::value(g2.k);
-    // nx.maximum propagates NaN, and NaN <= stopThr is false (:1063, :1085)
-    const bool stop = !nan1 && !nan2 && fmax(m1, m2) <= stop_thr;
-    if (!nan1 && !nan2 && m1 > m2) {
+    // nx.maximum propagates NaN, and NaN <= stopThr is false (:1063, :1085);
+    // on non-NaN keys, key order is value order
+    const bool stop = !nan1 && !nan2 && thr_ok && (g1.k > g2.k ? g1.k : g2.k) <= thr_key;
+    if (!nan1 && !nan2 && g1.k > g2.k) {
       // rescale row r (:1066-1073)
       const int r = g1.i;
       const T* Kr = K + (int64_t)r * m;
@@ -264,25 +269,21 @@ __global__ void __launch_bounds__(GK_THREADS, 1)
       if (tid == 0) {
         const T old_u = u[r];
         const T new_u = a[r] / dot1;
-        sh.bc[0] = new_u;
-        sh.bc[1] = sub_rn(new_u, old_u);
+        sh.bc[0] = sub_rn(new_u, old_u);
         u[r] = new_u;  // nothing else reads u[r] in a row step
+        // the row's own violation, new_u (K_r . v) - a_r: the reference forms
+        // (new_u K_r) . v - a_r (:1070); both are rounding noise around zero
+        viol[r] = sub_rn(mul_rn(new_u, dot1), a[r]);
       }
       __syncthreads();
-      const T new_u = sh.bc[0], du = sh.bc[1];
-      T p2 = 0;
+      const T du = sh.bc[0];
       own2 = gk_none();
 #pragma unroll 4
       for (int j = tid; j < m; j += GK_THREADS) {
-        const T k = Kr[j], vj = v[j];
-        p2 += mul_rn(mul_rn(new_u, k), vj);
-        const T nv = add_rn(viol2[j], mul_rn(mul_rn(k, du), vj));
+        const T nv = fma(mul_rn(Kr[j], du), v[j], viol2[j]);
         viol2[j] = nv;
         gk_take(own2, GkKey<T>::of(nv), j);
       }
-      const T dot2 = gk_fold(sh, p2);
-      if (tid == 0) viol[r] = sub_rn(dot2, a[r]);
-      __syncthreads();
       if (r % GK_THREADS == tid) own1 = gk_scan(viol, n);
     } else {
       // rescale column c (:1074-1083)
@@ -304,7 +305,7 @@ __global__ void __launch_bounds__(GK_THREADS, 1)
       own1 = gk_none();
 #pragma unroll 4
       for (int i = tid; i < n; i += GK_THREADS) {
-        const T nv = add_rn(viol[i], mul_rn(mul_rn(dv, Kc[i]), u[i]));
+        const T nv = fma(mul_rn(dv, Kc[i]), u[i], viol[i]);
         viol[i] = nv;
         gk_take(own1, GkKey<T>::of(nv), i);
       }
