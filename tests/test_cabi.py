@@ -85,3 +85,33 @@ def test_invalid_arguments_are_rejected_before_any_device_work():
     assert lib.otg_mlp_encode_pool(fake, 1, 1, 5, 32, 32, fake, fake, fake, fake, fake, None) == ERR_UNSUPPORTED
     assert lib.otg_mlp_head(fake, 1, 1, 7, 32, 64, fake, fake, fake, fake, fake, fake, fake, fake, fake,
                             None) == ERR_UNSUPPORTED
+
+
+def test_greenkhorn_entry_checks_before_device_work():
+    """otg_greenkhorn rejects bad arguments (null buffers, ldm < m, a warm
+    start for one side only, unknown dtype, short workspace) before it touches
+    a device, and sizes its workspace as K + K^T + both violation vectors."""
+    from pot_gb300 import _build, _lib
+    lib = ctypes.CDLL(_build.build())
+    for name in ("otg_greenkhorn", "otg_greenkhorn_workspace_bytes"):
+        fn = getattr(lib, name)
+        fn.restype, fn.argtypes = _lib.SIGNATURES[name]
+    ERR_ARG, ERR_DTYPE, ERR_WORKSPACE = -1, -2, -3
+    f = ctypes.c_void_p(256)
+    info = ctypes.c_void_p(512)
+
+    def call(dtype=1, M=f, n=4, m=5, ldm=5, wu=None, wv=None, iters=10, ws=f, wsb=1 << 20):
+        return lib.otg_greenkhorn(dtype, M, n, m, ldm, f, f, 1.0, wu, wv, iters, 1e-9, f, m, f, f, info, ws, wsb,
+                                  None)
+
+    assert call(M=None) == ERR_ARG
+    assert call(ldm=4) == ERR_ARG
+    assert call(n=0) == ERR_ARG
+    assert call(iters=-1) == ERR_ARG
+    assert call(wu=f) == ERR_ARG
+    assert call(dtype=7) == ERR_DTYPE
+    assert call(wsb=16) == ERR_WORKSPACE
+    assert call(ws=None) == ERR_WORKSPACE
+    assert lib.otg_greenkhorn_workspace_bytes(1, 1024, 1024) == 2 * (8 << 20) + 2 * 8192
+    assert lib.otg_greenkhorn_workspace_bytes(0, 3, 5) == 2 * 256 + 256 + 256
+    assert lib.otg_greenkhorn_workspace_bytes(1, 0, 5) == 0
