@@ -546,7 +546,11 @@ def sinkhorn(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, ver
 def sinkhorn2(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, verbose=False,
               log=False, warn=False, warmstart=None, **kwargs):
     """GPU ``ot.sinkhorn2``: the loss ``<P, M>`` (fp64 accumulation) for 1-D
-    ``b``; the per-histogram losses for 2-D ``b`` (``_sinkhorn.py:435-484``)."""
+    ``b``; the per-histogram losses for 2-D ``b`` (``_sinkhorn.py:435-484``).
+    For torch inputs that require gradients (1-D ``b``, methods 'sinkhorn' and
+    'sinkhorn_log') the loss carries the gradients the reference's autodiff
+    through its iterations converges to, by implicit differentiation at the
+    solution (``_autograd.implicit_grads``)."""
     meth = method.lower()
     if meth == "sinkhorn_stabilized":
         bd, Md, ad, bdv = _prep(a, b, M)
@@ -568,15 +572,15 @@ def sinkhorn2(a, b, M, reg, method="sinkhorn", numItermax=1000, stopThr=1e-9, ve
         fn = sinkhorn_knopp if meth == "sinkhorn" else sinkhorn_log
         return fn(a, b, M, reg, numItermax=numItermax, stopThr=stopThr, verbose=verbose, log=log,
                   warn=warn, warmstart=warmstart)
-    need_grad = isinstance(M, torch.Tensor) and (M.requires_grad or
-                                                 (isinstance(a, torch.Tensor) and a.requires_grad) or
-                                                 (isinstance(b, torch.Tensor) and b.requires_grad))
+    need_grad = any(isinstance(x, torch.Tensor) and x.requires_grad for x in (a, b, M))
     r, P = _run_single(bd, ad, bdv, Md, reg, code, numItermax, stopThr, verbose, warn, warmstart,
                        need_grad)
     loss = _loss(Md, r, reg, code)
     if need_grad:
-        from ._autograd import envelope_loss
-        loss = envelope_loss(loss, P, r, code, float(reg), a, b, M)
+        # the reference's autodiff through its iterations, taken at the
+        # solution by implicit differentiation
+        from ._autograd import implicit_loss
+        loss = implicit_loss(loss, P, Md, ad, bdv, float(reg), a, b, M)
     out = bd.scalar(loss)
     if log:
         if code == _lib.OTG_METHOD_KNOPP:

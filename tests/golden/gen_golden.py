@@ -456,6 +456,41 @@ def greenkhorn():
 SECTIONS["green"] = greenkhorn
 
 
+def sinkhorn2_grads():
+    # 13. gradients of sinkhorn2 by the reference's own autodiff through its
+    # torch-backend iterations (ot/bregman/_sinkhorn.py:435-438; the scenario
+    # of test/test_bregman.py:203-225 with values recorded)
+    import torch
+
+    def case(name, a, b, M, reg, method, **kw):
+        a1 = torch.tensor(a, requires_grad=True)
+        b1 = torch.tensor(b, requires_grad=True)
+        M1 = torch.tensor(M, requires_grad=True)
+        val = ot.sinkhorn2(a1, b1, M1, reg, method=method, **kw)
+        val.backward()
+        save(name, a=a, b=b, M=M, reg=reg, method=method, loss=float(val.detach()), grad_a=a1.grad.numpy(),
+             grad_b=b1.grad.numpy(), grad_M=M1.grad.numpy(), **{"kw_" + k: v for k, v in kw.items()})
+
+    rng = np.random.default_rng(51)
+    x = rng.standard_normal((30, 2))
+    y = rng.standard_normal((40, 2)) + 0.5
+    M = ot.dist(x, y)
+    M /= M.max()
+    a = rng.random(30) + 0.2
+    a /= a.sum()
+    b = rng.random(40) + 0.2
+    b /= b.sum()
+    case("grad2_30x40_knopp", a, b, M, 0.1, "sinkhorn", stopThr=1e-12, numItermax=100000)
+    case("grad2_30x40_log", a, b, M, 0.1, "sinkhorn_log", stopThr=1e-12, numItermax=100000)
+    x = rng.standard_normal((100, 2))
+    y = rng.standard_normal((100, 2))
+    u = ot.unif(100)
+    case("grad2_100_reg1", u, u, ot.dist(x, y), 1.0, "sinkhorn")
+
+
+SECTIONS["grad"] = sinkhorn2_grads
+
+
 def main(names):
     for k in names or list(SECTIONS):
         SECTIONS[k]()
