@@ -77,7 +77,10 @@ def implicit_grads(P, M, a, b, reg, rtol=1e-12, max_iter=None):
     b = b.double()
     MP = M * P
     r, c = MP.sum(1), MP.sum(0)
-    ia = 1.0 / a
+    # bins of zero mass have zero rows / columns in P and drop out of the
+    # system (their own gradient entries are then the gauge constant alone)
+    ia = torch.where(a > 0, 1.0 / a, torch.zeros_like(a))
+    ib = torch.where(b > 0, 1.0 / b, torch.zeros_like(b))
     beta = 1.0 / b.sum()
 
     # S + beta b b^T: the rank-one term lifts S's null direction (the constant
@@ -90,7 +93,7 @@ def implicit_grads(P, M, a, b, reg, rtol=1e-12, max_iter=None):
     rhs = c - P.t().mv(ia * r)
     mu = torch.zeros_like(b)
     res = rhs.clone()
-    z = res / b
+    z = res * ib
     p = z.clone()
     rz = torch.dot(res, z)
     stop = (rtol * torch.linalg.vector_norm(rhs)) ** 2
@@ -105,7 +108,7 @@ def implicit_grads(P, M, a, b, reg, rtol=1e-12, max_iter=None):
         alpha = rz / pSp
         mu = mu + alpha * p
         res = res - alpha * Sp
-        z = res / b
+        z = res * ib
         rz_new = torch.dot(res, z)
         p = z + (rz_new / rz) * p
         rz = rz_new

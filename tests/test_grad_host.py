@@ -55,3 +55,18 @@ def test_short_solve_keeps_the_gauge_direction_out():
     gM, ga, gb = [x.numpy() for x in implicit_grads(t(P), t(g["M"]), t(g["a"]), t(g["b"]), 1.0)]
     assert _rel(gM, g["grad_M"]) < 1e-6
     assert _rel(gb, g["grad_b"]) < 1e-6
+
+
+def test_zero_mass_bins_stay_finite():
+    """Histograms with empty bins: the gradients stay finite, and the M
+    gradient of the occupied block is unchanged by appending empty bins."""
+    g = golden("grad2_30x40_knopp")
+    a0 = np.concatenate([g["a"], [0.0]])
+    b0 = np.concatenate([g["b"], [0.0, 0.0]])
+    M0 = np.pad(g["M"], ((0, 1), (0, 2)), constant_values=0.5)
+    P, lg = oracle.sinkhorn_log(a0, b0, M0, 0.1, stopThr=1e-12, numItermax=100000)
+    assert not lg["_warnings"] and P[30].max() == 0.0 and P[:, 40:].max() == 0.0
+    t = lambda x: torch.tensor(x, dtype=torch.float64)  # noqa: E731
+    gM, ga, gb = [x.numpy() for x in implicit_grads(t(P), t(M0), t(a0), t(b0), 0.1)]
+    assert np.all(np.isfinite(gM)) and np.all(np.isfinite(ga)) and np.all(np.isfinite(gb))
+    assert _rel(gM[:30, :40], g["grad_M"]) < 1e-8
