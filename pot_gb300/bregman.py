@@ -153,7 +153,27 @@ def _print_errs(errs, check_before_print):
         print("{:5d}|{:8e}|".format(ii, e))
 
 
+def _shape(x):
+    return tuple(x.shape) if hasattr(x, "shape") else np.shape(x)
+
+
+def _check_shapes(a, b, M):
+    """Histogram lengths against the cost's sides, before any device work:
+    the kernels read a[0..n) and b[0..m), so a short histogram is an error
+    here (the reference fails in numpy broadcasting), not an out-of-bounds
+    read on the GPU."""
+    sM = _shape(M)
+    if len(sM) != 2:
+        raise ValueError("M must be a 2-D cost matrix")
+    n, m = sM
+    if not is_empty(a) and _shape(a)[:1] != (n,):
+        raise ValueError("a has %s entries, M has %d rows" % (_shape(a)[:1] or "no", n))
+    if not is_empty(b) and _shape(b)[:1] != (m,):
+        raise ValueError("b has %s entries, M has %d columns" % (_shape(b)[:1] or "no", m))
+
+
 def _prep(a, b, M):
+    _check_shapes(a, b, M)
     bd = Boundary(M, a, b)
     Md = bd.to_dev(M)
     if Md.dim() != 2:
@@ -166,14 +186,18 @@ def _prep(a, b, M):
     return bd, Md, ad.contiguous(), bdv.contiguous()
 
 
-def _warm(bd, warmstart, dtype):
+def _warm(bd, warmstart, dtype, n=None, m=None):
     if warmstart is None:
         return None, None
-    return bd.to_dev(warmstart[0], dtype).contiguous(), bd.to_dev(warmstart[1], dtype).contiguous()
+    wu, wv = bd.to_dev(warmstart[0], dtype).contiguous(), bd.to_dev(warmstart[1], dtype).contiguous()
+    if (n is not None and wu.shape[:1] != (n,)) or (m is not None and wv.shape[:1] != (m,)):
+        raise ValueError("warmstart potentials of lengths %s, %s for a %s x %s problem"
+                         % (tuple(wu.shape[:1]), tuple(wv.shape[:1]), n, m))
+    return wu, wv
 
 
 def _run_single(bd, a, b, M, reg, method, numItermax, stopThr, verbose, warn, warmstart, want_plan):
-    wu, wv = _warm(bd, warmstart, M.dtype)
+    wu, wv = _warm(bd, warmstart, M.dtype, M.shape[0], M.shape[1])
     r = solve_dense(M, a, b, reg, method, numItermax, stopThr, wu, wv)
     if r.status == _lib.STATUS_NUMERICAL:
         warnings.warn("Warning: numerical errors at iteration %d" % r.niter)
@@ -376,7 +400,7 @@ def _stab_solve(bd, a, b, M, reg, numItermax, tau, stopThr, warmstart, print_per
     reference's ``logu, logv`` (its gauge: shifted by the absorptions)."""
     wu = wv = None
     if warmstart is not None:
-        al, be = _warm(bd, warmstart, M.dtype)
+        al, be = _warm(bd, warmstart, M.dtype, M.shape[0], M.shape[1])
         wu, wv = (al / reg).contiguous(), (be / reg).contiguous()
     r = solve_dense(M, a, b, reg, _lib.OTG_METHOD_STAB, numItermax, stopThr, wu, wv, tau=tau,
                     check_period=print_period)
@@ -445,7 +469,7 @@ def sinkhorn_epsilon_scaling(a, b, M, reg, numItermax=100, epsilon0=1e4, numInne
     lib = _lib.load()
     n, m = Md.shape
     numItermax = max(35, numItermax)
-    ws = None if warmstart is None else _warm(bd, warmstart, Md.dtype)
+    ws = None if warmstart is None else _warm(bd, warmstart, Md.dtype, n, m)
     rows = torch.empty(n, dtype=torch.float64, device=Md.device)
     cols = torch.empty(m, dtype=torch.float64, device=Md.device)
     a64, b64 = ad.double(), bdv.double()
@@ -499,7 +523,7 @@ def greenkhorn(a, b, M, reg, numItermax=10000, stopThr=1e-9, verbose=False, log=
     if bdv.dim() > 1:
         raise ValueError("greenkhorn takes one target histogram (1-D b)")
     n, m = Md.shape
-    wu, wv = _warm(bd, warmstart, Md.dtype)
+    wu, wv = _warm(bd, warmstart, Md.dtype, n, m)
     lib = _lib.load()
     code = _lib.dtype_code(Md.dtype)
     dev = Md.device

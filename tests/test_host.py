@@ -21,6 +21,25 @@ def test_unknown_method_raises_before_any_device_work():
         pg.sinkhorn2([0.5, 0.5], [0.5, 0.5], [[0.0, 1.0], [1.0, 0.0]], 1.0, method="new_method")
 
 
+def test_histogram_lengths_checked_before_device_work():
+    """A histogram whose length does not match the cost's side is a ValueError
+    on the host (the kernels would otherwise read past it); 2-D b (several
+    histograms) and empty weights pass the check."""
+    from pot_gb300.bregman import _check_shapes
+    M = np.zeros((4, 3))
+    with pytest.raises(ValueError):
+        pg.sinkhorn(np.full(3, 1 / 3), np.full(3, 1 / 3), M, 1.0)
+    with pytest.raises(ValueError):
+        pg.sinkhorn2(np.full(4, 0.25), [0.5, 0.5], M, 1.0)
+    with pytest.raises(ValueError):
+        pg.greenkhorn(np.full(4, 0.25), np.full(4, 0.25), M, 1.0)
+    with pytest.raises(ValueError):
+        _check_shapes([], [], np.zeros(5))
+    _check_shapes(np.full(4, 0.25), np.full((3, 2), 1 / 3), M)
+    _check_shapes([], None, [[0.0, 1.0], [1.0, 0.0]])
+    _check_shapes(torch.full((4,), 0.25), torch.full((3,), 1 / 3), torch.zeros(4, 3))
+
+
 def test_one_histogram_methods_have_no_loss_form():
     """test/test_bregman.py:1404-1407: sinkhorn2 accepts neither 'greenkhorn'
     nor 'sinkhorn_epsilon_scaling' (ValueError, before any device work)."""
