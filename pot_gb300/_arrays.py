@@ -64,6 +64,23 @@ class Boundary:
         return t
 
 
+def shape_of(x):
+    """Shape of a caller's array (list, numpy array or tensor) without copying it."""
+    return tuple(x.shape) if hasattr(x, "shape") else np.shape(x)
+
+
+def check_shape(name, x, shapes):
+    """Raise ValueError unless `x` (when given and non-empty) has one of
+    `shapes`.  Called on the caller's arrays before any device work: the
+    kernels read as many entries as the problem's sizes say, so a wrong
+    shape must stop here rather than become an out-of-bounds read."""
+    if x is None or is_empty(x):
+        return
+    s = shape_of(x)
+    if s not in [tuple(t) for t in shapes]:
+        raise ValueError("%s has shape %s, expected %s" % (name, s, " or ".join(str(tuple(t)) for t in shapes)))
+
+
 def is_empty(x):
     if x is None:
         return True

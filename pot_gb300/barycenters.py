@@ -32,7 +32,8 @@ def _run(A, M, reg, weights, method, numItermax, stopThr, verbose, log, warn):
     if weights is None:
         wd = torch.full((H,), 1.0 / H, dtype=Ad.dtype, device=Ad.device)
     else:
-        assert len(weights) == H
+        if len(weights) != H:
+            raise ValueError("weights has %d entries for %d histograms" % (len(weights), H))
         wd = bd.to_dev(weights, Ad.dtype).contiguous()
     lib = _lib.load()
     dt = _lib.dtype_code(Ad.dtype)

@@ -21,7 +21,7 @@ import numpy as np
 import torch
 
 from . import _lib, tune
-from ._arrays import Boundary
+from ._arrays import Boundary, check_shape, shape_of
 from .utils import OTResult
 
 
@@ -327,6 +327,25 @@ def _solve_uniform(Md, a, b, reg, method, max_iter, tol, kl, per_problem=False):
     return T, u.view(B, n), v.view(B, m), vals, niter, status
 
 
+def _batch_dims(K, a, b, name="M"):
+    """(B, n, m) of a batch cost (or kernel) and the check of its weights:
+    each (B, n) / (B, m), or one (n,) / (m,) histogram for the whole batch
+    (the reference's arithmetic broadcasts it); on the caller's arrays,
+    before any device work."""
+    sK = shape_of(K)
+    if len(sK) != 3:
+        raise ValueError("%s must be a (B, n, m) batch, got shape %s" % (name, sK))
+    B, n, m = sK
+    check_shape("a", a, [(B, n), (n,)])
+    check_shape("b", b, [(B, m), (m,)])
+    return B, n, m
+
+
+def _per_problem(w, B, k):
+    """(B, k) device weights from (B, k) or a broadcast (k,) histogram."""
+    return w.expand(B, k).contiguous() if w.dim() == 1 else w.contiguous()
+
+
 def solve_batch(M, reg, a=None, b=None, max_iter=1000, tol=1e-5, solver="log_sinkhorn", reg_type="entropy",
                 grad="envelope", per_problem=False):
     """GPU ``ot.batch.solve_batch`` (``ot/batch/_linear.py:236``).
@@ -336,11 +355,14 @@ def solve_batch(M, reg, a=None, b=None, max_iter=1000, tol=1e-5, solver="log_sin
         raise ValueError(f"Unknown solver: {solver}")
     if reg_type.lower() not in ("entropy", "kl"):
         raise ValueError(f"Unknown reg_type: {reg_type}")
+    _batch_dims(M, a, b)
     bd = Boundary(M, a, b)
     Md = bd.to_dev(M)
     B, n, m = Md.shape
-    ad = torch.full((B, n), 1.0 / n, dtype=Md.dtype, device=Md.device) if a is None else bd.to_dev(a, Md.dtype)
-    bv = torch.full((B, m), 1.0 / m, dtype=Md.dtype, device=Md.device) if b is None else bd.to_dev(b, Md.dtype)
+    ad = torch.full((B, n), 1.0 / n, dtype=Md.dtype, device=Md.device) if a is None else \
+        _per_problem(bd.to_dev(a, Md.dtype), B, n)
+    bv = torch.full((B, m), 1.0 / m, dtype=Md.dtype, device=Md.device) if b is None else \
+        _per_problem(bd.to_dev(b, Md.dtype), B, m)
     method = _lib.OTG_METHOD_LOG if solver == "log_sinkhorn" else _lib.OTG_METHOD_KNOPP
     T, u, v, vals, niter, _ = _solve_uniform(Md, ad, bv, float(reg), method, max_iter, tol,
                                              reg_type.lower() == "kl", per_problem)
@@ -388,11 +410,14 @@ def bregman_log_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol
                                  per_problem=False):
     """GPU ``ot.batch.bregman_log_projection_batch`` (``_utils.py:165``):
     ``K = -M/reg`` is solved as cost ``-K`` with unit regularisation."""
+    _batch_dims(K, a, b, "K")
     bd = Boundary(K, a, b)
     Kd = bd.to_dev(K)
     B, n, m = Kd.shape
-    ad = torch.ones((B, n), dtype=Kd.dtype, device=Kd.device) / n if a is None else bd.to_dev(a, Kd.dtype)
-    bv = torch.ones((B, m), dtype=Kd.dtype, device=Kd.device) / m if b is None else bd.to_dev(b, Kd.dtype)
+    ad = torch.ones((B, n), dtype=Kd.dtype, device=Kd.device) / n if a is None else \
+        _per_problem(bd.to_dev(a, Kd.dtype), B, n)
+    bv = torch.ones((B, m), dtype=Kd.dtype, device=Kd.device) / m if b is None else \
+        _per_problem(bd.to_dev(b, Kd.dtype), B, m)
     T, u, v, _, niter, _ = _solve_uniform((-Kd).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_LOG, max_iter, tol, False,
                                           per_problem)
     log_T = Kd + u[:, :, None] + v[:, None, :]
@@ -404,11 +429,14 @@ def bregman_projection_batch(K, a=None, b=None, nx=None, max_iter=10000, tol=1e-
                              per_problem=False):
     """GPU ``ot.batch.bregman_projection_batch`` (``_utils.py:46``): the
     affinity ``K`` is solved as cost ``-log K`` with unit regularisation."""
+    _batch_dims(K, a, b, "K")
     bd = Boundary(K, a, b)
     Kd = bd.to_dev(K)
     B, n, m = Kd.shape
-    ad = torch.ones((B, n), dtype=Kd.dtype, device=Kd.device) / n if a is None else bd.to_dev(a, Kd.dtype)
-    bv = torch.ones((B, m), dtype=Kd.dtype, device=Kd.device) / m if b is None else bd.to_dev(b, Kd.dtype)
+    ad = torch.ones((B, n), dtype=Kd.dtype, device=Kd.device) / n if a is None else \
+        _per_problem(bd.to_dev(a, Kd.dtype), B, n)
+    bv = torch.ones((B, m), dtype=Kd.dtype, device=Kd.device) / m if b is None else \
+        _per_problem(bd.to_dev(b, Kd.dtype), B, m)
     T, f, g, _, niter, _ = _solve_uniform((-torch.log(Kd)).contiguous(), ad, bv, 1.0, _lib.OTG_METHOD_KNOPP,
                                           max_iter, tol, False, per_problem)
     return {"T": bd.out(T), "n_iters": int(niter.max().item()), "potentials": (bd.out(f), bd.out(g))}
@@ -647,6 +675,14 @@ def solve_gromov_batch(C1, C2, reg=1e-2, a=None, b=None, loss="sqeuclidean", sym
         raise ValueError(f"Unknown loss function: {loss}")
     if loss != "sqeuclidean":
         raise NotImplementedError("pot_gb300 solve_gromov_batch: loss '%s' is not on the GPU path" % loss)
+    s1, s2 = shape_of(C1), shape_of(C2)
+    if len(s1) == 3 and len(s2) == 3:
+        if s1[1] != s1[2] or s2[1] != s2[2] or s1[0] != s2[0]:
+            raise ValueError("C1 and C2 must be (B, n, n) and (B, m, m) batches, got %s and %s" % (s1, s2))
+        check_shape("a", a, [(s1[0], s1[1]), (s1[1],)])
+        check_shape("b", b, [(s1[0], s2[1]), (s2[1],)])
+        check_shape("M", M, [(s1[0], s1[1], s2[1])])
+        check_shape("T_init", T_init, [(s1[0], s1[1], s2[1])])
     bd = Boundary(C1, C2, a, b, M, T_init)
     C1d = bd.to_dev(C1)
     C2d = bd.to_dev(C2, C1d.dtype)
@@ -654,8 +690,8 @@ def solve_gromov_batch(C1, C2, reg=1e-2, a=None, b=None, loss="sqeuclidean", sym
         raise NotImplementedError("pot_gb300 solve_gromov_batch: vector-valued (4-D) costs are not on the GPU path")
     dt, dev = C1d.dtype, C1d.device
     B, n, m = C1d.shape[0], C1d.shape[1], C2d.shape[1]
-    ad = torch.ones((B, n), dtype=dt, device=dev) / n if a is None else bd.to_dev(a, dt)
-    bv = torch.ones((B, m), dtype=dt, device=dev) / m if b is None else bd.to_dev(b, dt)
+    ad = torch.ones((B, n), dtype=dt, device=dev) / n if a is None else _per_problem(bd.to_dev(a, dt), B, n)
+    bv = torch.ones((B, m), dtype=dt, device=dev) / m if b is None else _per_problem(bd.to_dev(b, dt), B, m)
     tr = lambda X: X.transpose(1, 2).contiguous()  # noqa: E731
     if symmetric is None:
         symmetric = bool(torch.allclose(C1d, tr(C1d), atol=1e-10) and torch.allclose(C2d, tr(C2d), atol=1e-10))

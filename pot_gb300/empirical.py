@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._arrays import Boundary
+from ._arrays import Boundary, check_shape, shape_of
 from . import bregman
 from . import batch as pb
 from .gromov import pow2_scale
@@ -102,6 +102,14 @@ def empirical_sinkhorn(X_s, X_t, reg, a=None, b=None, metric="sqeuclidean", numI
         raise NotImplementedError("pot_gb300 empirical_sinkhorn: metric '%s' is not on the GPU path" % metric)
     if isLazy and not (isinstance(batchSize, int) or (isinstance(batchSize, tuple) and len(batchSize) == 2)):
         raise ValueError("Batch size must be in integer or a tuple of two integers")
+    sX, sY = shape_of(X_s), shape_of(X_t)
+    if len(sX) != 2 or len(sY) != 2 or sX[1] != sY[1]:
+        raise ValueError("X_s and X_t must be point arrays (ns, d) and (nt, d), got %s and %s" % (sX, sY))
+    check_shape("a", a, [(sX[0],)])
+    check_shape("b", b, [(sY[0],)])
+    if warmstart is not None:
+        check_shape("warmstart[0]", warmstart[0], [(sX[0],)])
+        check_shape("warmstart[1]", warmstart[1], [(sY[0],)])
     bd = Boundary(X_s, X_t, a, b)
     Xd = bd.to_dev(X_s)
     Yd = bd.to_dev(X_t, Xd.dtype)

@@ -21,7 +21,7 @@ import warnings
 import torch
 
 from . import _lib
-from ._arrays import Boundary
+from ._arrays import Boundary, check_shape, shape_of
 from . import bregman
 
 
@@ -129,6 +129,19 @@ class TensorProduct:
             raise RuntimeError("pot_gb300: a device-side wait of the tensor-core GEMM timed out")
 
 
+def _check_gw_shapes(C1, C2, p, q, G0=None, Mf=None):
+    """Structure matrices square, marginals and (n, m) inputs of matching
+    sizes, checked on the caller's arrays before any device work."""
+    s1, s2 = shape_of(C1), shape_of(C2)
+    if len(s1) != 2 or s1[0] != s1[1] or len(s2) != 2 or s2[0] != s2[1]:
+        raise ValueError("C1 and C2 must be square matrices, got %s and %s" % (s1, s2))
+    n, m = s1[0], s2[0]
+    check_shape("p", p, [(n,)])
+    check_shape("q", q, [(m,)])
+    check_shape("G0", G0, [(n, m)])
+    check_shape("M", Mf, [(n, m)])
+
+
 def _validate(loss_fun, solver):
     if solver not in ["PGD", "PPA"]:
         raise ValueError("Unknown solver '%s'. Pick one in ['PGD', 'PPA']." % solver)
@@ -190,6 +203,7 @@ def _entropic_gw(Mf, C1, C2, p, q, loss_fun, epsilon, symmetric, alpha, G0, max_
     if "method" in kwargs:
         raise TypeError("sinkhorn() got multiple values for keyword argument 'method'")
     kwargs = dict(kwargs)
+    _check_gw_shapes(C1, C2, p, q, G0, Mf)
     bd = Boundary(C1, C2, p, q, G0, Mf)
     C1d = bd.to_dev(C1)
     C2d = bd.to_dev(C2, C1d.dtype)
@@ -269,6 +283,7 @@ def entropic_gromov_wasserstein_log(C1, C2, p=None, q=None, epsilon=5e-3, max_it
     started from the previous outer iteration's potentials: the same outer
     loop with ``sinkhorn_log`` inside.  Returns (T, log) with ``gw_dist``,
     ``err`` and the inner iteration counts."""
+    _check_gw_shapes(C1, C2, p, q)
     bd = Boundary(C1, C2, p, q)
     C1d = bd.to_dev(C1)
     C2d = bd.to_dev(C2, C1d.dtype)

@@ -40,6 +40,40 @@ def test_histogram_lengths_checked_before_device_work():
     _check_shapes(torch.full((4,), 0.25), torch.full((3,), 1 / 3), torch.zeros(4, 3))
 
 
+def test_point_gw_and_batch_shapes_checked_before_device_work():
+    """The point-cloud, GW and batch drop-ins check their weights and side
+    inputs against the problem sizes on the host; shapes the reference
+    accepts pass the check (and then need the GPU)."""
+    from pot_gb300 import batch as pb
+    from pot_gb300 import gromov as pgw
+    X, Y = np.zeros((5, 2)), np.zeros((4, 2))
+    with pytest.raises(ValueError):
+        pg.empirical_sinkhorn(X, Y, 1.0, a=np.full(4, 0.25))
+    with pytest.raises(ValueError):
+        pg.empirical_sinkhorn(X, np.zeros((4, 3)), 1.0)
+    C1, C2 = np.zeros((5, 5)), np.zeros((4, 4))
+    with pytest.raises(ValueError):
+        pgw.entropic_gromov_wasserstein(C1, C2, np.full(4, 0.25), None)
+    with pytest.raises(ValueError):
+        pgw.entropic_gromov_wasserstein(np.zeros((5, 4)), C2)
+    with pytest.raises(ValueError):
+        pgw.entropic_fused_gromov_wasserstein(np.zeros((4, 5)), C1, C2)
+    M = np.zeros((3, 5, 4))
+    with pytest.raises(ValueError):
+        pb.solve_batch(M, 0.1, a=np.full((3, 4), 0.25))
+    with pytest.raises(ValueError):
+        pb.bregman_log_projection_batch(M, b=np.full((2, 4), 0.25))
+    with pytest.raises(ValueError):
+        pb.solve_gromov_batch(np.zeros((3, 5, 5)), np.zeros((3, 4, 4)), b=np.full((3, 5), 0.2))
+    if not torch.cuda.is_available():
+        # shapes the reference accepts get past the check, to the device
+        for call in (lambda: pb.solve_batch(M, 0.1, a=np.full(5, 0.2), b=np.full((3, 4), 0.25)),
+                     lambda: pg.empirical_sinkhorn(X, Y, 1.0, a=np.full(5, 0.2)),
+                     lambda: pgw.entropic_gromov_wasserstein(C1, C2, np.full(5, 0.2), np.full(4, 0.25))):
+            with pytest.raises(RuntimeError, match="CUDA"):
+                call()
+
+
 def test_one_histogram_methods_have_no_loss_form():
     """test/test_bregman.py:1404-1407: sinkhorn2 accepts neither 'greenkhorn'
     nor 'sinkhorn_epsilon_scaling' (ValueError, before any device work)."""
